@@ -1,0 +1,461 @@
+// capi.cu -- the C ABI (include/sipg_gb300.h): operator lifetime, the fused
+// apply, the graph-driven conjugate gradient, host-buffer apply, tables.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "sipg_cg.cuh"
+
+namespace sipg {
+
+std::atomic<unsigned long long> g_launches{0};
+static thread_local std::string t_last_error;
+void set_error(const std::string& msg) { t_last_error = msg; }
+
+cudaError_t launch_apply_f64_lo(int, const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_hi(int, const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_lo(int, const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_hi(int, const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+
+cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
+                             cudaStream_t s) {
+  return p <= 4 ? launch_apply_f64_lo(p, cfg, mode, a, h, s) : launch_apply_f64_hi(p, cfg, mode, a, h, s);
+}
+cudaError_t launch_apply_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const HostTables& h,
+                             cudaStream_t s) {
+  return p <= 4 ? launch_apply_f32_lo(p, cfg, mode, a, h, s) : launch_apply_f32_hi(p, cfg, mode, a, h, s);
+}
+
+template <typename T>
+cudaError_t launch_apply(const sipg_op* op, int mode, const ApplyArgs<T>& a, cudaStream_t s);
+template <>
+cudaError_t launch_apply<double>(const sipg_op* op, int mode, const ApplyArgs<double>& a, cudaStream_t s) {
+  return launch_apply_f64(op->p, op->cfg64, mode, a, op->tab, s);
+}
+template <>
+cudaError_t launch_apply<float>(const sipg_op* op, int mode, const ApplyArgs<float>& a, cudaStream_t s) {
+  return launch_apply_f32(op->p, op->cfg32, mode, a, op->tab, s);
+}
+
+sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, cudaStream_t s);
+sipg_status err_norms_f64(const sipg_op* op, int sol, const sipg_modes* modes, const double* d_u, double* err,
+                          cudaStream_t s);
+
+// Default tile shapes (rows of 32 elements; TY rows per CTA).
+static TileCfg default_cfg(int p, bool f64) {
+  TileCfg c;
+  c.tx = 32;
+  if (f64)
+    c.ty = (p <= 3) ? 8 : 4;
+  else
+    c.ty = (p <= 4) ? 8 : 4;
+  return c;
+}
+
+static int vec_blocks(size_t n) {
+  const size_t want = (n + kVecThreads - 1) / kVecThreads;
+  return (int)std::max<size_t>(1, std::min<size_t>(want, 152 * 8));
+}
+
+}  // namespace sipg
+
+using namespace sipg;
+
+// CG workspace: vectors, device state, reduction scratch, the cached graph.
+struct sipg_cg_workspace {
+  int elem = 8;  // sizeof(T)
+  size_t n = 0;
+  void* r = nullptr;
+  void* p[2] = {nullptr, nullptr};
+  void* Ap = nullptr;
+  void* st = nullptr;      // CgState<T>
+  void* st_host = nullptr; // pinned mirror
+  ReduceScratch red;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* exec_x = nullptr;
+  int exec_k = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static void ws_free(sipg_cg_workspace* w) {
+  if (!w) return;
+  if (w->exec) cudaGraphExecDestroy(w->exec);
+  cudaFree(w->r);
+  cudaFree(w->p[0]);
+  cudaFree(w->p[1]);
+  cudaFree(w->Ap);
+  cudaFree(w->st);
+  cudaFreeHost(w->st_host);
+  cudaFree(w->red.partials);
+  cudaFree(w->red.counter);
+  if (w->cap) cudaStreamDestroy(w->cap);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+template <typename T>
+static sipg_status ws_get(sipg_op* op, sipg_cg_workspace** out) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  sipg_cg_workspace*& slot = (sizeof(T) == 8) ? op->ws64 : op->ws32;
+  if (slot) {
+    *out = slot;
+    return SIPG_OK;
+  }
+  sipg_cg_workspace* w = new (std::nothrow) sipg_cg_workspace;
+  if (!w) return SIPG_ERR_NOMEM;
+  w->elem = sizeof(T);
+  w->n = (size_t)op->ndof;
+  const size_t bytes = w->n * sizeof(T);
+  const TileCfg cfg = (sizeof(T) == 8) ? op->cfg64 : op->cfg32;
+  (void)cfg;
+  const int cap = reduce_capacity(op->dim);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&w->r, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->p[0], bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->p[1], bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->Ap, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->st, sizeof(CgState<T>));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->st_host, sizeof(CgState<T>));
+  if (e == cudaSuccess) e = cudaMalloc(&w->red.partials, sizeof(double) * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&w->red.counter, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(w->red.counter, 0, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(w->st, 0, sizeof(CgState<T>));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
+  w->red.capacity = cap;
+  if (e != cudaSuccess) {
+    set_error(std::string("CG workspace allocation failed: ") + cudaGetErrorString(e));
+    ws_free(w);
+    return e == cudaErrorMemoryAllocation ? SIPG_ERR_NOMEM : SIPG_ERR_CUDA;
+  }
+  slot = w;
+  *out = w;
+  return SIPG_OK;
+}
+
+// Iterations per graph launch: small systems are launch-bound, so batch more.
+static int graph_iters(long long ndof) { return ndof <= (1LL << 20) ? 32 : 8; }
+
+// Capture K CG iterations (apply + update, direction buffers alternating).
+template <typename T>
+static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, int K) {
+  if (w->exec && w->exec_x == x && w->exec_k == K) return SIPG_OK;
+  if (w->exec) {
+    cudaGraphExecDestroy(w->exec);
+    w->exec = nullptr;
+  }
+  {
+    ApplyArgs<T> prep{};
+    prep.dim = op->dim;
+    SIPG_CUDA_TRY(launch_apply<T>(op, APPLY_PREPARE, prep, w->cap));
+  }
+  cudaGraph_t g = nullptr;
+  SIPG_CUDA_TRY(cudaStreamBeginCapture(w->cap, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  const int vb = vec_blocks(w->n);
+  for (int k = 0; k < K && err == cudaSuccess; ++k) {
+    ApplyArgs<T> a{};
+    a.in = (const T*)w->r;
+    a.pold = (const T*)w->p[k & 1];
+    a.pnew = (T*)w->p[(k + 1) & 1];
+    a.out = (T*)w->Ap;
+    a.b = nullptr;
+    a.dim = op->dim;
+    a.nu = (T)op->pen;
+    a.st = (CgState<T>*)w->st;
+    a.red = w->red;
+    err = launch_apply<T>(op, APPLY_CG, a, w->cap);
+    if (err != cudaSuccess) break;
+    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[(k + 1) & 1], (T*)w->r, (const T*)w->Ap, w->n,
+                                                   (CgState<T>*)w->st, w->red);
+    err = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamEndCapture(w->cap, &g);
+  if (err != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    set_error(std::string("CG graph capture failed: ") + cudaGetErrorString(err != cudaSuccess ? err : e2));
+    return SIPG_ERR_CUDA;
+  }
+  cudaError_t e3 = cudaGraphInstantiate(&w->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e3 != cudaSuccess) {
+    w->exec = nullptr;
+    set_error(std::string("CG graph instantiate failed: ") + cudaGetErrorString(e3));
+    return SIPG_ERR_CUDA;
+  }
+  w->exec_x = x;
+  w->exec_k = K;
+  return SIPG_OK;
+}
+
+template <typename T>
+static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int max_it, sipg_cg_result* res,
+                            cudaStream_t s) {
+  if (!op || !x || !b) {
+    set_error("sipg_cg: null argument");
+    return SIPG_ERR_INVALID;
+  }
+  SIPG_CUDA_TRY(cudaSetDevice(op->device));
+  sipg_cg_workspace* w = nullptr;
+  sipg_status st = ws_get<T>(op, &w);
+  if (st != SIPG_OK) return st;
+  const long long mx = (max_it > 0) ? max_it : op->ndof;
+  const int max_i = (int)std::min<long long>(mx, 2000000000LL);
+  const int K = graph_iters(op->ndof);
+  st = capture_iterations<T>(op, w, x, K);
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(cudaEventRecord(w->ev0, s));
+  k_cg_init<T><<<vec_blocks(w->n), kVecThreads, 0, s>>>(b, w->n, (CgState<T>*)w->st, tol, rel, max_i, w->red);
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  ApplyArgs<T> a{};
+  a.in = x;
+  a.out = (T*)w->r;
+  a.b = b;
+  a.dim = op->dim;
+  a.nu = (T)op->pen;
+  a.st = (CgState<T>*)w->st;
+  a.red = w->red;
+  SIPG_CUDA_TRY(launch_apply<T>(op, APPLY_RESID, a, s));
+  CgState<T>* hs = (CgState<T>*)w->st_host;
+  long long launched = 0;
+  for (;;) {
+    SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
+    count_launch(2ULL * K);
+    launched += K;
+    SIPG_CUDA_TRY(cudaMemcpyAsync(hs, w->st, sizeof(CgState<T>), cudaMemcpyDeviceToHost, s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs->done) break;
+    if (launched > (long long)max_i + K) {  // cannot happen unless the device state is corrupt
+      set_error("sipg_cg: iteration bookkeeping lost");
+      return SIPG_ERR_CUDA;
+    }
+  }
+  SIPG_CUDA_TRY(cudaEventRecord(w->ev1, s));
+  SIPG_CUDA_TRY(cudaEventSynchronize(w->ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+  const bool conv = !(std::sqrt((double)hs->rr) > (double)hs->stop);
+  if (res) {
+    res->iterations = hs->it;
+    res->rr = (double)hs->rr;
+    res->stop = (double)hs->stop;
+    res->time_ms = ms;
+    res->converged = conv ? 1 : 0;
+  }
+  if (hs->status == (int)SIPG_ERR_BREAKDOWN) {
+    set_error("sipg_cg: breakdown (p.Ap <= 0 or non-finite scalar)");
+    return SIPG_ERR_BREAKDOWN;
+  }
+  return conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* sipg_last_error(void) { return t_last_error.c_str(); }
+const char* sipg_version(void) { return "sipg-gb300 0.1 (sm_103a)"; }
+unsigned long long sipg_launch_count(void) { return g_launches.load(); }
+
+sipg_status sipg_lgl_table(int npts, double* nodes, double* weights) {
+  if (npts < 2 || npts > SIPG_MAX_N || !nodes || !weights) {
+    set_error("sipg_lgl_table: npts must be in 2..9 and pointers non-null");
+    return SIPG_ERR_INVALID;
+  }
+  HostTables t;
+  build_host_tables(npts - 1, &t);
+  for (int i = 0; i < npts; ++i) {
+    nodes[i] = t.nodes[i];
+    weights[i] = t.w[i];
+  }
+  return SIPG_OK;
+}
+
+sipg_status sipg_dphi_table(int degree, double* D) {
+  if (degree < 1 || degree > SIPG_MAX_P || !D) {
+    set_error("sipg_dphi_table: degree must be in 1..8");
+    return SIPG_ERR_INVALID;
+  }
+  HostTables t;
+  build_host_tables(degree, &t);
+  const int n = degree + 1;
+  for (int i = 0; i < n * n; ++i) D[i] = t.D[i];
+  return SIPG_OK;
+}
+
+sipg_status sipg_square_mesh_coords(int dim, double* x, double* y) {
+  if (dim < 1 || !x || !y) {
+    set_error("sipg_square_mesh_coords: dim >= 1 and non-null pointers required");
+    return SIPG_ERR_INVALID;
+  }
+  const long long noe = (long long)dim * dim;
+  const double delta = 1. / (double)dim;
+  double xx = 0, yy = 1;
+  for (int i = 0; i < dim; ++i) {
+    xx = 0;
+    yy -= delta;
+    for (int j = 0; j < dim; ++j) {
+      const long long id = (long long)i * dim + j;
+      x[0 * noe + id] = xx;
+      y[0 * noe + id] = yy;
+      x[1 * noe + id] = xx + delta;
+      y[1 * noe + id] = yy;
+      x[2 * noe + id] = xx + delta;
+      y[2 * noe + id] = yy + delta;
+      x[3 * noe + id] = xx;
+      y[3 * noe + id] = yy + delta;
+      xx += delta;
+    }
+  }
+  return SIPG_OK;
+}
+
+sipg_status sipg_op_create(int dim, int degree, double pen, sipg_op** out) {
+  if (!out) {
+    set_error("sipg_op_create: null output");
+    return SIPG_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (dim < 1 || dim > 65535) {
+    set_error("sipg_op_create: dim must be in 1..65535");
+    return SIPG_ERR_INVALID;
+  }
+  if (degree < 1 || degree > SIPG_MAX_P) {
+    set_error("sipg_op_create: degree must be in 1..8");
+    return SIPG_ERR_UNSUPPORTED;
+  }
+  if (!std::isfinite(pen)) {
+    set_error("sipg_op_create: penalty must be finite");
+    return SIPG_ERR_INVALID;
+  }
+  int dev = 0, major = 0, minor = 0;
+  SIPG_CUDA_TRY(cudaGetDevice(&dev));
+  SIPG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  SIPG_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (major * 10 + minor != 103) {
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "sipg_op_create: device %d is sm_%d%d; this build targets sm_103a", dev, major,
+                  minor);
+    set_error(buf);
+    return SIPG_ERR_UNSUPPORTED;
+  }
+  sipg_op* op = new (std::nothrow) sipg_op;
+  if (!op) return SIPG_ERR_NOMEM;
+  op->dim = dim;
+  op->p = degree;
+  op->pen = pen;
+  op->device = dev;
+  op->noe = (long long)dim * dim;
+  op->ndof = op->noe * (degree + 1) * (degree + 1);
+  build_host_tables(degree, &op->tab);
+  op->cfg64 = default_cfg(degree, true);
+  op->cfg32 = default_cfg(degree, false);
+  *out = op;
+  return SIPG_OK;
+}
+
+sipg_status sipg_op_destroy(sipg_op* op) {
+  if (!op) return SIPG_OK;
+  cudaSetDevice(op->device);
+  ws_free(op->ws64);
+  ws_free(op->ws32);
+  cudaFree(op->stage_in);
+  cudaFree(op->stage_out);
+  delete op;
+  return SIPG_OK;
+}
+
+size_t sipg_op_solve_footprint(int dim, int degree, sipg_precision prec) {
+  const size_t ndof = (size_t)dim * dim * (degree + 1) * (degree + 1);
+  const size_t e = prec == SIPG_F32 ? 4 : 8;
+  // x, b (caller) + r, p0, p1, Ap (workspace)
+  return ndof * e * 6 + 64 * 1024;
+}
+
+sipg_status sipg_apply_f64(const sipg_op* op, const double* d_in, double* d_out, void* stream) {
+  if (!op || !d_in || !d_out || d_in == d_out) {
+    set_error("sipg_apply_f64: null or aliased vectors");
+    return SIPG_ERR_INVALID;
+  }
+  ApplyArgs<double> a{};
+  a.in = d_in;
+  a.out = d_out;
+  a.dim = op->dim;
+  a.nu = op->pen;
+  SIPG_CUDA_TRY(launch_apply<double>(op, APPLY_PLAIN, a, (cudaStream_t)stream));
+  return SIPG_OK;
+}
+
+sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, void* stream) {
+  if (!op || !d_in || !d_out || d_in == d_out) {
+    set_error("sipg_apply_f32: null or aliased vectors");
+    return SIPG_ERR_INVALID;
+  }
+  ApplyArgs<float> a{};
+  a.in = d_in;
+  a.out = d_out;
+  a.dim = op->dim;
+  a.nu = (float)op->pen;
+  SIPG_CUDA_TRY(launch_apply<float>(op, APPLY_PLAIN, a, (cudaStream_t)stream));
+  return SIPG_OK;
+}
+
+sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream) {
+  if (!op || !h_in || !h_out) {
+    set_error("sipg_apply_host_f64: null argument");
+    return SIPG_ERR_INVALID;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = (size_t)op->ndof * sizeof(double);
+  {
+    std::lock_guard<std::mutex> lk(op->mu);
+    if (!op->stage_in) SIPG_CUDA_TRY(cudaMalloc(&op->stage_in, bytes));
+    if (!op->stage_out) SIPG_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
+  }
+  SIPG_CUDA_TRY(cudaMemcpyAsync(op->stage_in, h_in, bytes, cudaMemcpyHostToDevice, s));
+  sipg_status st = sipg_apply_f64(op, op->stage_in, op->stage_out, stream);
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(cudaMemcpyAsync(h_out, op->stage_out, bytes, cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return SIPG_OK;
+}
+
+sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol, int tol_relative, int max_it,
+                        sipg_cg_result* res, void* stream) {
+  return cg_solve<double>(op, d_x, d_b, tol, tol_relative, max_it, res, (cudaStream_t)stream);
+}
+
+sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
+                        sipg_cg_result* res, void* stream) {
+  return cg_solve<float>(op, d_x, d_b, tol, tol_relative, max_it, res, (cudaStream_t)stream);
+}
+
+sipg_status sipg_rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, void* stream) {
+  if (!op || !d_b || sol < SIPG_SOL_A || sol > SIPG_SOL_MODES || (sol == SIPG_SOL_MODES && !modes) ||
+      (modes && (modes->nmodes < 0 || modes->nmodes > 8))) {
+    set_error("sipg_rhs_f64: invalid arguments");
+    return SIPG_ERR_INVALID;
+  }
+  return rhs_f64(op, sol, modes, d_b, (cudaStream_t)stream);
+}
+
+sipg_status sipg_err_norms_f64(const sipg_op* op, int sol, const sipg_modes* modes, const double* d_u, double* err,
+                               void* stream) {
+  if (!op || !d_u || !err || sol < SIPG_SOL_A || sol > SIPG_SOL_MODES || (sol == SIPG_SOL_MODES && !modes)) {
+    set_error("sipg_err_norms_f64: invalid arguments");
+    return SIPG_ERR_INVALID;
+  }
+  return err_norms_f64(op, sol, modes, d_u, err, (cudaStream_t)stream);
+}
+
+sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
+                             sipg_mixed_result* res, void* stream);
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// sipg_cg.cuh -- conjugate-gradient building blocks: the vector update with
+// its fused r.r reduction, the solve set-up, and the host driver that runs the
+// iterations as CUDA graphs with every scalar kept on the device.
+//
+// One iteration is two kernels (the reference's is three kernels plus two
+// blocking cuBLAS dots, conjugate_gradient_gpu.hpp:69-99):
+//   k_sipg_apply<APPLY_CG>:  p = r + beta p_old (first: p = r), Ap = A p,
+//                            pAp reduced, alpha = rr / pAp        (32 B/DoF)
+//   k_cg_update:             x += alpha p, r -= alpha Ap, rr' reduced,
+//                            beta = rr'/rr, it++, done test        (48 B/DoF)
+// The direction is double-buffered (p_old, p_new alternate), so a CTA reading
+// a neighbour's halo never sees a half-updated direction.
+#pragma once
+
+#include "sipg_apply.cuh"
+
+namespace sipg {
+
+constexpr int kVecThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, const T* __restrict__ p,
+                                                           T* __restrict__ r, const T* __restrict__ Ap, size_t n,
+                                                           CgState<T>* st, ReduceScratch red) {
+  __shared__ T sh[32];
+  if (*(volatile int*)&st->done) return;
+  const T alpha = st->alpha;
+  T acc = T(0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, Ap[i], r[i]);
+    r[i] = ri;
+    acc = fma(ri, ri, acc);
+  }
+  const T bt = block_sum<T, kVecThreads>(acc, sh);
+  T total;
+  if (grid_sum_last<T, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
+    const T rr_old = st->rr;
+    st->beta = total / rr_old;
+    st->rr = total;
+    st->it += 1;
+    st->first = 0;
+    st->done = !(sqrt(total) > st->stop && st->it < st->max_it);
+    if (!isfinite(total)) {
+      st->status = (int)SIPG_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+  }
+}
+
+// b.b, and the stop threshold: tol (absolute) or tol*||b|| (relative).
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_init(const T* __restrict__ b, size_t n, CgState<T>* st, T tol,
+                                                         int rel, int max_it, ReduceScratch red) {
+  __shared__ T sh[32];
+  T acc = T(0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) acc = fma(b[i], b[i], acc);
+  const T bt = block_sum<T, kVecThreads>(acc, sh);
+  T total;
+  if (grid_sum_last<T, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
+    st->bb = total;
+    st->stop = rel ? tol * sqrt(total) : tol;
+    st->max_it = max_it;
+    st->it = 0;
+    st->done = 0;
+    st->first = 1;
+    st->status = (int)SIPG_OK;
+    st->alpha = st->beta = st->pAp = T(0);
+  }
+}
+
+}  // namespace sipg

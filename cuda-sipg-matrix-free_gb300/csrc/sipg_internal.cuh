@@ -1,0 +1,165 @@
+// sipg_internal.cuh -- shared definitions of the GB300 SIPG-SEM library:
+// per-degree operator tables (passed to kernels by value, so they live in the
+// kernel-parameter constant bank and no process-global __constant__ state
+// exists), the operator object, CG device state, error plumbing.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include "sipg_gb300.h"
+
+#define SIPG_MAX_P SIPG_MAX_DEGREE
+#define SIPG_MAX_N (SIPG_MAX_P + 1)
+
+namespace sipg {
+
+// ---------------------------------------------------------------------------
+// Degree-P tables.  w: LGL weights; D0[i] = derivative of basis i at node 0,
+// DN[i] = at node P (the face columns of the reference's D table,
+// device_const.hpp:216-234); K[a*n+b] = sum_k w_k D[a][k] D[b][k], the 1-D
+// stiffness that the reference's volume kernel recomputes per thread
+// (volume_gpu_kernels.hpp:46-80).
+// ---------------------------------------------------------------------------
+template <typename T, int P>
+struct Tab {
+  static constexpr int N1 = P + 1;
+  T w[N1];
+  T D0[N1];
+  T DN[N1];
+  T K[N1 * N1];
+};
+
+// Host-side double tables for one degree (filled by tables.cpp).
+struct HostTables {
+  int p;
+  double nodes[SIPG_MAX_N];
+  double w[SIPG_MAX_N];
+  double D[SIPG_MAX_N * SIPG_MAX_N];  // D[mode*n+node]
+  double K[SIPG_MAX_N * SIPG_MAX_N];
+};
+int build_host_tables(int p, HostTables* t);  // 0 on success
+
+template <typename T, int P>
+inline Tab<T, P> make_tab(const HostTables& h) {
+  Tab<T, P> t;
+  const int n = P + 1;
+  for (int i = 0; i < n; ++i) {
+    t.w[i] = (T)h.w[i];
+    t.D0[i] = (T)h.D[i * n + 0];
+    t.DN[i] = (T)h.D[i * n + P];
+  }
+  for (int i = 0; i < n * n; ++i) t.K[i] = (T)h.K[i];
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// CG state kept on the device (one per solve); scalars of type T.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct CgState {
+  T rr;      // r.r of the current residual (the reference's rr_old)
+  T pAp;     // p.Ap of the current direction
+  T alpha;   // rr / pAp
+  T beta;    // rr_new / rr_old
+  T stop;    // absolute stop threshold on sqrt(r.r)
+  T bb;      // b.b (for relative tolerances)
+  int it;    // iterations done
+  int max_it;
+  int done;  // 1 once sqrt(rr) <= stop, it == max_it, or breakdown
+  int first; // 1 before the first direction p = r is formed
+  int status;  // SIPG_OK / SIPG_ERR_BREAKDOWN
+  int pad;
+};
+
+// Deterministic grid reduction scratch: per-block partials, reduced in a fixed
+// order by whichever block arrives last.
+struct ReduceScratch {
+  double* partials = nullptr;  // capacity entries
+  unsigned int* counter = nullptr;
+  int capacity = 0;
+};
+
+// Kernel modes of the fused apply.
+enum ApplyMode : int {
+  APPLY_PREPARE = -1,  // set kernel attributes only (before a graph capture)
+  APPLY_PLAIN = 0,  // y = A u
+  APPLY_CG = 1,     // u = r + beta p_old (u = r on the first iteration); p_new = u; y = A u; pAp -> alpha
+  APPLY_RESID = 2   // y = b - A u; r.r -> rr, stop/done set
+};
+
+template <typename T>
+struct ApplyArgs {
+  const T* in;     // u (PLAIN, RESID) or r (CG)
+  const T* pold;   // CG: previous direction
+  T* pnew;         // CG: new direction (written)
+  T* out;          // y
+  const T* b;      // RESID: right-hand side
+  int dim;
+  T nu;            // penalty (the reference's `pen`)
+  CgState<T>* st;  // CG / RESID
+  ReduceScratch red;
+};
+
+// Tile shape chosen for one (precision, degree).
+struct TileCfg {
+  int tx = 32, ty = 4;
+};
+
+// Launch the fused apply for degree p (dispatches on p and the tile shape).
+// Returns cudaGetLastError() of the launch.
+cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
+                             cudaStream_t s);
+cudaError_t launch_apply_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const HostTables& h,
+                             cudaStream_t s);
+// Number of blocks the apply launches for this tile shape.
+inline int apply_grid_blocks(int dim, const TileCfg& c) {
+  return ((dim + c.tx - 1) / c.tx) * ((dim + c.ty - 1) / c.ty);
+}
+// Reduction-scratch entries that cover every apply tile shape (the smallest
+// compiled tile is 32 x 2) and every vector kernel grid (at most 152 * 8).
+inline int reduce_capacity(int dim) {
+  const int a = ((dim + 31) / 32) * ((dim + 1) / 2);
+  return a > 152 * 8 ? a : 152 * 8;
+}
+
+// ---------------------------------------------------------------------------
+// Error plumbing and launch accounting.
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+#define SIPG_CUDA_TRY(call)                                                                      \
+  do {                                                                                           \
+    cudaError_t _e = (call);                                                                     \
+    if (_e != cudaSuccess) {                                                                     \
+      ::sipg::set_error(std::string(#call) + " failed: " + cudaGetErrorString(_e));              \
+      return (_e == cudaErrorMemoryAllocation) ? SIPG_ERR_NOMEM : SIPG_ERR_CUDA;                 \
+    }                                                                                            \
+  } while (0)
+
+}  // namespace sipg
+
+// ---------------------------------------------------------------------------
+// The operator object behind the opaque sipg_op handle.
+// ---------------------------------------------------------------------------
+struct sipg_cg_workspace;
+
+struct sipg_op {
+  int dim = 0, p = 0;
+  double pen = 0;
+  int device = 0;
+  long long noe = 0, ndof = 0;
+  sipg::HostTables tab;
+  sipg::TileCfg cfg64, cfg32;
+  std::mutex mu;  // guards the lazily allocated workspaces below
+  sipg_cg_workspace* ws64 = nullptr;
+  sipg_cg_workspace* ws32 = nullptr;
+  double* stage_in = nullptr;  // host-buffer apply staging (device)
+  double* stage_out = nullptr;
+};

@@ -1,0 +1,252 @@
+"""Python binding of the GB300 SIPG-SEM library (libsipg_gb300.so) via ctypes.
+
+The C ABI in include/sipg_gb300.h is the product boundary; this module only
+marshals torch tensors (device memory and streams) and numpy arrays onto it.
+There is no fallback: if the CUDA library is missing or the device is not
+sm_103a, every call raises SipgError.
+
+Vectors are node-major: entry (i1, i2) of element e at ((i1*(p+1)+i2)*noe + e),
+the layout of the reference's mode_vector (mode_vector.hpp:108-120).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsipg_gb300.so")
+
+SIPG_OK = 0
+STATUS_NAMES = {
+    0: "SIPG_OK", 1: "SIPG_ERR_INVALID", 2: "SIPG_ERR_CUDA", 3: "SIPG_ERR_NOT_CONVERGED",
+    4: "SIPG_ERR_BREAKDOWN", 5: "SIPG_ERR_UNSUPPORTED", 6: "SIPG_ERR_NOMEM", 7: "SIPG_ERR_REJECTED",
+    8: "SIPG_ERR_TIMEOUT",
+}
+SOL = {"A": 1, "B": 2, "C": 3, "D": 4, "E": 5, "sinsin": 6, "modes": 7}
+MAX_DEGREE = 8
+
+
+class SipgError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
+
+
+class CgResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rr", C.c_double), ("stop", C.c_double), ("time_ms", C.c_double),
+                ("converged", C.c_int)]
+
+
+class MixedOpts(C.Structure):
+    _fields_ = [("inner_tol", C.c_double), ("outer_tol", C.c_double), ("max_outer", C.c_int), ("max_inner", C.c_int)]
+
+
+class MixedResult(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("rel_residual", C.c_double),
+                ("time_ms", C.c_double), ("converged", C.c_int)]
+
+
+class Modes(C.Structure):
+    _fields_ = [("nmodes", C.c_int), ("amp", C.c_double * 8), ("k", C.c_int * 8), ("l", C.c_int * 8)]
+
+    @staticmethod
+    def make(amps, ks, ls):
+        m = Modes()
+        m.nmodes = len(amps)
+        for i, (a, k, l) in enumerate(zip(amps, ks, ls)):
+            m.amp[i], m.k[i], m.l[i] = float(a), int(k), int(l)
+        return m
+
+
+_lib = None
+
+_VP = C.c_void_p
+_SIGS = {
+    "sipg_lgl_table": (C.c_int, [C.c_int, _VP, _VP]),
+    "sipg_dphi_table": (C.c_int, [C.c_int, _VP]),
+    "sipg_square_mesh_coords": (C.c_int, [C.c_int, _VP, _VP]),
+    "sipg_op_create": (C.c_int, [C.c_int, C.c_int, C.c_double, C.POINTER(_VP)]),
+    "sipg_op_destroy": (C.c_int, [_VP]),
+    "sipg_op_solve_footprint": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "sipg_apply_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_apply_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_apply_host_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_cg_f64": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
+    "sipg_cg_f32": (C.c_int, [_VP, _VP, _VP, C.c_float, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
+    "sipg_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), C.POINTER(MixedResult), _VP]),
+    "sipg_rhs_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP]),
+    "sipg_err_norms_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP, _VP]),
+    "sipg_last_error": (C.c_char_p, []),
+    "sipg_version": (C.c_char_p, []),
+    "sipg_launch_count": (C.c_ulonglong, []),
+    "sipg_probe_fma_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+}
+
+
+def lib():
+    """Load libsipg_gb300.so (raises SipgError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SipgError(5, "CUDA library not built: %s (run __graft_entry__.build())" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status, what=""):
+    if status != SIPG_OK:
+        raise SipgError(status, "%s %s" % (what, lib().sipg_last_error().decode()))
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    if stream is not None:
+        return C.c_void_p(stream)
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def launch_count():
+    return int(lib().sipg_launch_count())
+
+
+def probe_fma_peak():
+    """(FP64, FP32) FMA throughput of the current device in TFLOP/s."""
+    a, b = C.c_double(), C.c_double()
+    _check(lib().sipg_probe_fma_peak(C.byref(a), C.byref(b)), "probe")
+    return a.value, b.value
+
+
+def version():
+    return lib().sipg_version().decode()
+
+
+def lgl_table(npts):
+    x, w = np.zeros(npts), np.zeros(npts)
+    _check(lib().sipg_lgl_table(npts, x.ctypes.data, w.ctypes.data), "sipg_lgl_table")
+    return x, w
+
+
+def dphi_table(p):
+    D = np.zeros((p + 1) * (p + 1))
+    _check(lib().sipg_dphi_table(p, D.ctypes.data), "sipg_dphi_table")
+    return D
+
+
+def square_mesh_coords(dim):
+    x, y = np.zeros(4 * dim * dim), np.zeros(4 * dim * dim)
+    _check(lib().sipg_square_mesh_coords(dim, x.ctypes.data, y.ctypes.data), "sipg_square_mesh_coords")
+    return x, y
+
+
+class Operator:
+    """The SIPG operator of a dim x dim mesh of degree p with kernel penalty pen."""
+
+    def __init__(self, dim, degree, pen):
+        h = C.c_void_p()
+        _check(lib().sipg_op_create(int(dim), int(degree), float(pen), C.byref(h)), "sipg_op_create")
+        self._h = h
+        self.dim, self.degree, self.pen = int(dim), int(degree), float(pen)
+        self.noe = self.dim * self.dim
+        self.ndof = self.noe * (self.degree + 1) ** 2
+
+    def close(self):
+        if self._h:
+            lib().sipg_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _vec(self, t, dtype=None):
+        import torch
+
+        assert t.is_cuda and t.is_contiguous() and t.numel() == self.ndof, "expected a contiguous CUDA vector"
+        if dtype is not None:
+            assert t.dtype == dtype
+        return t
+
+    def empty(self, dtype=None):
+        import torch
+
+        return torch.empty(self.ndof, dtype=dtype or torch.float64, device="cuda")
+
+    def apply(self, x, out=None, stream=None):
+        """out = A x (float64 or float32 CUDA tensors)."""
+        import torch
+
+        self._vec(x)
+        if out is None:
+            out = torch.empty_like(x)
+        self._vec(out, x.dtype)
+        f = lib().sipg_apply_f64 if x.dtype == torch.float64 else lib().sipg_apply_f32
+        _check(f(self._h, _ptr(x), _ptr(out), _stream(stream)), "apply")
+        return out
+
+    def apply_host(self, x, out=None, stream=0):
+        """Host numpy float64 in and out (copies inside)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if out is None:
+            out = np.empty_like(x)
+        _check(lib().sipg_apply_host_f64(self._h, x.ctypes.data, out.ctypes.data, C.c_void_p(stream)),
+               "apply_host")
+        return out
+
+    def cg(self, x, b, tol, relative=False, max_it=0, stream=None, raise_on=("breakdown",)):
+        """Conjugate gradient from x (in place).  Returns (status, CgResult)."""
+        import torch
+
+        self._vec(x)
+        self._vec(b, x.dtype)
+        res = CgResult()
+        if x.dtype == torch.float64:
+            st = lib().sipg_cg_f64(self._h, _ptr(x), _ptr(b), float(tol), int(bool(relative)), int(max_it),
+                                   C.byref(res), _stream(stream))
+        else:
+            st = lib().sipg_cg_f32(self._h, _ptr(x), _ptr(b), float(tol), int(bool(relative)), int(max_it),
+                                   C.byref(res), _stream(stream))
+        if st not in (0, 3, 4):
+            _check(st, "cg")
+        return st, res
+
+    def solve_mixed(self, x, b, inner_tol=1e-5, outer_tol=1e-10, max_outer=50, max_inner=0, stream=None):
+        """FP32-inner / FP64-outer defect correction.  Returns (status, MixedResult)."""
+        import torch
+
+        self._vec(x, torch.float64)
+        self._vec(b, torch.float64)
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner))
+        res = MixedResult()
+        st = lib().sipg_solve_mixed(self._h, _ptr(x), _ptr(b), C.byref(o), C.byref(res), _stream(stream))
+        if st not in (0, 3, 4):
+            _check(st, "solve_mixed")
+        return st, res
+
+    def rhs(self, sol, modes=None, out=None, stream=None):
+        """Right-hand side of a test problem (SOL name or id) as a float64 CUDA vector."""
+        sid = SOL[sol] if isinstance(sol, str) else int(sol)
+        if out is None:
+            out = self.empty()
+        m = C.byref(modes) if modes is not None else None
+        _check(lib().sipg_rhs_f64(self._h, sid, m, _ptr(out), _stream(stream)), "rhs")
+        return out
+
+    def err_norms(self, sol, u, modes=None, stream=None):
+        """(L2, H1, max) nodal errors of u against test problem sol."""
+        sid = SOL[sol] if isinstance(sol, str) else int(sol)
+        e = np.zeros(3)
+        m = C.byref(modes) if modes is not None else None
+        _check(lib().sipg_err_norms_f64(self._h, sid, m, _ptr(u), e.ctypes.data, _stream(stream)), "err_norms")
+        return float(e[0]), float(e[1]), float(e[2])

@@ -1,0 +1,168 @@
+/*
+ * sipg_gb300.h -- C ABI of the GB300-native matrix-free SIPG-SEM Poisson
+ * solver (sm_103a).  Plain pointers and sizes only; every call returns a
+ * sipg_status and nothing calls exit().
+ *
+ * Vectors use the reference's node-major layout: value (i1,i2) of element e
+ * at ((i1*(p+1)+i2)*noe + e), noe = dim*dim, element e = row*dim + col with row
+ * 0 at the top of the unit square (mode_vector.hpp:108-120 and
+ * build_square_mesh.hpp:250-288 of paogor/CUDA-SIPG-matrix-free), so the
+ * device pointer of a reference mode_vector<T,int> drops straight in.
+ *
+ * Device pointers ("d_") must be cudaMalloc'ed on the op's device; host
+ * pointers ("h_") are ordinary or pinned host memory.  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).
+ */
+#ifndef SIPG_GB300_H
+#define SIPG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SIPG_OK = 0,
+  SIPG_ERR_INVALID = 1,       /* bad argument (null pointer, degree or size out of range) */
+  SIPG_ERR_CUDA = 2,          /* a CUDA runtime call failed; see sipg_last_error() */
+  SIPG_ERR_NOT_CONVERGED = 3, /* CG reached max_it before the tolerance */
+  SIPG_ERR_BREAKDOWN = 4,     /* CG met p.Ap <= 0 or a non-finite scalar */
+  SIPG_ERR_UNSUPPORTED = 5,   /* degree outside 1..SIPG_MAX_DEGREE, or no sm_103a device */
+  SIPG_ERR_NOMEM = 6,         /* device allocation failed */
+  SIPG_ERR_REJECTED = 7,      /* serving: request does not fit the memory budget */
+  SIPG_ERR_TIMEOUT = 8        /* a bounded device wait gave up */
+} sipg_status;
+
+typedef enum { SIPG_F64 = 0, SIPG_F32 = 1 } sipg_precision;
+
+#define SIPG_MAX_DEGREE 8
+
+/* Analytic test problems for the on-device right-hand side and error norms:
+ * 1..5 = the reference's solutions A..E (validation_tests/analytical_solutions.hpp:7-94,
+ * with its PI = 3.14159265359); 6 = sin(2 pi x) sin(2 pi y), f = 8 pi^2 u;
+ * 7 = sum of modes A_m sin(k_m pi x) sin(l_m pi y) (f), u = f-modes / ((k^2+l^2) pi^2). */
+typedef enum {
+  SIPG_SOL_A = 1, SIPG_SOL_B = 2, SIPG_SOL_C = 3, SIPG_SOL_D = 4, SIPG_SOL_E = 5,
+  SIPG_SOL_SINSIN = 6, SIPG_SOL_MODES = 7
+} sipg_solution;
+
+typedef struct {
+  int nmodes; /* 0..8 */
+  double amp[8];
+  int k[8], l[8];
+} sipg_modes;
+
+/* One SIPG operator: a dim x dim uniform mesh of the unit square, degree p,
+ * penalty `pen` (the reference's kernel penalty nu: interior faces get 2*nu,
+ * boundary faces nu, sipg_sem_2d_gpu_kernels.hpp:300,333-334).  Opaque. */
+typedef struct sipg_op sipg_op;
+
+typedef struct {
+  int iterations;      /* CG iterations performed */
+  double rr;           /* final r.r */
+  double stop;         /* absolute stop threshold used on sqrt(r.r) */
+  double time_ms;      /* device time of the solve (CUDA events) */
+  int converged;       /* 1 if sqrt(r.r) <= stop */
+} sipg_cg_result;
+
+typedef struct {
+  double inner_tol;    /* inner FP32 CG relative tolerance (1e-5) */
+  double outer_tol;    /* outer FP64 relative residual ||b-Ax||/||b|| (1e-10) */
+  int max_outer;       /* outer defect-correction steps cap (50) */
+  int max_inner;       /* per inner solve iteration cap (0 = DoF) */
+} sipg_mixed_opts;
+
+typedef struct {
+  int outer_iterations;
+  int inner_iterations; /* summed over all outer steps */
+  double rel_residual;  /* final ||b - A x|| / ||b|| in FP64 */
+  double time_ms;
+  int converged;
+} sipg_mixed_result;
+
+/* ---- tables and mesh (host side, no device needed) ---- */
+
+/* LGL nodes/weights on [-1,1], npts = p+1 in 2..SIPG_MAX_DEGREE+1.
+ * Replaces LGL_quadrature_table<T>::LGL_quadrature_table (LGL_quadrature_table.hpp:84-146). */
+sipg_status sipg_lgl_table(int npts, double* nodes, double* weights);
+/* D[mode*(p+1)+node]: derivative of Lagrange basis `mode` at LGL node `node`.
+ * Replaces sem_function<T>::d_phi / DbaseVALUES (sem_function.hpp:86-110, device_const.hpp:115-127). */
+sipg_status sipg_dphi_table(int degree, double* D);
+/* Element corner coordinates x[c*noe+e], y[c*noe+e], c=0..3.
+ * Replaces square_mesh<T>::compute_coordinates (build_square_mesh.hpp:250-288). */
+sipg_status sipg_square_mesh_coords(int dim, double* x, double* y);
+
+/* ---- operator lifetime ---- */
+
+/* Creates the operator on the current CUDA device: uploads the degree-p tables
+ * once per device and picks the tile shape.  Replaces the setup in the
+ * sipg_sem_2d<T> constructor (sipg_sem_2d.hpp:96-113) and load_Dphi_table /
+ * load_lgl_quadrature_table (device_const.hpp:70-174), without their
+ * process-global __constant__ state: operators of different degree coexist. */
+sipg_status sipg_op_create(int dim, int degree, double pen, sipg_op** op);
+sipg_status sipg_op_destroy(sipg_op* op);
+/* Bytes of device memory one FP64 CG solve on this op keeps resident. */
+size_t sipg_op_solve_footprint(int dim, int degree, sipg_precision prec);
+
+/* ---- the operator apply (the hot path) ---- */
+
+/* d_out = A d_in, one fused pass (volume + all faces).  Replaces
+ * sipg_sem_2d<T>::_mvm (sipg_sem_2d.hpp:167-201: volume, flux_term6a,
+ * flux_term6b) and the free function mvm (sipg_sem_2d_gpu_kernels.hpp:410-454). */
+sipg_status sipg_apply_f64(const sipg_op* op, const double* d_in, double* d_out, void* stream);
+sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, void* stream);
+/* The same with host buffers: copies h_in to the device, applies, copies the
+ * result back, synchronously.  Device staging buffers are kept in the op. */
+sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream);
+
+/* ---- conjugate gradient ---- */
+
+/* Solves A x = b from the x passed in.  Stops when sqrt(r.r) <= tol
+ * (tol_relative = 0, the reference's absolute test,
+ * conjugate_gradient_gpu.hpp:63-69) or <= tol*||b|| (tol_relative = 1), or
+ * after max_it iterations (max_it <= 0: DoF, as the reference).  Replaces
+ * conjugate_gradient<T> (conjugate_gradient_gpu.hpp:18-109).  Scalars stay on
+ * the device; iterations run as CUDA graphs.  Returns SIPG_OK,
+ * SIPG_ERR_NOT_CONVERGED or SIPG_ERR_BREAKDOWN; `res` may be NULL. */
+sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol, int tol_relative, int max_it,
+                        sipg_cg_result* res, void* stream);
+sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
+                        sipg_cg_result* res, void* stream);
+
+/* Mixed precision: FP32 operator and inner CG (values and accumulation)
+ * inside FP64 defect correction; the outer residual b - A x, the update of x
+ * and the outer norms stay FP64 on the device.  No reference counterpart. */
+sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
+                             sipg_mixed_result* res, void* stream);
+
+/* ---- either side of the solve ---- */
+
+/* d_b = the right-hand side of test problem `sol` (f term + Nitsche terms of
+ * the Dirichlet data u_exact).  Replaces sipg_sem_2d<T>::compute_rhs
+ * (sipg_sem_2d.hpp:232-305), on the device.  `modes` is used by SIPG_SOL_MODES. */
+sipg_status sipg_rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, void* stream);
+/* err[0] = L2, err[1] = broken H1, err[2] = max nodal error of d_u against
+ * test problem `sol`, at the LGL nodes as sipg_sem_2d<T>::err_norms
+ * (sipg_sem_2d.hpp:311-370), on the device.  Synchronous. */
+sipg_status sipg_err_norms_f64(const sipg_op* op, int sol, const sipg_modes* modes, const double* d_u, double* err,
+                               void* stream);
+
+/* ---- diagnostics ---- */
+
+/* Text of the last error on this host thread. */
+const char* sipg_last_error(void);
+/* Library version string. */
+const char* sipg_version(void);
+/* Kernel launches issued by this process so far (all entry points). */
+unsigned long long sipg_launch_count(void);
+/* FP64 and FP32 FMA throughput of the current device in TFLOP/s, measured with
+ * independent FMA chains (about 0.1 s); the denominator of the FP64-pipe
+ * fraction that bench.py reports beside the HBM roofline. */
+sipg_status sipg_probe_fma_peak(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

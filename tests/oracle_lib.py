@@ -1,0 +1,113 @@
+"""ctypes binding of oracle/liboracle.so -- the CPU checker (tests only)."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "liboracle.so")
+
+dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+
+
+class OrModes(C.Structure):
+    _fields_ = [("nmodes", C.c_int), ("amp", C.c_double * 8), ("k", C.c_int * 8), ("l", C.c_int * 8)]
+
+
+class Oracle:
+    def __init__(self, L):
+        self.L = L
+        L.sipg_oracle_lgl.argtypes = [C.c_int, dp, dp]
+        L.sipg_oracle_dphi.argtypes = [C.c_int, dp]
+        L.sipg_oracle_laplace2d.argtypes = [C.c_int, dp]
+        L.sipg_oracle_mesh_coords.argtypes = [C.c_int, dp, dp]
+        L.sipg_oracle_apply.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp, C.c_int]
+        L.sipg_oracle_apply_f32.argtypes = [C.c_int, C.c_int, C.c_float, fp, fp, C.c_int]
+        L.sipg_oracle_volume.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.sipg_oracle_cg.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, C.c_int,
+                                     C.POINTER(C.c_double), C.c_int]
+        L.sipg_oracle_rhs.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, dp]
+        L.sipg_oracle_err_norms.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, dp, dp]
+        L.sipg_oracle_u_exact.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double]
+        L.sipg_oracle_u_exact.restype = C.c_double
+        self.nthreads = max(1, min(16, os.cpu_count() or 1))
+
+    def lgl(self, n):
+        x, w = np.zeros(n), np.zeros(n)
+        assert self.L.sipg_oracle_lgl(n, x, w) == 0
+        return x, w
+
+    def dphi(self, p):
+        D = np.zeros((p + 1) ** 2)
+        assert self.L.sipg_oracle_dphi(p, D) == 0
+        return D
+
+    def laplace2d(self, p):
+        Lm = np.zeros((p + 1) ** 4)
+        assert self.L.sipg_oracle_laplace2d(p, Lm) == 0
+        return Lm
+
+    def mesh_coords(self, dim):
+        x, y = np.zeros(4 * dim * dim), np.zeros(4 * dim * dim)
+        assert self.L.sipg_oracle_mesh_coords(dim, x, y) == 0
+        return x, y
+
+    def apply(self, p, dim, pen, x, nthreads=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        assert self.L.sipg_oracle_apply(p, dim, pen, x, y, nthreads or self.nthreads) == 0
+        return y
+
+    def apply_f32(self, p, dim, pen, x, nthreads=None):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros_like(x)
+        assert self.L.sipg_oracle_apply_f32(p, dim, pen, x, y, nthreads or self.nthreads) == 0
+        return y
+
+    def volume(self, p, dim, x):
+        y = np.zeros_like(x)
+        assert self.L.sipg_oracle_volume(p, dim, np.ascontiguousarray(x), y) == 0
+        return y
+
+    def cg(self, p, dim, pen, b, tol, rel=False, max_it=0, x0=None, nthreads=1):
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        rr = C.c_double()
+        it = self.L.sipg_oracle_cg(p, dim, pen, x, np.ascontiguousarray(b), tol, int(rel), max_it, C.byref(rr),
+                                   nthreads)
+        return it, x, rr.value
+
+    @staticmethod
+    def modes(amps, ks, ls):
+        m = OrModes()
+        m.nmodes = len(amps)
+        for i, (a, k, l) in enumerate(zip(amps, ks, ls)):
+            m.amp[i], m.k[i], m.l[i] = a, k, l
+        return m
+
+    def rhs(self, p, dim, pen, sol, modes=None):
+        b = np.zeros(dim * dim * (p + 1) ** 2)
+        assert self.L.sipg_oracle_rhs(p, dim, pen, sol, C.byref(modes) if modes else None, b) == 0
+        return b
+
+    def err_norms(self, p, dim, sol, u, modes=None):
+        e = np.zeros(3)
+        assert self.L.sipg_oracle_err_norms(p, dim, sol, C.byref(modes) if modes else None,
+                                            np.ascontiguousarray(u), e) == 0
+        return e
+
+
+_cached = None
+
+
+def load():
+    """Build (if needed) and load the oracle library."""
+    global _cached
+    if _cached is None:
+        src = [os.path.join(ORACLE_DIR, f) for f in ("sipg_oracle.c", "sipg_oracle_real.inc", "sipg_oracle.h")]
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(s) for s in src):
+            subprocess.check_call(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"])
+        _cached = Oracle(C.CDLL(LIB))
+    return _cached

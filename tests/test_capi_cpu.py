@@ -1,0 +1,79 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every symbol the
+header declares, and its host-only entry points (tables, mesh) agree with the
+reference's outputs."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "sipg_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sipg_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    import sipg_gb300
+
+    if not os.path.exists(sipg_gb300.LIB_PATH):
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("sipg_build", os.path.join(ROOT, "cuda-sipg-matrix-free_gb300",
+                                                                               "build.py"))
+        m = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        m.build()
+    return sipg_gb300
+
+
+def test_header_compiles_as_c(tmp_path):
+    src = tmp_path / "h.c"
+    src.write_text('#include "sipg_gb300.h"\nint main(void){return (int)SIPG_OK;}\n')
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
+                           str(src)])
+
+
+def test_exports_every_declared_symbol(built_lib):
+    L = built_lib.lib()
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_host_tables_match_reference(built_lib, golden):
+    for n in range(2, 10):
+        x, w = built_lib.lgl_table(n)
+        np.testing.assert_allclose(x, golden["lgl_nodes_%d" % n], rtol=0, atol=2e-16)
+        np.testing.assert_allclose(w, golden["lgl_weights_%d" % n], rtol=4e-15, atol=0)
+    for p in range(1, 9):
+        D = built_lib.dphi_table(p)
+        ref = golden["dphi_%d" % p]
+        assert np.max(np.abs(D - ref)) <= 2e-14 * np.max(np.abs(ref)), p
+
+
+def test_mesh_coords_match_reference(built_lib, golden):
+    for d in (1, 2, 3, 16):
+        x, y = built_lib.square_mesh_coords(d)
+        assert np.array_equal(x, golden["mesh_x_%d" % d])
+        assert np.array_equal(y, golden["mesh_y_%d" % d])
+
+
+def test_invalid_arguments_are_errors_not_crashes(built_lib):
+    L = built_lib.lib()
+    assert L.sipg_lgl_table(1, None, None) == 1
+    assert L.sipg_dphi_table(9, None) == 1
+    h = C.c_void_p()
+    assert L.sipg_op_create(0, 4, 1.0, C.byref(h)) == 1
+    assert L.sipg_op_create(4, 9, 1.0, C.byref(h)) == 5
+    assert b"degree" in L.sipg_last_error()
+    assert L.sipg_op_destroy(None) == 0
+    assert L.sipg_op_solve_footprint(1024, 4, 0) > 6 * 26214400 * 8 - 1

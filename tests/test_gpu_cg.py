@@ -1,0 +1,153 @@
+"""CUDA conjugate gradient, RHS and error norms against the reference.
+
+Iteration counts must be within +-1 of the reference's own CG on the same
+problem (its dots are cuBLAS, order unspecified); solutions agree to the CG
+tolerance; error norms reproduce the reference's and the thesis's values.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+
+    assert t.cuda.is_available()
+    return t
+
+
+def test_rhs_matches_oracle(sipg, oracle, torch):
+    for sol in (1, 2, 3, 4, 5, 6):
+        for p, d in ((2, 4), (4, 7), (3, 1), (6, 33)):
+            pen = float(p * p)
+            op = sipg.Operator(d, p, pen)
+            b = op.rhs(sol).cpu().numpy()
+            op.close()
+            ref = oracle.rhs(p, d, pen, sol)
+            assert np.max(np.abs(b - ref)) <= 1e-13 * max(1.0, np.max(np.abs(ref))), (sol, p, d)
+
+
+def test_rhs_modes_matches_oracle(sipg, oracle, torch):
+    amps, ks, ls = [0.3, -1.2, 0.7, 2.0], [1, 3, 8, 5], [2, 7, 1, 5]
+    p, d, pen = 4, 20, 16.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("modes", sipg.Modes.make(amps, ks, ls)).cpu().numpy()
+    ref = oracle.rhs(p, d, pen, 7, oracle.modes(amps, ks, ls))
+    assert np.max(np.abs(b - ref)) <= 1e-13 * np.max(np.abs(ref))
+    op.close()
+
+
+def test_cg_matches_reference_solves(sipg, golden, torch):
+    for i, row in enumerate(golden["solve_table"]):
+        sol, p, d, pen, tol = int(row[0]), int(row[1]), int(row[2]), float(row[3]), float(row[4])
+        it_ref, l2_ref, h1_ref, mx_ref = row[5:9]
+        op = sipg.Operator(d, p, pen)
+        b = torch.from_numpy(golden["solve_rhs_%d" % i]).cuda()
+        x = torch.zeros_like(b)
+        st, res = op.cg(x, b, tol)
+        assert st == 0, (i, st)
+        assert abs(res.iterations - int(it_ref)) <= 1, (i, res.iterations, it_ref)
+        u_ref = golden["solve_u_%d" % i]
+        assert np.max(np.abs(x.cpu().numpy() - u_ref)) <= 1e-8 * np.max(np.abs(u_ref)), i
+        l2, h1, mx = op.err_norms(sol, x)
+        assert l2 == pytest.approx(l2_ref, rel=1e-6) and h1 == pytest.approx(h1_ref, rel=1e-6)
+        assert mx == pytest.approx(mx_ref, rel=1e-6)
+        op.close()
+
+
+def test_poisson16_relative_tolerance(sipg, golden, torch):
+    # 16x16, p = 4, sin-sin, pen = p^2, CG from 0 to ||r|| <= 1e-12 ||b||
+    p, d, pen, tol_abs, it_ref, l2_ref, h1_ref, mx_ref = golden["poisson16_stats"]
+    op = sipg.Operator(int(d), int(p), pen)
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-12, relative=True)
+    assert st == 0
+    assert abs(res.iterations - int(it_ref)) <= 1
+    assert res.stop == pytest.approx(tol_abs, rel=1e-12)
+    l2, h1, mx = op.err_norms("sinsin", x)
+    assert l2 == pytest.approx(l2_ref, rel=1e-4) and h1 == pytest.approx(h1_ref, rel=1e-4)
+    op.close()
+
+
+@pytest.mark.parametrize("p,d", [(2, 16), (3, 16), (4, 16), (5, 8), (6, 8)])
+def test_thesis_table_4_10_on_gpu(sipg, torch, p, d):
+    from test_oracle_golden import THESIS_T4_10
+
+    H1, L2, LI = THESIS_T4_10[(p, d)]
+    op = sipg.Operator(d, p, 100.0 * p * p)
+    b = op.rhs("E")
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-15)
+    l2, h1, mx = op.err_norms("E", x)
+    assert h1 == pytest.approx(H1, rel=1e-5) and l2 == pytest.approx(L2, rel=1e-5)
+    op.close()
+
+
+def test_cg_larger_mesh_vs_oracle_iterations(sipg, oracle, torch):
+    p, d, pen = 4, 48, 16.0
+    b_np = oracle.rhs(p, d, pen, 1)
+    it_ref, x_ref, _ = oracle.cg(p, d, pen, b_np, 1e-10, rel=True, nthreads=8)
+    op = sipg.Operator(d, p, pen)
+    b = torch.from_numpy(b_np).cuda()
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-10, relative=True)
+    assert st == 0 and abs(res.iterations - it_ref) <= 1
+    assert np.max(np.abs(x.cpu().numpy() - x_ref)) <= 1e-8 * np.max(np.abs(x_ref))
+    op.close()
+
+
+def test_cg_max_it_and_breakdown_statuses(sipg, torch):
+    op = sipg.Operator(8, 3, 9.0)
+    b = op.rhs("A")
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-30, max_it=5)
+    assert st == 3 and res.iterations == 5 and res.converged == 0
+    # a negative penalty makes the operator indefinite: CG reports breakdown
+    bad = sipg.Operator(8, 3, -50.0)
+    x2 = torch.zeros_like(b)
+    st2, res2 = bad.cg(x2, b, 1e-12, max_it=500)
+    assert st2 in (3, 4)
+    op.close()
+    bad.close()
+
+
+def test_cg_zero_rhs_returns_immediately(sipg, torch):
+    op = sipg.Operator(4, 2, 4.0)
+    b = torch.zeros(op.ndof, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-12, relative=False)
+    assert st == 0 and res.iterations == 0
+    op.close()
+
+
+def test_cg_f32(sipg, oracle, torch):
+    p, d, pen = 3, 24, 9.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("A")
+    x = torch.zeros_like(b, dtype=torch.float32)
+    st, res = op.cg(x, b.float(), 1e-5, relative=True)
+    assert st == 0
+    it_ref, x_ref, _ = oracle.cg(p, d, pen, b.cpu().numpy(), 1e-12, rel=True, nthreads=4)
+    assert np.max(np.abs(x.double().cpu().numpy() - x_ref)) <= 1e-3 * np.max(np.abs(x_ref))
+    op.close()
+
+
+def test_mixed_precision_reaches_fp64_accuracy(sipg, oracle, torch):
+    p, d, pen = 6, 32, 36.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("sinsin")
+    x64 = torch.zeros_like(b)
+    st, r64 = op.cg(x64, b, 1e-10, relative=True)
+    assert st == 0
+    xm = torch.zeros_like(b)
+    st, rm = op.solve_mixed(xm, b, inner_tol=1e-5, outer_tol=1e-10)
+    assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10
+    assert rm.outer_iterations >= 2 and rm.inner_iterations > 0
+    e64 = op.err_norms("sinsin", x64)
+    em = op.err_norms("sinsin", xm)
+    assert em[0] <= 1.05 * e64[0]
+    assert (xm - x64).abs().max().item() <= 1e-8 * x64.abs().max().item()
+    op.close()
