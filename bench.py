@@ -141,6 +141,19 @@ def cpu_apply_rate(seconds=10.0, max_reps=20):
             "sample": "%d full applies of the 1024x1024 p=4 workload (%.1f s)" % (reps, dt)}
 
 
+def reference_kernels_same_gpu(x, y, reps=20):
+    """The reference's own volume + flux_term6a + flux_term6b, compiled for sm_103a
+    from its headers (oracle/_ref/ref_kernels.cubin), timed on this GPU."""
+    import oracle_lib
+
+    if not oracle_lib.ref_gpu_available():
+        return None
+    ms = oracle_lib.ref_gpu().apply(DEGREE, DIM, PEN, x.data_ptr(), y.data_ptr(), reps)
+    return {"value": reps * NDOF / (ms * 1e-3) / 1e9, "unit": "GDoF/s", "applies": reps,
+            "source": "reference kernels (volume, flux_term6a, flux_term6b) built unchanged for sm_103a, "
+                      "launched with the reference geometry, CUDA events"}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -280,6 +293,10 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_apply_rate()
+        try:
+            line["reference_kernels_same_gpu"] = reference_kernels_same_gpu(x, y)
+        except Exception as exc:  # the baseline is optional; the product line stands
+            line["reference_kernels_same_gpu"] = {"unavailable": str(exc)}
     op.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -14,10 +14,15 @@ what the GPU computes.  This recipe:
    (the only change; written to a temporary directory under oracle/_ref/
    that is deleted after the compile);
 3. compiles oracle/ref_emul.cpp with oracle/cuda_emul.h against them with
-   g++ -O2 -ffp-contract=off into oracle/_ref/libref_emul.so.
+   g++ -O2 -ffp-contract=off into oracle/_ref/libref_emul.so;
+4. compiles the reference's FP64 kernels, unchanged, for sm_103a into
+   oracle/_ref/ref_kernels.cubin (oracle/ref_gpu_kernels.cu holds only their
+   explicit instantiations).  The cubin is device code and travels with the
+   repository to the GPU machine, where oracle/ref_gpu.cpp runs it as the
+   "reference kernels on the same GPU" baseline.
 
-The output is an x86/aarch64 host library used to generate and check the
-golden fixtures under tests/golden/; nothing in the product links it.
+The outputs are test infrastructure: libref_emul.so generates and checks the
+golden fixtures under tests/golden/; nothing in the product links either.
 Exit status 0 on success, 2 if the reference checkout is absent (skipped).
 """
 import os
@@ -69,6 +74,14 @@ def build(ref_dir=None, verbose=False):
         if verbose:
             print(" ".join(cmd))
         subprocess.check_call(cmd)
+        cubin = os.path.join(OUT_DIR, "ref_kernels.cubin")
+        cmd = [os.environ.get("NVCC", "nvcc"), "-std=c++14", "-O3", "-cubin", "-gencode",
+               "arch=compute_103a,code=sm_103a", "-w", "-I", inc, os.path.join(HERE, "ref_gpu_kernels.cu"),
+               "-o", cubin + ".tmp"]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+        os.replace(cubin + ".tmp", cubin)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     return 0

@@ -111,3 +111,53 @@ def load():
             subprocess.check_call(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"])
         _cached = Oracle(C.CDLL(LIB))
     return _cached
+
+
+REF_GPU_LIB = os.path.join(ORACLE_DIR, "_ref", "libref_gpu.so")
+REF_CUBIN = os.path.join(ORACLE_DIR, "_ref", "ref_kernels.cubin")
+
+
+class RefGpu:
+    """The reference's own CUDA kernels (oracle/ref_gpu.cpp over the cubin built
+    from the reference headers): same-GPU parity and baseline timing."""
+
+    def __init__(self):
+        L = C.CDLL(REF_GPU_LIB)
+        L.refgpu_init.argtypes = [C.c_char_p]
+        L.refgpu_apply.argtypes = [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_int,
+                                   C.POINTER(C.c_float)]
+        L.refgpu_cg.argtypes = [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_double,
+                                C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        L.refgpu_last_error.restype = C.c_char_p
+        self.L = L
+        rc = L.refgpu_init(REF_CUBIN.encode())
+        if rc:
+            raise RuntimeError("refgpu_init: " + L.refgpu_last_error().decode())
+
+    def apply(self, p, dim, pen, d_in, d_out, reps=1):
+        ms = C.c_float()
+        rc = self.L.refgpu_apply(p, dim, pen, C.c_void_p(d_in), C.c_void_p(d_out), reps, C.byref(ms))
+        if rc:
+            raise RuntimeError("refgpu_apply: " + self.L.refgpu_last_error().decode())
+        return ms.value
+
+    def cg(self, p, dim, pen, d_x, d_b, tol):
+        it, ms = C.c_int(), C.c_float()
+        rc = self.L.refgpu_cg(p, dim, pen, C.c_void_p(d_x), C.c_void_p(d_b), tol, C.byref(it), C.byref(ms))
+        if rc:
+            raise RuntimeError("refgpu_cg: " + self.L.refgpu_last_error().decode())
+        return it.value, ms.value
+
+
+def ref_gpu_available():
+    return os.path.exists(REF_GPU_LIB) and os.path.exists(REF_CUBIN)
+
+
+_ref_gpu = None
+
+
+def ref_gpu():
+    global _ref_gpu
+    if _ref_gpu is None:
+        _ref_gpu = RefGpu()
+    return _ref_gpu
