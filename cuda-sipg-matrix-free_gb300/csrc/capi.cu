@@ -265,28 +265,22 @@ const char* sipg_version(void) { return "sipg-gb300 0.1 (sm_103a)"; }
 unsigned long long sipg_launch_count(void) { return g_launches.load(); }
 
 sipg_status sipg_lgl_table(int npts, double* nodes, double* weights) {
-  if (npts < 2 || npts > SIPG_MAX_N || !nodes || !weights) {
-    set_error("sipg_lgl_table: npts must be in 2..9 and pointers non-null");
+  if (npts < 2 || npts > 64 || !nodes || !weights) {
+    set_error("sipg_lgl_table: npts must be in 2..64 and pointers non-null");
     return SIPG_ERR_INVALID;
   }
-  HostTables t;
-  build_host_tables(npts - 1, &t);
-  for (int i = 0; i < npts; ++i) {
-    nodes[i] = t.nodes[i];
-    weights[i] = t.w[i];
-  }
+  lgl_compute(npts - 1, nodes, weights);
   return SIPG_OK;
 }
 
 sipg_status sipg_dphi_table(int degree, double* D) {
-  if (degree < 1 || degree > SIPG_MAX_P || !D) {
-    set_error("sipg_dphi_table: degree must be in 1..8");
+  if (degree < 1 || degree > 63 || !D) {
+    set_error("sipg_dphi_table: degree must be in 1..63");
     return SIPG_ERR_INVALID;
   }
-  HostTables t;
-  build_host_tables(degree, &t);
-  const int n = degree + 1;
-  for (int i = 0; i < n * n; ++i) D[i] = t.D[i];
+  double x[64], w[64];
+  lgl_compute(degree, x, w);
+  dphi_compute(degree, x, D);
   return SIPG_OK;
 }
 

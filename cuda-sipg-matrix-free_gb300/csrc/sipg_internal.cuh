@@ -43,6 +43,9 @@ struct HostTables {
   double K[SIPG_MAX_N * SIPG_MAX_N];
 };
 int build_host_tables(int p, HostTables* t);  // 0 on success
+// LGL nodes/weights and the derivative matrix for any degree 1..63 (host).
+int lgl_compute(int N, double* x, double* w);
+int dphi_compute(int N, const double* x, double* D);
 
 template <typename T, int P>
 inline Tab<T, P> make_tab(const HostTables& h) {

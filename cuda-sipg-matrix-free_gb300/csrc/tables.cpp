@@ -39,12 +39,9 @@ void legendre(int N, double x, double* P, double* dP) {
 
 }  // namespace
 
-int build_host_tables(int p, HostTables* t) {
-  if (p < 1 || p > SIPG_MAX_P || !t) return -1;
-  std::memset(t, 0, sizeof(*t));
-  const int N = p, n = p + 1;
-  t->p = p;
-  double* x = t->nodes;
+int lgl_compute(int N, double* x, double* w) {
+  if (N < 1 || N > 63) return -1;
+  const int n = N + 1;
   x[0] = -1.0;
   x[N] = 1.0;
   for (int k = 1; k < N; ++k) {
@@ -67,12 +64,21 @@ int build_host_tables(int p, HostTables* t) {
     x[N - k] = m;
   }
   if (N % 2 == 0) x[N / 2] = 0.0;
-  double PN[SIPG_MAX_N];
   for (int k = 0; k < n; ++k) {
     double P, dP;
     legendre(N, x[k], &P, &dP);
-    PN[k] = P;
-    t->w[k] = 2.0 / (N * (N + 1) * P * P);
+    w[k] = 2.0 / (N * (N + 1) * P * P);
+  }
+  return 0;
+}
+
+int dphi_compute(int N, const double* x, double* D) {
+  if (N < 1 || N > 63) return -1;
+  const int n = N + 1;
+  double PN[64];
+  for (int k = 0; k < n; ++k) {
+    double dP;
+    legendre(N, x[k], &PN[k], &dP);
   }
   for (int i = 0; i < n; ++i)
     for (int k = 0; k < n; ++k) {
@@ -81,8 +87,18 @@ int build_host_tables(int p, HostTables* t) {
         v = (k == 0) ? -0.25 * N * (N + 1) : (k == N ? 0.25 * N * (N + 1) : 0.0);
       else
         v = PN[k] / (PN[i] * (x[k] - x[i]));
-      t->D[i * n + k] = v;
+      D[i * n + k] = v;
     }
+  return 0;
+}
+
+int build_host_tables(int p, HostTables* t) {
+  if (p < 1 || p > SIPG_MAX_P || !t) return -1;
+  std::memset(t, 0, sizeof(*t));
+  const int n = p + 1;
+  t->p = p;
+  lgl_compute(p, t->nodes, t->w);
+  dphi_compute(p, t->nodes, t->D);
   for (int a = 0; a < n; ++a)
     for (int b = 0; b < n; ++b) {
       double s = 0.0;

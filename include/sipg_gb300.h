@@ -84,10 +84,12 @@ typedef struct {
 
 /* ---- tables and mesh (host side, no device needed) ---- */
 
-/* LGL nodes/weights on [-1,1], npts = p+1 in 2..SIPG_MAX_DEGREE+1.
+/* LGL nodes/weights on [-1,1], npts = p+1 in 2..64 (the operator itself
+ * supports p <= SIPG_MAX_DEGREE).
  * Replaces LGL_quadrature_table<T>::LGL_quadrature_table (LGL_quadrature_table.hpp:84-146). */
 sipg_status sipg_lgl_table(int npts, double* nodes, double* weights);
-/* D[mode*(p+1)+node]: derivative of Lagrange basis `mode` at LGL node `node`.
+/* D[mode*(p+1)+node]: derivative of Lagrange basis `mode` at LGL node `node`,
+ * degree 1..63.
  * Replaces sem_function<T>::d_phi / DbaseVALUES (sem_function.hpp:86-110, device_const.hpp:115-127). */
 sipg_status sipg_dphi_table(int degree, double* D);
 /* Element corner coordinates x[c*noe+e], y[c*noe+e], c=0..3.
@@ -96,11 +98,12 @@ sipg_status sipg_square_mesh_coords(int dim, double* x, double* y);
 
 /* ---- operator lifetime ---- */
 
-/* Creates the operator on the current CUDA device: uploads the degree-p tables
- * once per device and picks the tile shape.  Replaces the setup in the
- * sipg_sem_2d<T> constructor (sipg_sem_2d.hpp:96-113) and load_Dphi_table /
- * load_lgl_quadrature_table (device_const.hpp:70-174), without their
- * process-global __constant__ state: operators of different degree coexist. */
+/* Creates the operator on the current CUDA device: builds the degree-p tables
+ * (passed to every kernel launch as parameters) and picks the tile shape.
+ * Replaces the setup in the sipg_sem_2d<T> constructor (sipg_sem_2d.hpp:96-113)
+ * and load_Dphi_table / load_lgl_quadrature_table (device_const.hpp:70-174),
+ * without their process-global __constant__ state: operators of different
+ * degree coexist in one process. */
 sipg_status sipg_op_create(int dim, int degree, double pen, sipg_op** op);
 sipg_status sipg_op_destroy(sipg_op* op);
 /* Bytes of device memory one FP64 CG solve on this op keeps resident. */
@@ -136,6 +139,21 @@ sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, in
  * and the outer norms stay FP64 on the device.  No reference counterpart. */
 sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
                              sipg_mixed_result* res, void* stream);
+
+/* The vector steps of the reference's CG, for callers that iterate around
+ * their own operator (an abs_mvm implementation).  sipg_dot_* is
+ * synchronous and deterministic; the others are stream-ordered.
+ *   sipg_dot:      *result = x.y       (replaces cublas_dot, cublas_wrapper.hpp:62-84)
+ *   sipg_cg_step:  x += a p, r -= a Ap (replaces alpha_kernel, conjugate_gradient_kernels.hpp:5-23)
+ *   sipg_xpby:     y = x + b y         (replaces beta_kernel, conjugate_gradient_kernels.hpp:26-38) */
+sipg_status sipg_dot_f64(size_t n, const double* d_x, const double* d_y, double* result, void* stream);
+sipg_status sipg_dot_f32(size_t n, const float* d_x, const float* d_y, float* result, void* stream);
+sipg_status sipg_cg_step_f64(size_t n, double alpha, double* d_x, const double* d_p, double* d_r, const double* d_Ap,
+                             void* stream);
+sipg_status sipg_cg_step_f32(size_t n, float alpha, float* d_x, const float* d_p, float* d_r, const float* d_Ap,
+                             void* stream);
+sipg_status sipg_xpby_f64(size_t n, const double* d_x, double beta, double* d_y, void* stream);
+sipg_status sipg_xpby_f32(size_t n, const float* d_x, float beta, float* d_y, void* stream);
 
 /* ---- either side of the solve ---- */
 
