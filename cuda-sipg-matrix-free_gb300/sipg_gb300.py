@@ -80,6 +80,8 @@ _SIGS = {
     "sipg_version": (C.c_char_p, []),
     "sipg_launch_count": (C.c_ulonglong, []),
     "sipg_probe_fma_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "sipg_dot_f64": (C.c_int, [C.c_size_t, _VP, _VP, C.POINTER(C.c_double), _VP]),
+    "sipg_dot_f64_noalloc": (C.c_int, [C.c_size_t, _VP, _VP, C.POINTER(C.c_double), _VP]),
 }
 
 

@@ -154,6 +154,18 @@ sipg_status sipg_cg_step_f32(size_t n, float alpha, float* d_x, const float* d_p
                              void* stream);
 sipg_status sipg_xpby_f64(size_t n, const double* d_x, double beta, double* d_y, void* stream);
 sipg_status sipg_xpby_f32(size_t n, const float* d_x, float beta, float* d_y, void* stream);
+/* *result = x.y like sipg_dot_f64, but without allocating any device memory;
+ * no counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * code whose device memory belongs to another allocator that reserved the pool
+ * up front, or that must not risk an allocation's implicit synchronisation or
+ * out-of-memory failure mid-sequence.  Its scratch is a fixed 64 KB device
+ * array in the library (held by every GPU that loads it until exit), so
+ * n <= 16,777,216; larger n returns SIPG_ERR_INVALID.  The first call on each
+ * device looks up the array's device address: make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (concurrent streams or threads) race and must be serialised by the caller.
+ * Synchronous; deterministic. */
+sipg_status sipg_dot_f64_noalloc(size_t n, const double* d_x, const double* d_y, double* result, void* stream);
 
 /* ---- either side of the solve ---- */
 
