@@ -1,0 +1,72 @@
+"""The C++ host API (cuda-sipg-matrix-free_gb300/host/: abs_mvm, mode_vector,
+square_mesh, sipg_sem_2d, conjugate_gradient) driven like the reference's own
+validation drivers, compiled on this machine and checked against the oracle:
+iteration counts within max(1, 1 %) of the oracle's CG (the reference's
+algorithm), error norms to 1e-6 relative, the thesis table where it applies."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "cuda-sipg-matrix-free_gb300")
+
+
+@pytest.fixture(scope="module")
+def driver_output(sipg, tmp_path_factory):
+    sipg.lib()  # built
+    exe = str(tmp_path_factory.mktemp("cpp") / "host_api_driver")
+    subprocess.check_call(["nvcc", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I",
+                           os.path.join(PKG, "host"), os.path.join(ROOT, "tests", "cpp", "host_api_driver.cpp"),
+                           "-L", os.path.join(PKG, "lib"), "-lsipg_gb300", "-Xlinker",
+                           "-rpath=" + os.path.join(PKG, "lib"), "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    return [json.loads(line) for line in out.stdout.splitlines() if line.startswith("{")]
+
+
+def _close_iterations(it, it_ref):
+    return abs(it - it_ref) <= max(1, int(0.01 * it_ref))
+
+
+def test_p_and_h_sweeps_match_oracle(driver_output, oracle):
+    rows = [r for r in driver_output if r["case"] in ("p", "h")]
+    assert len(rows) == 8 + 9
+    for r in rows:
+        p, d, pen, tol = r["p"], r["dim"], r["pen"], r["tol"]
+        b = oracle.rhs(p, d, pen, 5)
+        it, x, _ = oracle.cg(p, d, pen, b, tol, nthreads=8)
+        l2, h1, mx = oracle.err_norms(p, d, 5, x)
+        assert _close_iterations(r["it"], it), (r, it)
+        assert r["L2"] == pytest.approx(l2, rel=1e-6), (r, l2)
+        assert r["H1"] == pytest.approx(h1, rel=1e-6), (r, h1)
+
+
+def test_thesis_rows_through_host_api(driver_output):
+    from test_oracle_golden import THESIS_T4_10
+
+    seen = 0
+    for r in driver_output:
+        key = (r["p"], r["dim"])
+        if r["case"] == "h" and key in THESIS_T4_10:
+            H1, L2, _ = THESIS_T4_10[key]
+            assert r["H1"] == pytest.approx(H1, rel=1e-5) and r["L2"] == pytest.approx(L2, rel=1e-5)
+            seen += 1
+    assert seen >= 6
+
+
+def test_device_problem_and_fp32_and_generic_cg(driver_output):
+    dev = next(r for r in driver_output if r["case"] == "device")
+    from test_oracle_golden import THESIS_T4_10
+
+    H1, L2, _ = THESIS_T4_10[(4, 16)]
+    assert dev["H1"] == pytest.approx(H1, rel=1e-5) and dev["L2"] == pytest.approx(L2, rel=1e-5)
+    f32 = next(r for r in driver_output if r["case"] == "f32")
+    assert np.isfinite(f32["L2"]) and f32["it"] > 0
+    gen = next(r for r in driver_output if r["case"] == "generic")
+    assert abs(gen["it_generic"] - gen["it_fused"]) <= 1
+    assert gen["rel_diff"] <= 1e-9
