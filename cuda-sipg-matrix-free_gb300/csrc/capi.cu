@@ -141,7 +141,8 @@ static sipg_status ws_get(sipg_op* op, sipg_cg_workspace** out) {
 // Iterations per graph launch: small systems are launch-bound, so batch more.
 static int graph_iters(long long ndof) { return ndof <= (1LL << 20) ? 32 : 8; }
 
-// Capture K CG iterations (apply + update, direction buffers alternating).
+// Capture K CG iterations (apply + update; the direction buffers alternate by
+// the parity kept in the device state, so a chunk may stop at any iteration).
 template <typename T>
 static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, int K) {
   if (w->exec && w->exec_x == x && w->exec_k == K) return SIPG_OK;
@@ -161,8 +162,8 @@ static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, i
   for (int k = 0; k < K && err == cudaSuccess; ++k) {
     ApplyArgs<T> a{};
     a.in = (const T*)w->r;
-    a.pold = (const T*)w->p[k & 1];
-    a.pnew = (T*)w->p[(k + 1) & 1];
+    a.pbuf0 = (T*)w->p[0];
+    a.pbuf1 = (T*)w->p[1];
     a.out = (T*)w->Ap;
     a.b = nullptr;
     a.dim = op->dim;
@@ -171,8 +172,8 @@ static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, i
     a.red = w->red;
     err = launch_apply<T>(op, APPLY_CG, a, w->cap);
     if (err != cudaSuccess) break;
-    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[(k + 1) & 1], (T*)w->r, (const T*)w->Ap, w->n,
-                                                   (CgState<T>*)w->st, w->red);
+    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[1], (T*)w->r,
+                                                   (const T*)w->Ap, w->n, (CgState<T>*)w->st, w->red);
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(w->cap, &g);
@@ -254,6 +255,34 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   }
   return conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED;
 }
+
+namespace sipg {
+
+sipg_status cg_f32_prepare(sipg_op* op, float* x, CgF32View* v) {
+  sipg_cg_workspace* w = nullptr;
+  sipg_status st = ws_get<float>(op, &w);
+  if (st != SIPG_OK) return st;
+  st = capture_iterations<float>(op, w, x, graph_iters(op->ndof));
+  if (st != SIPG_OK) return st;
+  v->r = (float*)w->r;
+  v->st = (CgState<float>*)w->st;
+  return SIPG_OK;
+}
+
+sipg_status cg_f32_launch_chunk(sipg_op* op, cudaStream_t s, CgState<float>* host_state) {
+  sipg_cg_workspace* w = op->ws32;
+  if (!w || !w->exec) {
+    set_error("cg_f32_launch_chunk: no FP32 iteration graph");
+    return SIPG_ERR_INVALID;
+  }
+  SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
+  count_launch(2ULL * w->exec_k);
+  SIPG_CUDA_TRY(cudaMemcpyAsync(host_state, w->st, sizeof(CgState<float>), cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return SIPG_OK;
+}
+
+}  // namespace sipg
 
 // ---------------------------------------------------------------------------
 // C ABI

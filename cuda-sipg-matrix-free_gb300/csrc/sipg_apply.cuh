@@ -129,14 +129,18 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
 
   bool first = true;
   T beta = T(0);
+  int par = 0;
   if (MODE == APPLY_CG) {
     first = a.st->first != 0;
     beta = a.st->beta;
+    par = a.st->parity;
   }
+  const T* __restrict__ pold = par ? a.pbuf1 : a.pbuf0;
+  T* __restrict__ pnew = par ? a.pbuf0 : a.pbuf1;
   // value k of element ee as the operator sees it (CG: p = r + beta p_old)
   auto ld = [&](int k, size_t ee) -> T {
     const T r = __ldg(a.in + (size_t)k * noe + ee);
-    if (MODE == APPLY_CG) return first ? r : fma(beta, __ldg(a.pold + (size_t)k * noe + ee), r);
+    if (MODE == APPLY_CG) return first ? r : fma(beta, __ldg(pold + (size_t)k * noe + ee), r);
     return r;
   };
   auto U = [&](int i1, int i2) -> T& { return us[(i1 * N1 + i2) * TE + t]; };
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
   for (int k = 0; k < NN; ++k) {
     const T v = act ? ld(k, e) : T(0);
     us[k * TE + t] = v;
-    if (MODE == APPLY_CG && act) a.pnew[(size_t)k * noe + e] = v;
+    if (MODE == APPLY_CG && act) pnew[(size_t)k * noe + e] = v;
   }
   __syncthreads();
 
@@ -434,6 +438,7 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
         const T alpha = st->rr / total;
         st->pAp = total;
         st->alpha = alpha;
+        st->parity = 1 - par;  // every block read the parity before arriving here
         if (!(total > T(0)) || !isfinite(alpha)) {
           st->status = (int)SIPG_ERR_BREAKDOWN;
           st->done = 1;

@@ -19,12 +19,14 @@ namespace sipg {
 constexpr int kVecThreads = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, const T* __restrict__ p,
-                                                           T* __restrict__ r, const T* __restrict__ Ap, size_t n,
-                                                           CgState<T>* st, ReduceScratch red) {
+__global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, const T* __restrict__ pb0,
+                                                           const T* __restrict__ pb1, T* __restrict__ r,
+                                                           const T* __restrict__ Ap, size_t n, CgState<T>* st,
+                                                           ReduceScratch red) {
   __shared__ T sh[32];
   if (*(volatile int*)&st->done) return;
   const T alpha = st->alpha;
+  const T* __restrict__ p = st->parity ? pb1 : pb0;  // the direction the apply just wrote
   T acc = T(0);
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -36,12 +38,21 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, co
   const T bt = block_sum<T, kVecThreads>(acc, sh);
   T total;
   if (grid_sum_last<T, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
-    const T rr_old = st->rr;
-    st->beta = total / rr_old;
-    st->rr = total;
+    const T rn = sqrt(total);
     st->it += 1;
     st->first = 0;
-    st->done = !(sqrt(total) > st->stop && st->it < st->max_it);
+    if (st->delta > T(0) && rn < st->delta * st->rmax) {
+      // reliable update due: keep rr (the previous r.r, for beta after the
+      // correction) and stop; the host replaces r by the FP64 residual
+      st->need_update = 1;
+      st->done = 1;
+    } else {
+      const T rr_old = st->rr;
+      st->beta = total / rr_old;
+      st->rr = total;
+      st->rmax = fmax(st->rmax, rn);
+      st->done = !(rn > st->stop && st->it < st->max_it);
+    }
     if (!isfinite(total)) {
       st->status = (int)SIPG_ERR_BREAKDOWN;
       st->done = 1;
@@ -67,6 +78,10 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_init(const T* __restrict__ b
     st->done = 0;
     st->first = 1;
     st->status = (int)SIPG_OK;
+    st->parity = 0;
+    st->need_update = 0;
+    st->delta = T(0);
+    st->rmax = T(0);
     st->alpha = st->beta = st->pAp = T(0);
   }
 }

@@ -71,11 +71,15 @@ struct CgState {
   T beta;    // rr_new / rr_old
   T stop;    // absolute stop threshold on sqrt(r.r)
   T bb;      // b.b (for relative tolerances)
+  T rmax;    // reliable updates: largest sqrt(rr) since the last FP64 correction
+  T delta;   // reliable updates: correct when sqrt(rr) < delta * rmax (0: never)
   int it;    // iterations done
   int max_it;
-  int done;  // 1 once sqrt(rr) <= stop, it == max_it, or breakdown
+  int done;  // 1 once sqrt(rr) <= stop, it == max_it, breakdown, or an update is due
   int first; // 1 before the first direction p = r is formed
   int status;  // SIPG_OK / SIPG_ERR_BREAKDOWN
+  int parity;  // which direction buffer holds the current p
+  int need_update;  // reliable updates: an FP64 correction is due
   int pad;
 };
 
@@ -91,15 +95,16 @@ struct ReduceScratch {
 enum ApplyMode : int {
   APPLY_PREPARE = -1,  // set kernel attributes only (before a graph capture)
   APPLY_PLAIN = 0,  // y = A u
-  APPLY_CG = 1,     // u = r + beta p_old (u = r on the first iteration); p_new = u; y = A u; pAp -> alpha
+  APPLY_CG = 1,     // u = r + beta p_old (u = r on the first iteration); p_new = u; y = A u; pAp -> alpha;
+                    // the parity of the direction buffers flips
   APPLY_RESID = 2   // y = b - A u; r.r -> rr, stop/done set
 };
 
 template <typename T>
 struct ApplyArgs {
   const T* in;     // u (PLAIN, RESID) or r (CG)
-  const T* pold;   // CG: previous direction
-  T* pnew;         // CG: new direction (written)
+  T* pbuf0;        // CG: the two direction buffers; CgState::parity says which
+  T* pbuf1;        //     holds the previous direction, the other gets the new one
   T* out;          // y
   const T* b;      // RESID: right-hand side
   int dim;
@@ -130,6 +135,14 @@ inline int reduce_capacity(int dim) {
   return a > 152 * 8 ? a : 152 * 8;
 }
 
+// FP32 CG pieces (capi.cu) used by the mixed-precision solver: the op's FP32
+// workspace with the iteration graph captured for iterate x, and one graph
+// chunk of iterations followed by a read of the device state.
+struct CgF32View {
+  float* r;
+  CgState<float>* st;
+};
+
 // ---------------------------------------------------------------------------
 // Error plumbing and launch accounting.
 // ---------------------------------------------------------------------------
@@ -152,6 +165,11 @@ inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std
 // The operator object behind the opaque sipg_op handle.
 // ---------------------------------------------------------------------------
 struct sipg_cg_workspace;
+
+namespace sipg {
+sipg_status cg_f32_prepare(sipg_op* op, float* x, CgF32View* v);
+sipg_status cg_f32_launch_chunk(sipg_op* op, cudaStream_t s, CgState<float>* host_state);
+}  // namespace sipg
 
 struct sipg_op {
   int dim = 0, p = 0;

@@ -223,8 +223,10 @@ class Operator:
             _check(st, "cg")
         return st, res
 
-    def solve_mixed(self, x, b, inner_tol=1e-5, outer_tol=1e-10, max_outer=50, max_inner=0, stream=None):
-        """FP32-inner / FP64-outer defect correction.  Returns (status, MixedResult)."""
+    def solve_mixed(self, x, b, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, stream=None):
+        """FP32 CG inside FP64 defect correction with reliable updates: an FP64
+        correction whenever the FP32 residual fell by inner_tol since the last
+        one; stops at ||b - Ax|| <= outer_tol ||b|| (FP64).  Returns (status, MixedResult)."""
         import torch
 
         self._vec(x, torch.float64)

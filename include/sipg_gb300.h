@@ -68,10 +68,10 @@ typedef struct {
 } sipg_cg_result;
 
 typedef struct {
-  double inner_tol;    /* inner FP32 CG relative tolerance (1e-5) */
-  double outer_tol;    /* outer FP64 relative residual ||b-Ax||/||b|| (1e-10) */
-  int max_outer;       /* outer defect-correction steps cap (50) */
-  int max_inner;       /* per inner solve iteration cap (0 = DoF) */
+  double inner_tol;    /* FP64 correction once the FP32 residual fell by this factor since the last one (0.1) */
+  double outer_tol;    /* stop at the FP64 relative residual ||b-Ax||/||b|| <= outer_tol (1e-10) */
+  int max_outer;       /* cap on FP64 corrections (200) */
+  int max_inner;       /* cap on FP32 iterations in total (0 = DoF) */
 } sipg_mixed_opts;
 
 typedef struct {
@@ -134,9 +134,12 @@ sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol,
 sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
                         sipg_cg_result* res, void* stream);
 
-/* Mixed precision: FP32 operator and inner CG (values and accumulation)
- * inside FP64 defect correction; the outer residual b - A x, the update of x
- * and the outer norms stay FP64 on the device.  No reference counterpart. */
+/* Mixed precision: FP32 operator and CG (values and accumulation) inside FP64
+ * defect correction with reliable updates -- whenever the FP32 residual has
+ * fallen by inner_tol, x += e in FP64, r = b - A x in FP64, and the FP32 CG
+ * continues with its search direction.  The residual b - A x, the update of x
+ * and the outer norms stay FP64 on the device.  `opts` may be NULL (defaults
+ * in sipg_mixed_opts).  No reference counterpart. */
 sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
                              sipg_mixed_result* res, void* stream);
 

@@ -145,9 +145,11 @@ def test_mixed_precision_reaches_fp64_accuracy(sipg, oracle, torch):
     st, r64 = op.cg(x64, b, 1e-10, relative=True)
     assert st == 0
     xm = torch.zeros_like(b)
-    st, rm = op.solve_mixed(xm, b, inner_tol=1e-5, outer_tol=1e-10)
+    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10)
     assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10
     assert rm.outer_iterations >= 2 and rm.inner_iterations > 0
+    # reliable updates keep the Krylov space: about as many FP32 iterations as FP64 ones
+    assert rm.inner_iterations <= 2 * r64.iterations
     e64 = op.err_norms("sinsin", x64)
     em = op.err_norms("sinsin", xm)
     assert em[0] <= 1.05 * e64[0]
