@@ -1,0 +1,15 @@
+// Instantiates the fused apply (single-operator and batched launches) for
+// double, degree 2: one translation unit per precision and degree, so the
+// build compiles them in parallel.
+#include "sipg_apply.cuh"
+namespace sipg {
+cudaError_t launch_apply_f64_p2(const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
+                                  cudaStream_t s) {
+  return launch_apply_p<double, 2>(cfg, mode, a, h, s);
+}
+cudaError_t launch_apply_batched_f64_p2(const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,
+                                          const int* tile_start, int ninst, int total_tiles, const HostTables& h,
+                                          cudaStream_t s) {
+  return launch_apply_batched_p<double, 2>(cfg, mode, insts, tile_start, ninst, total_tiles, h, s);
+}
+}  // namespace sipg

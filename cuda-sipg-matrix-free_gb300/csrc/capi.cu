@@ -14,18 +14,85 @@ std::atomic<unsigned long long> g_launches{0};
 static thread_local std::string t_last_error;
 void set_error(const std::string& msg) { t_last_error = msg; }
 
-cudaError_t launch_apply_f64_lo(int, const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
-cudaError_t launch_apply_f64_hi(int, const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
-cudaError_t launch_apply_f32_lo(int, const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
-cudaError_t launch_apply_f32_hi(int, const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p1(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p1(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p2(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p2(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p3(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p3(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p4(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p4(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p5(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p5(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p6(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p6(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p7(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p7(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f64_p8(const TileCfg&, int, const ApplyArgs<double>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f64_p8(const TileCfg&, int, const ApplyArgs<double>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p1(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p1(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p2(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p2(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p3(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p3(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p4(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p4(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p5(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p5(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p6(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p6(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p7(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p7(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+cudaError_t launch_apply_f32_p8(const TileCfg&, int, const ApplyArgs<float>&, const HostTables&, cudaStream_t);
+cudaError_t launch_apply_batched_f32_p8(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
+                                          const HostTables&, cudaStream_t);
+
+#define SIPG_DISPATCH_P(FN, P, ...) \
+  switch (P) {                      \
+    case 1: return FN##_p1(__VA_ARGS__); \
+    case 2: return FN##_p2(__VA_ARGS__); \
+    case 3: return FN##_p3(__VA_ARGS__); \
+    case 4: return FN##_p4(__VA_ARGS__); \
+    case 5: return FN##_p5(__VA_ARGS__); \
+    case 6: return FN##_p6(__VA_ARGS__); \
+    case 7: return FN##_p7(__VA_ARGS__); \
+    case 8: return FN##_p8(__VA_ARGS__); \
+  }                                 \
+  return cudaErrorInvalidValue;
 
 cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
                              cudaStream_t s) {
-  return p <= 4 ? launch_apply_f64_lo(p, cfg, mode, a, h, s) : launch_apply_f64_hi(p, cfg, mode, a, h, s);
+  SIPG_DISPATCH_P(launch_apply_f64, p, cfg, mode, a, h, s)
 }
 cudaError_t launch_apply_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const HostTables& h,
                              cudaStream_t s) {
-  return p <= 4 ? launch_apply_f32_lo(p, cfg, mode, a, h, s) : launch_apply_f32_hi(p, cfg, mode, a, h, s);
+  SIPG_DISPATCH_P(launch_apply_f32, p, cfg, mode, a, h, s)
+}
+cudaError_t launch_apply_batched_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,
+                                     const int* tile_start, int ninst, int total_tiles, const HostTables& h,
+                                     cudaStream_t s) {
+  SIPG_DISPATCH_P(launch_apply_batched_f64, p, cfg, mode, insts, tile_start, ninst, total_tiles, h, s)
+}
+cudaError_t launch_apply_batched_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>* insts,
+                                     const int* tile_start, int ninst, int total_tiles, const HostTables& h,
+                                     cudaStream_t s) {
+  SIPG_DISPATCH_P(launch_apply_batched_f32, p, cfg, mode, insts, tile_start, ninst, total_tiles, h, s)
 }
 
 template <typename T>

@@ -22,6 +22,9 @@
 using namespace sipg;
 
 namespace sipg {
+// FP32 iterations after which an FP64 correction is forced
+constexpr int kCorrectEvery = 1000;
+
 cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
                              cudaStream_t s);
 
@@ -56,7 +59,9 @@ __global__ void __launch_bounds__(kVecThreads)
     st->rmax = sqrtf(total);
     st->delta = delta;
     st->stop = 0.f;  // the FP32 loop stops only for corrections, breakdown or max_it
-    st->max_it = max_it;
+    // a correction is forced after max_it more FP32 iterations even if the
+    // residual stagnates above delta * rmax (FP32 rounding floor)
+    st->max_it = st->it + max_it;
     st->need_update = 0;
     st->done = 0;
   }
@@ -178,7 +183,7 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     // the FP32 residual and CG state; after the first correction the search
     // direction is kept
     k_mixed_restart<<<vb, kVecThreads, 0, s>>>(mw.r64, v32.r, mw.e32, n, v32.st, mw.red32, corrections == 0 ? 1 : 0,
-                                               (float)o.inner_tol, (int)std::min<long long>(max_inner, 2000000000LL));
+                                               (float)o.inner_tol, kCorrectEvery);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
     const int it_before = (corrections == 0) ? 0 : mw.st32_host->it;

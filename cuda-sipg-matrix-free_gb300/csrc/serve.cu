@@ -1,0 +1,858 @@
+// serve.cu -- a continuous-batching solve server on one GPU (no counterpart in
+// the reference).
+//
+// Requests (mesh size, degree, penalty, right-hand side, relative tolerance,
+// precision) wait in a FIFO queue.  Each sipg_server_step():
+//   1. admits queued requests while their device footprint fits the budget and
+//      a state slot is free (a request larger than the whole budget is
+//      rejected); an admitted request gets its vectors from the stream-ordered
+//      pool allocator, its right-hand side built on the device, x = 0, and a
+//      slot in the device state arrays;
+//   2. runs K CG iterations of every active request together: per degree one
+//      batched apply launch (k_sipg_apply_batched, the requests' tiles
+//      concatenated) for the mixed requests (FP32) and one for the FP64 ones,
+//      then one batched update per precision -- requests admitted while others
+//      are mid-solve simply join the next launches;
+//   3. reads all active states with one copy; mixed requests due for a
+//      reliable update get x += e and their FP64 residual (batched FP64
+//      applies), then retire or continue; FP64 requests that converged retire.
+// Retired requests free their vectors at once (their results stay until the
+// caller releases them), so memory and slots turn over while others run.
+// Meshes/operators are cached and shared; all solver state stays on the device.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <deque>
+#include <map>
+#include <new>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "sipg_cg.cuh"
+
+using namespace sipg;
+
+namespace sipg {
+sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, cudaStream_t s);
+
+struct ServeMixed {  // one mixed request's operands for the vector kernels
+  double* x64;
+  const double* b64;
+  double* r64;
+  float* e32;
+  float* r32;
+  CgState<float>* st32;
+  CgState<double>* st64;
+  ReduceScratch red32;
+  ReduceScratch red64;
+  size_t n;
+  int first;
+  float delta;
+  double tol;  // relative FP64 tolerance
+  int nblk;    // blocks this request uses (see VecInst)
+  int pad;
+};
+
+// FP64 request start: r = b (x = 0), stop = tol ||b||, p = r on the first iteration
+__global__ void __launch_bounds__(kVecThreads) k_serve_init_f64(const VecInst<double>* __restrict__ insts,
+                                                                const double* __restrict__ tols,
+                                                                const double* const* __restrict__ bs) {
+  __shared__ double sh[32];
+  const VecInst<double> v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  const double* __restrict__ b = bs[blockIdx.y];
+  double acc = 0.0;
+  const size_t stride = (size_t)v.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += stride) {
+    const double bi = b[i];
+    v.r[i] = bi;
+    v.x[i] = 0.0;
+    acc = fma(bi, bi, acc);
+  }
+  const double bt = block_sum<double, kVecThreads>(acc, sh);
+  double total;
+  if (grid_sum_last<double, kVecThreads>(bt, v.red, blockIdx.x, v.nblk, sh, &total) && threadIdx.x == 0) {
+    CgState<double>* st = v.st;
+    st->bb = total;
+    st->rr = total;
+    st->stop = tols[blockIdx.y] * sqrt(total);
+    st->max_it = (int)(v.n < 2000000000 ? v.n : 2000000000);  // as the reference: at most DoF iterations
+    st->it = 0;
+    st->first = 1;
+    st->parity = 0;
+    st->status = (int)SIPG_OK;
+    st->need_update = 0;
+    st->delta = 0.0;
+    st->rmax = 0.0;
+    st->done = !(sqrt(total) > st->stop);
+  }
+}
+
+// mixed request start: ||b||, r64 = b (x = 0), then the FP32 state (first run)
+__global__ void __launch_bounds__(kVecThreads) k_serve_init_mixed(const ServeMixed* __restrict__ insts) {
+  __shared__ float shf[32];
+  const ServeMixed m = insts[blockIdx.y];
+  if ((int)blockIdx.x >= m.nblk) return;
+  double acc = 0.0;
+  float accf = 0.f;
+  const size_t stride = (size_t)m.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+    const double bi = m.b64[i];
+    m.x64[i] = 0.0;
+    m.r64[i] = bi;
+    const float v = (float)bi;
+    m.r32[i] = v;
+    m.e32[i] = 0.f;
+    acc = fma(bi, bi, acc);
+    accf = fmaf(v, v, accf);
+  }
+  // two reductions through the two scratch areas
+  __shared__ double shd[32];
+  const double bt = block_sum<double, kVecThreads>(acc, shd);
+  double total;
+  if (grid_sum_last<double, kVecThreads>(bt, m.red64, blockIdx.x, m.nblk, shd, &total) && threadIdx.x == 0) {
+    m.st64->bb = total;
+    m.st64->rr = total;
+  }
+  const float btf = block_sum<float, kVecThreads>(accf, shf);
+  float totalf;
+  if (grid_sum_last<float, kVecThreads>(btf, m.red32, blockIdx.x, m.nblk, shf, &totalf) && threadIdx.x == 0) {
+    CgState<float>* st = m.st32;
+    st->first = 1;
+    st->it = 0;
+    st->parity = 0;
+    st->beta = 0.f;
+    st->status = (int)SIPG_OK;
+    st->rr = totalf;
+    st->rmax = sqrtf(totalf);
+    st->delta = m.delta;
+    st->stop = 0.f;
+    st->max_it = 1000;  // a correction is forced after 1000 FP32 iterations
+    st->need_update = 0;
+    st->done = (totalf == 0.f) ? 1 : 0;
+  }
+}
+
+// x64 += e32 for every listed mixed request
+__global__ void __launch_bounds__(kVecThreads) k_serve_fold(const ServeMixed* __restrict__ insts) {
+  const ServeMixed m = insts[blockIdx.y];
+  if ((int)blockIdx.x >= m.nblk) return;
+  const size_t stride = (size_t)m.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
+    m.x64[i] += (double)m.e32[i];
+}
+
+// after a correction: r32 = (float) r64, e = 0, beta = r_new.r_new / r_old.r_old,
+// and the FP32 iterations continue with the kept search direction
+__global__ void __launch_bounds__(kVecThreads) k_serve_restart(const ServeMixed* __restrict__ insts) {
+  __shared__ float sh[32];
+  const ServeMixed m = insts[blockIdx.y];
+  if ((int)blockIdx.x >= m.nblk) return;
+  float acc = 0.f;
+  const size_t stride = (size_t)m.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
+    const float v = (float)m.r64[i];
+    m.r32[i] = v;
+    m.e32[i] = 0.f;
+    acc = fmaf(v, v, acc);
+  }
+  const float bt = block_sum<float, kVecThreads>(acc, sh);
+  float total;
+  if (grid_sum_last<float, kVecThreads>(bt, m.red32, blockIdx.x, m.nblk, sh, &total) && threadIdx.x == 0) {
+    CgState<float>* st = m.st32;
+    st->beta = total / st->rr;
+    st->first = 0;
+    st->rr = total;
+    st->rmax = sqrtf(total);
+    st->max_it = st->it + 1000;
+    st->need_update = 0;
+    st->done = 0;
+  }
+}
+
+}  // namespace sipg
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  unsigned long long id = 0;
+  sipg_request req{};
+  sipg_op* op = nullptr;
+  size_t n = 0;
+  size_t footprint = 0;
+  int slot = -1;
+  // device memory: the solution (kept until release) and one pool
+  // allocation carved into the solver vectors (freed at retirement)
+  char* mem = nullptr;
+  double* x64 = nullptr;
+  size_t x_bytes = 0;
+  double* b64 = nullptr;
+  double* r64 = nullptr;     // mixed: FP64 residual; FP64: r
+  float* e32 = nullptr;
+  float* r32 = nullptr;
+  float* p32[2] = {nullptr, nullptr};
+  float* Ap32 = nullptr;
+  double* p64[2] = {nullptr, nullptr};
+  double* Ap64 = nullptr;
+  ReduceScratch red32, red64;
+  int corrections = 0;
+  int started = 0;
+  Clock::time_point t_submit, t_admit, t_done;
+  sipg_request_result result{};
+  int state = 0;  // 0 queued, 1 active, 2 done
+};
+
+struct Slots {
+  CgState<float>* d32 = nullptr;
+  CgState<double>* d64 = nullptr;
+  CgState<float>* h32 = nullptr;
+  CgState<double>* h64 = nullptr;
+};
+
+}  // namespace
+
+struct sipg_server {
+  sipg_server_opts opts{};
+  cudaStream_t s = nullptr;
+  Slots slots;
+  std::vector<int> free_slots;
+  std::deque<Request*> queue;
+  std::vector<Request*> active;
+  std::unordered_map<unsigned long long, Request*> all;
+  std::map<std::tuple<int, int, double>, sipg_op*> ops;
+  unsigned long long next_id = 1;
+  size_t used = 0;
+  // pinned staging and device descriptor arrays (capacity max_active; tile
+  // starts max_active + 16): FP32 CG applies, FP64 CG applies, FP64 residuals
+  ApplyArgs<float>* h_a32 = nullptr;
+  ApplyArgs<float>* d_a32 = nullptr;
+  ApplyArgs<double>* h_a64 = nullptr;
+  ApplyArgs<double>* d_a64 = nullptr;
+  ApplyArgs<double>* h_r64 = nullptr;
+  ApplyArgs<double>* d_r64 = nullptr;
+  int* h_t32 = nullptr;
+  int* d_t32 = nullptr;
+  int* h_t64 = nullptr;
+  int* d_t64 = nullptr;
+  int* h_tr = nullptr;
+  int* d_tr = nullptr;
+  VecInst<float>* h_v32 = nullptr;
+  VecInst<float>* d_v32 = nullptr;
+  VecInst<double>* h_v64 = nullptr;
+  VecInst<double>* d_v64 = nullptr;
+  ServeMixed* h_m = nullptr;
+  ServeMixed* d_m = nullptr;
+  double* h_tol = nullptr;
+  double* d_tol = nullptr;
+  const double** h_bptr = nullptr;
+  const double** d_bptr = nullptr;
+  unsigned long long completed = 0, rejected = 0;
+};
+
+namespace {
+
+// grid width of a batched vector launch: the widest listed instance
+int vec_bpi(size_t nmax, int) { return inst_blocks(nmax); }
+
+size_t footprint_of(int dim, int p, int precision) {
+  const size_t n = (size_t)dim * dim * (p + 1) * (p + 1);
+  const size_t red = 2 * (sizeof(double) * (size_t)reduce_capacity(dim) + 256);
+  if (precision == SIPG_F64) return n * (8 * 2 + 8 * 4) + red + 4096;  // x, b, r, p0, p1, Ap
+  return n * (8 * 3 + 4 * 5) + red + 4096;                             // x, b, r64 + e, r, p0, p1, Ap
+}
+
+sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
+  const auto key = std::make_tuple(dim, p, pen);
+  auto it = sv->ops.find(key);
+  if (it != sv->ops.end()) {
+    *out = it->second;
+    return SIPG_OK;
+  }
+  sipg_op* op = nullptr;
+  sipg_status st = sipg_op_create(dim, p, pen, &op);
+  if (st != SIPG_OK) return st;
+  sv->ops[key] = op;
+  *out = op;
+  return SIPG_OK;
+}
+
+// carve one pool allocation into the request's vectors
+sipg_status admit(sipg_server* sv, Request* r) {
+  r->x_bytes = r->n * sizeof(double);
+  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->x64, r->x_bytes, sv->s));
+  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->mem, r->footprint - r->x_bytes, sv->s));
+  char* p = r->mem;
+  auto take = [&](size_t bytes) {
+    char* q = p;
+    p += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  const size_t n = r->n;
+  const int cap = reduce_capacity(r->req.dim);
+  r->b64 = (double*)take(n * 8);
+  r->r64 = (double*)take(n * 8);
+  if (r->req.precision == SIPG_F64) {
+    r->p64[0] = (double*)take(n * 8);
+    r->p64[1] = (double*)take(n * 8);
+    r->Ap64 = (double*)take(n * 8);
+  } else {
+    r->e32 = (float*)take(n * 4);
+    r->r32 = (float*)take(n * 4);
+    r->p32[0] = (float*)take(n * 4);
+    r->p32[1] = (float*)take(n * 4);
+    r->Ap32 = (float*)take(n * 4);
+  }
+  r->red32.partials = (double*)take(sizeof(double) * cap);
+  r->red32.counter = (unsigned int*)take(256);
+  r->red32.capacity = cap;
+  r->red64.partials = (double*)take(sizeof(double) * cap);
+  r->red64.counter = (unsigned int*)take(256);
+  r->red64.capacity = cap;
+  SIPG_CUDA_TRY(cudaMemsetAsync(r->red32.counter, 0, 4, sv->s));
+  SIPG_CUDA_TRY(cudaMemsetAsync(r->red64.counter, 0, 4, sv->s));
+  const sipg_modes* modes = (r->req.sol == SIPG_SOL_MODES) ? &r->req.modes : nullptr;
+  sipg_status st = rhs_f64(r->op, r->req.sol, modes, r->b64, sv->s);
+  if (st != SIPG_OK) return st;
+  r->slot = sv->free_slots.back();
+  sv->free_slots.pop_back();
+  sv->used += r->footprint;
+  r->state = 1;
+  r->started = 0;
+  r->t_admit = Clock::now();
+  return SIPG_OK;
+}
+
+void retire(sipg_server* sv, Request* r, sipg_status status, int iterations, double rel) {
+  r->t_done = Clock::now();
+  r->result.status = status;
+  r->result.iterations = iterations;
+  r->result.corrections = r->corrections;
+  r->result.rel_residual = rel;
+  r->result.queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
+  r->result.latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  r->result.done = 1;
+  cudaFreeAsync(r->mem, sv->s);
+  r->mem = nullptr;
+  sv->used -= r->footprint - r->x_bytes;  // the solution stays until release
+  sv->free_slots.push_back(r->slot);
+  r->slot = -1;
+  r->state = 2;
+  sv->completed++;
+}
+
+ApplyArgs<float> cg_args32(const Request* r, sipg_server* sv) {
+  ApplyArgs<float> a{};
+  a.in = r->r32;
+  a.pbuf0 = r->p32[0];
+  a.pbuf1 = r->p32[1];
+  a.out = r->Ap32;
+  a.dim = r->req.dim;
+  a.nu = (float)r->req.pen;
+  a.st = sv->slots.d32 + r->slot;
+  a.red = r->red32;
+  return a;
+}
+
+ApplyArgs<double> cg_args64(const Request* r, sipg_server* sv) {
+  ApplyArgs<double> a{};
+  a.in = r->r64;
+  a.pbuf0 = r->p64[0];
+  a.pbuf1 = r->p64[1];
+  a.out = r->Ap64;
+  a.dim = r->req.dim;
+  a.nu = r->req.pen;
+  a.st = sv->slots.d64 + r->slot;
+  a.red = r->red64;
+  return a;
+}
+
+ServeMixed mixed_of(const Request* r, sipg_server* sv, int first) {
+  ServeMixed m;
+  m.x64 = r->x64;
+  m.b64 = r->b64;
+  m.r64 = r->r64;
+  m.e32 = r->e32;
+  m.r32 = r->r32;
+  m.st32 = sv->slots.d32 + r->slot;
+  m.st64 = sv->slots.d64 + r->slot;
+  m.red32 = r->red32;
+  m.red64 = r->red64;
+  m.n = r->n;
+  m.first = first;
+  m.delta = (float)sv->opts.inner_tol;
+  m.tol = r->req.tol;
+  m.nblk = inst_blocks(r->n);
+  m.pad = 0;
+  return m;
+}
+
+// A list of requests grouped by degree, packed into one descriptor array
+// (group g's arguments from `off`, its tile starts from `toff`).
+struct GroupLaunch {
+  int p;
+  TileCfg cfg;
+  int off, m, toff, total;
+  const HostTables* tab;
+};
+
+template <typename T, typename Build>
+std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArgs<T>* h_a, int* h_t, Build build) {
+  std::map<int, std::vector<Request*>> by_p;
+  for (Request* r : list) by_p[r->req.degree].push_back(r);
+  std::vector<GroupLaunch> out;
+  int off = 0, toff = 0;
+  for (auto& kv : by_p) {
+    const std::vector<Request*>& g = kv.second;
+    GroupLaunch gl;
+    gl.p = kv.first;
+    gl.cfg = (sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfg32;
+    gl.off = off;
+    gl.m = (int)g.size();
+    gl.toff = toff;
+    gl.tab = &g[0]->op->tab;
+    h_t[toff] = 0;
+    for (int j = 0; j < gl.m; ++j) {
+      h_a[off + j] = build(g[j]);
+      h_t[toff + j + 1] = h_t[toff + j] + apply_grid_blocks(g[j]->req.dim, gl.cfg);
+    }
+    gl.total = h_t[toff + gl.m];
+    off += gl.m;
+    toff += gl.m + 1;
+    out.push_back(gl);
+  }
+  return out;
+}
+
+template <typename T>
+sipg_status upload_groups(const std::vector<GroupLaunch>& gs, const ApplyArgs<T>* h_a, ApplyArgs<T>* d_a, const int* h_t,
+                          int* d_t, cudaStream_t s) {
+  if (gs.empty()) return SIPG_OK;
+  const GroupLaunch& last = gs.back();
+  SIPG_CUDA_TRY(cudaMemcpyAsync(d_a, h_a, sizeof(ApplyArgs<T>) * (last.off + last.m), cudaMemcpyHostToDevice, s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(d_t, h_t, sizeof(int) * (last.toff + last.m + 1), cudaMemcpyHostToDevice, s));
+  return SIPG_OK;
+}
+
+template <typename T>
+sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const ApplyArgs<T>* d_a, const int* d_t,
+                          cudaStream_t s) {
+  for (const GroupLaunch& g : gs) {
+    cudaError_t e = (sizeof(T) == 8)
+                        ? launch_apply_batched_f64(g.p, g.cfg, mode, (const ApplyArgs<double>*)(d_a + g.off),
+                                                   d_t + g.toff, g.m, g.total, *g.tab, s)
+                        : launch_apply_batched_f32(g.p, g.cfg, mode, (const ApplyArgs<float>*)(d_a + g.off),
+                                                   d_t + g.toff, g.m, g.total, *g.tab, s);
+    SIPG_CUDA_TRY(e);
+  }
+  return SIPG_OK;
+}
+
+sipg_status server_alloc(sipg_server* sv) {
+  const int cap = sv->opts.max_active;
+  SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d64, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMemset(sv->slots.d64, 0, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h32, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h64, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_a32, sizeof(ApplyArgs<float>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_a32, sizeof(ApplyArgs<float>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_a64, sizeof(ApplyArgs<double>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_a64, sizeof(ApplyArgs<double>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_r64, sizeof(ApplyArgs<double>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_r64, sizeof(ApplyArgs<double>) * cap));
+  int** tiles_h[3] = {&sv->h_t32, &sv->h_t64, &sv->h_tr};
+  int** tiles_d[3] = {&sv->d_t32, &sv->d_t64, &sv->d_tr};
+  for (int k = 0; k < 3; ++k) {
+    SIPG_CUDA_TRY(cudaMallocHost(tiles_h[k], sizeof(int) * (cap + 16)));
+    SIPG_CUDA_TRY(cudaMalloc(tiles_d[k], sizeof(int) * (cap + 16)));
+  }
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v32, sizeof(VecInst<float>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v32, sizeof(VecInst<float>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v64, sizeof(VecInst<double>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v64, sizeof(VecInst<double>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_m, sizeof(ServeMixed) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_m, sizeof(ServeMixed) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_tol, sizeof(double) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_tol, sizeof(double) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_bptr, sizeof(double*) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_bptr, sizeof(double*) * cap));
+  for (int k = cap - 1; k >= 0; --k) sv->free_slots.push_back(k);
+  return SIPG_OK;
+}
+
+void server_free(sipg_server* sv) {
+  if (!sv) return;
+  if (sv->s) cudaStreamSynchronize(sv->s);
+  for (auto& kv : sv->all) {
+    if (kv.second->mem) cudaFreeAsync(kv.second->mem, sv->s);
+    if (kv.second->x64) cudaFreeAsync(kv.second->x64, sv->s);
+    delete kv.second;
+  }
+  for (Request* r : sv->queue)
+    if (!sv->all.count(r->id)) delete r;
+  if (sv->s) cudaStreamSynchronize(sv->s);
+  cudaFree(sv->slots.d32);
+  cudaFree(sv->slots.d64);
+  cudaFreeHost(sv->slots.h32);
+  cudaFreeHost(sv->slots.h64);
+  cudaFreeHost(sv->h_a32);
+  cudaFree(sv->d_a32);
+  cudaFreeHost(sv->h_a64);
+  cudaFree(sv->d_a64);
+  cudaFreeHost(sv->h_r64);
+  cudaFree(sv->d_r64);
+  cudaFreeHost(sv->h_t32);
+  cudaFree(sv->d_t32);
+  cudaFreeHost(sv->h_t64);
+  cudaFree(sv->d_t64);
+  cudaFreeHost(sv->h_tr);
+  cudaFree(sv->d_tr);
+  cudaFreeHost(sv->h_v32);
+  cudaFree(sv->d_v32);
+  cudaFreeHost(sv->h_v64);
+  cudaFree(sv->d_v64);
+  cudaFreeHost(sv->h_m);
+  cudaFree(sv->d_m);
+  cudaFreeHost(sv->h_tol);
+  cudaFree(sv->d_tol);
+  cudaFreeHost(sv->h_bptr);
+  cudaFree(sv->d_bptr);
+  for (auto& kv : sv->ops) sipg_op_destroy(kv.second);
+  if (sv->s) cudaStreamDestroy(sv->s);
+  delete sv;
+}
+
+}  // namespace
+
+extern "C" {
+
+sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** out) {
+  if (!out) return SIPG_ERR_INVALID;
+  *out = nullptr;
+  sipg_server* sv = new (std::nothrow) sipg_server;
+  if (!sv) return SIPG_ERR_NOMEM;
+  sipg_server_opts o = {150ull << 30, 256, 8, 0.1};
+  if (opts) o = *opts;
+  if (o.max_active < 1 || o.max_active > 4096 || o.iters_per_step < 1 || !(o.inner_tol > 0 && o.inner_tol < 1)) {
+    set_error("sipg_server_create: need 1 <= max_active <= 4096, iters_per_step >= 1, 0 < inner_tol < 1");
+    delete sv;
+    return SIPG_ERR_INVALID;
+  }
+  sv->opts = o;
+  sipg_status st = server_alloc(sv);
+  if (st != SIPG_OK) {
+    server_free(sv);
+    return st;
+  }
+  *out = sv;
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_destroy(sipg_server* sv) {
+  server_free(sv);
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_submit(sipg_server* sv, const sipg_request* req, unsigned long long* id) {
+  if (!sv || !req || !id) return SIPG_ERR_INVALID;
+  if (req->dim < 1 || req->degree < 1 || req->degree > SIPG_MAX_DEGREE || !(req->tol > 0) ||
+      req->sol < SIPG_SOL_A || req->sol > SIPG_SOL_MODES || (req->precision != SIPG_F64 && req->precision != SIPG_F32)) {
+    set_error("sipg_server_submit: invalid request");
+    return SIPG_ERR_INVALID;
+  }
+  Request* r = new (std::nothrow) Request;
+  if (!r) return SIPG_ERR_NOMEM;
+  r->id = sv->next_id++;
+  r->req = *req;
+  r->n = (size_t)req->dim * req->dim * (req->degree + 1) * (req->degree + 1);
+  r->footprint = footprint_of(req->dim, req->degree, req->precision);
+  r->t_submit = Clock::now();
+  sv->all[r->id] = r;
+  *id = r->id;
+  if (r->footprint > sv->opts.budget_bytes) {
+    r->result.status = SIPG_ERR_REJECTED;
+    r->result.done = 1;
+    r->state = 2;
+    sv->rejected++;
+    set_error("sipg_server_submit: request footprint exceeds the memory budget");
+    return SIPG_ERR_REJECTED;
+  }
+  sv->queue.push_back(r);
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
+  if (!sv) return SIPG_ERR_INVALID;
+  const unsigned long long done_before = sv->completed;
+  // 1. admission
+  std::vector<Request*> fresh;
+  while (!sv->queue.empty() && !sv->free_slots.empty()) {
+    Request* r = sv->queue.front();
+    if (sv->used + r->footprint > sv->opts.budget_bytes) break;  // FIFO: wait for memory
+    sipg_status st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &r->op);
+    if (st != SIPG_OK) return st;
+    st = admit(sv, r);
+    if (st != SIPG_OK) return st;
+    sv->queue.pop_front();
+    sv->active.push_back(r);
+    fresh.push_back(r);
+  }
+  if (!fresh.empty()) {
+    // start the new requests (x = 0, r = b), one batched launch per precision
+    int m32 = 0, m64 = 0;
+    size_t nmax32 = 0, nmax64 = 0;
+    for (Request* r : fresh) {
+      if (r->req.precision == SIPG_F64) {
+        VecInst<double> v;
+        v.x = r->x64;
+        v.pb0 = r->p64[0];
+        v.pb1 = r->p64[1];
+        v.r = r->r64;
+        v.Ap = r->Ap64;
+        v.n = r->n;
+        v.st = sv->slots.d64 + r->slot;
+        v.red = r->red64;
+        v.nblk = inst_blocks(r->n);
+        v.pad = 0;
+        sv->h_v64[m64] = v;
+        sv->h_tol[m64] = r->req.tol;
+        sv->h_bptr[m64] = r->b64;
+        nmax64 = std::max(nmax64, r->n);
+        ++m64;
+      } else {
+        sv->h_m[m32++] = mixed_of(r, sv, 1);
+        nmax32 = std::max(nmax32, r->n);
+      }
+    }
+    if (m64) {
+      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v64, sv->h_v64, sizeof(VecInst<double>) * m64, cudaMemcpyHostToDevice, sv->s));
+      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_tol, sv->h_tol, sizeof(double) * m64, cudaMemcpyHostToDevice, sv->s));
+      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_bptr, sv->h_bptr, sizeof(double*) * m64, cudaMemcpyHostToDevice, sv->s));
+      k_serve_init_f64<<<dim3(vec_bpi(nmax64, m64), m64), kVecThreads, 0, sv->s>>>(sv->d_v64, sv->d_tol, sv->d_bptr);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+    if (m32) {
+      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m32, cudaMemcpyHostToDevice, sv->s));
+      k_serve_init_mixed<<<dim3(vec_bpi(nmax32, m32), m32), kVecThreads, 0, sv->s>>>(sv->d_m);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+  }
+  if (sv->active.empty()) {
+    if (n_active) *n_active = 0;
+    if (n_completed) *n_completed = (int)(sv->completed - done_before);
+    return SIPG_OK;
+  }
+  // 2. K iterations of every active request
+  std::vector<Request*> a32, a64;
+  for (Request* r : sv->active) (r->req.precision == SIPG_F64 ? a64 : a32).push_back(r);
+  size_t nmax32 = 0, nmax64 = 0;
+  for (int j = 0; j < (int)a32.size(); ++j) {
+    Request* r = a32[j];
+    VecInst<float> v;
+    v.x = r->e32;
+    v.pb0 = r->p32[0];
+    v.pb1 = r->p32[1];
+    v.r = r->r32;
+    v.Ap = r->Ap32;
+    v.n = r->n;
+    v.st = sv->slots.d32 + r->slot;
+    v.red = r->red32;
+    v.nblk = inst_blocks(r->n);
+    v.pad = 0;
+    sv->h_v32[j] = v;
+    nmax32 = std::max(nmax32, r->n);
+  }
+  for (int j = 0; j < (int)a64.size(); ++j) {
+    Request* r = a64[j];
+    VecInst<double> v;
+    v.x = r->x64;
+    v.pb0 = r->p64[0];
+    v.pb1 = r->p64[1];
+    v.r = r->r64;
+    v.Ap = r->Ap64;
+    v.n = r->n;
+    v.st = sv->slots.d64 + r->slot;
+    v.red = r->red64;
+    v.nblk = inst_blocks(r->n);
+    v.pad = 0;
+    sv->h_v64[j] = v;
+    nmax64 = std::max(nmax64, r->n);
+  }
+  if (!a32.empty())
+    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v32, sv->h_v32, sizeof(VecInst<float>) * a32.size(), cudaMemcpyHostToDevice, sv->s));
+  if (!a64.empty())
+    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v64, sv->h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, sv->s));
+  const std::vector<GroupLaunch> g32 =
+      pack_groups<float>(a32, sv->h_a32, sv->h_t32, [&](const Request* r) { return cg_args32(r, sv); });
+  const std::vector<GroupLaunch> g64 =
+      pack_groups<double>(a64, sv->h_a64, sv->h_t64, [&](const Request* r) { return cg_args64(r, sv); });
+  {
+    sipg_status st = upload_groups<float>(g32, sv->h_a32, sv->d_a32, sv->h_t32, sv->d_t32, sv->s);
+    if (st == SIPG_OK) st = upload_groups<double>(g64, sv->h_a64, sv->d_a64, sv->h_t64, sv->d_t64, sv->s);
+    if (st != SIPG_OK) return st;
+  }
+  for (int k = 0; k < sv->opts.iters_per_step; ++k) {
+    if (!a32.empty()) {
+      sipg_status st = launch_groups<float>(g32, APPLY_CG, sv->d_a32, sv->d_t32, sv->s);
+      if (st != SIPG_OK) return st;
+      k_cg_update_batched<float><<<dim3(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size()), kVecThreads, 0, sv->s>>>(
+          sv->d_v32);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+    if (!a64.empty()) {
+      sipg_status st = launch_groups<double>(g64, APPLY_CG, sv->d_a64, sv->d_t64, sv->s);
+      if (st != SIPG_OK) return st;
+      k_cg_update_batched<double><<<dim3(vec_bpi(nmax64, (int)a64.size()), (unsigned)a64.size()), kVecThreads, 0, sv->s>>>(
+          sv->d_v64);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  // 3. states, corrections, retirements
+  const int cap = sv->opts.max_active;
+  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h32, sv->slots.d32, sizeof(CgState<float>) * cap, cudaMemcpyDeviceToHost, sv->s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, sv->s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+  std::vector<Request*> keep, fix;
+  for (Request* r : a64) {
+    const CgState<double>& h = sv->slots.h64[r->slot];
+    if (h.done) {
+      const bool conv = !(std::sqrt(h.rr) > h.stop);
+      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
+      retire(sv, r, h.status == (int)SIPG_ERR_BREAKDOWN ? SIPG_ERR_BREAKDOWN : (conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED),
+             h.it, rel);
+    } else {
+      keep.push_back(r);
+    }
+  }
+  for (Request* r : a32) {
+    const CgState<float>& h = sv->slots.h32[r->slot];
+    if (h.done) fix.push_back(r);
+    else keep.push_back(r);
+  }
+  if (!fix.empty()) {
+    // x += e and the FP64 residual of the mixed requests due a correction
+    int m = 0;
+    size_t nmax = 0;
+    for (Request* r : fix) {
+      sv->h_m[m++] = mixed_of(r, sv, 0);
+      nmax = std::max(nmax, r->n);
+    }
+    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, sv->s));
+    k_serve_fold<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, sv->s>>>(sv->d_m);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    const std::vector<GroupLaunch> gr = pack_groups<double>(fix, sv->h_r64, sv->h_tr, [&](const Request* r) {
+      ApplyArgs<double> a{};
+      a.in = r->x64;
+      a.out = r->r64;
+      a.b = r->b64;
+      a.dim = r->req.dim;
+      a.nu = r->req.pen;
+      a.st = sv->slots.d64 + r->slot;
+      a.red = r->red64;
+      return a;
+    });
+    sipg_status st = upload_groups<double>(gr, sv->h_r64, sv->d_r64, sv->h_tr, sv->d_tr, sv->s);
+    if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, sv->d_r64, sv->d_tr, sv->s);
+    if (st != SIPG_OK) return st;
+    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, sv->s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+    std::vector<Request*> cont;
+    for (Request* r : fix) {
+      r->corrections++;
+      const CgState<double>& h = sv->slots.h64[r->slot];
+      const CgState<float>& h32 = sv->slots.h32[r->slot];
+      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
+      if (!std::isfinite(rel) || h32.status == (int)SIPG_ERR_BREAKDOWN) {
+        retire(sv, r, SIPG_ERR_BREAKDOWN, h32.it, rel);
+      } else if (rel <= r->req.tol || h.rr == 0.0) {
+        retire(sv, r, SIPG_OK, h32.it, rel);
+      } else if (r->corrections >= 1000) {
+        retire(sv, r, SIPG_ERR_NOT_CONVERGED, h32.it, rel);
+      } else {
+        cont.push_back(r);
+      }
+    }
+    if (!cont.empty()) {
+      m = 0;
+      nmax = 0;
+      for (Request* r : cont) {
+        sv->h_m[m++] = mixed_of(r, sv, 0);
+        nmax = std::max(nmax, r->n);
+      }
+      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, sv->s));
+      k_serve_restart<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, sv->s>>>(sv->d_m);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+      for (Request* r : cont) keep.push_back(r);
+    }
+    // the pinned staging (h_m) is rewritten in the next step
+    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+  }
+  sv->active = keep;
+  if (n_active) *n_active = (int)sv->active.size();
+  if (n_completed) *n_completed = (int)(sv->completed - done_before);
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_poll(sipg_server* sv, unsigned long long id, sipg_request_result* out) {
+  if (!sv || !out) return SIPG_ERR_INVALID;
+  auto it = sv->all.find(id);
+  if (it == sv->all.end()) {
+    set_error("sipg_server_poll: unknown request id");
+    return SIPG_ERR_INVALID;
+  }
+  *out = it->second->result;
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_release(sipg_server* sv, unsigned long long id) {
+  if (!sv) return SIPG_ERR_INVALID;
+  auto it = sv->all.find(id);
+  if (it == sv->all.end() || it->second->state != 2) {
+    set_error("sipg_server_release: unknown or unfinished request");
+    return SIPG_ERR_INVALID;
+  }
+  Request* r = it->second;
+  if (r->x64) {
+    cudaFreeAsync(r->x64, sv->s);
+    sv->used -= r->x_bytes;
+  }
+  delete r;
+  sv->all.erase(it);
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_solution(sipg_server* sv, unsigned long long id, double* h_x, size_t n) {
+  if (!sv || !h_x) return SIPG_ERR_INVALID;
+  auto it = sv->all.find(id);
+  if (it == sv->all.end() || it->second->state != 2 || !it->second->x64 || n != it->second->n) {
+    set_error("sipg_server_solution: unknown, unfinished or released request, or wrong length");
+    return SIPG_ERR_INVALID;
+  }
+  SIPG_CUDA_TRY(cudaMemcpyAsync(h_x, it->second->x64, n * sizeof(double), cudaMemcpyDeviceToHost, sv->s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+  return SIPG_OK;
+}
+
+sipg_status sipg_server_stats(const sipg_server* sv, sipg_server_stats_t* out) {
+  if (!sv || !out) return SIPG_ERR_INVALID;
+  out->queued = (int)sv->queue.size();
+  out->active = (int)sv->active.size();
+  out->completed = sv->completed;
+  out->rejected = sv->rejected;
+  out->bytes_in_use = sv->used;
+  return SIPG_OK;
+}
+
+}  // extern "C"

@@ -59,10 +59,10 @@ __device__ __forceinline__ A block_sum(A v, A* sh) {
 // arrives last sums all partials in index order.  Returns true in the last
 // block; *total is then valid in linear thread 0 of that block.
 template <typename A, int NT>
-__device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch& red, int nblocks, A* sh, A* total) {
+__device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch& red, int bid, int nblocks, A* sh,
+                                              A* total) {
   __shared__ int s_last;
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
   if (t == 0) {
     red.partials[bid] = (double)block_total;
     __threadfence();
@@ -80,6 +80,12 @@ __device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch
     *red.counter = 0u;  // ready for the next launch on this scratch
   }
   return true;
+}
+
+// The same with the block id of a one-dimensional or two-dimensional grid.
+template <typename A, int NT>
+__device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch& red, int nblocks, A* sh, A* total) {
+  return grid_sum_last<A, NT>(block_total, red, (int)(blockIdx.y * gridDim.x + blockIdx.x), nblocks, sh, total);
 }
 
 template <typename T, int P, int TX, int TY>
@@ -104,8 +110,11 @@ struct ApplyColumnForm {
   static constexpr int col_unroll = (sizeof(T) == 8 && P >= 5) ? 1 : (P + 1);
 };
 
+// One CTA's work: tile (bx, by) of the operator in `a`; `bid` / `nblocks` name
+// the block among the blocks that reduce into a.red (CG / residual modes).
 template <typename T, int P, int TX, int TY, int MODE>
-__global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ ApplyArgs<T> a, const __grid_constant__ Tab<T, P> tb) {
+__device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P>& tb, int bx, int by, int bid,
+                                           int nblocks) {
   constexpr int N = P, N1 = P + 1, NN = N1 * N1, TE = TX * TY;
   constexpr bool kCols = ApplyColumnForm<T, P>::value;
   using S = ApplySmem<T, P, TX, TY>;
@@ -121,7 +130,7 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
 
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
   const int dim = a.dim;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int x0 = bx * TX, y0 = by * TY;
   const int gx = x0 + tx, gy = y0 + ty;
   const bool act = (gx < dim) && (gy < dim);
   const size_t noe = (size_t)dim * dim;
@@ -431,8 +440,7 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
   if (MODE != APPLY_PLAIN) {
     const T bt = block_sum<T, TE>(acc, red_sh);
     T total;
-    const int nblocks = gridDim.x * gridDim.y;
-    if (grid_sum_last<T, TE>(bt, a.red, nblocks, red_sh, &total) && t == 0) {
+    if (grid_sum_last<T, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0) {
       CgState<T>* st = a.st;
       if (MODE == APPLY_CG) {
         const T alpha = st->rr / total;
@@ -456,6 +464,34 @@ __global__ void __launch_bounds__(TX* TY) k_sipg_apply(const __grid_constant__ A
       }
     }
   }
+}
+
+template <typename T, int P, int TX, int TY, int MODE>
+__global__ void __launch_bounds__(TX* TY)
+    k_sipg_apply(const __grid_constant__ ApplyArgs<T> a, const __grid_constant__ Tab<T, P> tb) {
+  apply_tile<T, P, TX, TY, MODE>(a, tb, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x,
+                                 gridDim.x * gridDim.y);
+}
+
+// Many operators of the same degree in one launch: block g works on tile
+// g - tile_start[i] of instance i, where tile_start[i] <= g < tile_start[i+1]
+// (the instances' tiles concatenated; each instance reduces into its own
+// scratch and state, and a converged instance's blocks return at once).
+template <typename T, int P, int TX, int TY, int MODE>
+__global__ void __launch_bounds__(TX* TY)
+    k_sipg_apply_batched(const ApplyArgs<T>* __restrict__ insts, const int* __restrict__ tile_start, int ninst,
+                         const __grid_constant__ Tab<T, P> tb) {
+  const int g = blockIdx.x;
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(tile_start + mid) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  const ApplyArgs<T> a = insts[lo];
+  const int lt = g - __ldg(tile_start + lo);
+  const int tiles_x = (a.dim + TX - 1) / TX, tiles_y = (a.dim + TY - 1) / TY;
+  apply_tile<T, P, TX, TY, MODE>(a, tb, lt % tiles_x, lt / tiles_x, lt, tiles_x * tiles_y);
 }
 
 template <typename T, int P, int TX, int TY>
@@ -508,6 +544,57 @@ cudaError_t launch_apply_p(const TileCfg& cfg, int mode, const ApplyArgs<T>& a, 
     case 8:
       if (!fits8) return cudaErrorInvalidConfiguration;
       return launch_apply_tile<T, P, 32, (fits8 ? 8 : 4)>(mode, a, tb, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename T, int P, int TX, int TY>
+cudaError_t launch_apply_batched_tile(int mode, const ApplyArgs<T>* insts, const int* tile_start, int ninst,
+                                      int total_tiles, const Tab<T, P>& tb, cudaStream_t s) {
+  const size_t smem = ApplySmem<T, P, TX, TY>::bytes;
+  cudaError_t err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_PLAIN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_CG>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess || mode == APPLY_PREPARE || total_tiles == 0) return err;
+  const dim3 grid(total_tiles), block(TX, TY);
+  switch (mode) {
+    case APPLY_PLAIN:
+      k_sipg_apply_batched<T, P, TX, TY, APPLY_PLAIN><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    case APPLY_CG:
+      k_sipg_apply_batched<T, P, TX, TY, APPLY_CG><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    case APPLY_RESID:
+      k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <typename T, int P>
+cudaError_t launch_apply_batched_p(const TileCfg& cfg, int mode, const ApplyArgs<T>* insts, const int* tile_start,
+                                   int ninst, int total_tiles, const HostTables& h, cudaStream_t s) {
+  const Tab<T, P> tb = make_tab<T, P>(h);
+  constexpr size_t kMax = 227 * 1024;
+  constexpr bool fits8 = ApplySmem<T, P, 32, 8>::bytes <= kMax;
+  if (cfg.tx != 32) return cudaErrorInvalidValue;
+  switch (cfg.ty) {
+    case 2:
+      return launch_apply_batched_tile<T, P, 32, 2>(mode, insts, tile_start, ninst, total_tiles, tb, s);
+    case 4:
+      return launch_apply_batched_tile<T, P, 32, 4>(mode, insts, tile_start, ninst, total_tiles, tb, s);
+    case 8:
+      if (!fits8) return cudaErrorInvalidConfiguration;
+      return launch_apply_batched_tile<T, P, 32, (fits8 ? 8 : 4)>(mode, insts, tile_start, ninst, total_tiles, tb,
+                                                                  s);
   }
   return cudaErrorInvalidValue;
 }

@@ -18,18 +18,20 @@ namespace sipg {
 
 constexpr int kVecThreads = 256;
 
+// x += alpha p, r -= alpha Ap, r.r reduced; then the iteration bookkeeping
+// (beta, it, done, or a reliable update due).  Block `bid` of `nblocks` works
+// on a grid-stride slice of the vectors.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, const T* __restrict__ pb0,
-                                                           const T* __restrict__ pb1, T* __restrict__ r,
-                                                           const T* __restrict__ Ap, size_t n, CgState<T>* st,
-                                                           ReduceScratch red) {
+__device__ __forceinline__ void cg_update_body(T* __restrict__ x, const T* __restrict__ pb0, const T* __restrict__ pb1,
+                                               T* __restrict__ r, const T* __restrict__ Ap, size_t n, CgState<T>* st,
+                                               const ReduceScratch& red, int bid, int nblocks) {
   __shared__ T sh[32];
   if (*(volatile int*)&st->done) return;
   const T alpha = st->alpha;
   const T* __restrict__ p = st->parity ? pb1 : pb0;  // the direction the apply just wrote
   T acc = T(0);
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) {
     x[i] = fma(alpha, p[i], x[i]);
     const T ri = fma(-alpha, Ap[i], r[i]);
     r[i] = ri;
@@ -37,7 +39,7 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, co
   }
   const T bt = block_sum<T, kVecThreads>(acc, sh);
   T total;
-  if (grid_sum_last<T, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
+  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
     const T rn = sqrt(total);
     st->it += 1;
     st->first = 0;
@@ -60,17 +62,56 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, co
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, const T* __restrict__ pb0,
+                                                           const T* __restrict__ pb1, T* __restrict__ r,
+                                                           const T* __restrict__ Ap, size_t n, CgState<T>* st,
+                                                           ReduceScratch red) {
+  cg_update_body<T>(x, pb0, pb1, r, Ap, n, st, red, blockIdx.x, gridDim.x);
+}
+
+// Per-instance vector operands of a batch (instance = blockIdx.y).  Each
+// instance uses its own nblk blocks (the rest of the grid row returns at
+// once), so its reductions -- and so its iterates -- do not depend on which
+// other instances share the launch.
+template <typename T>
+struct VecInst {
+  T* x;
+  T* pb0;
+  T* pb1;
+  T* r;
+  T* Ap;
+  size_t n;
+  CgState<T>* st;
+  ReduceScratch red;
+  int nblk;
+  int pad;
+};
+
+// Blocks one instance of n values uses in the batched vector kernels.
+inline int inst_blocks(size_t n) {
+  const size_t b = (n + 2047) / 2048;
+  return (int)(b < 1 ? 1 : (b > 64 ? 64 : b));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_update_batched(const VecInst<T>* __restrict__ insts) {
+  const VecInst<T> v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  cg_update_body<T>(v.x, v.pb0, v.pb1, v.r, v.Ap, v.n, v.st, v.red, blockIdx.x, v.nblk);
+}
+
 // b.b, and the stop threshold: tol (absolute) or tol*||b|| (relative).
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_cg_init(const T* __restrict__ b, size_t n, CgState<T>* st, T tol,
-                                                         int rel, int max_it, ReduceScratch red) {
+__device__ __forceinline__ void cg_init_body(const T* __restrict__ b, size_t n, CgState<T>* st, T tol, int rel,
+                                             int max_it, const ReduceScratch& red, int bid, int nblocks) {
   __shared__ T sh[32];
   T acc = T(0);
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) acc = fma(b[i], b[i], acc);
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) acc = fma(b[i], b[i], acc);
   const T bt = block_sum<T, kVecThreads>(acc, sh);
   T total;
-  if (grid_sum_last<T, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
+  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
     st->bb = total;
     st->stop = rel ? tol * sqrt(total) : tol;
     st->max_it = max_it;
@@ -84,6 +125,12 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_init(const T* __restrict__ b
     st->rmax = T(0);
     st->alpha = st->beta = st->pAp = T(0);
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_init(const T* __restrict__ b, size_t n, CgState<T>* st, T tol,
+                                                         int rel, int max_it, ReduceScratch red) {
+  cg_init_body<T>(b, n, st, tol, rel, max_it, red, blockIdx.x, gridDim.x);
 }
 
 }  // namespace sipg

@@ -124,6 +124,14 @@ cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArg
                              cudaStream_t s);
 cudaError_t launch_apply_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const HostTables& h,
                              cudaStream_t s);
+// The same for many operators of degree p in one launch (instances' tiles
+// concatenated, tile_start[i] = first tile of instance i; device arrays).
+cudaError_t launch_apply_batched_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,
+                                     const int* tile_start, int ninst, int total_tiles, const HostTables& h,
+                                     cudaStream_t s);
+cudaError_t launch_apply_batched_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>* insts,
+                                     const int* tile_start, int ninst, int total_tiles, const HostTables& h,
+                                     cudaStream_t s);
 // Number of blocks the apply launches for this tile shape.
 inline int apply_grid_blocks(int dim, const TileCfg& c) {
   return ((dim + c.tx - 1) / c.tx) * ((dim + c.ty - 1) / c.ty);

@@ -46,6 +46,25 @@ class MixedResult(C.Structure):
                 ("time_ms", C.c_double), ("converged", C.c_int)]
 
 
+class Problem(C.Structure):
+    _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("pen", C.c_double)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("budget_bytes", C.c_size_t), ("max_active", C.c_int), ("iters_per_step", C.c_int),
+                ("inner_tol", C.c_double)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("done", C.c_int), ("status", C.c_int), ("iterations", C.c_int), ("corrections", C.c_int),
+                ("rel_residual", C.c_double), ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int), ("active", C.c_int), ("completed", C.c_ulonglong), ("rejected", C.c_ulonglong),
+                ("bytes_in_use", C.c_size_t)]
+
+
 class Modes(C.Structure):
     _fields_ = [("nmodes", C.c_int), ("amp", C.c_double * 8), ("k", C.c_int * 8), ("l", C.c_int * 8)]
 
@@ -80,6 +99,19 @@ _SIGS = {
     "sipg_version": (C.c_char_p, []),
     "sipg_launch_count": (C.c_ulonglong, []),
     "sipg_probe_fma_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "sipg_batch_create": (C.c_int, [C.c_int, _VP, C.POINTER(_VP)]),
+    "sipg_batch_destroy": (C.c_int, [_VP]),
+    "sipg_batch_op": (C.c_int, [_VP, C.c_int, C.POINTER(_VP)]),
+    "sipg_batch_footprint": (C.c_size_t, [_VP]),
+    "sipg_batch_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), _VP, _VP]),
+    "sipg_server_create": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "sipg_server_destroy": (C.c_int, [_VP]),
+    "sipg_server_submit": (C.c_int, [_VP, _VP, C.POINTER(C.c_ulonglong)]),
+    "sipg_server_step": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sipg_server_poll": (C.c_int, [_VP, C.c_ulonglong, C.POINTER(RequestResult)]),
+    "sipg_server_release": (C.c_int, [_VP, C.c_ulonglong]),
+    "sipg_server_solution": (C.c_int, [_VP, C.c_ulonglong, _VP, C.c_size_t]),
+    "sipg_server_stats": (C.c_int, [_VP, C.POINTER(ServerStats)]),
     "sipg_dot_f64": (C.c_int, [C.c_size_t, _VP, _VP, C.POINTER(C.c_double), _VP]),
     "sipg_dot_f64_noalloc": (C.c_int, [C.c_size_t, _VP, _VP, C.POINTER(C.c_double), _VP]),
 }
@@ -153,18 +185,23 @@ def square_mesh_coords(dim):
 class Operator:
     """The SIPG operator of a dim x dim mesh of degree p with kernel penalty pen."""
 
-    def __init__(self, dim, degree, pen):
-        h = C.c_void_p()
-        _check(lib().sipg_op_create(int(dim), int(degree), float(pen), C.byref(h)), "sipg_op_create")
+    def __init__(self, dim, degree, pen, _handle=None):
+        if _handle is None:
+            h = C.c_void_p()
+            _check(lib().sipg_op_create(int(dim), int(degree), float(pen), C.byref(h)), "sipg_op_create")
+            self._owned = True
+        else:  # an operator owned by a Batch
+            h = _handle
+            self._owned = False
         self._h = h
         self.dim, self.degree, self.pen = int(dim), int(degree), float(pen)
         self.noe = self.dim * self.dim
         self.ndof = self.noe * (self.degree + 1) ** 2
 
     def close(self):
-        if self._h:
+        if self._h and self._owned:
             lib().sipg_op_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -254,3 +291,117 @@ class Operator:
         m = C.byref(modes) if modes is not None else None
         _check(lib().sipg_err_norms_f64(self._h, sid, m, _ptr(u), e.ctypes.data, _stream(stream)), "err_norms")
         return float(e[0]), float(e[1]), float(e[2])
+
+
+class Batch:
+    """Many SIPG problems solved together (sipg_batch_*): problems is a list of
+    (dim, degree, pen)."""
+
+    def __init__(self, problems):
+        arr = (Problem * len(problems))(*[Problem(int(d), int(p), float(pen)) for d, p, pen in problems])
+        h = C.c_void_p()
+        _check(lib().sipg_batch_create(len(problems), C.cast(arr, C.c_void_p), C.byref(h)), "sipg_batch_create")
+        self._h = h
+        self.problems = [(int(d), int(p), float(pen)) for d, p, pen in problems]
+
+    def __len__(self):
+        return len(self.problems)
+
+    def op(self, i):
+        h = C.c_void_p()
+        _check(lib().sipg_batch_op(self._h, int(i), C.byref(h)), "sipg_batch_op")
+        d, p, pen = self.problems[i]
+        return Operator(d, p, pen, _handle=h)
+
+    def footprint(self):
+        return int(lib().sipg_batch_footprint(self._h))
+
+    def solve_mixed(self, xs, bs, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, stream=None):
+        n = len(self.problems)
+        assert len(xs) == n and len(bs) == n
+        px = (C.c_void_p * n)(*[x.data_ptr() for x in xs])
+        pb = (C.c_void_p * n)(*[b.data_ptr() for b in bs])
+        res = (MixedResult * n)()
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner))
+        st = lib().sipg_batch_solve_mixed(self._h, C.cast(px, C.c_void_p), C.cast(pb, C.c_void_p), C.byref(o),
+                                          C.cast(res, C.c_void_p), _stream(stream))
+        if st not in (0, 3, 4):
+            _check(st, "batch_solve_mixed")
+        return st, list(res)
+
+    def close(self):
+        if self._h:
+            lib().sipg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Request(C.Structure):
+    _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("pen", C.c_double), ("sol", C.c_int), ("modes", Modes),
+                ("tol", C.c_double), ("precision", C.c_int)]
+
+
+F64, F32 = 0, 1
+
+
+class Server:
+    """Continuous-batching solve server (sipg_server_*).  submit() queues a
+    request, step() runs one scheduling step, poll() reads a result."""
+
+    def __init__(self, budget_bytes=150 << 30, max_active=256, iters_per_step=8, inner_tol=0.1):
+        o = ServerOpts(int(budget_bytes), int(max_active), int(iters_per_step), float(inner_tol))
+        h = C.c_void_p()
+        _check(lib().sipg_server_create(C.byref(o), C.byref(h)), "sipg_server_create")
+        self._h = h
+
+    def submit(self, dim, degree, pen, tol, sol="modes", modes=None, precision=F32):
+        r = Request()
+        r.dim, r.degree, r.pen, r.tol, r.precision = int(dim), int(degree), float(pen), float(tol), int(precision)
+        r.sol = SOL[sol] if isinstance(sol, str) else int(sol)
+        if modes is not None:
+            r.modes = modes
+        rid = C.c_ulonglong()
+        st = lib().sipg_server_submit(self._h, C.byref(r), C.byref(rid))
+        if st not in (0, 7):
+            _check(st, "sipg_server_submit")
+        return rid.value, st
+
+    def step(self):
+        a, c = C.c_int(), C.c_int()
+        _check(lib().sipg_server_step(self._h, C.byref(a), C.byref(c)), "sipg_server_step")
+        return a.value, c.value
+
+    def poll(self, rid):
+        res = RequestResult()
+        _check(lib().sipg_server_poll(self._h, C.c_ulonglong(rid), C.byref(res)), "sipg_server_poll")
+        return res
+
+    def solution(self, rid, ndof):
+        x = np.empty(int(ndof))
+        _check(lib().sipg_server_solution(self._h, C.c_ulonglong(rid), x.ctypes.data, C.c_size_t(int(ndof))),
+               "sipg_server_solution")
+        return x
+
+    def release(self, rid):
+        _check(lib().sipg_server_release(self._h, C.c_ulonglong(rid)), "sipg_server_release")
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().sipg_server_stats(self._h, C.byref(s)), "sipg_server_stats")
+        return s
+
+    def close(self):
+        if self._h:
+            lib().sipg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -170,6 +170,92 @@ sipg_status sipg_xpby_f32(size_t n, const float* d_x, float beta, float* d_y, vo
  * Synchronous; deterministic. */
 sipg_status sipg_dot_f64_noalloc(size_t n, const double* d_x, const double* d_y, double* result, void* stream);
 
+/* ---- many problems at once (no reference counterpart) ---- */
+
+/* One problem of a batch: a dim x dim mesh, degree 1..SIPG_MAX_DEGREE, penalty. */
+typedef struct {
+  int dim;
+  int degree;
+  double pen;
+} sipg_problem;
+
+/* A batch keeps, for each problem, an operator (shared by problems with equal
+ * dim, degree and pen), FP32 CG vectors, an FP64 residual, device CG states and
+ * reduction scratch, all resident until sipg_batch_destroy.  Opaque. */
+typedef struct sipg_batch sipg_batch;
+
+sipg_status sipg_batch_create(int n, const sipg_problem* problems, sipg_batch** batch);
+sipg_status sipg_batch_destroy(sipg_batch* batch);
+/* The operator of problem i (owned by the batch), e.g. for sipg_rhs_f64. */
+sipg_status sipg_batch_op(const sipg_batch* batch, int i, sipg_op** op);
+/* Device bytes the batch holds (besides the callers' x and b). */
+size_t sipg_batch_footprint(const sipg_batch* batch);
+/* Solves A_i x_i = b_i for every problem with the mixed-precision scheme of
+ * sipg_solve_mixed, all problems together: one batched FP32 apply launch per
+ * degree present and one batched update per iteration, replayed as a CUDA
+ * graph; problems retire as they converge.  d_x[i], d_b[i]: FP64 device
+ * vectors (x holds x0).  res (array of n, may be NULL) gets each problem's
+ * corrections, FP32 iterations, final FP64 relative residual; time_ms is the
+ * whole batch's. */
+sipg_status sipg_batch_solve_mixed(sipg_batch* batch, double* const* d_x, const double* const* d_b,
+                                   const sipg_mixed_opts* opts, sipg_mixed_result* res, void* stream);
+
+/* ---- continuous-batching server (no reference counterpart) ---- */
+
+typedef struct {
+  size_t budget_bytes;  /* device memory the active requests may hold (150 GB) */
+  int max_active;       /* requests solved concurrently, 1..4096 (256) */
+  int iters_per_step;   /* CG iterations per sipg_server_step (8) */
+  double inner_tol;     /* mixed requests: reliable-update threshold (0.1) */
+} sipg_server_opts;
+
+typedef struct {
+  int dim;
+  int degree;
+  double pen;
+  int sol;              /* test problem (sipg_solution) whose right-hand side is built on the device */
+  sipg_modes modes;     /* for SIPG_SOL_MODES */
+  double tol;           /* relative FP64 residual ||b - Ax|| <= tol ||b|| */
+  int precision;        /* SIPG_F32: mixed (FP32 CG, FP64 corrections); SIPG_F64: plain FP64 CG */
+} sipg_request;
+
+typedef struct {
+  int done;             /* 1 once the request retired */
+  sipg_status status;   /* SIPG_OK, SIPG_ERR_NOT_CONVERGED, SIPG_ERR_BREAKDOWN, SIPG_ERR_REJECTED */
+  int iterations;       /* CG iterations (FP32 ones for mixed requests) */
+  int corrections;      /* FP64 corrections (mixed) */
+  double rel_residual;  /* final FP64 ||b - Ax|| / ||b|| */
+  double queue_ms;      /* submit -> admission */
+  double latency_ms;    /* submit -> retirement */
+} sipg_request_result;
+
+typedef struct {
+  int queued;
+  int active;
+  unsigned long long completed;
+  unsigned long long rejected;
+  size_t bytes_in_use;
+} sipg_server_stats_t;
+
+typedef struct sipg_server sipg_server;
+
+/* opts may be NULL (defaults in sipg_server_opts). */
+sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** server);
+sipg_status sipg_server_destroy(sipg_server* server);
+/* Queues a request (FIFO); returns SIPG_ERR_REJECTED (and a retired result)
+ * when its device footprint alone exceeds the budget. */
+sipg_status sipg_server_submit(sipg_server* server, const sipg_request* req, unsigned long long* id);
+/* One scheduling step: admit what fits, run iters_per_step CG iterations of
+ * every active request in batched launches, correct / retire.  Synchronous. */
+sipg_status sipg_server_step(sipg_server* server, int* n_active, int* n_completed);
+sipg_status sipg_server_poll(sipg_server* server, unsigned long long id, sipg_request_result* result);
+/* Copies a retired request's solution (n = its DoF) to host memory; the
+ * solution stays on the device until sipg_server_release. */
+sipg_status sipg_server_solution(sipg_server* server, unsigned long long id, double* h_x, size_t n);
+/* Forgets a retired request: frees its solution and result. */
+sipg_status sipg_server_release(sipg_server* server, unsigned long long id);
+sipg_status sipg_server_stats(const sipg_server* server, sipg_server_stats_t* stats);
+
 /* ---- either side of the solve ---- */
 
 /* d_b = the right-hand side of test problem `sol` (f term + Nitsche terms of

@@ -35,7 +35,7 @@ def _close_iterations(it, it_ref):
 
 def test_p_and_h_sweeps_match_oracle(driver_output, oracle):
     rows = [r for r in driver_output if r["case"] in ("p", "h")]
-    assert len(rows) == 8 + 9
+    assert len(rows) == 8 + 12
     for r in rows:
         p, d, pen, tol = r["p"], r["dim"], r["pen"], r["tol"]
         b = oracle.rhs(p, d, pen, 5)

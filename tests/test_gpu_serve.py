@@ -1,0 +1,112 @@
+"""The continuous-batching server (sipg_server_*): requests of mixed sizes,
+degrees, precisions and tolerances submitted while others are mid-solve all
+retire with ||b - Ax|| <= tol ||b||, and each result is the same alone and in
+the mix: within 1e-6 relative of the single-problem FP64 CG solution to 1e-12
+(the served solves stop at 1e-8 / 1e-10).  Admission respects the memory
+budget and rejects requests larger than it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+
+    return t
+
+
+def _requests(sipg, rng, n):
+    out = []
+    for _ in range(n):
+        dim = int(np.exp(rng.uniform(np.log(8), np.log(40))))
+        p = int(rng.integers(2, 9))
+        modes = sipg.Modes.make(rng.normal(size=4), rng.integers(1, 9, 4), rng.integers(1, 9, 4))
+        tol = float(rng.choice([1e-8, 1e-10]))
+        prec = int(rng.integers(0, 2))
+        out.append((dim, p, float(p * p), tol, modes, prec))
+    return out
+
+
+def _reference(sipg, torch, dim, p, pen, modes):
+    op = sipg.Operator(dim, p, pen)
+    b = op.rhs("modes", modes)
+    x = torch.zeros_like(b)
+    st, _ = op.cg(x, b, 1e-12, relative=True)
+    assert st == 0
+    op.close()
+    return x.cpu().numpy()
+
+
+def test_server_mixed_stream_matches_single_solves(sipg, torch):
+    rng = np.random.default_rng(3)
+    reqs = _requests(sipg, rng, 24)
+    sv = sipg.Server(budget_bytes=2 << 30, max_active=8, iters_per_step=8)
+    ids = []
+    pending = list(reqs)
+    # submit a few, step, submit more while the first are mid-solve
+    for _ in range(3):
+        ids.append(sv.submit(*pending.pop(0)[:4], modes=reqs[len(ids)][4], precision=reqs[len(ids)][5])[0])
+    sv.step()
+    while pending:
+        d, p, pen, tol, modes, prec = pending.pop(0)
+        ids.append(sv.submit(d, p, pen, tol, modes=modes, precision=prec)[0])
+        sv.step()
+    for _ in range(100000):
+        active, _ = sv.step()
+        if active == 0 and sv.stats().queued == 0:
+            break
+    assert sv.stats().completed == len(reqs)
+    for rid, (d, p, pen, tol, modes, prec) in zip(ids, reqs):
+        res = sv.poll(rid)
+        assert res.done == 1 and res.status == 0, (d, p, prec, res.status)
+        assert res.rel_residual <= tol
+        x = sv.solution(rid, d * d * (p + 1) ** 2)
+        ref = _reference(sipg, torch, d, p, pen, modes)
+        assert np.max(np.abs(x - ref)) <= (1e-4 if tol == 1e-8 else 1e-6) * np.max(np.abs(ref)), (d, p, tol, prec)
+        sv.release(rid)
+    assert sv.stats().bytes_in_use == 0
+    sv.close()
+
+
+def test_server_alone_equals_in_mix(sipg, torch):
+    rng = np.random.default_rng(5)
+    d, p, pen, tol = 24, 5, 25.0, 1e-10
+    modes = sipg.Modes.make([1.0, -0.5, 0.25, 2.0], [1, 2, 5, 3], [3, 1, 4, 6])
+    alone = sipg.Server(max_active=1)
+    rid, _ = alone.submit(d, p, pen, tol, modes=modes)
+    while alone.step()[0] or alone.stats().queued:
+        pass
+    xa = alone.solution(rid, d * d * (p + 1) ** 2)
+    mix = sipg.Server(max_active=16)
+    others = _requests(sipg, rng, 10)
+    for o in others[:5]:
+        mix.submit(*o[:4], modes=o[4], precision=o[5])
+    rid2, _ = mix.submit(d, p, pen, tol, modes=modes)
+    for o in others[5:]:
+        mix.submit(*o[:4], modes=o[4], precision=o[5])
+    while mix.step()[0] or mix.stats().queued:
+        pass
+    xm = mix.solution(rid2, d * d * (p + 1) ** 2)
+    # the batched kernels give every request the same arithmetic whatever runs beside it
+    assert np.array_equal(xa, xm)
+    alone.close()
+    mix.close()
+
+
+def test_server_budget_admission_and_rejection(sipg, torch):
+    sv = sipg.Server(budget_bytes=64 << 20, max_active=64)
+    modes = sipg.Modes.make([1.0], [1], [1])
+    big, st = sv.submit(512, 8, 64.0, 1e-8, modes=modes)
+    assert st == 7 and sv.poll(big).status == 7  # SIPG_ERR_REJECTED
+    ids = [sv.submit(48, 4, 16.0, 1e-8, modes=modes)[0] for _ in range(12)]
+    peak = 0
+    while True:
+        active, _ = sv.step()
+        peak = max(peak, sv.stats().bytes_in_use)
+        if active == 0 and sv.stats().queued == 0:
+            break
+    assert peak <= 64 << 20
+    assert all(sv.poll(i).status == 0 for i in ids)
+    sv.close()
