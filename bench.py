@@ -305,16 +305,354 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The other benchmark configurations (parity-test cases of the headline path
+# and the solver additions), one JSON line each: --config sweep | solve16 |
+# mixed | batch | serve.  Each keeps the timing rules: warm-up first, CUDA
+# events or a synchronised wall clock, clocks sampled during the timed part.
+# ---------------------------------------------------------------------------
+
+
+def _base_line(args, metric, value, unit, higher, dtype, config, **extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": "synthetic (seeded)", "config": config}
+    line.update(extra)
+    return line
+
+
+def _timed(torch, fn, steps):
+    """ms per call of fn() over `steps` calls, CUDA events on the current stream."""
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        fn()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_sweep(args):
+    """Apply throughput at ~16M DoF for p = 1..8, N = round(4000 / (p + 1))."""
+    import numpy as np
+    import torch
+
+    import sipg_gb300 as sipg
+
+    rows = {}
+    tot_dof = tot_ms = 0.0
+    sampler = ClockSampler(0)
+    sampler.start()
+    n0 = sipg.launch_count()
+    for p in range(1, 9):
+        d = round(4000 / (p + 1))
+        op = sipg.Operator(d, p, float(p * p))
+        x = torch.from_numpy(np.random.default_rng(0).uniform(-1.0, 1.0, op.ndof)).cuda()
+        y = torch.empty_like(x)
+        for _ in range(args.warmup):
+            op.apply(x, y)
+        ms = _timed(torch, lambda: op.apply(x, y), max(args.steps, 10))
+        row = {"dim": d, "ndof": op.ndof, "gdofs": op.ndof / ms / 1e6, "gbs": 16 * op.ndof / ms / 1e6}
+        try:
+            import oracle_lib
+
+            if oracle_lib.ref_gpu_available():
+                reps = 5
+                rms = oracle_lib.ref_gpu().apply(p, d, float(p * p), x.data_ptr(), y.data_ptr(), reps) / reps
+                row["reference_kernels_gdofs"] = op.ndof / rms / 1e6
+                row["speedup_vs_reference_kernels"] = rms / ms
+        except Exception as exc:
+            row["reference_kernels"] = "unavailable: %s" % exc
+        rows["p%d" % p] = row
+        tot_dof += op.ndof
+        tot_ms += ms
+        op.close()
+    clocks = sampler.stop()
+    value = tot_dof / tot_ms / 1e6
+    line = _base_line(args, "GDoF/s per SIPG apply, ~16M DoF, p = 1..8 (aggregate: total DoF / total time)", value,
+                      "GDoF/s", True, "f64",
+                      {"workload": "apply sweep: N = round(4000/(p+1)), p = 1..8, pen p^2, u ~ U[-1,1] seed 0",
+                       "l2": "inputs 128 MB+ per vector"},
+                      per_degree=rows, clocks=clocks, gpu_launches=sipg.launch_count() - n0)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_solve16(args):
+    """The 16 x 16, p = 4 solve to relative residual 1e-12 (one solve per step),
+    end to end from a host right-hand side to a host solution."""
+    import numpy as np
+    import torch
+
+    import sipg_gb300 as sipg
+
+    dim, p, pen = 16, 4, 16.0
+    op = sipg.Operator(dim, p, pen)
+    b_dev = op.rhs("sinsin")
+    h_b = b_dev.cpu().pin_memory()
+    h_x = torch.empty_like(h_b).pin_memory()
+    x = torch.zeros_like(b_dev)
+    b = torch.empty_like(b_dev)
+    res = {}
+
+    def step():
+        b.copy_(h_b, non_blocking=True)
+        x.zero_()
+        st, r = op.cg(x, b, 1e-12, relative=True)
+        h_x.copy_(x, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        res["r"] = r
+
+    for _ in range(args.warmup):
+        step()
+    sampler = ClockSampler(0)
+    sampler.start()
+    n0 = sipg.launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    wall = (time.perf_counter() - t0) / args.steps
+    launches = sipg.launch_count() - n0
+    clocks = sampler.stop()
+    r = res["r"]
+    l2, h1, mx = op.err_norms("sinsin", x)
+    extra = {"iterations": r.iterations, "device_ms_per_solve": r.time_ms, "L2": l2, "H1": h1, "max_err": mx,
+             "e2e": {"value": 1e3 / wall, "unit": "solves/s", "h2d_bytes_per_step": op.ndof * 8,
+                     "d2h_bytes_per_step": op.ndof * 8, "api": "sipg_cg_f64 with host b in, host x out"},
+             "ms_per_step": wall * 1e3, "clocks": clocks, "gpu_launches": launches}
+    try:
+        import oracle_lib
+
+        if oracle_lib.ref_gpu_available():
+            xr = torch.zeros_like(b_dev)
+            it, ms = oracle_lib.ref_gpu().cg(p, dim, pen, xr.data_ptr(), b_dev.data_ptr(),
+                                             1e-12 * float(b_dev.norm().item()))
+            extra["reference_kernels_same_gpu"] = {"iterations": it, "ms_per_solve": ms,
+                                                   "solves_per_s": 1e3 / ms,
+                                                   "source": "reference kernels + its CG loop (cuBLAS dots)"}
+    except Exception as exc:
+        extra["reference_kernels_same_gpu"] = {"unavailable": str(exc)}
+    if not args.no_cpu_baseline:
+        import oracle_lib
+
+        orc = oracle_lib.load()
+        bn = b_dev.cpu().numpy()
+        t0 = time.perf_counter()
+        reps = 0
+        while reps < 3 or time.perf_counter() - t0 < 2.0:
+            it, _, _ = orc.cg(p, dim, pen, bn, 1e-12, rel=True)
+            reps += 1
+        dt = (time.perf_counter() - t0) / reps
+        extra["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                                 "sample": "%d solves, %d iterations each" % (reps, it)}
+    line = _base_line(args, "solves/s, 16x16 quads p=4 SIPG-SEM Poisson CG to relative residual 1e-12",
+                      1e3 / r.time_ms, "solves/s", True, "f64",
+                      {"workload": "16x16 quads, p=4 (6400 DoF), pen 16, f = 8 pi^2 sin(2 pi x) sin(2 pi y), x0 = 0"},
+                      **extra)
+    print(json.dumps(line), flush=True)
+    op.close()
+    return 0
+
+
+def run_mixed(args):
+    """512 x 512, p = 6: mixed-precision solve vs the FP64 CG, both to 1e-10."""
+    import torch
+
+    import sipg_gb300 as sipg
+
+    dim, p, pen = 512, 6, 36.0
+    op = sipg.Operator(dim, p, pen)
+    b = op.rhs("sinsin")
+    x64 = torch.zeros_like(b)
+    xm = torch.zeros_like(b)
+    out = {}
+
+    def fp64():
+        x64.zero_()
+        out["r64"] = op.cg(x64, b, 1e-10, relative=True)[1]
+
+    def mixed():
+        xm.zero_()
+        out["st"], out["rm"] = op.solve_mixed(xm, b, 0.1, 1e-10)
+
+    for _ in range(max(1, args.warmup // 3)):
+        fp64()
+        mixed()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    n0 = sipg.launch_count()
+    steps = max(2, min(args.steps, 5))
+    ms64 = _timed(torch, fp64, steps)
+    msm = _timed(torch, mixed, steps)
+    launches = sipg.launch_count() - n0
+    clocks = sampler.stop()
+    r64, rm = out["r64"], out["rm"]
+    e64 = op.err_norms("sinsin", x64)
+    em = op.err_norms("sinsin", xm)
+    diff = float(((xm - x64).norm() / x64.norm()).item())
+    line = _base_line(args, "solves/s to relative residual 1e-10, 512x512 quads p=6, mixed precision", 1e3 / msm,
+                      "solves/s", True, "f32 pairs (inner) + f64 (outer)",
+                      {"workload": "512x512 quads, p=6 (12.8M DoF), pen 36, sin-sin f, x0 = 0, rel. residual 1e-10"},
+                      ms_per_step=msm, fp64={"solves_per_s": 1e3 / ms64, "iterations": r64.iterations,
+                                             "L2": e64[0], "H1": e64[1]},
+                      mixed={"status": out["st"], "inner_kind": ["", "f32", "pairs"][rm.inner_kind],
+                             "inner_iterations": rm.inner_iterations, "fp64_updates": rm.outer_iterations,
+                             "rel_residual": rm.rel_residual, "L2": em[0], "H1": em[1],
+                             "rel_diff_vs_fp64_solution": diff},
+                      speedup_vs_fp64=ms64 / msm, clocks=clocks, gpu_launches=launches)
+    print(json.dumps(line), flush=True)
+    op.close()
+    return 0
+
+
+def _batch_case(torch, sipg, workloads, probs):
+    """Batched mixed solve of `probs` [(dim, p, pen, modes)] vs one-at-a-time FP64."""
+    batch = sipg.Batch([(d, p, pen) for d, p, pen, _ in probs])
+    bs = [batch.op(k).rhs("modes", sipg.Modes.make(*m)) for k, (_, _, _, m) in enumerate(probs)]
+    xs = [torch.zeros_like(b) for b in bs]
+
+    def solve_batch():
+        for x in xs:
+            x.zero_()
+        return batch.solve_mixed(xs, bs)
+
+    solve_batch()  # warm-up: graph capture
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, res = solve_batch()
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    ok = sum(1 for r in res if r.converged)
+    # one at a time, plain FP64 CG (operators reused across equal problems)
+    ops = {}
+    t_seq = 0.0
+    worst = 0.0
+    for k, (d, p, pen, _) in enumerate(probs):
+        key = (d, p, pen)
+        if key not in ops:
+            ops[key] = sipg.Operator(d, p, pen)
+        x = torch.zeros_like(bs[k])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ops[key].cg(x, bs[k], 1e-10, relative=True)
+        torch.cuda.synchronize()
+        t_seq += time.perf_counter() - t0
+        worst = max(worst, float(((xs[k] - x).norm() / max(x.norm().item(), 1e-300)).item()))
+    for op in ops.values():
+        op.close()
+    n = len(probs)
+    out = {"problems": n, "status": st, "converged": ok, "batch_solves_per_s": n / t_batch,
+           "fp64_one_at_a_time_solves_per_s": n / t_seq, "speedup": t_seq / t_batch,
+           "max_rel_diff_vs_fp64": worst, "total_dof": sum(workloads.ndof(d, p) for d, p, _, _ in probs),
+           "inner_iterations_max": max(r.inner_iterations for r in res)}
+    batch.close()
+    return out
+
+
+def run_batch(args):
+    import torch
+
+    import sipg_gb300 as sipg
+    import workloads
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    n0 = sipg.launch_count()
+    a = _batch_case(torch, sipg, workloads, workloads.shared_mesh_rhs(64, 256, 4, seed=1))
+    b = _batch_case(torch, sipg, workloads, workloads.uneven_problems(args.uneven, seed=2))
+    launches = sipg.launch_count() - n0
+    clocks = sampler.stop()
+    line = _base_line(args, "solves/s, batched mixed-precision solves to 1e-10 (64 RHS on 256x256 p=4)",
+                      a["batch_solves_per_s"], "solves/s", True, "f32 pairs (inner) + f64 (outer)",
+                      {"workload": "(a) 64 RHS, 256x256 quads p=4, 4 sine modes each (seed 1); "
+                                   "(b) %d problems, N log-uniform [16,256], p in 2..8 (seed 2)" % args.uneven},
+                      shared_mesh=a, uneven=b, clocks=clocks, gpu_launches=launches)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _serve_stream(sipg, reqs, precision, max_active=256):
+    srv = sipg.Server(budget_bytes=150 << 30, max_active=max_active, iters_per_step=8)
+    pending = list(reqs)
+    inflight = {}
+    lat, failed = [], 0
+    t0 = time.perf_counter()
+    i = 0
+    while i < len(pending) or inflight:
+        now = time.perf_counter() - t0
+        while i < len(pending) and pending[i][0] <= now:
+            _, d, p, pen, m, tol = pending[i]
+            rid, st = srv.submit(d, p, pen, tol, "modes", sipg.Modes.make(*m), precision=precision)
+            if st == 0:
+                inflight[rid] = i
+            else:
+                failed += 1
+            i += 1
+        if not inflight:
+            time.sleep(max(0.0, min(0.01, pending[i][0] - now)) if i < len(pending) else 0)
+            continue
+        srv.step()
+        for rid in list(inflight):
+            r = srv.poll(rid)
+            if r.done:
+                if r.status == 0:
+                    lat.append(r.latency_ms)
+                else:
+                    failed += 1
+                srv.release(rid)
+                del inflight[rid]
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat.sort()
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
+    return {"requests": len(reqs), "completed": len(lat), "failed": failed, "wall_s": wall,
+            "solves_per_s": len(lat) / wall, "p50_ms": q(0.5), "p99_ms": q(0.99), "max_ms": lat[-1] if lat else None}
+
+
+def run_serve(args):
+    import sipg_gb300 as sipg
+    import workloads
+
+    reqs = workloads.request_stream(count=args.requests, rate=args.rate, seed=3)
+    sampler = ClockSampler(0)
+    sampler.start()
+    n0 = sipg.launch_count()
+    mixed = _serve_stream(sipg, reqs, sipg.F32)
+    fp64 = _serve_stream(sipg, reqs, sipg.F64)
+    launches = sipg.launch_count() - n0
+    clocks = sampler.stop()
+    line = _base_line(args, "p99 latency (ms), solve server, mixed precision", mixed["p99_ms"], "ms", False,
+                      "f32 pairs (inner) + f64 (outer)",
+                      {"workload": "%d requests, Poisson arrivals at %g/s, N log-uniform [8,512], p in 2..8, "
+                                   "tol in {1e-8, 1e-10} (seed 3); 150 GB budget" % (args.requests, args.rate)},
+                      mixed=mixed, fp64=fp64, clocks=clocks, gpu_launches=launches)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", choices=("apply", "sweep", "solve16", "mixed", "batch", "serve"), default="apply",
+                    help="apply: the headline (1024x1024 p=4 apply); the others are the solver's other workloads")
+    ap.add_argument("--uneven", type=int, default=200, help="batch: number of uneven problems")
+    ap.add_argument("--requests", type=int, default=200, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=100.0, help="serve: arrivals per second")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config != "apply":
+        import torch
+
+        torch.cuda.set_device(0)
+        return {"sweep": run_sweep, "solve16": run_solve16, "mixed": run_mixed, "batch": run_batch,
+                "serve": run_serve}[args.config](args)
     return run_ours(args)
 
 

@@ -2,17 +2,19 @@
 // reference): many right-hand sides on one mesh, or uneven (dim, p) problems.
 //
 // Every instance keeps its own operator (shared between instances with the
-// same dim, p and penalty), FP32 CG vectors, FP64 residual, device CG states
-// and reduction scratch, resident on the device for the life of the batch.
-// One FP32 CG iteration of the whole batch is one batched apply launch per
-// degree present (k_sipg_apply_batched: the instances' tiles concatenated into
-// one grid) plus one batched update launch (k_cg_update_batched); K iterations
-// are captured once as a CUDA graph and replayed.  The mixed-precision scheme
-// is the reliable-update one of mixed.cu, per instance: an instance whose
-// FP32 residual has fallen by inner_tol stops iterating (its blocks return at
-// once) until the host, between graph replays, folds its correction into x in
-// FP64, recomputes its FP64 residual (batched FP64 applies over the instances
-// that need it) and restarts it -- or retires it once ||b - Ax|| <= outer_tol
+// same dim, p and penalty), inner CG vectors (double-float pairs: the inner
+// kind SIPG_INNER_PAIRS of mixed.cu, which converges at every condition
+// number), FP64 residual, device CG states and reduction scratch, resident on
+// the device for the life of the batch.  One inner iteration of the whole
+// batch is one batched compensated apply launch per degree present
+// (k_sipg_apply_df_batched: the instances' tiles concatenated into one grid)
+// plus one batched update launch (k_cg_update_pairs_batched); K iterations are
+// captured once as a CUDA graph and replayed.  The mixed-precision scheme is
+// the reliable-update one of mixed.cu, per instance: an instance whose inner
+// residual has fallen by inner_tol stops iterating (its blocks return at once)
+// until the host, between graph replays, folds its correction into x in FP64,
+// recomputes its FP64 residual (batched FP64 applies over the instances that
+// need it) and restarts it -- or retires it once ||b - Ax|| <= outer_tol
 // ||b||.  Converged instances retire mid-batch while the others go on.
 #include <algorithm>
 #include <cmath>
@@ -21,7 +23,7 @@
 #include <tuple>
 #include <vector>
 
-#include "sipg_cg.cuh"
+#include "sipg_cg_df.cuh"
 
 using namespace sipg;
 
@@ -31,15 +33,16 @@ struct MixedInst {
   double* x64;
   const double* b64;
   double* r64;
-  float* e32;
-  float* r32;
-  CgState<float>* st32;
+  float* r32;  // pair vectors
+  float* e;
+  CgState<double>* st32;  // the inner state (FP64 scalars)
   CgState<double>* st64;
   ReduceScratch red32;
   ReduceScratch red64;
   size_t n;
   int first;
-  float delta;
+  double delta;
+  double stop;  // the outer target in inner residual units
   int max_it;
   int nblk;  // blocks this instance uses (see VecInst)
 };
@@ -51,50 +54,20 @@ __global__ void __launch_bounds__(kVecThreads) k_batch_norm_b(const MixedInst* _
   cg_init_body<double>(m.b64, m.n, m.st64, 0.0, 0, 1, m.red64, blockIdx.x, m.nblk);
 }
 
-// r32 = (float) r64, e = 0, FP32 CG state for the next run (see k_mixed_restart)
+// inner residual = r64 as pairs, e = 0, inner CG state for the next run (see
+// inner_restart_body)
 __global__ void __launch_bounds__(kVecThreads) k_batch_restart(const MixedInst* __restrict__ insts) {
-  __shared__ float sh[32];
   const MixedInst m = insts[blockIdx.y];
   if ((int)blockIdx.x >= m.nblk) return;
-  float acc = 0.f;
-  const size_t stride = (size_t)m.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-    const float v = (float)m.r64[i];
-    m.r32[i] = v;
-    m.e32[i] = 0.f;
-    acc = fmaf(v, v, acc);
-  }
-  const float bt = block_sum<float, kVecThreads>(acc, sh);
-  float total;
-  if (grid_sum_last<float, kVecThreads>(bt, m.red32, blockIdx.x, m.nblk, sh, &total) && threadIdx.x == 0) {
-    CgState<float>* st = m.st32;
-    if (m.first) {
-      st->first = 1;
-      st->it = 0;
-      st->parity = 0;
-      st->beta = 0.f;
-      st->status = (int)SIPG_OK;
-    } else {
-      st->beta = total / st->rr;
-      st->first = 0;
-    }
-    st->rr = total;
-    st->rmax = sqrtf(total);
-    st->delta = m.delta;
-    st->stop = 0.f;
-    st->max_it = st->it + m.max_it;  // a correction is forced after max_it more iterations
-    st->need_update = 0;
-    st->done = 0;
-  }
+  inner_restart_body<INNER_PAIRS>(m.r64, m.r32, m.e, m.n, m.st32, m.red32, m.first, m.delta, m.stop, m.max_it,
+                                  blockIdx.x, m.nblk);
 }
 
-// x64 += e32
+// x64 += e
 __global__ void __launch_bounds__(kVecThreads) k_batch_fold(const MixedInst* __restrict__ insts) {
   const MixedInst m = insts[blockIdx.y];
   if ((int)blockIdx.x >= m.nblk) return;
-  const size_t stride = (size_t)m.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-    m.x64[i] += (double)m.e32[i];
+  inner_fold_body<INNER_PAIRS>(m.x64, m.e, m.n, blockIdx.x, m.nblk);
 }
 
 // park instances: the FP32 iterations skip them
@@ -116,24 +89,24 @@ struct BInst {
   sipg_op* op = nullptr;
   size_t n = 0;
   double* r64 = nullptr;
-  float* e32 = nullptr;
-  float* r32 = nullptr;
+  float* r32 = nullptr;  // pair vectors (2 n floats) from here
+  float* e = nullptr;
   float* p0 = nullptr;
   float* p1 = nullptr;
   float* Ap = nullptr;
-  CgState<float>* st32 = nullptr;
+  CgState<double>* st32 = nullptr;  // inner state
   CgState<double>* st64 = nullptr;
   ReduceScratch red32, red64;
-  int tiles32 = 0, tiles64 = 0;
+  int tilesdf = 0, tiles64 = 0;
 };
 
 struct BGroup {
   int p = 0;
   std::vector<int> members;
-  TileCfg cfg32, cfg64;
-  ApplyArgs<float>* d_cg = nullptr;  // all members, FP32 CG mode
-  int* d_tiles32 = nullptr;
-  int total32 = 0;
+  TileCfg cfgdf, cfg64;
+  ApplyArgs<float>* d_cg = nullptr;  // all members, compensated FP32 CG mode
+  int* d_tilesdf = nullptr;
+  int totaldf = 0;
   ApplyArgs<double>* d_res = nullptr;  // a subset, FP64 residual mode (rebuilt per round)
   int* d_tiles64 = nullptr;
 };
@@ -147,12 +120,12 @@ struct sipg_batch {
   std::vector<BInst> inst;
   std::vector<BGroup> groups;
   std::vector<sipg_op*> owned;
-  VecInst<float>* d_vec = nullptr;
+  PairInst* d_vec = nullptr;
   MixedInst* d_sel = nullptr;  // selection list (capacity n)
   MixedInst* h_sel = nullptr;  // pinned
   ApplyArgs<double>* h_res = nullptr;  // pinned staging for FP64 residual args
   int* h_tiles = nullptr;              // pinned staging for tile starts
-  CgState<float>* h_st32 = nullptr;    // pinned mirrors, n each
+  CgState<double>* h_st32 = nullptr;   // pinned mirrors, n each
   CgState<double>* h_st64 = nullptr;
   cudaStream_t cap = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -166,8 +139,8 @@ static void batch_free(sipg_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   for (BInst& i : b->inst) {
     cudaFree(i.r64);
-    cudaFree(i.e32);
     cudaFree(i.r32);
+    cudaFree(i.e);
     cudaFree(i.p0);
     cudaFree(i.p1);
     cudaFree(i.Ap);
@@ -180,7 +153,7 @@ static void batch_free(sipg_batch* b) {
   }
   for (BGroup& g : b->groups) {
     cudaFree(g.d_cg);
-    cudaFree(g.d_tiles32);
+    cudaFree(g.d_tilesdf);
     cudaFree(g.d_res);
     cudaFree(g.d_tiles64);
   }
@@ -204,15 +177,16 @@ static sipg_status batch_alloc(sipg_batch* b) {
   for (const BInst& i : b->inst) b->bpi = std::max(b->bpi, inst_blocks(i.n));
   for (BInst& i : b->inst) {
     const int cap = reduce_capacity(i.dim);
+    const size_t pair_bytes = 2 * i.n * sizeof(float);
     SIPG_CUDA_TRY(cudaMalloc(&i.r64, i.n * sizeof(double)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.e32, i.n * sizeof(float)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.r32, i.n * sizeof(float)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.p0, i.n * sizeof(float)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.p1, i.n * sizeof(float)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.Ap, i.n * sizeof(float)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.st32, sizeof(CgState<float>)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.r32, pair_bytes));
+    SIPG_CUDA_TRY(cudaMalloc(&i.e, pair_bytes));
+    SIPG_CUDA_TRY(cudaMalloc(&i.p0, pair_bytes));
+    SIPG_CUDA_TRY(cudaMalloc(&i.p1, pair_bytes));
+    SIPG_CUDA_TRY(cudaMalloc(&i.Ap, pair_bytes));
+    SIPG_CUDA_TRY(cudaMalloc(&i.st32, sizeof(CgState<double>)));
     SIPG_CUDA_TRY(cudaMalloc(&i.st64, sizeof(CgState<double>)));
-    SIPG_CUDA_TRY(cudaMemset(i.st32, 0, sizeof(CgState<float>)));
+    SIPG_CUDA_TRY(cudaMemset(i.st32, 0, sizeof(CgState<double>)));
     SIPG_CUDA_TRY(cudaMemset(i.st64, 0, sizeof(CgState<double>)));
     ReduceScratch* reds[2] = {&i.red32, &i.red64};
     for (ReduceScratch* r : reds) {
@@ -230,7 +204,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
       gidx[p] = (int)b->groups.size();
       BGroup g;
       g.p = p;
-      g.cfg32 = b->inst[k].op->cfg32;
+      g.cfgdf = b->inst[k].op->cfgdf;
       g.cfg64 = b->inst[k].op->cfg64;
       b->groups.push_back(g);
     }
@@ -242,7 +216,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
     std::vector<int> ts(m + 1, 0);
     for (int j = 0; j < m; ++j) {
       BInst& i = b->inst[g.members[j]];
-      i.tiles32 = tiles_of(i.dim, g.cfg32);
+      i.tilesdf = tiles_of(i.dim, g.cfgdf);
       i.tiles64 = tiles_of(i.dim, g.cfg64);
       ApplyArgs<float> a{};
       a.in = i.r32;
@@ -251,24 +225,25 @@ static sipg_status batch_alloc(sipg_batch* b) {
       a.out = i.Ap;
       a.dim = i.dim;
       a.nu = (float)i.pen;
-      a.st = i.st32;
+      a.nu_lo = (float)(i.pen - (double)a.nu);
+      a.stp = i.st32;
       a.red = i.red32;
       args[j] = a;
-      ts[j + 1] = ts[j] + i.tiles32;
+      ts[j + 1] = ts[j] + i.tilesdf;
     }
-    g.total32 = ts[m];
+    g.totaldf = ts[m];
     SIPG_CUDA_TRY(cudaMalloc(&g.d_cg, sizeof(ApplyArgs<float>) * m));
-    SIPG_CUDA_TRY(cudaMalloc(&g.d_tiles32, sizeof(int) * (m + 1)));
+    SIPG_CUDA_TRY(cudaMalloc(&g.d_tilesdf, sizeof(int) * (m + 1)));
     SIPG_CUDA_TRY(cudaMalloc(&g.d_res, sizeof(ApplyArgs<double>) * m));
     SIPG_CUDA_TRY(cudaMalloc(&g.d_tiles64, sizeof(int) * (m + 1)));
     SIPG_CUDA_TRY(cudaMemcpy(g.d_cg, args.data(), sizeof(ApplyArgs<float>) * m, cudaMemcpyHostToDevice));
-    SIPG_CUDA_TRY(cudaMemcpy(g.d_tiles32, ts.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+    SIPG_CUDA_TRY(cudaMemcpy(g.d_tilesdf, ts.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
   }
-  std::vector<VecInst<float>> vec(n);
+  std::vector<PairInst> vec(n);
   for (int k = 0; k < n; ++k) {
     BInst& i = b->inst[k];
-    VecInst<float> v;
-    v.x = i.e32;
+    PairInst v;
+    v.x = i.e;
     v.pb0 = i.p0;
     v.pb1 = i.p1;
     v.r = i.r32;
@@ -280,13 +255,13 @@ static sipg_status batch_alloc(sipg_batch* b) {
     v.pad = 0;
     vec[k] = v;
   }
-  SIPG_CUDA_TRY(cudaMalloc(&b->d_vec, sizeof(VecInst<float>) * n));
-  SIPG_CUDA_TRY(cudaMemcpy(b->d_vec, vec.data(), sizeof(VecInst<float>) * n, cudaMemcpyHostToDevice));
+  SIPG_CUDA_TRY(cudaMalloc(&b->d_vec, sizeof(PairInst) * n));
+  SIPG_CUDA_TRY(cudaMemcpy(b->d_vec, vec.data(), sizeof(PairInst) * n, cudaMemcpyHostToDevice));
   SIPG_CUDA_TRY(cudaMalloc(&b->d_sel, sizeof(MixedInst) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_sel, sizeof(MixedInst) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_res, sizeof(ApplyArgs<double>) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_tiles, sizeof(int) * (n + 1)));
-  SIPG_CUDA_TRY(cudaMallocHost(&b->h_st32, sizeof(CgState<float>) * n));
+  SIPG_CUDA_TRY(cudaMallocHost(&b->h_st32, sizeof(CgState<double>) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_st64, sizeof(CgState<double>) * n));
   SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   SIPG_CUDA_TRY(cudaEventCreate(&b->ev0));
@@ -302,19 +277,19 @@ static sipg_status batch_alloc(sipg_batch* b) {
 static sipg_status batch_capture(sipg_batch* b) {
   if (b->exec) return SIPG_OK;
   for (BGroup& g : b->groups)
-    SIPG_CUDA_TRY(launch_apply_batched_f32(g.p, g.cfg32, APPLY_PREPARE, nullptr, nullptr, 0, 0,
-                                           b->inst[g.members[0]].op->tab, b->cap));
+    SIPG_CUDA_TRY(launch_apply_df(g.p, g.cfgdf, APPLY_PREPARE, ApplyArgs<float>{}, nullptr, nullptr, 0, 0,
+                                  b->inst[g.members[0]].op->tab, b->cap));
   cudaGraph_t graph = nullptr;
   SIPG_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int k = 0; k < b->K && err == cudaSuccess; ++k) {
     for (BGroup& g : b->groups) {
-      err = launch_apply_batched_f32(g.p, g.cfg32, APPLY_CG, g.d_cg, g.d_tiles32, (int)g.members.size(), g.total32,
-                                     b->inst[g.members[0]].op->tab, b->cap);
+      err = launch_apply_df(g.p, g.cfgdf, APPLY_CG, ApplyArgs<float>{}, g.d_cg, g.d_tilesdf, (int)g.members.size(),
+                            g.totaldf, b->inst[g.members[0]].op->tab, b->cap);
       if (err != cudaSuccess) break;
     }
     if (err != cudaSuccess) break;
-    k_cg_update_batched<float><<<dim3(b->bpi, b->n), kVecThreads, 0, b->cap>>>(b->d_vec);
+    k_cg_update_pairs_batched<<<dim3(b->bpi, b->n), kVecThreads, 0, b->cap>>>(b->d_vec);
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(b->cap, &graph);
@@ -366,7 +341,7 @@ static sipg_status batch_residuals(sipg_batch* b, const std::vector<int>& sel, d
 }
 
 static int fill_sel(sipg_batch* b, const std::vector<int>& sel, double* const* d_x, const double* const* d_b,
-                    int first, float delta, int max_it) {
+                    int first, double delta, const std::vector<double>& stop, int max_it) {
   int m = 0;
   for (int k : sel) {
     BInst& i = b->inst[k];
@@ -374,7 +349,7 @@ static int fill_sel(sipg_batch* b, const std::vector<int>& sel, double* const* d
     mi.x64 = d_x[k];
     mi.b64 = d_b[k];
     mi.r64 = i.r64;
-    mi.e32 = i.e32;
+    mi.e = i.e;
     mi.r32 = i.r32;
     mi.st32 = i.st32;
     mi.st64 = i.st64;
@@ -383,6 +358,7 @@ static int fill_sel(sipg_batch* b, const std::vector<int>& sel, double* const* d
     mi.n = i.n;
     mi.first = first;
     mi.delta = delta;
+    mi.stop = stop[k];
     mi.max_it = max_it;
     mi.nblk = inst_blocks(i.n);
     b->h_sel[m++] = mi;
@@ -451,7 +427,7 @@ sipg_status sipg_batch_op(const sipg_batch* b, int i, sipg_op** op) {
 size_t sipg_batch_footprint(const sipg_batch* b) {
   if (!b) return 0;
   size_t bytes = 0;
-  for (const BInst& i : b->inst) bytes += i.n * (8 + 5 * 4) + 2 * sizeof(double) * reduce_capacity(i.dim);
+  for (const BInst& i : b->inst) bytes += i.n * (8 + 5 * 8) + 2 * sizeof(double) * reduce_capacity(i.dim);
   return bytes;
 }
 
@@ -485,7 +461,8 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
   for (int k = 0; k < n; ++k) max_inner[k] = o.max_inner > 0 ? o.max_inner : (long long)b->inst[k].n;
 
   // ||b|| of every instance, and park every FP32 state
-  int m = fill_sel(b, all, d_x, d_b, 1, (float)o.inner_tol, 0);
+  std::vector<double> stop(n, 0.0);
+  int m = fill_sel(b, all, d_x, d_b, 1, o.inner_tol, stop, 0);
   SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
   k_batch_norm_b<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
   k_batch_park<<<(m + 127) / 128, 128, 0, s>>>(b->d_sel, m);
@@ -494,7 +471,10 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
   for (int k = 0; k < n; ++k)
     SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st64 + k, b->inst[k].st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-  for (int k = 0; k < n; ++k) bnorm[k] = std::sqrt(b->h_st64[k].bb);
+  for (int k = 0; k < n; ++k) {
+    bnorm[k] = std::sqrt(b->h_st64[k].bb);
+    stop[k] = 0.5 * o.outer_tol * (bnorm[k] > 0 ? bnorm[k] : 1.0);
+  }
 
   std::vector<int> sel = all;
   bool first_round = true;
@@ -530,7 +510,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
       for (int pass = 0; pass < 2; ++pass) {
         const std::vector<int>& list = pass ? restart_cont : restart_first;
         if (list.empty()) continue;
-        m = fill_sel(b, list, d_x, d_b, pass ? 0 : 1, (float)o.inner_tol, 1000);
+        m = fill_sel(b, list, d_x, d_b, pass ? 0 : 1, o.inner_tol, stop, 1000);
         SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
         k_batch_restart<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
         count_launch();
@@ -547,7 +527,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     unsigned long long per_iter = (unsigned long long)b->groups.size() + 1;
     count_launch(per_iter * b->K);
     for (int k = 0; k < n; ++k)
-      SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st32 + k, b->inst[k].st32, sizeof(CgState<float>), cudaMemcpyDeviceToHost, s));
+      SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st32 + k, b->inst[k].st32, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(s));
     sel.clear();
     for (int k = 0; k < n; ++k) {
@@ -560,12 +540,12 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
       sel.push_back(k);
     }
     if (!sel.empty()) {
-      m = fill_sel(b, sel, d_x, d_b, 0, (float)o.inner_tol, 0);
+      m = fill_sel(b, sel, d_x, d_b, 0, o.inner_tol, stop, 0);
       SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
       k_batch_fold<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
-      SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+      SIPG_CUDA_TRY(cudaStreamSynchronize(s));  // h_sel is reused
       for (int k : sel) corrections[k] += 1;
     }
   }

@@ -63,6 +63,23 @@ cudaError_t launch_apply_f32_p8(const TileCfg&, int, const ApplyArgs<float>&, co
 cudaError_t launch_apply_batched_f32_p8(const TileCfg&, int, const ApplyArgs<float>*, const int*, int, int,
                                           const HostTables&, cudaStream_t);
 
+cudaError_t launch_apply_df_p1(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p2(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p3(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p4(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p5(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p6(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p7(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+cudaError_t launch_apply_df_p8(const TileCfg&, int, const ApplyArgs<float>&, const ApplyArgs<float>*, const int*, int, int,
+                                 const HostTables&, cudaStream_t);
+
 #define SIPG_DISPATCH_P(FN, P, ...) \
   switch (P) {                      \
     case 1: return FN##_p1(__VA_ARGS__); \
@@ -83,6 +100,10 @@ cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArg
 cudaError_t launch_apply_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const HostTables& h,
                              cudaStream_t s) {
   SIPG_DISPATCH_P(launch_apply_f32, p, cfg, mode, a, h, s)
+}
+cudaError_t launch_apply_df(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const ApplyArgs<float>* insts,
+                            const int* tile_start, int ninst, int total_tiles, const HostTables& h, cudaStream_t s) {
+  SIPG_DISPATCH_P(launch_apply_df, p, cfg, mode, a, insts, tile_start, ninst, total_tiles, h, s)
 }
 cudaError_t launch_apply_batched_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,
                                      const int* tile_start, int ninst, int total_tiles, const HostTables& h,
@@ -144,6 +165,7 @@ struct sipg_cg_workspace {
   cudaGraphExec_t exec = nullptr;
   const void* exec_x = nullptr;
   int exec_k = 0;
+  int exec_gen = -1;  // the op's tile generation the graph was captured with
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -212,7 +234,7 @@ static int graph_iters(long long ndof) { return ndof <= (1LL << 20) ? 32 : 8; }
 // the parity kept in the device state, so a chunk may stop at any iteration).
 template <typename T>
 static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, int K) {
-  if (w->exec && w->exec_x == x && w->exec_k == K) return SIPG_OK;
+  if (w->exec && w->exec_x == x && w->exec_k == K && w->exec_gen == op->tile_gen) return SIPG_OK;
   if (w->exec) {
     cudaGraphExecDestroy(w->exec);
     w->exec = nullptr;
@@ -258,6 +280,7 @@ static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, i
   }
   w->exec_x = x;
   w->exec_k = K;
+  w->exec_gen = op->tile_gen;
   return SIPG_OK;
 }
 
@@ -323,33 +346,6 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   return conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED;
 }
 
-namespace sipg {
-
-sipg_status cg_f32_prepare(sipg_op* op, float* x, CgF32View* v) {
-  sipg_cg_workspace* w = nullptr;
-  sipg_status st = ws_get<float>(op, &w);
-  if (st != SIPG_OK) return st;
-  st = capture_iterations<float>(op, w, x, graph_iters(op->ndof));
-  if (st != SIPG_OK) return st;
-  v->r = (float*)w->r;
-  v->st = (CgState<float>*)w->st;
-  return SIPG_OK;
-}
-
-sipg_status cg_f32_launch_chunk(sipg_op* op, cudaStream_t s, CgState<float>* host_state) {
-  sipg_cg_workspace* w = op->ws32;
-  if (!w || !w->exec) {
-    set_error("cg_f32_launch_chunk: no FP32 iteration graph");
-    return SIPG_ERR_INVALID;
-  }
-  SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
-  count_launch(2ULL * w->exec_k);
-  SIPG_CUDA_TRY(cudaMemcpyAsync(host_state, w->st, sizeof(CgState<float>), cudaMemcpyDeviceToHost, s));
-  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-  return SIPG_OK;
-}
-
-}  // namespace sipg
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -447,6 +443,12 @@ sipg_status sipg_op_create(int dim, int degree, double pen, sipg_op** out) {
   build_host_tables(degree, &op->tab);
   op->cfg64 = default_cfg(degree, true);
   op->cfg32 = default_cfg(degree, false);
+  op->cfgdf.tx = 32;
+  op->cfgdf.ty = 4;
+  // shapes the autotuner already chose for this (degree, dim) in this process
+  autotune_lookup(degree, dim, SIPG_TUNE_F64, &op->cfg64);
+  autotune_lookup(degree, dim, SIPG_TUNE_F32, &op->cfg32);
+  autotune_lookup(degree, dim, SIPG_TUNE_PAIRS, &op->cfgdf);
   *out = op;
   return SIPG_OK;
 }
@@ -456,6 +458,7 @@ sipg_status sipg_op_destroy(sipg_op* op) {
   cudaSetDevice(op->device);
   ws_free(op->ws64);
   ws_free(op->ws32);
+  if (op->mixed_free) op->mixed_free(op->mixed);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
   delete op;
@@ -494,6 +497,21 @@ sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, v
   a.dim = op->dim;
   a.nu = (float)op->pen;
   SIPG_CUDA_TRY(launch_apply<float>(op, APPLY_PLAIN, a, (cudaStream_t)stream));
+  return SIPG_OK;
+}
+
+sipg_status sipg_apply_pairs(const sipg_op* op, const float* d_in, float* d_out, void* stream) {
+  if (!op || !d_in || !d_out || d_in == d_out) {
+    set_error("sipg_apply_pairs: null or aliased vectors");
+    return SIPG_ERR_INVALID;
+  }
+  ApplyArgs<float> a{};
+  a.in = d_in;
+  a.out = d_out;
+  a.dim = op->dim;
+  a.nu = (float)op->pen;
+  a.nu_lo = (float)(op->pen - (double)a.nu);
+  SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_PLAIN, a, nullptr, nullptr, 0, 0, op->tab, (cudaStream_t)stream));
   return SIPG_OK;
 }
 

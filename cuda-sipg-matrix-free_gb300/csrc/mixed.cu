@@ -1,94 +1,152 @@
-// mixed.cu -- FP32 CG inside FP64 defect correction (no counterpart in the
-// reference), with reliable updates.
+// mixed.cu -- the mixed-precision solve (no counterpart in the reference):
+// an inner CG on the FP32 pipes inside FP64 defect correction with reliable
+// updates.
 //
-// The FP64 part: x (the solution), b, the true residual r = b - A x (fused
-// FP64 apply, APPLY_RESID) and the outer norms, all on the device.  The FP32
-// part: the CG iteration itself (fused FP32 apply and update, graph-captured)
-// on a correction e ~ A^-1 r.  Whenever the FP32 iterated residual has fallen
-// by `inner_tol` relative to its largest value since the last correction
-// (sqrt(r32.r32) < inner_tol * rmax), the correction is folded into x in FP64
-// (x += e), r is recomputed in FP64 and rounded into the FP32 residual, and the
-// FP32 CG *continues with its search direction* (beta = r_new.r_new / r_old.r_old):
-// the reliable-update scheme of Sleijpen & van der Vorst (1996), as used for
-// mixed-precision CG on GPUs by Clark et al. (2010).  Restarting the FP32 CG
-// from scratch at every correction instead (classic iterative refinement)
-// loses the Krylov space and, on this operator (condition number ~ p^4 / h^2),
-// needs two orders of magnitude more FP32 iterations.
+// FP64 part: the solution x, b, the true residual r = b - A x (fused FP64
+// apply, APPLY_RESID) and the outer norms, all on the device.  Inner part: a
+// CG on the correction e ~ A^-1 r in one of two formats (sipg_inner_kind):
+//   * INNER_F32: FP32 vectors and the FP32 apply;
+//   * INNER_PAIRS: double-float pair vectors (two FP32 planes) and the
+//     compensated apply (sipg_apply_df.cuh) -- FP32 instructions only, ~48
+//     significant bits.
+// FP32 vectors fail on this operator once its condition number approaches
+// 1 / eps_32: the rounding noise of a smooth FP32 vector is spread over all
+// frequencies, A amplifies it by up to kappa, and each step's correction then
+// carries a residual error as large as the residual it removes (measured: 512
+// x 512, p = 6, kappa ~ 2e7, no convergence in 190,000 FP32 iterations).
+// Pairs push that limit to kappa ~ 1e12.
+//
+// Whenever the inner residual has fallen by `inner_tol` relative to its
+// largest value since the last update (sqrt(r.r) < inner_tol * rmax) or after
+// kCorrectEvery inner iterations, e is folded into x in FP64, r is recomputed
+// in FP64 and rounded into the inner residual, and the inner CG *continues
+// with its search direction* (beta = r_new.r_new / r_prev.r_prev): the
+// reliable-update scheme of Sleijpen & van der Vorst (1996), as used for
+// mixed-precision CG on GPUs by Clark et al. (2010).
 #include <cmath>
 #include <new>
 
-#include "sipg_cg.cuh"
+#include "sipg_apply_df.cuh"
+#include "sipg_cg_df.cuh"
 
 using namespace sipg;
 
 namespace sipg {
-// FP32 iterations after which an FP64 correction is forced
+// inner iterations after which an FP64 update is forced
 constexpr int kCorrectEvery = 1000;
 
-cudaError_t launch_apply_f64(int p, const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
-                             cudaStream_t s);
-
-// r32 = (float) r64, e = 0, and the FP32 CG state for the next run of
-// iterations: on the first call p = r; afterwards beta = r_new.r_new / r_old.r_old.
+template <int KIND>
 __global__ void __launch_bounds__(kVecThreads)
-    k_mixed_restart(const double* __restrict__ r64, float* __restrict__ r32, float* __restrict__ e, size_t n,
-                    CgState<float>* st, ReduceScratch red, int first, float delta, int max_it) {
-  __shared__ float sh[32];
-  float acc = 0.f;
+    k_mixed_restart(const double* __restrict__ r64, float* __restrict__ r, float* __restrict__ e, size_t n,
+                    CgState<typename InnerScalar<KIND>::type>* st, ReduceScratch red, int first, double delta,
+                    double stop, int max_it) {
+  inner_restart_body<KIND>(r64, r, e, n, st, red, first, delta, stop, max_it, blockIdx.x, gridDim.x);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kVecThreads) k_mixed_fold(double* __restrict__ x, const float* __restrict__ e,
+                                                            size_t n) {
+  inner_fold_body<KIND>(x, e, n, blockIdx.x, gridDim.x);
+}
+
+// the FP64 kind: r = r64, e = 0, state as inner_restart_body
+__global__ void __launch_bounds__(kVecThreads)
+    k_mixed_restart_f64(const double* __restrict__ r64, double* __restrict__ r, double* __restrict__ e, size_t n,
+                        CgState<double>* st, ReduceScratch red, int first, double delta, double stop, int max_it) {
+  __shared__ double sh[32];
+  double acc = 0.0;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const float v = (float)r64[i];
-    r32[i] = v;
-    e[i] = 0.f;
-    acc = fmaf(v, v, acc);
+    const double v = r64[i];
+    r[i] = v;
+    e[i] = 0.0;
+    acc = fma(v, v, acc);
   }
-  const float bt = block_sum<float, kVecThreads>(acc, sh);
-  float total;
-  if (grid_sum_last<float, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
+  const double bt = block_sum<double, kVecThreads>(acc, sh);
+  double total;
+  if (grid_sum_last<double, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
     if (first) {
       st->first = 1;
       st->it = 0;
       st->parity = 0;
-      st->beta = 0.f;
+      st->beta = 0.0;
       st->status = (int)SIPG_OK;
     } else {
-      st->beta = total / st->rr;
+      st->beta = total / st->rr_prev;
       st->first = 0;
     }
     st->rr = total;
-    st->rmax = sqrtf(total);
+    st->rmax = sqrt(total);
     st->delta = delta;
-    st->stop = 0.f;  // the FP32 loop stops only for corrections, breakdown or max_it
-    // a correction is forced after max_it more FP32 iterations even if the
-    // residual stagnates above delta * rmax (FP32 rounding floor)
+    st->stop = stop;
     st->max_it = st->it + max_it;
     st->need_update = 0;
-    st->done = 0;
+    st->done = (total == 0.0) ? 1 : 0;
   }
 }
 
-__global__ void __launch_bounds__(kVecThreads) k_fold_correction(double* __restrict__ x, const float* __restrict__ e,
-                                                                 size_t n) {
+__global__ void __launch_bounds__(kVecThreads) k_mixed_fold_f64(double* __restrict__ x, const double* __restrict__ e,
+                                                                size_t n) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) x[i] += (double)e[i];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) x[i] += e[i];
+}
+
+// Condition-number estimate kappa ~ c_p dim^2 (penalty p^2; grows with larger
+// penalties), from the extreme eigenvalues of the assembled operator at
+// dim = 8 (the ratio kappa(8) / kappa(4) is 3.9-4.0 for every p).
+double kappa_estimate(int p, int dim, double pen) {
+  static const double c[9] = {0, 0.81, 4.76, 12.0, 25.9, 45.7, 75.6, 114.1, 167.1};
+  const double pp = (double)p * p;
+  const double scale = pen > pp ? pen / pp : 1.0;
+  return c[p < 1 ? 1 : (p > 8 ? 8 : p)] * (double)dim * dim * scale;
+}
+
+int choose_inner(int requested, int p, int dim, double pen) {
+  if (requested == SIPG_INNER_F32 || requested == SIPG_INNER_PAIRS || requested == SIPG_INNER_F64) return requested;
+  return kappa_estimate(p, dim, pen) * std::ldexp(1.0, -24) < 0.01 ? SIPG_INNER_F32 : SIPG_INNER_PAIRS;
 }
 }  // namespace sipg
 
 namespace {
-struct MixedWorkspace {
+// Everything one mixed solve on an op needs on the device, kept in the op
+// between solves.  Inner vectors are 8 n bytes (pairs: 2 n floats; FP64: n
+// doubles; FP32: the first n floats); one K-iteration graph per inner kind
+// (its kernels read x only through the fold, outside the graph).
+struct MixedCache {
+  size_t n = 0;
   double* r64 = nullptr;
-  float* e32 = nullptr;
+  float* r = nullptr;
+  float* e = nullptr;
+  float* p[2] = {nullptr, nullptr};
+  float* Ap = nullptr;
   CgState<double>* st64 = nullptr;
+  CgState<float>* st32 = nullptr;   // inner state, FP32 kind
+  CgState<double>* stp = nullptr;   // inner state, pairs kind
   CgState<double>* st64_host = nullptr;
   CgState<float>* st32_host = nullptr;
-  ReduceScratch red64, red32;
+  CgState<double>* stp_host = nullptr;
+  ReduceScratch red64{}, red32{};
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
+  int exec_k[4] = {0, 0, 0, 0};
+  int exec_gen[4] = {-1, -1, -1, -1};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  ~MixedWorkspace() {
+  ~MixedCache() {
+    for (cudaGraphExec_t g : exec)
+      if (g) cudaGraphExecDestroy(g);
+    if (cap) cudaStreamDestroy(cap);
     cudaFree(r64);
-    cudaFree(e32);
+    cudaFree(r);
+    cudaFree(e);
+    cudaFree(p[0]);
+    cudaFree(p[1]);
+    cudaFree(Ap);
     cudaFree(st64);
+    cudaFree(st32);
+    cudaFree(stp);
     cudaFreeHost(st64_host);
     cudaFreeHost(st32_host);
+    cudaFreeHost(stp_host);
     cudaFree(red64.partials);
     cudaFree(red64.counter);
     cudaFree(red32.partials);
@@ -98,22 +156,132 @@ struct MixedWorkspace {
   }
 };
 
-sipg_status alloc_workspace(MixedWorkspace& m, size_t n, int cap, cudaStream_t s) {
+void mixed_cache_free(void* p) { delete static_cast<MixedCache*>(p); }
+
+int vec_grid(size_t n) {
+  return (int)std::max<size_t>(1, std::min<size_t>((n + kVecThreads - 1) / kVecThreads, 152 * 8));
+}
+
+sipg_status cache_alloc(MixedCache& m, size_t n, int cap) {
+  m.n = n;
+  const size_t pair_bytes = 2 * n * sizeof(float);
   SIPG_CUDA_TRY(cudaMalloc(&m.r64, n * sizeof(double)));
-  SIPG_CUDA_TRY(cudaMalloc(&m.e32, n * sizeof(float)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.r, pair_bytes));
+  SIPG_CUDA_TRY(cudaMalloc(&m.e, pair_bytes));
+  SIPG_CUDA_TRY(cudaMalloc(&m.p[0], pair_bytes));
+  SIPG_CUDA_TRY(cudaMalloc(&m.p[1], pair_bytes));
+  SIPG_CUDA_TRY(cudaMalloc(&m.Ap, pair_bytes));
   SIPG_CUDA_TRY(cudaMalloc(&m.st64, sizeof(CgState<double>)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.st32, sizeof(CgState<float>)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.stp, sizeof(CgState<double>)));
   SIPG_CUDA_TRY(cudaMallocHost(&m.st64_host, sizeof(CgState<double>)));
   SIPG_CUDA_TRY(cudaMallocHost(&m.st32_host, sizeof(CgState<float>)));
+  SIPG_CUDA_TRY(cudaMallocHost(&m.stp_host, sizeof(CgState<double>)));
   ReduceScratch* reds[2] = {&m.red64, &m.red32};
   for (ReduceScratch* r : reds) {
     SIPG_CUDA_TRY(cudaMalloc(&r->partials, sizeof(double) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&r->counter, sizeof(unsigned int)));
-    SIPG_CUDA_TRY(cudaMemsetAsync(r->counter, 0, sizeof(unsigned int), s));
+    SIPG_CUDA_TRY(cudaMemset(r->counter, 0, sizeof(unsigned int)));
     r->capacity = cap;
   }
-  SIPG_CUDA_TRY(cudaMemsetAsync(m.st64, 0, sizeof(CgState<double>), s));
+  SIPG_CUDA_TRY(cudaMemset(m.st64, 0, sizeof(CgState<double>)));
+  SIPG_CUDA_TRY(cudaMemset(m.st32, 0, sizeof(CgState<float>)));
+  SIPG_CUDA_TRY(cudaMemset(m.stp, 0, sizeof(CgState<double>)));
+  SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&m.cap, cudaStreamNonBlocking));
   SIPG_CUDA_TRY(cudaEventCreate(&m.ev0));
   SIPG_CUDA_TRY(cudaEventCreate(&m.ev1));
+  return SIPG_OK;
+}
+
+sipg_status cache_get(sipg_op* op, MixedCache** out) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (!op->mixed) {
+    MixedCache* m = new (std::nothrow) MixedCache;
+    if (!m) return SIPG_ERR_NOMEM;
+    const sipg_status st = cache_alloc(*m, (size_t)op->ndof, reduce_capacity(op->dim));
+    if (st != SIPG_OK) {
+      delete m;
+      return st;
+    }
+    op->mixed = m;
+    op->mixed_free = mixed_cache_free;
+  }
+  *out = static_cast<MixedCache*>(op->mixed);
+  return SIPG_OK;
+}
+
+// One inner iteration: apply in CG mode (p = r + beta p_old, A p, p.Ap,
+// alpha), then e += alpha p, r -= alpha Ap, r.r, beta, stop test.
+sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t s) {
+  ApplyArgs<float> a{};
+  a.in = m.r;
+  a.pbuf0 = m.p[0];
+  a.pbuf1 = m.p[1];
+  a.out = m.Ap;
+  a.dim = op->dim;
+  a.nu = (float)op->pen;
+  a.st = m.st32;
+  a.red = m.red32;
+  if (kind == SIPG_INNER_F64) {
+    ApplyArgs<double> d{};
+    d.in = (const double*)m.r;
+    d.pbuf0 = (double*)m.p[0];
+    d.pbuf1 = (double*)m.p[1];
+    d.out = (double*)m.Ap;
+    d.dim = op->dim;
+    d.nu = op->pen;
+    d.st = m.stp;
+    d.red = m.red32;
+    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_CG, d, op->tab, s));
+    k_cg_update<double><<<vec_grid(m.n), kVecThreads, 0, s>>>((double*)m.e, (const double*)m.p[0],
+                                                              (const double*)m.p[1], (double*)m.r,
+                                                              (const double*)m.Ap, m.n, m.stp, m.red32);
+  } else if (kind == SIPG_INNER_PAIRS) {
+    a.nu_lo = (float)(op->pen - (double)a.nu);
+    a.st = nullptr;
+    a.stp = m.stp;
+    SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_CG, a, nullptr, nullptr, 0, 0, op->tab, s));
+    k_cg_update_pairs<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[1], m.r, m.Ap, m.n, m.stp, m.red32);
+  } else {
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_CG, a, op->tab, s));
+    k_cg_update<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[1], m.r, m.Ap, m.n, m.st32, m.red32);
+  }
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+sipg_status capture(sipg_op* op, MixedCache& m, int kind, int K) {
+  if (m.exec[kind] && m.exec_k[kind] == K && m.exec_gen[kind] == op->tile_gen) return SIPG_OK;
+  if (m.exec[kind]) {
+    cudaGraphExecDestroy(m.exec[kind]);
+    m.exec[kind] = nullptr;
+  }
+  ApplyArgs<float> none{};
+  none.dim = op->dim;
+  if (kind == SIPG_INNER_F64) {
+    ApplyArgs<double> prep{};
+    prep.dim = op->dim;
+    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_PREPARE, prep, op->tab, m.cap));
+  } else if (kind == SIPG_INNER_PAIRS)
+    SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_PREPARE, none, nullptr, nullptr, 0, 0, op->tab, m.cap));
+  else
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_PREPARE, none, op->tab, m.cap));
+  SIPG_CUDA_TRY(cudaStreamBeginCapture(m.cap, cudaStreamCaptureModeThreadLocal));
+  sipg_status st = SIPG_OK;
+  for (int k = 0; k < K && st == SIPG_OK; ++k) st = enqueue_iteration(op, m, kind, m.cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(m.cap, &g);
+  if (st != SIPG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  SIPG_CUDA_TRY(end);
+  const cudaError_t inst = cudaGraphInstantiate(&m.exec[kind], g, 0);
+  cudaGraphDestroy(g);
+  SIPG_CUDA_TRY(inst);
+  m.exec_k[kind] = K;
+  m.exec_gen[kind] = op->tile_gen;
   return SIPG_OK;
 }
 }  // namespace
@@ -124,34 +292,44 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     set_error("sipg_solve_mixed: null argument");
     return SIPG_ERR_INVALID;
   }
-  sipg_mixed_opts o = {0.1, 1e-10, 200, 0};
+  sipg_mixed_opts o = {0.1, 1e-10, 200, 0, SIPG_INNER_AUTO, 0};
   if (opts) o = *opts;
-  if (!(o.inner_tol > 0) || !(o.inner_tol < 1) || !(o.outer_tol > 0) || o.max_outer < 1) {
-    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1");
+  if (!(o.inner_tol > 0) || !(o.inner_tol < 1) || !(o.outer_tol > 0) || o.max_outer < 1 || o.inner < 0 ||
+      o.inner > 3) {
+    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1, inner in 0..3");
     return SIPG_ERR_INVALID;
   }
   cudaStream_t s = (cudaStream_t)stream;
   SIPG_CUDA_TRY(cudaSetDevice(op->device));
   const size_t n = (size_t)op->ndof;
-  const int vb = (int)std::max<size_t>(1, std::min<size_t>((n + kVecThreads - 1) / kVecThreads, 152 * 8));
-  MixedWorkspace mw;
-  sipg_status st = alloc_workspace(mw, n, reduce_capacity(op->dim), s);
+  const int kind = choose_inner(o.inner, op->p, op->dim, op->pen);
+  MixedCache* mp = nullptr;
+  sipg_status st = cache_get(op, &mp);
   if (st != SIPG_OK) return st;
-  CgF32View v32;  // the op's FP32 CG workspace, iterating on the correction e
-  st = cg_f32_prepare(op, mw.e32, &v32);
+  MixedCache& m = *mp;
+  const int K = n <= (1u << 20) ? 32 : 8;  // inner iterations per graph launch
+  st = capture(op, m, kind, K);
   if (st != SIPG_OK) return st;
   const long long max_inner = o.max_inner > 0 ? o.max_inner : op->ndof;
-  SIPG_CUDA_TRY(cudaEventRecord(mw.ev0, s));
+  const int vb = vec_grid(n);
+  SIPG_CUDA_TRY(cudaEventRecord(m.ev0, s));
 
   // ||b|| in FP64
-  k_cg_init<double><<<vb, kVecThreads, 0, s>>>(d_b, n, mw.st64, 0.0, 0, 1, mw.red64);
+  k_cg_init<double><<<vb, kVecThreads, 0, s>>>(d_b, n, m.st64, 0.0, 0, 1, m.red64);
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
-  SIPG_CUDA_TRY(cudaMemcpyAsync(mw.st64_host, mw.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-  const double bnorm = std::sqrt(mw.st64_host->bb);
+  const double bnorm = std::sqrt(m.st64_host->bb);
+  // the inner loop may also stop once its own residual is under the target
+  const double stop_in = 0.5 * o.outer_tol * (bnorm > 0 ? bnorm : 1.0);
+  // the inner state as the host last read it
+  const bool st_double = kind != SIPG_INNER_F32;  // pairs and FP64 keep FP64 scalars in stp
+  auto inner_done = [&]() { return st_double ? m.stp_host->done : m.st32_host->done; };
+  auto inner_it = [&]() { return st_double ? m.stp_host->it : m.st32_host->it; };
+  auto inner_status = [&]() { return st_double ? m.stp_host->status : m.st32_host->status; };
 
-  int corrections = 0;
+  int updates = 0;
   long long inner_total = 0;
   double rel = INFINITY;
   sipg_status status = SIPG_OK;
@@ -159,16 +337,16 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     // the true residual in FP64
     ApplyArgs<double> a{};
     a.in = d_x;
-    a.out = mw.r64;
+    a.out = m.r64;
     a.b = d_b;
     a.dim = op->dim;
     a.nu = op->pen;
-    a.st = mw.st64;
-    a.red = mw.red64;
+    a.st = m.st64;
+    a.red = m.red64;
     SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_RESID, a, op->tab, s));
-    SIPG_CUDA_TRY(cudaMemcpyAsync(mw.st64_host, mw.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-    const double rr = mw.st64_host->rr;
+    const double rr = m.st64_host->rr;
     rel = (bnorm > 0) ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (!std::isfinite(rel)) {
       set_error("sipg_solve_mixed: non-finite residual");
@@ -176,44 +354,61 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
       break;
     }
     if (rel <= o.outer_tol || rr == 0.0) break;
-    if (corrections >= o.max_outer || inner_total >= max_inner) {
+    if (updates >= o.max_outer || inner_total >= max_inner) {
       status = SIPG_ERR_NOT_CONVERGED;
       break;
     }
-    // the FP32 residual and CG state; after the first correction the search
-    // direction is kept
-    k_mixed_restart<<<vb, kVecThreads, 0, s>>>(mw.r64, v32.r, mw.e32, n, v32.st, mw.red32, corrections == 0 ? 1 : 0,
-                                               (float)o.inner_tol, kCorrectEvery);
+    // the inner residual and CG state; after the first update the direction is kept
+    if (kind == SIPG_INNER_F64)
+      k_mixed_restart_f64<<<vb, kVecThreads, 0, s>>>(m.r64, (double*)m.r, (double*)m.e, n, m.stp, m.red32,
+                                                     updates == 0, o.inner_tol, stop_in, kCorrectEvery);
+    else if (kind == SIPG_INNER_PAIRS)
+      k_mixed_restart<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.stp, m.red32, updates == 0,
+                                                               o.inner_tol, stop_in, kCorrectEvery);
+    else
+      k_mixed_restart<INNER_F32><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.st32, m.red32, updates == 0,
+                                                             o.inner_tol, stop_in, kCorrectEvery);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
-    const int it_before = (corrections == 0) ? 0 : mw.st32_host->it;
-    // FP32 iterations until a correction is due
+    const int it_before = (updates == 0) ? 0 : inner_it();
+    // inner iterations until an update is due (at most kCorrectEvery)
     for (;;) {
-      st = cg_f32_launch_chunk(op, s, mw.st32_host);
-      if (st != SIPG_OK) return st;
-      if (mw.st32_host->done) break;
+      SIPG_CUDA_TRY(cudaGraphLaunch(m.exec[kind], s));
+      count_launch(2ULL * K);
+      if (st_double)
+        SIPG_CUDA_TRY(cudaMemcpyAsync(m.stp_host, m.stp, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+      else
+        SIPG_CUDA_TRY(cudaMemcpyAsync(m.st32_host, m.st32, sizeof(CgState<float>), cudaMemcpyDeviceToHost, s));
+      SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+      if (inner_done()) break;
     }
-    inner_total += mw.st32_host->it - it_before;
-    if (mw.st32_host->status == (int)SIPG_ERR_BREAKDOWN) {
-      set_error("sipg_solve_mixed: FP32 CG breakdown");
+    inner_total += inner_it() - it_before;
+    if (inner_status() == (int)SIPG_ERR_BREAKDOWN) {
+      set_error("sipg_solve_mixed: inner CG breakdown");
       status = SIPG_ERR_BREAKDOWN;
       break;
     }
-    k_fold_correction<<<vb, kVecThreads, 0, s>>>(d_x, mw.e32, n);
+    if (kind == SIPG_INNER_F64)
+      k_mixed_fold_f64<<<vb, kVecThreads, 0, s>>>(d_x, (const double*)m.e, n);
+    else if (kind == SIPG_INNER_PAIRS)
+      k_mixed_fold<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(d_x, m.e, n);
+    else
+      k_mixed_fold<INNER_F32><<<vb, kVecThreads, 0, s>>>(d_x, m.e, n);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
-    ++corrections;
+    ++updates;
   }
-  SIPG_CUDA_TRY(cudaEventRecord(mw.ev1, s));
-  SIPG_CUDA_TRY(cudaEventSynchronize(mw.ev1));
+  SIPG_CUDA_TRY(cudaEventRecord(m.ev1, s));
+  SIPG_CUDA_TRY(cudaEventSynchronize(m.ev1));
   float ms = 0;
-  cudaEventElapsedTime(&ms, mw.ev0, mw.ev1);
+  cudaEventElapsedTime(&ms, m.ev0, m.ev1);
   if (res) {
-    res->outer_iterations = corrections;
+    res->outer_iterations = updates;
     res->inner_iterations = (int)inner_total;
     res->rel_residual = rel;
     res->time_ms = ms;
     res->converged = (status == SIPG_OK) ? 1 : 0;
+    res->inner_kind = kind;
   }
   return status;
 }

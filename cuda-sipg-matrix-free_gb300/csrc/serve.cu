@@ -9,10 +9,12 @@
 //      pool allocator, its right-hand side built on the device, x = 0, and a
 //      slot in the device state arrays;
 //   2. runs K CG iterations of every active request together: per degree one
-//      batched apply launch (k_sipg_apply_batched, the requests' tiles
-//      concatenated) for the mixed requests (FP32) and one for the FP64 ones,
-//      then one batched update per precision -- requests admitted while others
-//      are mid-solve simply join the next launches;
+//      batched apply launch for the mixed requests (inner CG on double-float
+//      pair vectors with the compensated apply, k_sipg_apply_df_batched, the
+//      requests' tiles concatenated) and one for the FP64 ones
+//      (k_sipg_apply_batched), then one batched update per precision --
+//      requests admitted while others are mid-solve simply join the next
+//      launches;
 //   3. reads all active states with one copy; mixed requests due for a
 //      reliable update get x += e and their FP64 residual (batched FP64
 //      applies), then retire or continue; FP64 requests that converged retire.
@@ -29,7 +31,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "sipg_cg.cuh"
+#include "sipg_cg_df.cuh"
 
 using namespace sipg;
 
@@ -40,15 +42,15 @@ struct ServeMixed {  // one mixed request's operands for the vector kernels
   double* x64;
   const double* b64;
   double* r64;
-  float* e32;
-  float* r32;
-  CgState<float>* st32;
+  float* r32;  // pair vectors
+  float* e;
+  CgState<double>* st32;  // the inner state (FP64 scalars)
   CgState<double>* st64;
   ReduceScratch red32;
   ReduceScratch red64;
   size_t n;
   int first;
-  float delta;
+  double delta;
   double tol;  // relative FP64 tolerance
   int nblk;    // blocks this request uses (see VecInst)
   int pad;
@@ -91,11 +93,10 @@ __global__ void __launch_bounds__(kVecThreads) k_serve_init_f64(const VecInst<do
 
 // mixed request start: ||b||, r64 = b (x = 0), then the FP32 state (first run)
 __global__ void __launch_bounds__(kVecThreads) k_serve_init_mixed(const ServeMixed* __restrict__ insts) {
-  __shared__ float shf[32];
+  __shared__ double sh[32];
   const ServeMixed m = insts[blockIdx.y];
   if ((int)blockIdx.x >= m.nblk) return;
   double acc = 0.0;
-  float accf = 0.f;
   const size_t stride = (size_t)m.nblk * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
     const double bi = m.b64[i];
@@ -103,72 +104,48 @@ __global__ void __launch_bounds__(kVecThreads) k_serve_init_mixed(const ServeMix
     m.r64[i] = bi;
     const float v = (float)bi;
     m.r32[i] = v;
-    m.e32[i] = 0.f;
+    m.r32[m.n + i] = (float)(bi - (double)v);
+    m.e[i] = 0.f;
+    m.e[m.n + i] = 0.f;
     acc = fma(bi, bi, acc);
-    accf = fmaf(v, v, accf);
   }
-  // two reductions through the two scratch areas
-  __shared__ double shd[32];
-  const double bt = block_sum<double, kVecThreads>(acc, shd);
+  const double bt = block_sum<double, kVecThreads>(acc, sh);
   double total;
-  if (grid_sum_last<double, kVecThreads>(bt, m.red64, blockIdx.x, m.nblk, shd, &total) && threadIdx.x == 0) {
+  if (grid_sum_last<double, kVecThreads>(bt, m.red64, blockIdx.x, m.nblk, sh, &total) && threadIdx.x == 0) {
     m.st64->bb = total;
     m.st64->rr = total;
-  }
-  const float btf = block_sum<float, kVecThreads>(accf, shf);
-  float totalf;
-  if (grid_sum_last<float, kVecThreads>(btf, m.red32, blockIdx.x, m.nblk, shf, &totalf) && threadIdx.x == 0) {
-    CgState<float>* st = m.st32;
+    CgState<double>* st = m.st32;
     st->first = 1;
     st->it = 0;
     st->parity = 0;
-    st->beta = 0.f;
+    st->beta = 0.0;
     st->status = (int)SIPG_OK;
-    st->rr = totalf;
-    st->rmax = sqrtf(totalf);
+    st->rr = total;
+    st->rmax = sqrt(total);
     st->delta = m.delta;
-    st->stop = 0.f;
-    st->max_it = 1000;  // a correction is forced after 1000 FP32 iterations
+    // the inner loop also stops under the request's target, for the FP64 check
+    st->stop = 0.5 * m.tol * sqrt(total);
+    st->max_it = 1000;  // an FP64 update is forced after 1000 inner iterations
     st->need_update = 0;
-    st->done = (totalf == 0.f) ? 1 : 0;
+    st->done = (total == 0.0) ? 1 : 0;
   }
 }
 
-// x64 += e32 for every listed mixed request
+// x64 += e for every listed mixed request
 __global__ void __launch_bounds__(kVecThreads) k_serve_fold(const ServeMixed* __restrict__ insts) {
   const ServeMixed m = insts[blockIdx.y];
   if ((int)blockIdx.x >= m.nblk) return;
-  const size_t stride = (size_t)m.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride)
-    m.x64[i] += (double)m.e32[i];
+  inner_fold_body<INNER_PAIRS>(m.x64, m.e, m.n, blockIdx.x, m.nblk);
 }
 
-// after a correction: r32 = (float) r64, e = 0, beta = r_new.r_new / r_old.r_old,
-// and the FP32 iterations continue with the kept search direction
+// after an FP64 update: the inner residual = r64 as pairs, e = 0, beta =
+// r_new.r_new / r_prev.r_prev, and the inner iterations continue with the
+// kept search direction
 __global__ void __launch_bounds__(kVecThreads) k_serve_restart(const ServeMixed* __restrict__ insts) {
-  __shared__ float sh[32];
   const ServeMixed m = insts[blockIdx.y];
   if ((int)blockIdx.x >= m.nblk) return;
-  float acc = 0.f;
-  const size_t stride = (size_t)m.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-    const float v = (float)m.r64[i];
-    m.r32[i] = v;
-    m.e32[i] = 0.f;
-    acc = fmaf(v, v, acc);
-  }
-  const float bt = block_sum<float, kVecThreads>(acc, sh);
-  float total;
-  if (grid_sum_last<float, kVecThreads>(bt, m.red32, blockIdx.x, m.nblk, sh, &total) && threadIdx.x == 0) {
-    CgState<float>* st = m.st32;
-    st->beta = total / st->rr;
-    st->first = 0;
-    st->rr = total;
-    st->rmax = sqrtf(total);
-    st->max_it = st->it + 1000;
-    st->need_update = 0;
-    st->done = 0;
-  }
+  const double stop = 0.5 * m.tol * sqrt(m.st64->bb);  // as at the start
+  inner_restart_body<INNER_PAIRS>(m.r64, m.r32, m.e, m.n, m.st32, m.red32, 0, m.delta, stop, 1000, blockIdx.x, m.nblk);
 }
 
 }  // namespace sipg
@@ -191,7 +168,7 @@ struct Request {
   size_t x_bytes = 0;
   double* b64 = nullptr;
   double* r64 = nullptr;     // mixed: FP64 residual; FP64: r
-  float* e32 = nullptr;
+  float* e32 = nullptr;      // mixed: pair vectors (2 n floats) from here
   float* r32 = nullptr;
   float* p32[2] = {nullptr, nullptr};
   float* Ap32 = nullptr;
@@ -206,9 +183,9 @@ struct Request {
 };
 
 struct Slots {
-  CgState<float>* d32 = nullptr;
+  CgState<double>* d32 = nullptr;  // mixed requests' inner states
   CgState<double>* d64 = nullptr;
-  CgState<float>* h32 = nullptr;
+  CgState<double>* h32 = nullptr;
   CgState<double>* h64 = nullptr;
 };
 
@@ -239,8 +216,8 @@ struct sipg_server {
   int* d_t64 = nullptr;
   int* h_tr = nullptr;
   int* d_tr = nullptr;
-  VecInst<float>* h_v32 = nullptr;
-  VecInst<float>* d_v32 = nullptr;
+  PairInst* h_v32 = nullptr;
+  PairInst* d_v32 = nullptr;
   VecInst<double>* h_v64 = nullptr;
   VecInst<double>* d_v64 = nullptr;
   ServeMixed* h_m = nullptr;
@@ -261,7 +238,7 @@ size_t footprint_of(int dim, int p, int precision) {
   const size_t n = (size_t)dim * dim * (p + 1) * (p + 1);
   const size_t red = 2 * (sizeof(double) * (size_t)reduce_capacity(dim) + 256);
   if (precision == SIPG_F64) return n * (8 * 2 + 8 * 4) + red + 4096;  // x, b, r, p0, p1, Ap
-  return n * (8 * 3 + 4 * 5) + red + 4096;                             // x, b, r64 + e, r, p0, p1, Ap
+  return n * (8 * 3 + 8 * 5) + red + 4096;                             // x, b, r64 + pairs e, r, p0, p1, Ap
 }
 
 sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
@@ -299,11 +276,11 @@ sipg_status admit(sipg_server* sv, Request* r) {
     r->p64[1] = (double*)take(n * 8);
     r->Ap64 = (double*)take(n * 8);
   } else {
-    r->e32 = (float*)take(n * 4);
-    r->r32 = (float*)take(n * 4);
-    r->p32[0] = (float*)take(n * 4);
-    r->p32[1] = (float*)take(n * 4);
-    r->Ap32 = (float*)take(n * 4);
+    r->e32 = (float*)take(n * 8);
+    r->r32 = (float*)take(n * 8);
+    r->p32[0] = (float*)take(n * 8);
+    r->p32[1] = (float*)take(n * 8);
+    r->Ap32 = (float*)take(n * 8);
   }
   r->red32.partials = (double*)take(sizeof(double) * cap);
   r->red32.counter = (unsigned int*)take(256);
@@ -351,7 +328,8 @@ ApplyArgs<float> cg_args32(const Request* r, sipg_server* sv) {
   a.out = r->Ap32;
   a.dim = r->req.dim;
   a.nu = (float)r->req.pen;
-  a.st = sv->slots.d32 + r->slot;
+  a.nu_lo = (float)(r->req.pen - (double)a.nu);
+  a.stp = sv->slots.d32 + r->slot;
   a.red = r->red32;
   return a;
 }
@@ -374,7 +352,7 @@ ServeMixed mixed_of(const Request* r, sipg_server* sv, int first) {
   m.x64 = r->x64;
   m.b64 = r->b64;
   m.r64 = r->r64;
-  m.e32 = r->e32;
+  m.e = r->e32;
   m.r32 = r->r32;
   m.st32 = sv->slots.d32 + r->slot;
   m.st64 = sv->slots.d64 + r->slot;
@@ -382,7 +360,7 @@ ServeMixed mixed_of(const Request* r, sipg_server* sv, int first) {
   m.red64 = r->red64;
   m.n = r->n;
   m.first = first;
-  m.delta = (float)sv->opts.inner_tol;
+  m.delta = sv->opts.inner_tol;
   m.tol = r->req.tol;
   m.nblk = inst_blocks(r->n);
   m.pad = 0;
@@ -408,7 +386,7 @@ std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArg
     const std::vector<Request*>& g = kv.second;
     GroupLaunch gl;
     gl.p = kv.first;
-    gl.cfg = (sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfg32;
+    gl.cfg = (sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfgdf;
     gl.off = off;
     gl.m = (int)g.size();
     gl.toff = toff;
@@ -443,8 +421,8 @@ sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const Ap
     cudaError_t e = (sizeof(T) == 8)
                         ? launch_apply_batched_f64(g.p, g.cfg, mode, (const ApplyArgs<double>*)(d_a + g.off),
                                                    d_t + g.toff, g.m, g.total, *g.tab, s)
-                        : launch_apply_batched_f32(g.p, g.cfg, mode, (const ApplyArgs<float>*)(d_a + g.off),
-                                                   d_t + g.toff, g.m, g.total, *g.tab, s);
+                        : launch_apply_df(g.p, g.cfg, mode, ApplyArgs<float>{}, (const ApplyArgs<float>*)(d_a + g.off),
+                                          d_t + g.toff, g.m, g.total, *g.tab, s);
     SIPG_CUDA_TRY(e);
   }
   return SIPG_OK;
@@ -453,11 +431,11 @@ sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const Ap
 sipg_status server_alloc(sipg_server* sv) {
   const int cap = sv->opts.max_active;
   SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d64, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMemset(sv->slots.d64, 0, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h32, sizeof(CgState<float>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h32, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h64, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMallocHost(&sv->h_a32, sizeof(ApplyArgs<float>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->d_a32, sizeof(ApplyArgs<float>) * cap));
@@ -471,8 +449,8 @@ sipg_status server_alloc(sipg_server* sv) {
     SIPG_CUDA_TRY(cudaMallocHost(tiles_h[k], sizeof(int) * (cap + 16)));
     SIPG_CUDA_TRY(cudaMalloc(tiles_d[k], sizeof(int) * (cap + 16)));
   }
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v32, sizeof(VecInst<float>) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v32, sizeof(VecInst<float>) * cap));
+  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v32, sizeof(PairInst) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v32, sizeof(PairInst) * cap));
   SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v64, sizeof(VecInst<double>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->d_v64, sizeof(VecInst<double>) * cap));
   SIPG_CUDA_TRY(cudaMallocHost(&sv->h_m, sizeof(ServeMixed) * cap));
@@ -656,7 +634,7 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   size_t nmax32 = 0, nmax64 = 0;
   for (int j = 0; j < (int)a32.size(); ++j) {
     Request* r = a32[j];
-    VecInst<float> v;
+    PairInst v;
     v.x = r->e32;
     v.pb0 = r->p32[0];
     v.pb1 = r->p32[1];
@@ -687,7 +665,8 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     nmax64 = std::max(nmax64, r->n);
   }
   if (!a32.empty())
-    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v32, sv->h_v32, sizeof(VecInst<float>) * a32.size(), cudaMemcpyHostToDevice, sv->s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v32, sv->h_v32, sizeof(PairInst) * a32.size(), cudaMemcpyHostToDevice,
+                                  sv->s));
   if (!a64.empty())
     SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v64, sv->h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, sv->s));
   const std::vector<GroupLaunch> g32 =
@@ -703,8 +682,8 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     if (!a32.empty()) {
       sipg_status st = launch_groups<float>(g32, APPLY_CG, sv->d_a32, sv->d_t32, sv->s);
       if (st != SIPG_OK) return st;
-      k_cg_update_batched<float><<<dim3(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size()), kVecThreads, 0, sv->s>>>(
-          sv->d_v32);
+      k_cg_update_pairs_batched<<<dim3(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size()), kVecThreads, 0,
+                                  sv->s>>>(sv->d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
     }
@@ -719,7 +698,8 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   }
   // 3. states, corrections, retirements
   const int cap = sv->opts.max_active;
-  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h32, sv->slots.d32, sizeof(CgState<float>) * cap, cudaMemcpyDeviceToHost, sv->s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h32, sv->slots.d32, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost,
+                                sv->s));
   SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, sv->s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
   std::vector<Request*> keep, fix;
@@ -735,12 +715,12 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     }
   }
   for (Request* r : a32) {
-    const CgState<float>& h = sv->slots.h32[r->slot];
+    const CgState<double>& h = sv->slots.h32[r->slot];
     if (h.done) fix.push_back(r);
     else keep.push_back(r);
   }
   if (!fix.empty()) {
-    // x += e and the FP64 residual of the mixed requests due a correction
+    // x += e and the FP64 residual of the mixed requests due an update
     int m = 0;
     size_t nmax = 0;
     for (Request* r : fix) {
@@ -771,7 +751,7 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     for (Request* r : fix) {
       r->corrections++;
       const CgState<double>& h = sv->slots.h64[r->slot];
-      const CgState<float>& h32 = sv->slots.h32[r->slot];
+      const CgState<double>& h32 = sv->slots.h32[r->slot];
       const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
       if (!std::isfinite(rel) || h32.status == (int)SIPG_ERR_BREAKDOWN) {
         retire(sv, r, SIPG_ERR_BREAKDOWN, h32.it, rel);

@@ -167,11 +167,12 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   };
 
   // ---- phase 0: the tile's nodal blocks -> smem --------------------------
+  // (loads only: CG mode writes the new direction in phase 2, so that no
+  // store sits between loads the compiler could otherwise batch)
 #pragma unroll(ApplyColumnForm<T, P>::load_unroll)
   for (int k = 0; k < NN; ++k) {
     const T v = act ? ld(k, e) : T(0);
     us[k * TE + t] = v;
-    if (MODE == APPLY_CG && act) pnew[(size_t)k * noe + e] = v;
   }
   __syncthreads();
 
@@ -379,7 +380,10 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
             acc = fma(rv, rv, acc);
           } else {
             a.out[gk] = o[j];
-            if (MODE == APPLY_CG) acc = fma(c[j], o[j], acc);
+            if (MODE == APPLY_CG) {
+              pnew[gk] = c[j];
+              acc = fma(c[j], o[j], acc);
+            }
           }
         }
       }
@@ -431,7 +435,11 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
           acc = fma(rv, rv, acc);
         } else {
           a.out[gk] = o[k];
-          if (MODE == APPLY_CG) acc = fma(us[k * TE + t], o[k], acc);
+          if (MODE == APPLY_CG) {
+            const T pk = us[k * TE + t];
+            pnew[gk] = pk;
+            acc = fma(pk, o[k], acc);
+          }
         }
       }
     }

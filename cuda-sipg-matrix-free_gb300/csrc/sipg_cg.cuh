@@ -18,9 +18,34 @@ namespace sipg {
 
 constexpr int kVecThreads = 256;
 
-// x += alpha p, r -= alpha Ap, r.r reduced; then the iteration bookkeeping
-// (beta, it, done, or a reliable update due).  Block `bid` of `nblocks` works
-// on a grid-stride slice of the vectors.
+// The iteration bookkeeping after r.r of the updated residual is known (one
+// thread): it, beta, the stop test, or a reliable update due.
+template <typename T>
+__device__ __forceinline__ void cg_bookkeep(CgState<T>* st, T total) {
+  const T rn = sqrt(total);
+  st->it += 1;
+  st->first = 0;
+  st->rr_prev = st->rr;
+  if (st->delta > T(0) && rn < st->delta * st->rmax) {
+    // reliable update due: keep rr (the previous r.r, for beta after the
+    // correction) and stop; the host replaces r by the FP64 residual
+    st->need_update = 1;
+    st->done = 1;
+  } else {
+    const T rr_old = st->rr;
+    st->beta = total / rr_old;
+    st->rr = total;
+    st->rmax = fmax(st->rmax, rn);
+    st->done = !(rn > st->stop && st->it < st->max_it);
+  }
+  if (!isfinite(total)) {
+    st->status = (int)SIPG_ERR_BREAKDOWN;
+    st->done = 1;
+  }
+}
+
+// x += alpha p, r -= alpha Ap, r.r reduced; then the bookkeeping.  Block
+// `bid` of `nblocks` works on a grid-stride slice of the vectors.
 template <typename T>
 __device__ __forceinline__ void cg_update_body(T* __restrict__ x, const T* __restrict__ pb0, const T* __restrict__ pb1,
                                                T* __restrict__ r, const T* __restrict__ Ap, size_t n, CgState<T>* st,
@@ -39,27 +64,7 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, const T* __res
   }
   const T bt = block_sum<T, kVecThreads>(acc, sh);
   T total;
-  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
-    const T rn = sqrt(total);
-    st->it += 1;
-    st->first = 0;
-    if (st->delta > T(0) && rn < st->delta * st->rmax) {
-      // reliable update due: keep rr (the previous r.r, for beta after the
-      // correction) and stop; the host replaces r by the FP64 residual
-      st->need_update = 1;
-      st->done = 1;
-    } else {
-      const T rr_old = st->rr;
-      st->beta = total / rr_old;
-      st->rr = total;
-      st->rmax = fmax(st->rmax, rn);
-      st->done = !(rn > st->stop && st->it < st->max_it);
-    }
-    if (!isfinite(total)) {
-      st->status = (int)SIPG_ERR_BREAKDOWN;
-      st->done = 1;
-    }
-  }
+  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) cg_bookkeep<T>(st, total);
 }
 
 template <typename T>

@@ -81,6 +81,8 @@ struct CgState {
   int parity;  // which direction buffer holds the current p
   int need_update;  // reliable updates: an FP64 correction is due
   int pad;
+  T rr_prev;  // r.r before the last update (beta after a forced correction)
+  T pad2;
 };
 
 // Deterministic grid reduction scratch: per-block partials, reduced in a fixed
@@ -109,8 +111,10 @@ struct ApplyArgs {
   const T* b;      // RESID: right-hand side
   int dim;
   T nu;            // penalty (the reference's `pen`)
+  T nu_lo;         // compensated apply: pen - (float) pen (0 otherwise)
   CgState<T>* st;  // CG / RESID
   ReduceScratch red;
+  CgState<double>* stp;  // compensated apply, CG mode: the inner state (FP64 scalars)
 };
 
 // Tile shape chosen for one (precision, degree).
@@ -132,6 +136,14 @@ cudaError_t launch_apply_batched_f64(int p, const TileCfg& cfg, int mode, const 
 cudaError_t launch_apply_batched_f32(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>* insts,
                                      const int* tile_start, int ninst, int total_tiles, const HostTables& h,
                                      cudaStream_t s);
+// The compensated FP32 apply on double-float vectors (2 n floats: the hi
+// plane, then the lo plane): one operator (insts == nullptr) or a batch of
+// degree-p operators; modes APPLY_PREPARE / PLAIN / CG.
+cudaError_t launch_apply_df(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const ApplyArgs<float>* insts,
+                            const int* tile_start, int ninst, int total_tiles, const HostTables& h, cudaStream_t s);
+// Tile shapes the autotuner chose for (degree, dim, precision) in this
+// process; false if none (autotune.cu).
+bool autotune_lookup(int p, int dim, int prec, TileCfg* cfg);
 // Number of blocks the apply launches for this tile shape.
 inline int apply_grid_blocks(int dim, const TileCfg& c) {
   return ((dim + c.tx - 1) / c.tx) * ((dim + c.ty - 1) / c.ty);
@@ -143,13 +155,6 @@ inline int reduce_capacity(int dim) {
   return a > 152 * 8 ? a : 152 * 8;
 }
 
-// FP32 CG pieces (capi.cu) used by the mixed-precision solver: the op's FP32
-// workspace with the iteration graph captured for iterate x, and one graph
-// chunk of iterations followed by a read of the device state.
-struct CgF32View {
-  float* r;
-  CgState<float>* st;
-};
 
 // ---------------------------------------------------------------------------
 // Error plumbing and launch accounting.
@@ -174,10 +179,6 @@ inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std
 // ---------------------------------------------------------------------------
 struct sipg_cg_workspace;
 
-namespace sipg {
-sipg_status cg_f32_prepare(sipg_op* op, float* x, CgF32View* v);
-sipg_status cg_f32_launch_chunk(sipg_op* op, cudaStream_t s, CgState<float>* host_state);
-}  // namespace sipg
 
 struct sipg_op {
   int dim = 0, p = 0;
@@ -185,10 +186,13 @@ struct sipg_op {
   int device = 0;
   long long noe = 0, ndof = 0;
   sipg::HostTables tab;
-  sipg::TileCfg cfg64, cfg32;
+  sipg::TileCfg cfg64, cfg32, cfgdf;  // FP64, FP32 and compensated-FP32 apply tiles
+  int tile_gen = 0;                    // bumped when a tile shape changes (graphs re-capture)
   std::mutex mu;  // guards the lazily allocated workspaces below
   sipg_cg_workspace* ws64 = nullptr;
   sipg_cg_workspace* ws32 = nullptr;
   double* stage_in = nullptr;  // host-buffer apply staging (device)
   double* stage_out = nullptr;
+  void* mixed = nullptr;  // the mixed-precision solver's cached workspace
+  void (*mixed_free)(void*) = nullptr;
 };

@@ -38,12 +38,16 @@ class CgResult(C.Structure):
 
 
 class MixedOpts(C.Structure):
-    _fields_ = [("inner_tol", C.c_double), ("outer_tol", C.c_double), ("max_outer", C.c_int), ("max_inner", C.c_int)]
+    _fields_ = [("inner_tol", C.c_double), ("outer_tol", C.c_double), ("max_outer", C.c_int), ("max_inner", C.c_int),
+                ("inner", C.c_int), ("reserved", C.c_int)]
+
+
+INNER = {"auto": 0, "f32": 1, "pairs": 2, "f64": 3}
 
 
 class MixedResult(C.Structure):
     _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("rel_residual", C.c_double),
-                ("time_ms", C.c_double), ("converged", C.c_int)]
+                ("time_ms", C.c_double), ("converged", C.c_int), ("inner_kind", C.c_int)]
 
 
 class Problem(C.Structure):
@@ -77,6 +81,12 @@ class Modes(C.Structure):
         return m
 
 
+class TileChoice(C.Structure):
+    _fields_ = [("elements_per_row", C.c_int), ("rows", C.c_int * 3), ("ms_per_apply", C.c_float * 3)]
+
+
+TILE_KINDS = {"f64": 0, "f32": 1, "pairs": 2}
+
 _lib = None
 
 _VP = C.c_void_p
@@ -87,8 +97,12 @@ _SIGS = {
     "sipg_op_create": (C.c_int, [C.c_int, C.c_int, C.c_double, C.POINTER(_VP)]),
     "sipg_op_destroy": (C.c_int, [_VP]),
     "sipg_op_solve_footprint": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "sipg_op_autotune": (C.c_int, [_VP, _VP, C.POINTER(TileChoice)]),
+    "sipg_op_set_tile": (C.c_int, [_VP, C.c_int, C.c_int]),
+    "sipg_op_get_tile": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int)]),
     "sipg_apply_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_apply_pairs": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_host_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_cg_f64": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
     "sipg_cg_f32": (C.c_int, [_VP, _VP, _VP, C.c_float, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
@@ -149,6 +163,21 @@ def _stream(stream=None):
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def to_pairs(x64):
+    """float64 tensor -> float32 pair vector (hi plane, lo plane)."""
+    import torch
+
+    hi = x64.float()
+    lo = (x64 - hi.double()).float()
+    return torch.cat([hi, lo])
+
+
+def from_pairs(v):
+    """float32 pair vector -> float64 tensor hi + lo."""
+    n = v.numel() // 2
+    return v[:n].double() + v[n:].double()
+
+
 def launch_count():
     return int(lib().sipg_launch_count())
 
@@ -203,6 +232,21 @@ class Operator:
             lib().sipg_op_destroy(self._h)
         self._h = None
 
+    def autotune(self, stream=None):
+        """Times the tile shapes on this operator and keeps the fastest per
+        apply kind; returns {kind: (rows, ms_per_apply)}."""
+        tc = TileChoice()
+        _check(lib().sipg_op_autotune(self._h, _stream(stream), C.byref(tc)), "autotune")
+        return {k: (tc.rows[i], tc.ms_per_apply[i]) for k, i in TILE_KINDS.items()}
+
+    def set_tile(self, kind, rows):
+        _check(lib().sipg_op_set_tile(self._h, TILE_KINDS[kind], int(rows)), "set_tile")
+
+    def get_tile(self, kind):
+        r = C.c_int()
+        _check(lib().sipg_op_get_tile(self._h, TILE_KINDS[kind], C.byref(r)), "get_tile")
+        return r.value
+
     def __del__(self):
         try:
             self.close()
@@ -234,6 +278,18 @@ class Operator:
         _check(f(self._h, _ptr(x), _ptr(out), _stream(stream)), "apply")
         return out
 
+    def apply_pairs(self, x, out=None, stream=None):
+        """A x on double-float pair vectors: float32 CUDA tensors of 2 ndof
+        values (hi plane, then lo plane), compensated arithmetic."""
+        import torch
+
+        assert x.dtype == torch.float32 and x.is_cuda and x.is_contiguous() and x.numel() == 2 * self.ndof
+        if out is None:
+            out = torch.empty_like(x)
+        assert out.dtype == torch.float32 and out.numel() == 2 * self.ndof and out.data_ptr() != x.data_ptr()
+        _check(lib().sipg_apply_pairs(self._h, _ptr(x), _ptr(out), _stream(stream)), "apply_pairs")
+        return out
+
     def apply_host(self, x, out=None, stream=0):
         """Host numpy float64 in and out (copies inside)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -260,15 +316,18 @@ class Operator:
             _check(st, "cg")
         return st, res
 
-    def solve_mixed(self, x, b, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, stream=None):
-        """FP32 CG inside FP64 defect correction with reliable updates: an FP64
-        correction whenever the FP32 residual fell by inner_tol since the last
-        one; stops at ||b - Ax|| <= outer_tol ||b|| (FP64).  Returns (status, MixedResult)."""
+    def solve_mixed(self, x, b, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, inner="auto",
+                    stream=None):
+        """Inner CG on the FP32 pipes (inner = "f32": FP32 vectors; "pairs":
+        double-float pairs; "auto": by the condition-number estimate) inside
+        FP64 defect correction with reliable updates: an FP64 correction
+        whenever the inner residual fell by inner_tol since the last one; stops
+        at ||b - Ax|| <= outer_tol ||b|| (FP64).  Returns (status, MixedResult)."""
         import torch
 
         self._vec(x, torch.float64)
         self._vec(b, torch.float64)
-        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner))
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER[inner], 0)
         res = MixedResult()
         st = lib().sipg_solve_mixed(self._h, _ptr(x), _ptr(b), C.byref(o), C.byref(res), _stream(stream))
         if st not in (0, 3, 4):
@@ -322,7 +381,7 @@ class Batch:
         px = (C.c_void_p * n)(*[x.data_ptr() for x in xs])
         pb = (C.c_void_p * n)(*[b.data_ptr() for b in bs])
         res = (MixedResult * n)()
-        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner))
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER["pairs"], 0)
         st = lib().sipg_batch_solve_mixed(self._h, C.cast(px, C.c_void_p), C.cast(pb, C.c_void_p), C.byref(o),
                                           C.cast(res, C.c_void_p), _stream(stream))
         if st not in (0, 3, 4):

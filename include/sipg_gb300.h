@@ -67,11 +67,27 @@ typedef struct {
   int converged;       /* 1 if sqrt(r.r) <= stop */
 } sipg_cg_result;
 
+/* Inner iteration of the mixed-precision solvers.  SIPG_INNER_F32: FP32
+ * vectors and the FP32 apply -- fastest, but an FP32 vector's rounding noise,
+ * amplified by A, limits it to condition numbers well below 1 / eps_32
+ * (~1.7e7; kappa ~ c_p dim^2, c_p = 0.8, 4.8, 12, 26, 46, 76, 114, 167 for
+ * p = 1..8 at penalty p^2).  SIPG_INNER_PAIRS: double-float vectors (two FP32
+ * planes) and the compensated apply, ~48-bit values on the FP32 pipes -- any
+ * condition number.  SIPG_INNER_AUTO picks F32 when kappa * 2^-24 < 0.01. */
+typedef enum { SIPG_INNER_AUTO = 0, SIPG_INNER_F32 = 1, SIPG_INNER_PAIRS = 2, SIPG_INNER_F64 = 3 } sipg_inner_kind;
+/* SIPG_INNER_F64 is the same reliable-update loop with FP64 vectors and the
+ * FP64 apply: the all-FP64 yardstick.  The plain CG (sipg_cg_f64, the
+ * reference's algorithm) stops on its recursively updated residual, whose gap
+ * to the true b - A x grows with kappa: on 512 x 512, p = 6 its true relative
+ * residual stalls near 1e-9 however small the tolerance. */
+
 typedef struct {
-  double inner_tol;    /* FP64 correction once the FP32 residual fell by this factor since the last one (0.1) */
+  double inner_tol;    /* FP64 correction once the inner residual fell by this factor since the last one (0.1) */
   double outer_tol;    /* stop at the FP64 relative residual ||b-Ax||/||b|| <= outer_tol (1e-10) */
   int max_outer;       /* cap on FP64 corrections (200) */
-  int max_inner;       /* cap on FP32 iterations in total (0 = DoF) */
+  int max_inner;       /* cap on inner iterations in total (0 = DoF) */
+  int inner;           /* sipg_inner_kind (0 = auto) */
+  int reserved;
 } sipg_mixed_opts;
 
 typedef struct {
@@ -80,6 +96,7 @@ typedef struct {
   double rel_residual;  /* final ||b - A x|| / ||b|| in FP64 */
   double time_ms;
   int converged;
+  int inner_kind;       /* the sipg_inner_kind used (F32, PAIRS or F64) */
 } sipg_mixed_result;
 
 /* ---- tables and mesh (host side, no device needed) ---- */
@@ -116,9 +133,35 @@ size_t sipg_op_solve_footprint(int dim, int degree, sipg_precision prec);
  * flux_term6b) and the free function mvm (sipg_sem_2d_gpu_kernels.hpp:410-454). */
 sipg_status sipg_apply_f64(const sipg_op* op, const double* d_in, double* d_out, void* stream);
 sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, void* stream);
+/* Double-float pair vectors (2 ndof floats: the hi plane, then the lo plane;
+ * value = hi + lo) and compensated arithmetic on the FP32 pipes: about 48
+ * significant bits, where FP32 keeps 24 -- on a smooth vector the plain FP32
+ * apply loses log10(condition number) of them.  The apply of the
+ * SIPG_INNER_PAIRS mixed solvers.  No reference counterpart. */
+sipg_status sipg_apply_pairs(const sipg_op* op, const float* d_in, float* d_out, void* stream);
 /* The same with host buffers: copies h_in to the device, applies, copies the
  * result back, synchronously.  Device staging buffers are kept in the op. */
 sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream);
+
+/* ---- tile shapes and the autotuner (no reference counterpart: the
+ * reference launches one fixed geometry) ----
+ * An apply tile is 32 elements along a mesh row (one thread each) by `rows`
+ * rows (2, 4 or 8).  Every shape gives bit-identical apply results; CG
+ * reductions regroup.  Tile indices for the three apply kinds: */
+enum { SIPG_TUNE_F64 = 0, SIPG_TUNE_F32 = 1, SIPG_TUNE_PAIRS = 2 /* compensated, pair vectors */ };
+typedef struct {
+  int elements_per_row;   /* 32 */
+  int rows[3];            /* chosen rows per tile, by SIPG_TUNE_* */
+  float ms_per_apply[3];  /* the winning candidate's time */
+} sipg_tile_choice;
+/* Times rows in {2, 4, 8} for each apply kind on this op (a few applies on
+ * scratch vectors of ndof doubles, allocated and freed here), keeps the
+ * fastest, and records it for (degree, dim) so ops created later in this
+ * process start with it.  Synchronous; not during stream capture.  `out` may
+ * be NULL. */
+sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out);
+sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows);
+sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows);
 
 /* ---- conjugate gradient ---- */
 
@@ -134,12 +177,14 @@ sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol,
 sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
                         sipg_cg_result* res, void* stream);
 
-/* Mixed precision: FP32 operator and CG (values and accumulation) inside FP64
- * defect correction with reliable updates -- whenever the FP32 residual has
- * fallen by inner_tol, x += e in FP64, r = b - A x in FP64, and the FP32 CG
- * continues with its search direction.  The residual b - A x, the update of x
- * and the outer norms stay FP64 on the device.  `opts` may be NULL (defaults
- * in sipg_mixed_opts).  No reference counterpart. */
+/* Mixed precision: the operator and CG run on the FP32 pipes (FP32 values,
+ * or double-float pairs, see sipg_inner_kind) inside FP64 defect correction
+ * with reliable updates -- whenever the inner residual has fallen by
+ * inner_tol (or after 1000 inner iterations), x += e in FP64, r = b - A x in
+ * FP64, and the inner CG continues with its search direction.  The residual
+ * b - A x, the update of x and the outer norms stay FP64 on the device.
+ * `opts` may be NULL (defaults in sipg_mixed_opts).  No reference
+ * counterpart. */
 sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
                              sipg_mixed_result* res, void* stream);
 

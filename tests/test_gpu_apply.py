@@ -122,3 +122,38 @@ def test_apply_on_side_stream_and_counts_launches(sipg, torch):
 def test_invalid_degree_raises(sipg):
     with pytest.raises(sipg.SipgError):
         sipg.Operator(8, 9, 1.0)
+
+
+def _rel_l2(y, ref):
+    return float(((y - ref).norm() / ref.norm()).item())
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7, 8])
+def test_apply_pairs_matches_f64_random(sipg, torch, p):
+    # double-float pair vectors, compensated arithmetic: the FP64 apply of the
+    # same value (hi + lo, exact in FP64) to the FP64 parity bar, 1e-12
+    d = 37
+    g = torch.Generator(device="cuda").manual_seed(p)
+    op = sipg.Operator(d, p, 100.0 * p * p + 0.3)  # a penalty with a non-zero FP32 remainder
+    xp = sipg.to_pairs(torch.rand(op.ndof, device="cuda", generator=g, dtype=torch.float64) * 2 - 1)
+    y64 = op.apply(sipg.from_pairs(xp))
+    y = sipg.from_pairs(op.apply_pairs(xp))
+    assert (y - y64).abs().max().item() <= 1e-12 * y64.abs().max().item(), p
+    op.close()
+
+
+def test_apply_pairs_on_smooth_vector(sipg, torch):
+    # A x for the discrete solution x of a fine mesh is b: the terms cancel to
+    # about 1 part in the condition number (~1e6 here).  The FP32 apply of the
+    # rounded vector loses that many of its 24 bits; pairs keep ~48.
+    d, p = 128, 6
+    op = sipg.Operator(d, p, float(p * p))
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    st, _ = op.cg(x, b, 1e-12, relative=True)
+    assert st == 0
+    e_pairs = _rel_l2(sipg.from_pairs(op.apply_pairs(sipg.to_pairs(x))), op.apply(x))
+    e_32 = _rel_l2(op.apply(x.float()).double(), op.apply(x))
+    assert e_pairs <= 3e-8, e_pairs
+    assert e_32 >= 1000 * e_pairs, (e_32, e_pairs)
+    op.close()

@@ -145,8 +145,8 @@ def test_mixed_precision_reaches_fp64_accuracy(sipg, oracle, torch):
     st, r64 = op.cg(x64, b, 1e-10, relative=True)
     assert st == 0
     xm = torch.zeros_like(b)
-    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10)
-    assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10
+    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10, inner="f32")
+    assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10 and rm.inner_kind == 1
     assert rm.outer_iterations >= 2 and rm.inner_iterations > 0
     # reliable updates keep the Krylov space: the FP32 iteration count stays within
     # a small factor of the FP64 one (a restarted inner solve needs orders of magnitude more)
@@ -156,4 +156,41 @@ def test_mixed_precision_reaches_fp64_accuracy(sipg, oracle, torch):
     assert em[0] <= 1.05 * e64[0]
     # both solves stop at ||b - Ax|| <= 1e-10 ||b||: their difference is bounded by the residuals
     assert (xm - x64).abs().max().item() <= 1e-7 * x64.abs().max().item()
+    op.close()
+
+
+def test_mixed_pairs_on_an_ill_conditioned_problem(sipg, torch):
+    # 256 x 256, p = 6: condition number ~5e6, a quarter of 1 / eps_32 -- FP32
+    # vectors cannot carry the iteration; double-float pairs reach a TRUE FP64
+    # relative residual of 1e-10.  (The FP64 CG stops on its iterated residual;
+    # here its true residual stalls near 3e-10, so its iteration count is only
+    # a yardstick.)
+    p, d, pen = 6, 256, 36.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("sinsin")
+    bn = b.norm().item()
+    x64 = torch.zeros_like(b)
+    st, r64 = op.cg(x64, b, 1e-10, relative=True)
+    assert st == 0
+    xm = torch.zeros_like(b)
+    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10)  # auto: pairs here
+    assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10
+    assert rm.inner_kind == 2
+    true_rel = (b - op.apply(xm)).norm().item() / bn
+    assert true_rel <= 1e-10, true_rel
+    assert rm.inner_iterations <= 3 * r64.iterations, (rm.inner_iterations, r64.iterations)
+    e64 = op.err_norms("sinsin", x64)
+    em = op.err_norms("sinsin", xm)
+    slack = 2.0 * (xm - x64).abs().max().item()
+    assert em[0] <= 1.05 * e64[0] + slack, (em, e64)
+    assert (xm - x64).abs().max().item() <= 1e-7 * x64.abs().max().item()
+    op.close()
+
+
+def test_mixed_auto_picks_f32_for_well_conditioned(sipg, torch):
+    op = sipg.Operator(16, 2, 4.0)
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    st, rm = op.solve_mixed(x, b)
+    assert st == 0 and rm.inner_kind == 1 and rm.rel_residual <= 1e-10
     op.close()
