@@ -41,7 +41,7 @@ cudaError_t run_apply(const sipg_op* op, int prec, const TileCfg& cfg, const voi
   if constexpr (sizeof(T) == 8) {
     return launch_apply_f64(op->p, cfg, APPLY_PLAIN, a, op->tab, s);
   } else {
-    a.nu_lo = (float)(op->pen - (double)a.nu);
+    set_penalty3(a, op->pen);
     if (prec == SIPG_TUNE_PAIRS) return launch_apply_df(op->p, cfg, APPLY_PLAIN, a, nullptr, nullptr, 0, 0, op->tab, s);
     return launch_apply_f32(op->p, cfg, APPLY_PLAIN, a, op->tab, s);
   }

@@ -8,7 +8,8 @@
 // the device for the life of the batch.  One inner iteration of the whole
 // batch is one batched compensated apply launch per degree present
 // (k_sipg_apply_df_batched: the instances' tiles concatenated into one grid)
-// plus one batched update launch (k_cg_update_pairs_batched); K iterations are
+// plus a batched direction launch before it and a batched update launch after
+// it (k_cg_direction_pairs_batched, k_cg_update_pairs_batched); K iterations are
 // captured once as a CUDA graph and replayed.  The mixed-precision scheme is
 // the reliable-update one of mixed.cu, per instance: an instance whose inner
 // residual has fallen by inner_tol stops iterating (its blocks return at once)
@@ -92,7 +93,6 @@ struct BInst {
   float* r32 = nullptr;  // pair vectors (2 n floats) from here
   float* e = nullptr;
   float* p0 = nullptr;
-  float* p1 = nullptr;
   float* Ap = nullptr;
   CgState<double>* st32 = nullptr;  // inner state
   CgState<double>* st64 = nullptr;
@@ -142,7 +142,6 @@ static void batch_free(sipg_batch* b) {
     cudaFree(i.r32);
     cudaFree(i.e);
     cudaFree(i.p0);
-    cudaFree(i.p1);
     cudaFree(i.Ap);
     cudaFree(i.st32);
     cudaFree(i.st64);
@@ -182,7 +181,6 @@ static sipg_status batch_alloc(sipg_batch* b) {
     SIPG_CUDA_TRY(cudaMalloc(&i.r32, pair_bytes));
     SIPG_CUDA_TRY(cudaMalloc(&i.e, pair_bytes));
     SIPG_CUDA_TRY(cudaMalloc(&i.p0, pair_bytes));
-    SIPG_CUDA_TRY(cudaMalloc(&i.p1, pair_bytes));
     SIPG_CUDA_TRY(cudaMalloc(&i.Ap, pair_bytes));
     SIPG_CUDA_TRY(cudaMalloc(&i.st32, sizeof(CgState<double>)));
     SIPG_CUDA_TRY(cudaMalloc(&i.st64, sizeof(CgState<double>)));
@@ -219,13 +217,11 @@ static sipg_status batch_alloc(sipg_batch* b) {
       i.tilesdf = tiles_of(i.dim, g.cfgdf);
       i.tiles64 = tiles_of(i.dim, g.cfg64);
       ApplyArgs<float> a{};
-      a.in = i.r32;
-      a.pbuf0 = i.p0;
-      a.pbuf1 = i.p1;
+      a.in = i.p0;  // the direction, formed by k_cg_direction_pairs_batched
       a.out = i.Ap;
       a.dim = i.dim;
       a.nu = (float)i.pen;
-      a.nu_lo = (float)(i.pen - (double)a.nu);
+      set_penalty3(a, i.pen);
       a.stp = i.st32;
       a.red = i.red32;
       args[j] = a;
@@ -245,7 +241,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
     PairInst v;
     v.x = i.e;
     v.pb0 = i.p0;
-    v.pb1 = i.p1;
+    v.pb1 = i.p0;
     v.r = i.r32;
     v.Ap = i.Ap;
     v.n = i.n;
@@ -283,8 +279,11 @@ static sipg_status batch_capture(sipg_batch* b) {
   SIPG_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int k = 0; k < b->K && err == cudaSuccess; ++k) {
+    k_cg_direction_pairs_batched<<<dim3(b->bpi, b->n), kVecThreads, 0, b->cap>>>(b->d_vec);
+    err = cudaGetLastError();
     for (BGroup& g : b->groups) {
-      err = launch_apply_df(g.p, g.cfgdf, APPLY_CG, ApplyArgs<float>{}, g.d_cg, g.d_tilesdf, (int)g.members.size(),
+      if (err != cudaSuccess) break;
+      err = launch_apply_df(g.p, g.cfgdf, APPLY_DOT, ApplyArgs<float>{}, g.d_cg, g.d_tilesdf, (int)g.members.size(),
                             g.totaldf, b->inst[g.members[0]].op->tab, b->cap);
       if (err != cudaSuccess) break;
     }
@@ -427,7 +426,7 @@ sipg_status sipg_batch_op(const sipg_batch* b, int i, sipg_op** op) {
 size_t sipg_batch_footprint(const sipg_batch* b) {
   if (!b) return 0;
   size_t bytes = 0;
-  for (const BInst& i : b->inst) bytes += i.n * (8 + 5 * 8) + 2 * sizeof(double) * reduce_capacity(i.dim);
+  for (const BInst& i : b->inst) bytes += i.n * (8 + 4 * 8) + 2 * sizeof(double) * reduce_capacity(i.dim);
   return bytes;
 }
 
@@ -524,7 +523,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     if (!active) break;
     // FP32 iterations of every active instance
     SIPG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
-    unsigned long long per_iter = (unsigned long long)b->groups.size() + 1;
+    unsigned long long per_iter = (unsigned long long)b->groups.size() + 2;
     count_launch(per_iter * b->K);
     for (int k = 0; k < n; ++k)
       SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st32 + k, b->inst[k].st32, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));

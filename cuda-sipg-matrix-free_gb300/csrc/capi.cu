@@ -249,19 +249,21 @@ static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, i
   cudaError_t err = cudaSuccess;
   const int vb = vec_blocks(w->n);
   for (int k = 0; k < K && err == cudaSuccess; ++k) {
+    // p = r + beta p; Ap, p.Ap, alpha; x += alpha p, r -= alpha Ap, r.r, beta
+    k_cg_direction<T><<<vb, kVecThreads, 0, w->cap>>>((T*)w->p[0], (const T*)w->r, w->n, (CgState<T>*)w->st);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) break;
     ApplyArgs<T> a{};
-    a.in = (const T*)w->r;
-    a.pbuf0 = (T*)w->p[0];
-    a.pbuf1 = (T*)w->p[1];
+    a.in = (const T*)w->p[0];
     a.out = (T*)w->Ap;
     a.b = nullptr;
     a.dim = op->dim;
     a.nu = (T)op->pen;
     a.st = (CgState<T>*)w->st;
     a.red = w->red;
-    err = launch_apply<T>(op, APPLY_CG, a, w->cap);
+    err = launch_apply<T>(op, APPLY_DOT, a, w->cap);
     if (err != cudaSuccess) break;
-    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[1], (T*)w->r,
+    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[0], (T*)w->r,
                                                    (const T*)w->Ap, w->n, (CgState<T>*)w->st, w->red);
     err = cudaGetLastError();
   }
@@ -317,7 +319,7 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   long long launched = 0;
   for (;;) {
     SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
-    count_launch(2ULL * K);
+    count_launch(3ULL * K);
     launched += K;
     SIPG_CUDA_TRY(cudaMemcpyAsync(hs, w->st, sizeof(CgState<T>), cudaMemcpyDeviceToHost, s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -510,7 +512,7 @@ sipg_status sipg_apply_pairs(const sipg_op* op, const float* d_in, float* d_out,
   a.out = d_out;
   a.dim = op->dim;
   a.nu = (float)op->pen;
-  a.nu_lo = (float)(op->pen - (double)a.nu);
+  set_penalty3(a, op->pen);
   SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_PLAIN, a, nullptr, nullptr, 0, 0, op->tab, (cudaStream_t)stream));
   return SIPG_OK;
 }

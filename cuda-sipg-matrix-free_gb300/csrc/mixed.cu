@@ -223,28 +223,35 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
   a.st = m.st32;
   a.red = m.red32;
   if (kind == SIPG_INNER_F64) {
+    k_cg_direction<double><<<vec_grid(m.n), kVecThreads, 0, s>>>((double*)m.p[0], (const double*)m.r, m.n, m.stp);
+    count_launch();
     ApplyArgs<double> d{};
-    d.in = (const double*)m.r;
-    d.pbuf0 = (double*)m.p[0];
-    d.pbuf1 = (double*)m.p[1];
+    d.in = (const double*)m.p[0];
     d.out = (double*)m.Ap;
     d.dim = op->dim;
     d.nu = op->pen;
     d.st = m.stp;
     d.red = m.red32;
-    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_CG, d, op->tab, s));
+    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_DOT, d, op->tab, s));
     k_cg_update<double><<<vec_grid(m.n), kVecThreads, 0, s>>>((double*)m.e, (const double*)m.p[0],
-                                                              (const double*)m.p[1], (double*)m.r,
+                                                              (const double*)m.p[0], (double*)m.r,
                                                               (const double*)m.Ap, m.n, m.stp, m.red32);
   } else if (kind == SIPG_INNER_PAIRS) {
-    a.nu_lo = (float)(op->pen - (double)a.nu);
+    // p = r + beta p (in place), then Ap and alpha, then the update
+    k_cg_direction_pairs<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], m.r, m.n, m.stp);
+    count_launch();
+    a.in = m.p[0];
+    set_penalty3(a, op->pen);
     a.st = nullptr;
     a.stp = m.stp;
-    SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_CG, a, nullptr, nullptr, 0, 0, op->tab, s));
-    k_cg_update_pairs<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[1], m.r, m.Ap, m.n, m.stp, m.red32);
+    SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_DOT, a, nullptr, nullptr, 0, 0, op->tab, s));
+    k_cg_update_pairs<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[0], m.r, m.Ap, m.n, m.stp, m.red32);
   } else {
-    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_CG, a, op->tab, s));
-    k_cg_update<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[1], m.r, m.Ap, m.n, m.st32, m.red32);
+    k_cg_direction<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], m.r, m.n, m.st32);
+    count_launch();
+    a.in = m.p[0];
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_DOT, a, op->tab, s));
+    k_cg_update<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.p[0], m.r, m.Ap, m.n, m.st32, m.red32);
   }
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
@@ -374,7 +381,7 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     // inner iterations until an update is due (at most kCorrectEvery)
     for (;;) {
       SIPG_CUDA_TRY(cudaGraphLaunch(m.exec[kind], s));
-      count_launch(2ULL * K);
+      count_launch(3ULL * K);
       if (st_double)
         SIPG_CUDA_TRY(cudaMemcpyAsync(m.stp_host, m.stp, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
       else

@@ -238,7 +238,7 @@ size_t footprint_of(int dim, int p, int precision) {
   const size_t n = (size_t)dim * dim * (p + 1) * (p + 1);
   const size_t red = 2 * (sizeof(double) * (size_t)reduce_capacity(dim) + 256);
   if (precision == SIPG_F64) return n * (8 * 2 + 8 * 4) + red + 4096;  // x, b, r, p0, p1, Ap
-  return n * (8 * 3 + 8 * 5) + red + 4096;                             // x, b, r64 + pairs e, r, p0, p1, Ap
+  return n * (8 * 3 + 8 * 4) + red + 4096;                             // x, b, r64 + pairs e, r, p, Ap
 }
 
 sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
@@ -279,7 +279,6 @@ sipg_status admit(sipg_server* sv, Request* r) {
     r->e32 = (float*)take(n * 8);
     r->r32 = (float*)take(n * 8);
     r->p32[0] = (float*)take(n * 8);
-    r->p32[1] = (float*)take(n * 8);
     r->Ap32 = (float*)take(n * 8);
   }
   r->red32.partials = (double*)take(sizeof(double) * cap);
@@ -322,13 +321,11 @@ void retire(sipg_server* sv, Request* r, sipg_status status, int iterations, dou
 
 ApplyArgs<float> cg_args32(const Request* r, sipg_server* sv) {
   ApplyArgs<float> a{};
-  a.in = r->r32;
-  a.pbuf0 = r->p32[0];
-  a.pbuf1 = r->p32[1];
+  a.in = r->p32[0];  // the direction, formed by k_cg_direction_pairs_batched
   a.out = r->Ap32;
   a.dim = r->req.dim;
   a.nu = (float)r->req.pen;
-  a.nu_lo = (float)(r->req.pen - (double)a.nu);
+  set_penalty3(a, r->req.pen);
   a.stp = sv->slots.d32 + r->slot;
   a.red = r->red32;
   return a;
@@ -637,7 +634,7 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     PairInst v;
     v.x = r->e32;
     v.pb0 = r->p32[0];
-    v.pb1 = r->p32[1];
+    v.pb1 = r->p32[0];
     v.r = r->r32;
     v.Ap = r->Ap32;
     v.n = r->n;
@@ -680,7 +677,11 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   }
   for (int k = 0; k < sv->opts.iters_per_step; ++k) {
     if (!a32.empty()) {
-      sipg_status st = launch_groups<float>(g32, APPLY_CG, sv->d_a32, sv->d_t32, sv->s);
+      const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
+      k_cg_direction_pairs_batched<<<vg, kVecThreads, 0, sv->s>>>(sv->d_v32);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+      sipg_status st = launch_groups<float>(g32, APPLY_DOT, sv->d_a32, sv->d_t32, sv->s);
       if (st != SIPG_OK) return st;
       k_cg_update_pairs_batched<<<dim3(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size()), kVecThreads, 0,
                                   sv->s>>>(sv->d_v32);

@@ -124,7 +124,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   T* __restrict__ xf = us + S::US;
   T* __restrict__ yf = xf + S::XF;
 
-  if (MODE == APPLY_CG) {
+  constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);  // p.Ap -> alpha
+  if (kDot) {
     if (*(volatile int*)&a.st->done) return;  // converged: the launch is a no-op
   }
 
@@ -380,10 +381,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
             acc = fma(rv, rv, acc);
           } else {
             a.out[gk] = o[j];
-            if (MODE == APPLY_CG) {
-              pnew[gk] = c[j];
-              acc = fma(c[j], o[j], acc);
-            }
+            if (MODE == APPLY_CG) pnew[gk] = c[j];
+            if (kDot) acc = fma(c[j], o[j], acc);
           }
         }
       }
@@ -435,9 +434,9 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
           acc = fma(rv, rv, acc);
         } else {
           a.out[gk] = o[k];
-          if (MODE == APPLY_CG) {
+          if (kDot) {
             const T pk = us[k * TE + t];
-            pnew[gk] = pk;
+            if (MODE == APPLY_CG) pnew[gk] = pk;
             acc = fma(pk, o[k], acc);
           }
         }
@@ -450,11 +449,11 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
     T total;
     if (grid_sum_last<T, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0) {
       CgState<T>* st = a.st;
-      if (MODE == APPLY_CG) {
+      if (kDot) {
         const T alpha = st->rr / total;
         st->pAp = total;
         st->alpha = alpha;
-        st->parity = 1 - par;  // every block read the parity before arriving here
+        if (MODE == APPLY_CG) st->parity = 1 - par;  // every block read the parity before arriving here
         if (!(total > T(0)) || !isfinite(alpha)) {
           st->status = (int)SIPG_ERR_BREAKDOWN;
           st->done = 1;
@@ -516,6 +515,9 @@ cudaError_t launch_apply_tile(int mode, const ApplyArgs<T>& a, const Tab<T, P>& 
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
   if (err != cudaSuccess) return err;
   switch (mode) {
     case APPLY_PREPARE:
@@ -528,6 +530,9 @@ cudaError_t launch_apply_tile(int mode, const ApplyArgs<T>& a, const Tab<T, P>& 
       break;
     case APPLY_RESID:
       k_sipg_apply<T, P, TX, TY, APPLY_RESID><<<grid, block, smem, s>>>(a, tb);
+      break;
+    case APPLY_DOT:
+      k_sipg_apply<T, P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(a, tb);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -14,8 +14,11 @@
 // relative noise instead, and this kernel keeps the matvec that accurate at
 // FP32-pipe cost (about ten FP32 instructions per multiply-add).
 //
-// Modes: APPLY_PLAIN (y = A u) and APPLY_CG (p = r + beta p_old as pairs, Ap,
-// p.Ap reduced from double-float products, alpha = rr / pAp).  The CG scalars
+// Modes: APPLY_PLAIN (y = A u), APPLY_CG (p = r + beta p_old as pairs, Ap,
+// p.Ap reduced from double-float products, alpha = rr / pAp) and APPLY_DOT (Ap
+// and alpha for a direction p formed beforehand, k_cg_direction_pairs: the
+// apply then reads one vector, which at this kernel's occupancy -- two CTAs
+// per SM, bound by shared memory -- halves its exposed load latency).  The CG scalars
 // are FP64 (ApplyArgs::stp): a CG whose alpha, beta and dots carry 24 bits
 // smears the low end of this operator's spectrum (relative rounding 6e-8
 // times kappa ~ 1) and needs about three times the iterations.
@@ -29,15 +32,17 @@ namespace sipg {
 template <int P>
 struct TabDF {
   static constexpr int N1 = P + 1;
-  float wh[N1], wl[N1];
-  float D0h[N1], D0l[N1];
-  float DNh[N1], DNl[N1];
-  float Kh[N1 * N1], Kl[N1 * N1];
+  cf w[N1], D0[N1], DN[N1], K[N1 * N1];
 };
 
-inline void split_df(double v, float& h, float& l) {
-  h = (float)v;
-  l = (float)(v - (double)h);
+// a double as three floats, h + m + l (exact to ~2^-72 relative)
+inline cf split_cf(double v) {
+  cf c;
+  c.h = (float)v;
+  const double r1 = v - (double)c.h;
+  c.m = (float)r1;
+  c.l = (float)(r1 - (double)c.m);
+  return c;
 }
 
 template <int P>
@@ -45,11 +50,11 @@ inline TabDF<P> make_tab_df(const HostTables& h) {
   TabDF<P> t;
   const int n = P + 1;
   for (int i = 0; i < n; ++i) {
-    split_df(h.w[i], t.wh[i], t.wl[i]);
-    split_df(h.D[i * n + 0], t.D0h[i], t.D0l[i]);
-    split_df(h.D[i * n + P], t.DNh[i], t.DNl[i]);
+    t.w[i] = split_cf(h.w[i]);
+    t.D0[i] = split_cf(h.D[i * n + 0]);
+    t.DN[i] = split_cf(h.D[i * n + P]);
   }
-  for (int i = 0; i < n * n; ++i) split_df(h.K[i], t.Kh[i], t.Kl[i]);
+  for (int i = 0; i < n * n; ++i) t.K[i] = split_cf(h.K[i]);
   return t;
 }
 
@@ -79,7 +84,8 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   float* __restrict__ xf = us + S::US;
   float* __restrict__ yf = xf + S::XF;
 
-  if (MODE == APPLY_CG) {
+  constexpr bool kReduce = (MODE == APPLY_CG || MODE == APPLY_DOT);  // p.Ap -> alpha
+  if (kReduce) {
     if (*(volatile int*)&a.stp->done) return;
   }
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
@@ -129,12 +135,12 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   auto combine = [&](int j, bool interior, df u0, df d0, df uN, df dN, df& J, df& Q) {
     const float kap = interior ? 0.5f : 1.f;
     const df jmp = df_add(u0, df_neg(uN));
-    const df wj = df_mul(tb.wh[j], tb.wl[j], jmp);
+    const df wj = df_mulc(tb.w[j], jmp);
     J = df{wj.hi * kap, wj.lo * kap};  // exact: kappa is a power of two
     df s = df_add(d0, dN);
     s = df{s.hi * kap, s.lo * kap};
-    s = df_mac2(s, a.nu, a.nu_lo, jmp);  // the penalty, per operator
-    Q = df_mul(tb.wh[j], tb.wl[j], s);
+    s = df_macc(s, cf{a.nu, a.nu_lo, a.nu_lo2}, jmp);  // the penalty, per operator
+    Q = df_mulc(tb.w[j], s);
   };
   auto put = [&](float& h, float& l, df v) {
     h = v.hi;
@@ -157,7 +163,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
     for (int j = 0; j < N1; ++j) {
       df d = df_zero();
 #pragma unroll
-      for (int i = 0; i < N1; ++i) d = df_mac2(d, tb.D0h[i], tb.D0l[i], U(i, j));
+      for (int i = 0; i < N1; ++i) d = df_macc(d, tb.D0[i], U(i, j));
       put(XFr(ty, 0, j, tx), XFr(ty, 1, j, tx), U(0, j));
       put(XFr(ty, 2, j, tx), XFr(ty, 3, j, tx), d);
     }
@@ -165,7 +171,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
     for (int j = 0; j < N1; ++j) {
       df d = df_zero();
 #pragma unroll
-      for (int i = 0; i < N1; ++i) d = df_mac2(d, tb.D0h[i], tb.D0l[i], U(j, i));
+      for (int i = 0; i < N1; ++i) d = df_macc(d, tb.D0[i], U(j, i));
       put(YFr(ty + 1, 0, j, tx), YFr(ty + 1, 1, j, tx), U(j, 0));
       put(YFr(ty + 1, 2, j, tx), YFr(ty + 1, 3, j, tx), d);
     }
@@ -181,7 +187,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         for (int i = 0; i < N1; ++i) {
           const df v = ld(j * N1 + i, he);
           if (i == 0) u0 = v;
-          d = df_mac2(d, tb.D0h[i], tb.D0l[i], v);
+          d = df_macc(d, tb.D0[i], v);
         }
         put(YFr(0, 0, j, t), YFr(0, 1, j, t), u0);
         put(YFr(0, 2, j, t), YFr(0, 3, j, t), d);
@@ -198,7 +204,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         for (int i = 0; i < N1; ++i) {
           const df v = ld(i * N1 + j, he);
           if (i == 0) u0 = v;
-          d = df_mac2(d, tb.D0h[i], tb.D0l[i], v);
+          d = df_macc(d, tb.D0[i], v);
         }
         put(XFr(r, 0, j, TX), XFr(r, 1, j, TX), u0);
         put(XFr(r, 2, j, TX), XFr(r, 3, j, TX), d);
@@ -214,7 +220,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
     for (int j = 0; j < N1; ++j) {
       df dN = df_zero();
 #pragma unroll
-      for (int i = 0; i < N1; ++i) dN = df_mac2(dN, tb.DNh[i], tb.DNl[i], U(i, j));
+      for (int i = 0; i < N1; ++i) dN = df_macc(dN, tb.DN[i], U(i, j));
       const df u0 = rint ? XF2(ty, 0, j, tx + 1) : df_zero();
       const df d0 = rint ? XF2(ty, 2, j, tx + 1) : df_zero();
       df J, Q;
@@ -227,7 +233,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
     for (int j = 0; j < N1; ++j) {
       df dN = df_zero();
 #pragma unroll
-      for (int i = 0; i < N1; ++i) dN = df_mac2(dN, tb.DNh[i], tb.DNl[i], U(j, i));
+      for (int i = 0; i < N1; ++i) dN = df_macc(dN, tb.DN[i], U(j, i));
       const df u0 = uint_ ? YF2(ty, 0, j, tx) : df_zero();
       const df d0 = uint_ ? YF2(ty, 2, j, tx) : df_zero();
       df J, Q;
@@ -265,7 +271,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         for (int i = 0; i < N1; ++i) {
           const df v = ld(j * N1 + i, he);
           if (i == N) uN = v;
-          dN = df_mac2(dN, tb.DNh[i], tb.DNl[i], v);
+          dN = df_macc(dN, tb.DN[i], v);
         }
         df J, Q;
         combine(j, true, YF2(TY, 0, j, t), YF2(TY, 2, j, t), uN, dN, J, Q);
@@ -284,7 +290,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         for (int i = 0; i < N1; ++i) {
           const df v = ld(i * N1 + j, he);
           if (i == N) uN = v;
-          dN = df_mac2(dN, tb.DNh[i], tb.DNl[i], v);
+          dN = df_macc(dN, tb.DN[i], v);
         }
         df J, Q;
         combine(j, true, XF2(r, 0, j, 0), XF2(r, 2, j, 0), uN, dN, J, Q);
@@ -305,28 +311,27 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       for (int j = 0; j < N1; ++j) o[j] = df_zero();
 #pragma unroll
       for (int i = 0; i < N1; ++i) {
-        const float kh = tb.Kh[i1 * N1 + i], kl = tb.Kl[i1 * N1 + i];
+        const cf kc = tb.K[i1 * N1 + i];
 #pragma unroll
-        for (int j = 0; j < N1; ++j) o[j] = df_mac2(o[j], kh, kl, Uv(i, j));
+        for (int j = 0; j < N1; ++j) o[j] = df_macc(o[j], kc, Uv(i, j));
       }
       df c[N1];
 #pragma unroll
       for (int i = 0; i < N1; ++i) c[i] = U(i1, i);
       const df gJ = YF2(ty + 1, 0, i1, tx);
       const df hJ = YF2(ty, 0, i1, tx);
-      const float d0i = tb.D0h[i1], d0il = tb.D0l[i1], dni = tb.DNh[i1], dnil = tb.DNl[i1];
-      const float wi = tb.wh[i1], wil = tb.wl[i1];
+      const cf d0i = tb.D0[i1], dni = tb.DN[i1], wi = tb.w[i1];
 #pragma unroll
       for (int j = 0; j < N1; ++j) {
         df s = df_zero();
 #pragma unroll
-        for (int i = 0; i < N1; ++i) s = df_mac2(s, tb.Kh[j * N1 + i], tb.Kl[j * N1 + i], c[i]);
-        df v = df_mul(tb.wh[j], tb.wl[j], o[j]);
-        v = df_mac2(v, d0i, d0il, XF2(ty, 0, j, tx));
-        v = df_mac2(v, dni, dnil, XF2(ty, 0, j, tx + 1));
-        v = df_mac2(v, wi, wil, s);
-        v = df_mac2(v, tb.D0h[j], tb.D0l[j], gJ);
-        v = df_mac2(v, tb.DNh[j], tb.DNl[j], hJ);
+        for (int i = 0; i < N1; ++i) s = df_macc(s, tb.K[j * N1 + i], c[i]);
+        df v = df_mulc(tb.w[j], o[j]);
+        v = df_macc(v, d0i, XF2(ty, 0, j, tx));
+        v = df_macc(v, dni, XF2(ty, 0, j, tx + 1));
+        v = df_macc(v, wi, s);
+        v = df_macc(v, tb.D0[j], gJ);
+        v = df_macc(v, tb.DN[j], hJ);
         if (i1 == 0) v = df_add(v, XF2(ty, 2, j, tx));
         if (i1 == N) v = df_add(v, df_neg(XF2(ty, 2, j, tx + 1)));
         if (j == 0) v = df_add(v, YF2(ty + 1, 2, i1, tx));
@@ -338,13 +343,13 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         if (MODE == APPLY_CG) {
           pnew[oi] = c[j].hi;
           pnew[lo_off + oi] = c[j].lo;
-          dot = df_mac2(dot, c[j].hi, c[j].lo, v);
         }
+        if (kReduce) dot = df_mac2(dot, c[j].hi, c[j].lo, v);
       }
     }
   }
 
-  if (MODE == APPLY_CG) {
+  if (kReduce) {
     const double bt = block_sum<double, TE>((double)dot.hi + (double)dot.lo, red_sh);
     double total;
     if (grid_sum_last<double, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0) {
@@ -353,7 +358,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       const double alpha = st->rr / pAp;
       st->pAp = pAp;
       st->alpha = alpha;
-      st->parity = 1 - par;
+      if (MODE == APPLY_CG) st->parity = 1 - par;
       if (!(pAp > 0.0) || !isfinite(alpha)) {
         st->status = (int)SIPG_ERR_BREAKDOWN;
         st->done = 1;
@@ -395,10 +400,12 @@ cudaError_t launch_apply_df_tile(int mode, const ApplyArgs<float>& a, const Appl
   constexpr int TX = 32;
   const size_t smem = ApplyDfSmem<P, TX, TY>::bytes;
   cudaError_t err = cudaSuccess;
-  const void* fns[4] = {(const void*)k_sipg_apply_df<P, TX, TY, APPLY_PLAIN>,
+  const void* fns[6] = {(const void*)k_sipg_apply_df<P, TX, TY, APPLY_PLAIN>,
                         (const void*)k_sipg_apply_df<P, TX, TY, APPLY_CG>,
+                        (const void*)k_sipg_apply_df<P, TX, TY, APPLY_DOT>,
                         (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_PLAIN>,
-                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_CG>};
+                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_CG>,
+                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_DOT>};
   for (const void* f : fns) {
     err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
@@ -409,6 +416,7 @@ cudaError_t launch_apply_df_tile(int mode, const ApplyArgs<float>& a, const Appl
     const dim3 grid((a.dim + TX - 1) / TX, (a.dim + TY - 1) / TY);
     if (mode == APPLY_PLAIN) k_sipg_apply_df<P, TX, TY, APPLY_PLAIN><<<grid, block, smem, s>>>(a, tb);
     else if (mode == APPLY_CG) k_sipg_apply_df<P, TX, TY, APPLY_CG><<<grid, block, smem, s>>>(a, tb);
+    else if (mode == APPLY_DOT) k_sipg_apply_df<P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(a, tb);
     else return cudaErrorInvalidValue;
   } else {
     if (total_tiles == 0) return cudaSuccess;
@@ -416,6 +424,8 @@ cudaError_t launch_apply_df_tile(int mode, const ApplyArgs<float>& a, const Appl
       k_sipg_apply_df_batched<P, TX, TY, APPLY_PLAIN><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
     else if (mode == APPLY_CG)
       k_sipg_apply_df_batched<P, TX, TY, APPLY_CG><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
+    else if (mode == APPLY_DOT)
+      k_sipg_apply_df_batched<P, TX, TY, APPLY_DOT><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
     else return cudaErrorInvalidValue;
   }
   count_launch();

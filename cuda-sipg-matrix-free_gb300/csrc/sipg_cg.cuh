@@ -75,6 +75,22 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, co
   cg_update_body<T>(x, pb0, pb1, r, Ap, n, st, red, blockIdx.x, gridDim.x);
 }
 
+// p = r on the first iteration of a solve, else p = r + beta p, in place:
+// the direction of an APPLY_DOT iteration.  Forming it here rather than in
+// the apply (APPLY_CG) costs one more pass over p and r but lets the apply --
+// whose occupancy shared memory caps at a few CTAs per SM -- read one vector
+// instead of two, which hides most of its load latency.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_direction(T* __restrict__ p, const T* __restrict__ r, size_t n,
+                                                              const CgState<T>* st) {
+  if (*(volatile const int*)&st->done) return;
+  const bool first = st->first != 0;
+  const T beta = st->beta;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    p[i] = first ? r[i] : fma(beta, p[i], r[i]);
+}
+
 // Per-instance vector operands of a batch (instance = blockIdx.y).  Each
 // instance uses its own nblk blocks (the rest of the grid row returns at
 // once), so its reductions -- and so its iterates -- do not depend on which

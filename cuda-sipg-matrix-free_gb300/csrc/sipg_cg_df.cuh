@@ -75,7 +75,44 @@ __device__ __forceinline__ void cg_update_pairs_body(float* __restrict__ x, cons
     cg_bookkeep<double>(st, total);
 }
 
+// p = r (first iteration after a start) or p = r + beta p, in place, on pair
+// vectors (beta FP64 as a double-float coefficient).  Runs before the
+// APPLY_DOT apply of the same iteration.
+__device__ __forceinline__ void cg_direction_pairs_body(float* __restrict__ p, const float* __restrict__ r, size_t n,
+                                                        const CgState<double>* st, int bid, int nblocks) {
+  if (*(volatile const int*)&st->done) return;
+  const bool first = st->first != 0;
+  const double beta = st->beta;
+  const float bh = (float)beta, bl = (float)(beta - (double)bh);
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const df ri{r[i], r[n + i]};
+    df v = ri;
+    if (!first) {
+      v = df_mac2(ri, bh, bl, df{p[i], p[n + i]});
+      const float s = __fadd_rn(v.hi, v.lo);
+      v = df{s, __fsub_rn(v.lo, __fsub_rn(s, v.hi))};
+    }
+    p[i] = v.hi;
+    p[n + i] = v.lo;
+  }
+}
+
 // (templates only so that every translation unit may instantiate them)
+template <int KIND = INNER_PAIRS>
+__global__ void __launch_bounds__(kVecThreads)
+    k_cg_direction_pairs(float* __restrict__ p, const float* __restrict__ r, size_t n, const CgState<double>* st) {
+  cg_direction_pairs_body(p, r, n, st, blockIdx.x, gridDim.x);
+}
+
+template <int KIND = INNER_PAIRS>
+__global__ void __launch_bounds__(kVecThreads)
+    k_cg_direction_pairs_batched(const PairInst* __restrict__ insts) {
+  const PairInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  cg_direction_pairs_body(v.pb0, v.r, v.n, v.st, blockIdx.x, v.nblk);
+}
+
 template <int KIND = INNER_PAIRS>
 __global__ void __launch_bounds__(kVecThreads)
     k_cg_update_pairs(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,

@@ -49,6 +49,30 @@ __device__ __forceinline__ df df_mac2(df acc, float ch, float cl, df x) {
   return df{s, __fadd_rn(acc.lo, __fadd_rn(err, small))};
 }
 
+// A table coefficient as three floats, c = h + m + l (about 72 bits): with
+// two, the coefficients of the operator itself would be off by 2^-48
+// relative -- a fixed perturbation whose effect on smooth vectors does not
+// average out and which a CG therefore cannot iterate past.
+struct cf {
+  float h, m, l;
+};
+
+// acc + c * x, c a three-float coefficient, x a df value; the terms below
+// 2^-48 |c x| that remain are rounding, not a perturbation of c
+__device__ __forceinline__ df df_macc(df acc, cf c, df x) {
+  const float p = __fmul_rn(c.h, x.hi);
+  const float e = __fmaf_rn(c.h, x.hi, -p);
+  float s, err;
+  two_sum(acc.hi, p, s, err);
+  float t = __fmul_rn(c.l, x.hi);
+  t = __fmaf_rn(c.m, x.lo, t);
+  t = __fmaf_rn(c.m, x.hi, t);
+  t = __fmaf_rn(c.h, x.lo, t);
+  return df{s, __fadd_rn(acc.lo, __fadd_rn(err, __fadd_rn(e, t)))};
+}
+
+__device__ __forceinline__ df df_mulc(cf c, df x) { return df_macc(df{0.f, 0.f}, c, x); }
+
 __device__ __forceinline__ df df_add(df a, df b) {
   float s, err;
   two_sum(a.hi, b.hi, s, err);

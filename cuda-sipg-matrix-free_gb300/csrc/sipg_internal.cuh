@@ -99,7 +99,8 @@ enum ApplyMode : int {
   APPLY_PLAIN = 0,  // y = A u
   APPLY_CG = 1,     // u = r + beta p_old (u = r on the first iteration); p_new = u; y = A u; pAp -> alpha;
                     // the parity of the direction buffers flips
-  APPLY_RESID = 2   // y = b - A u; r.r -> rr, stop/done set
+  APPLY_RESID = 2,  // y = b - A u; r.r -> rr, stop/done set
+  APPLY_DOT = 3     // y = A p for a direction p formed beforehand (k_cg_direction*); p.Ap -> alpha
 };
 
 template <typename T>
@@ -111,11 +112,19 @@ struct ApplyArgs {
   const T* b;      // RESID: right-hand side
   int dim;
   T nu;            // penalty (the reference's `pen`)
-  T nu_lo;         // compensated apply: pen - (float) pen (0 otherwise)
+  T nu_lo, nu_lo2;  // compensated apply: pen as three floats nu + nu_lo + nu_lo2
   CgState<T>* st;  // CG / RESID
   ReduceScratch red;
   CgState<double>* stp;  // compensated apply, CG mode: the inner state (FP64 scalars)
 };
+
+// The penalty of a compensated apply as three floats (nu + nu_lo + nu_lo2).
+inline void set_penalty3(ApplyArgs<float>& a, double pen) {
+  a.nu = (float)pen;
+  const double r1 = pen - (double)a.nu;
+  a.nu_lo = (float)r1;
+  a.nu_lo2 = (float)(r1 - (double)a.nu_lo);
+}
 
 // Tile shape chosen for one (precision, degree).
 struct TileCfg {
