@@ -612,22 +612,28 @@ def _serve_stream(sipg, reqs, precision, max_active=256):
 
 
 def run_serve(args):
+    """The request stream at a few arrival rates, mixed-precision requests and
+    plain FP64 requests through the same server."""
     import sipg_gb300 as sipg
     import workloads
 
-    reqs = workloads.request_stream(count=args.requests, rate=args.rate, seed=3)
+    rates = [float(r) for r in str(args.rate).split(",")]
     sampler = ClockSampler(0)
     sampler.start()
     n0 = sipg.launch_count()
-    mixed = _serve_stream(sipg, reqs, sipg.F32)
-    fp64 = _serve_stream(sipg, reqs, sipg.F64)
+    sweep = []
+    for rate in rates:
+        reqs = workloads.request_stream(count=args.requests, rate=rate, seed=3)
+        sweep.append({"rate_per_s": rate, "mixed": _serve_stream(sipg, reqs, sipg.F32),
+                      "fp64": _serve_stream(sipg, reqs, sipg.F64)})
     launches = sipg.launch_count() - n0
     clocks = sampler.stop()
-    line = _base_line(args, "p99 latency (ms), solve server, mixed precision", mixed["p99_ms"], "ms", False,
-                      "f32 pairs (inner) + f64 (outer)",
-                      {"workload": "%d requests, Poisson arrivals at %g/s, N log-uniform [8,512], p in 2..8, "
-                                   "tol in {1e-8, 1e-10} (seed 3); 150 GB budget" % (args.requests, args.rate)},
-                      mixed=mixed, fp64=fp64, clocks=clocks, gpu_launches=launches)
+    head = sweep[len(sweep) // 2]
+    line = _base_line(args, "p99 latency (ms), solve server, mixed precision, at %g requests/s" % head["rate_per_s"],
+                      head["mixed"]["p99_ms"], "ms", False, "f32 pairs (inner) + f64 (outer)",
+                      {"workload": "%d requests per rate, Poisson arrivals, N log-uniform [8,512], p in 2..8, "
+                                   "tol in {1e-8, 1e-10} (seed 3); 150 GB budget" % args.requests},
+                      sweep=sweep, clocks=clocks, gpu_launches=launches)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -641,8 +647,8 @@ def main():
     ap.add_argument("--config", choices=("apply", "sweep", "solve16", "mixed", "batch", "serve"), default="apply",
                     help="apply: the headline (1024x1024 p=4 apply); the others are the solver's other workloads")
     ap.add_argument("--uneven", type=int, default=200, help="batch: number of uneven problems")
-    ap.add_argument("--requests", type=int, default=200, help="serve: requests in the stream")
-    ap.add_argument("--rate", type=float, default=100.0, help="serve: arrivals per second")
+    ap.add_argument("--requests", type=int, default=100, help="serve: requests per arrival rate")
+    ap.add_argument("--rate", default="2,5,10", help="serve: arrival rates per second, comma-separated")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

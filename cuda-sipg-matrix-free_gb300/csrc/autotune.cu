@@ -1,16 +1,18 @@
 // autotune.cu -- picks the apply tile shape per operator by timing (no
 // counterpart in the reference, whose kernels use one fixed geometry).
 //
-// A tile is TX = 32 elements along a mesh row (one thread per element, so a
-// warp's loads of one node are 32 consecutive values) by TY rows; a CTA holds
-// TX * TY elements and their (p+1)^2 nodal blocks in shared memory.  TY trades
-// halo overhead (TX + TY halo elements per tile) and reduction partials
-// against shared memory per CTA and so resident CTAs per SM, and the best
-// choice depends on the degree, the mesh size (how many waves of CTAs fill the
-// 152 SMs) and the arithmetic (FP64, FP32, compensated FP32).  The tuner times
-// each candidate TY on the operator itself -- a few applies on scratch vectors
-// -- keeps the fastest, and remembers it for (degree, dim, precision) in a
-// process-wide table that new operators consult at creation.  Every tile
+// A tile is TX = 32 elements along a mesh row (a warp's loads of one node are
+// 32 consecutive values) by TY rows, with one or two threads per element; a
+// CTA holds TX * TY elements and their (p+1)^2 nodal blocks in shared memory.
+// TY trades halo overhead (TX + TY halo elements per tile) and reduction
+// partials against shared memory per CTA and so resident CTAs per SM; a
+// second thread per element doubles the resident warps at the same shared
+// memory, which pays where the apply waits on latency (the compensated one)
+// rather than on a pipe (FP64).  The best choice depends on the degree, the
+// mesh size (how many waves of CTAs fill the 152 SMs) and the arithmetic.  The
+// tuner times each candidate on the operator itself -- a few applies on
+// scratch vectors -- keeps the fastest, and remembers it for (degree, dim,
+// kind) in a process-wide table that new operators consult at creation.  Every tile
 // shape computes each output from the same operations in the same order, so
 // the apply's result does not depend on the choice (CG reductions sum
 // per-block partials, whose grouping does change with TY).
@@ -27,9 +29,11 @@ namespace sipg {
 
 namespace {
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, int> g_tuned;  // (p, dim, prec) -> TY
+std::map<std::tuple<int, int, int>, TileCfg> g_tuned;  // (p, dim, kind) -> shape
 
-constexpr int kCandidates[3] = {2, 4, 8};
+// (rows, threads per element); two threads per element only for the
+// compensated apply, the one limited by latency rather than a pipe
+constexpr int kCandidates[5][2] = {{2, 1}, {4, 1}, {8, 1}, {2, 2}, {4, 2}};
 
 template <typename T>
 cudaError_t run_apply(const sipg_op* op, int prec, const TileCfg& cfg, const void* in, void* out, cudaStream_t s) {
@@ -49,11 +53,12 @@ cudaError_t run_apply(const sipg_op* op, int prec, const TileCfg& cfg, const voi
 
 // average ms per apply of one candidate, or a negative value if it cannot run
 template <typename T>
-float time_candidate(const sipg_op* op, int prec, int ty, const void* in, void* out, cudaStream_t s, cudaEvent_t e0,
-                     cudaEvent_t e1, int reps) {
+float time_candidate(const sipg_op* op, int prec, int ty, int tpe, const void* in, void* out, cudaStream_t s,
+                     cudaEvent_t e0, cudaEvent_t e1, int reps) {
   TileCfg cfg;
   cfg.tx = 32;
   cfg.ty = ty;
+  cfg.tpe = tpe;
   if (run_apply<T>(op, prec, cfg, in, out, s) != cudaSuccess) {
     cudaGetLastError();  // a launch-configuration error (shared memory); clear it
     return -1.f;
@@ -70,15 +75,18 @@ float time_candidate(const sipg_op* op, int prec, int ty, const void* in, void* 
 }
 
 template <typename T>
-int tune_one(const sipg_op* op, int prec, const void* in, void* out, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
-             float* best_ms) {
+TileCfg tune_one(const sipg_op* op, int prec, const void* in, void* out, cudaStream_t s, cudaEvent_t e0,
+                 cudaEvent_t e1, float* best_ms) {
   const int reps = (int)std::max<long long>(3, std::min<long long>(50, (long long)(2.0e7 / (double)op->ndof)));
-  int best = 0;
+  TileCfg best;
+  best.ty = 0;
   float bms = 0.f;
-  for (int ty : kCandidates) {
-    const float ms = time_candidate<T>(op, prec, ty, in, out, s, e0, e1, reps);
-    if (ms > 0.f && (best == 0 || ms < bms)) {
-      best = ty;
+  for (const auto& c : kCandidates) {
+    if (c[1] != 1 && prec != SIPG_TUNE_PAIRS) continue;
+    const float ms = time_candidate<T>(op, prec, c[0], c[1], in, out, s, e0, e1, reps);
+    if (ms > 0.f && (best.ty == 0 || ms < bms)) {
+      best.ty = c[0];
+      best.tpe = c[1];
       bms = ms;
     }
   }
@@ -91,8 +99,7 @@ bool autotune_lookup(int p, int dim, int prec, TileCfg* cfg) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(p, dim, prec));
   if (it == g_tuned.end()) return false;
-  cfg->tx = 32;
-  cfg->ty = it->second;
+  *cfg = it->second;
   return true;
 }
 
@@ -112,7 +119,8 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const size_t bytes = (size_t)op->ndof * sizeof(double);
   sipg_status st = SIPG_OK;
-  int ty[3] = {0, 0, 0};
+  TileCfg ty[3];
+  for (TileCfg& c : ty) c.ty = 0;
   float ms[3] = {0.f, 0.f, 0.f};
   cudaError_t e = cudaMalloc(&in, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&outv, bytes);
@@ -128,7 +136,7 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   if (e != cudaSuccess) {
     set_error(std::string("sipg_op_autotune: ") + cudaGetErrorString(e));
     st = e == cudaErrorMemoryAllocation ? SIPG_ERR_NOMEM : SIPG_ERR_CUDA;
-  } else if (!ty[0] || !ty[1] || !ty[2]) {
+  } else if (!ty[0].ty || !ty[1].ty || !ty[2].ty) {
     set_error("sipg_op_autotune: no tile shape could be launched");
     st = SIPG_ERR_CUDA;
   }
@@ -139,9 +147,9 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   if (st != SIPG_OK) return st;
   {
     std::lock_guard<std::mutex> lk(op->mu);
-    op->cfg64.ty = ty[SIPG_TUNE_F64];
-    op->cfg32.ty = ty[SIPG_TUNE_F32];
-    op->cfgdf.ty = ty[SIPG_TUNE_PAIRS];
+    op->cfg64 = ty[SIPG_TUNE_F64];
+    op->cfg32 = ty[SIPG_TUNE_F32];
+    op->cfgdf = ty[SIPG_TUNE_PAIRS];
     op->tile_gen++;
   }
   {
@@ -150,7 +158,8 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   }
   if (out) {
     for (int k = 0; k < 3; ++k) {
-      out->rows[k] = ty[k];
+      out->rows[k] = ty[k].ty;
+      out->threads_per_element[k] = ty[k].tpe;
       out->ms_per_apply[k] = ms[k];
     }
     out->elements_per_row = 32;
@@ -158,25 +167,29 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   return SIPG_OK;
 }
 
-sipg_status sipg_op_set_tile(sipg_op* op, int precision, int rows) {
-  if (!op || precision < 0 || precision > 2 || (rows != 2 && rows != 4 && rows != 8)) {
-    set_error("sipg_op_set_tile: precision must be 0..2 and rows 2, 4 or 8");
+sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows, int threads_per_element) {
+  const bool tpe_ok = threads_per_element == 1 || (threads_per_element == 2 && kind == SIPG_TUNE_PAIRS && rows != 8);
+  if (!op || kind < 0 || kind > 2 || (rows != 2 && rows != 4 && rows != 8) || !tpe_ok) {
+    set_error("sipg_op_set_tile: kind must be 0..2, rows 2, 4 or 8, threads per element 1 (or 2 for the pairs "
+              "apply with 2 or 4 rows)");
     return SIPG_ERR_INVALID;
   }
   std::lock_guard<std::mutex> lk(op->mu);
-  TileCfg& c = precision == SIPG_TUNE_F64 ? op->cfg64 : (precision == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
+  TileCfg& c = kind == SIPG_TUNE_F64 ? op->cfg64 : (kind == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
   c.ty = rows;
+  c.tpe = threads_per_element;
   op->tile_gen++;
   return SIPG_OK;
 }
 
-sipg_status sipg_op_get_tile(const sipg_op* op, int precision, int* rows) {
-  if (!op || !rows || precision < 0 || precision > 2) {
+sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows, int* threads_per_element) {
+  if (!op || !rows || kind < 0 || kind > 2) {
     set_error("sipg_op_get_tile: bad argument");
     return SIPG_ERR_INVALID;
   }
-  const TileCfg& c = precision == SIPG_TUNE_F64 ? op->cfg64 : (precision == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
+  const TileCfg& c = kind == SIPG_TUNE_F64 ? op->cfg64 : (kind == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
   *rows = c.ty;
+  if (threads_per_element) *threads_per_element = c.tpe;
   return SIPG_OK;
 }
 

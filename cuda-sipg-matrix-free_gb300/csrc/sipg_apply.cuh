@@ -43,7 +43,7 @@ __device__ __forceinline__ A warp_sum(A v) {
 // Sum over the block; the result is valid in linear thread 0.  NT % 32 == 0.
 template <typename A, int NT>
 __device__ __forceinline__ A block_sum(A v, A* sh) {
-  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int t = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;  // linear thread id
   v = warp_sum(v);
   if ((t & 31) == 0) sh[t >> 5] = v;
   __syncthreads();
@@ -62,7 +62,7 @@ template <typename A, int NT>
 __device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch& red, int bid, int nblocks, A* sh,
                                               A* total) {
   __shared__ int s_last;
-  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int t = (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;  // linear thread id
   if (t == 0) {
     red.partials[bid] = (double)block_total;
     __threadfence();

@@ -73,10 +73,15 @@ __device__ __forceinline__ df df_norm(df v) {
   return df{s, __fsub_rn(v.lo, __fsub_rn(s, v.hi))};
 }
 
-template <int P, int TX, int TY, int MODE>
+// TPE threads per element (1 or 2; threadIdx.z = s): with 2, s = 0 takes the
+// x faces, s = 1 the y faces, and the two split the element's nodal loads and
+// output columns -- twice the resident warps for the same shared memory.
+template <int P, int TX, int TY, int TPE, int MODE>
 __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const TabDF<P>& tb, int bx, int by, int bid,
                                               int nblocks) {
-  constexpr int N = P, N1 = P + 1, NN = N1 * N1, TE = TX * TY;
+  constexpr int N = P, N1 = P + 1, NN = N1 * N1, TE = TX * TY, NT = TE * TPE;
+  static_assert(TPE == 1 || TPE == 2, "one or two threads per element");
+  static_assert(TPE == 2 || TE >= TX + TY, "halo threads");
   using S = ApplyDfSmem<P, TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red_sh[32];
@@ -89,6 +94,14 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
     if (*(volatile int*)&a.stp->done) return;
   }
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+  const int s = (TPE == 2) ? (int)threadIdx.z : 0;
+  const int lt = s * TE + t;  // linear thread id
+  const bool xs = (TPE == 1) || s == 0, ys = (TPE == 1) || s == 1;  // this thread's face directions
+  // halo roles: A (the row above / below, x index ha), B (the column right /
+  // left, row hb)
+  const bool haloA = (TPE == 1) ? (t < TX) : (s == 0 && t < TX);
+  const bool haloB = (TPE == 1) ? (t >= TX && t < TX + TY) : (s == 1 && t < TY);
+  const int hb = (TPE == 1) ? t - TX : t;
   const int dim = a.dim;
   const int x0 = bx * TX, y0 = by * TY;
   const int gx = x0 + tx, gy = y0 + ty;
@@ -150,7 +163,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   // ---- phase 0: nodal values of the tile's elements ------------------------
   // (loads only: CG mode writes the new direction in phase 2)
 #pragma unroll(ApplyColumnForm<float, P>::load_unroll)
-  for (int k = 0; k < NN; ++k) {
+  for (int k = s; k < NN; k += TPE) {
     const df v = act ? ld(k, e) : df_zero();
     us[k * TE + t] = v.hi;
     us[NN * TE + k * TE + t] = v.lo;
@@ -158,7 +171,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   __syncthreads();
 
   // ---- phase 1a: 0-side traces and derivatives -----------------------------
-  if (act) {
+  if (act && xs) {
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
       df d = df_zero();
@@ -167,6 +180,8 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       put(XFr(ty, 0, j, tx), XFr(ty, 1, j, tx), U(0, j));
       put(XFr(ty, 2, j, tx), XFr(ty, 3, j, tx), d);
     }
+  }
+  if (act && ys) {
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
       df d = df_zero();
@@ -176,7 +191,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       put(YFr(ty + 1, 2, j, tx), YFr(ty + 1, 3, j, tx), d);
     }
   }
-  if (t < TX) {  // halo above: its DOWN face
+  if (haloA) {  // halo above: its DOWN face
     const int hx = x0 + t;
     if (y0 > 0 && hx < dim) {
       const size_t he = (size_t)(y0 - 1) * dim + hx;
@@ -193,8 +208,9 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         put(YFr(0, 2, j, t), YFr(0, 3, j, t), d);
       }
     }
-  } else if (t < TX + TY) {  // halo right: its LEFT face
-    const int r = t - TX, hy = y0 + r, hx = x0 + TX;
+  }
+  if (haloB) {  // halo right: its LEFT face
+    const int r = hb, hy = y0 + r, hx = x0 + TX;
     if (hx < dim && hy < dim) {
       const size_t he = (size_t)hy * dim + hx;
 #pragma unroll 1
@@ -214,7 +230,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   __syncthreads();
 
   // ---- phase 1b: N-side combines (J, Q) ------------------------------------
-  if (act) {
+  if (act && xs) {
     const bool rint = gx < dim - 1;
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
@@ -228,6 +244,17 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       put(XFr(ty, 0, j, tx + 1), XFr(ty, 1, j, tx + 1), J);
       put(XFr(ty, 2, j, tx + 1), XFr(ty, 3, j, tx + 1), Q);
     }
+    if (gx == 0) {
+#pragma unroll
+      for (int j = 0; j < N1; ++j) {
+        df J, Q;
+        combine(j, false, XF2(ty, 0, j, tx), XF2(ty, 2, j, tx), df_zero(), df_zero(), J, Q);
+        put(XFr(ty, 0, j, tx), XFr(ty, 1, j, tx), J);
+        put(XFr(ty, 2, j, tx), XFr(ty, 3, j, tx), Q);
+      }
+    }
+  }
+  if (act && ys) {
     const bool uint_ = gy > 0;
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
@@ -241,15 +268,6 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       put(YFr(ty, 0, j, tx), YFr(ty, 1, j, tx), J);
       put(YFr(ty, 2, j, tx), YFr(ty, 3, j, tx), Q);
     }
-    if (gx == 0) {
-#pragma unroll
-      for (int j = 0; j < N1; ++j) {
-        df J, Q;
-        combine(j, false, XF2(ty, 0, j, tx), XF2(ty, 2, j, tx), df_zero(), df_zero(), J, Q);
-        put(XFr(ty, 0, j, tx), XFr(ty, 1, j, tx), J);
-        put(XFr(ty, 2, j, tx), XFr(ty, 3, j, tx), Q);
-      }
-    }
     if (gy == dim - 1) {
 #pragma unroll
       for (int j = 0; j < N1; ++j) {
@@ -260,7 +278,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
       }
     }
   }
-  if (t < TX) {  // halo below: N-side of y face TY
+  if (haloA) {  // halo below: N-side of y face TY
     const int hx = x0 + t, hy = y0 + TY;
     if (hy < dim && hx < dim) {
       const size_t he = (size_t)hy * dim + hx;
@@ -279,8 +297,9 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
         put(YFr(TY, 2, j, t), YFr(TY, 3, j, t), Q);
       }
     }
-  } else if (t < TX + TY) {  // halo left: N-side of x face 0
-    const int r = t - TX, hy = y0 + r;
+  }
+  if (haloB) {  // halo left: N-side of x face 0
+    const int r = hb, hy = y0 + r;
     if (x0 > 0 && hy < dim) {
       const size_t he = (size_t)hy * dim + (x0 - 1);
 #pragma unroll 1
@@ -305,7 +324,7 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   df dot = df_zero();
   if (act) {
 #pragma unroll 1
-    for (int i1 = 0; i1 < N1; ++i1) {
+    for (int i1 = s; i1 < N1; i1 += TPE) {
       df o[N1];
 #pragma unroll
       for (int j = 0; j < N1; ++j) o[j] = df_zero();
@@ -350,9 +369,9 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   }
 
   if (kReduce) {
-    const double bt = block_sum<double, TE>((double)dot.hi + (double)dot.lo, red_sh);
+    const double bt = block_sum<double, NT>((double)dot.hi + (double)dot.lo, red_sh);
     double total;
-    if (grid_sum_last<double, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0) {
+    if (grid_sum_last<double, NT>(bt, a.red, bid, nblocks, red_sh, &total) && lt == 0) {
       CgState<double>* st = a.stp;
       const double pAp = total;
       const double alpha = st->rr / pAp;
@@ -367,15 +386,15 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   }
 }
 
-template <int P, int TX, int TY, int MODE>
-__global__ void __launch_bounds__(TX* TY)
+template <int P, int TX, int TY, int TPE, int MODE>
+__global__ void __launch_bounds__(TX* TY* TPE)
     k_sipg_apply_df(const __grid_constant__ ApplyArgs<float> a, const __grid_constant__ TabDF<P> tb) {
-  apply_tile_df<P, TX, TY, MODE>(a, tb, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x,
-                                 gridDim.x * gridDim.y);
+  apply_tile_df<P, TX, TY, TPE, MODE>(a, tb, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x,
+                                      gridDim.x * gridDim.y);
 }
 
-template <int P, int TX, int TY, int MODE>
-__global__ void __launch_bounds__(TX* TY)
+template <int P, int TX, int TY, int TPE, int MODE>
+__global__ void __launch_bounds__(TX* TY* TPE)
     k_sipg_apply_df_batched(const ApplyArgs<float>* __restrict__ insts, const int* __restrict__ tile_start, int ninst,
                             const __grid_constant__ TabDF<P> tb) {
   const int g = blockIdx.x;
@@ -388,64 +407,78 @@ __global__ void __launch_bounds__(TX* TY)
   const ApplyArgs<float> a = insts[lo];
   const int lt = g - __ldg(tile_start + lo);
   const int tiles_x = (a.dim + TX - 1) / TX, tiles_y = (a.dim + TY - 1) / TY;
-  apply_tile_df<P, TX, TY, MODE>(a, tb, lt % tiles_x, lt / tiles_x, lt, tiles_x * tiles_y);
+  apply_tile_df<P, TX, TY, TPE, MODE>(a, tb, lt % tiles_x, lt / tiles_x, lt, tiles_x * tiles_y);
 }
 
 // Launch (single operator when insts == nullptr, else batched over `ninst`
-// operators of degree P; each carries its own penalty split into nu + nu_lo).
-template <int P, int TY>
+// operators of degree P; each carries its own penalty split into three floats).
+template <int P, int TY, int TPE>
 cudaError_t launch_apply_df_tile(int mode, const ApplyArgs<float>& a, const ApplyArgs<float>* insts,
                                  const int* tile_start, int ninst, int total_tiles, const TabDF<P>& tb,
                                  cudaStream_t s) {
   constexpr int TX = 32;
   const size_t smem = ApplyDfSmem<P, TX, TY>::bytes;
   cudaError_t err = cudaSuccess;
-  const void* fns[6] = {(const void*)k_sipg_apply_df<P, TX, TY, APPLY_PLAIN>,
-                        (const void*)k_sipg_apply_df<P, TX, TY, APPLY_CG>,
-                        (const void*)k_sipg_apply_df<P, TX, TY, APPLY_DOT>,
-                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_PLAIN>,
-                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_CG>,
-                        (const void*)k_sipg_apply_df_batched<P, TX, TY, APPLY_DOT>};
+  const void* fns[6] = {(const void*)k_sipg_apply_df<P, TX, TY, TPE, APPLY_PLAIN>,
+                        (const void*)k_sipg_apply_df<P, TX, TY, TPE, APPLY_CG>,
+                        (const void*)k_sipg_apply_df<P, TX, TY, TPE, APPLY_DOT>,
+                        (const void*)k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_PLAIN>,
+                        (const void*)k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_CG>,
+                        (const void*)k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_DOT>};
   for (const void* f : fns) {
     err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
   }
   if (mode == APPLY_PREPARE) return cudaSuccess;
-  const dim3 block(TX, TY);
+  const dim3 block(TX, TY, TPE);
   if (!insts) {
     const dim3 grid((a.dim + TX - 1) / TX, (a.dim + TY - 1) / TY);
-    if (mode == APPLY_PLAIN) k_sipg_apply_df<P, TX, TY, APPLY_PLAIN><<<grid, block, smem, s>>>(a, tb);
-    else if (mode == APPLY_CG) k_sipg_apply_df<P, TX, TY, APPLY_CG><<<grid, block, smem, s>>>(a, tb);
-    else if (mode == APPLY_DOT) k_sipg_apply_df<P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(a, tb);
+    if (mode == APPLY_PLAIN) k_sipg_apply_df<P, TX, TY, TPE, APPLY_PLAIN><<<grid, block, smem, s>>>(a, tb);
+    else if (mode == APPLY_CG) k_sipg_apply_df<P, TX, TY, TPE, APPLY_CG><<<grid, block, smem, s>>>(a, tb);
+    else if (mode == APPLY_DOT) k_sipg_apply_df<P, TX, TY, TPE, APPLY_DOT><<<grid, block, smem, s>>>(a, tb);
     else return cudaErrorInvalidValue;
   } else {
     if (total_tiles == 0) return cudaSuccess;
     if (mode == APPLY_PLAIN)
-      k_sipg_apply_df_batched<P, TX, TY, APPLY_PLAIN><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
+      k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_PLAIN><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst,
+                                                                                             tb);
     else if (mode == APPLY_CG)
-      k_sipg_apply_df_batched<P, TX, TY, APPLY_CG><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
+      k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_CG><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
     else if (mode == APPLY_DOT)
-      k_sipg_apply_df_batched<P, TX, TY, APPLY_DOT><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst, tb);
+      k_sipg_apply_df_batched<P, TX, TY, TPE, APPLY_DOT><<<total_tiles, block, smem, s>>>(insts, tile_start, ninst,
+                                                                                           tb);
     else return cudaErrorInvalidValue;
   }
   count_launch();
   return cudaGetLastError();
 }
 
+// Compiled shapes: rows TY in {2, 4, 8} with one thread per element, and TY in
+// {2, 4} with two (TY = 8 x 2 would be 512 threads of ~100 registers).
 template <int P>
 cudaError_t launch_apply_df_p(const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const ApplyArgs<float>* insts,
                               const int* tile_start, int ninst, int total_tiles, const HostTables& h, cudaStream_t s) {
   const TabDF<P> tb = make_tab_df<P>(h);
   constexpr size_t kMax = 227 * 1024;
   constexpr bool fits8 = ApplyDfSmem<P, 32, 8>::bytes <= kMax;
+  if (cfg.tpe == 2) {
+    switch (cfg.ty) {
+      case 2:
+        return launch_apply_df_tile<P, 2, 2>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
+      case 4:
+        return launch_apply_df_tile<P, 4, 2>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
+    }
+    return cudaErrorInvalidConfiguration;
+  }
+  if (cfg.tpe != 1) return cudaErrorInvalidConfiguration;
   switch (cfg.ty) {
     case 2:
-      return launch_apply_df_tile<P, 2>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
+      return launch_apply_df_tile<P, 2, 1>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
     case 4:
-      return launch_apply_df_tile<P, 4>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
+      return launch_apply_df_tile<P, 4, 1>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
     case 8:
       if (!fits8) return cudaErrorInvalidConfiguration;
-      return launch_apply_df_tile<P, (fits8 ? 8 : 4)>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
+      return launch_apply_df_tile<P, (fits8 ? 8 : 4), 1>(mode, a, insts, tile_start, ninst, total_tiles, tb, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -129,6 +129,7 @@ inline void set_penalty3(ApplyArgs<float>& a, double pen) {
 // Tile shape chosen for one (precision, degree).
 struct TileCfg {
   int tx = 32, ty = 4;
+  int tpe = 1;  // threads per element (the compensated apply compiles 1 and 2)
 };
 
 // Launch the fused apply for degree p (dispatches on p and the tile shape).

@@ -82,7 +82,8 @@ class Modes(C.Structure):
 
 
 class TileChoice(C.Structure):
-    _fields_ = [("elements_per_row", C.c_int), ("rows", C.c_int * 3), ("ms_per_apply", C.c_float * 3)]
+    _fields_ = [("elements_per_row", C.c_int), ("rows", C.c_int * 3), ("threads_per_element", C.c_int * 3),
+                ("ms_per_apply", C.c_float * 3)]
 
 
 TILE_KINDS = {"f64": 0, "f32": 1, "pairs": 2}
@@ -98,8 +99,8 @@ _SIGS = {
     "sipg_op_destroy": (C.c_int, [_VP]),
     "sipg_op_solve_footprint": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
     "sipg_op_autotune": (C.c_int, [_VP, _VP, C.POINTER(TileChoice)]),
-    "sipg_op_set_tile": (C.c_int, [_VP, C.c_int, C.c_int]),
-    "sipg_op_get_tile": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int)]),
+    "sipg_op_set_tile": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
+    "sipg_op_get_tile": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sipg_apply_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_pairs": (C.c_int, [_VP, _VP, _VP, _VP]),
@@ -234,18 +235,19 @@ class Operator:
 
     def autotune(self, stream=None):
         """Times the tile shapes on this operator and keeps the fastest per
-        apply kind; returns {kind: (rows, ms_per_apply)}."""
+        apply kind; returns {kind: (rows, threads_per_element, ms_per_apply)}."""
         tc = TileChoice()
         _check(lib().sipg_op_autotune(self._h, _stream(stream), C.byref(tc)), "autotune")
-        return {k: (tc.rows[i], tc.ms_per_apply[i]) for k, i in TILE_KINDS.items()}
+        return {k: (tc.rows[i], tc.threads_per_element[i], tc.ms_per_apply[i]) for k, i in TILE_KINDS.items()}
 
-    def set_tile(self, kind, rows):
-        _check(lib().sipg_op_set_tile(self._h, TILE_KINDS[kind], int(rows)), "set_tile")
+    def set_tile(self, kind, rows, threads_per_element=1):
+        _check(lib().sipg_op_set_tile(self._h, TILE_KINDS[kind], int(rows), int(threads_per_element)), "set_tile")
 
     def get_tile(self, kind):
-        r = C.c_int()
-        _check(lib().sipg_op_get_tile(self._h, TILE_KINDS[kind], C.byref(r)), "get_tile")
-        return r.value
+        """(rows, threads per element) of the apply kind's tile."""
+        r, t = C.c_int(), C.c_int()
+        _check(lib().sipg_op_get_tile(self._h, TILE_KINDS[kind], C.byref(r), C.byref(t)), "get_tile")
+        return r.value, t.value
 
     def __del__(self):
         try:

@@ -145,23 +145,25 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
 
 /* ---- tile shapes and the autotuner (no reference counterpart: the
  * reference launches one fixed geometry) ----
- * An apply tile is 32 elements along a mesh row (one thread each) by `rows`
- * rows (2, 4 or 8).  Every shape gives bit-identical apply results; CG
- * reductions regroup.  Tile indices for the three apply kinds: */
+ * An apply tile is 32 elements along a mesh row by `rows` rows (2, 4 or 8),
+ * with one thread per element (or two, pairs apply only).  Every shape gives
+ * bit-identical apply results; CG reductions regroup.  Tile indices for the three apply kinds: */
 enum { SIPG_TUNE_F64 = 0, SIPG_TUNE_F32 = 1, SIPG_TUNE_PAIRS = 2 /* compensated, pair vectors */ };
 typedef struct {
   int elements_per_row;   /* 32 */
-  int rows[3];            /* chosen rows per tile, by SIPG_TUNE_* */
-  float ms_per_apply[3];  /* the winning candidate's time */
+  int rows[3];                 /* chosen rows per tile, by SIPG_TUNE_* */
+  int threads_per_element[3];  /* chosen threads per element (1, or 2 for the pairs apply) */
+  float ms_per_apply[3];       /* the winning candidate's time */
 } sipg_tile_choice;
-/* Times rows in {2, 4, 8} for each apply kind on this op (a few applies on
- * scratch vectors of ndof doubles, allocated and freed here), keeps the
- * fastest, and records it for (degree, dim) so ops created later in this
- * process start with it.  Synchronous; not during stream capture.  `out` may
- * be NULL. */
+/* Times the tile shapes for each apply kind on this op -- rows in {2, 4, 8}
+ * with one thread per element, and for the pairs apply also rows in {2, 4}
+ * with two -- on scratch vectors of ndof doubles (allocated and freed here),
+ * keeps the fastest, and records it for (degree, dim) so ops created later in
+ * this process start with it.  Synchronous; not during stream capture.  `out`
+ * may be NULL. */
 sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out);
-sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows);
-sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows);
+sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows, int threads_per_element);
+sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows, int* threads_per_element);
 
 /* ---- conjugate gradient ---- */
 

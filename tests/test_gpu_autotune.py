@@ -1,11 +1,14 @@
 """The tile-shape autotuner (sipg_op_autotune / set_tile / get_tile): every
-tile shape gives the same apply result bit for bit (each output is the same
+tile shape -- rows per tile, and one or two threads per element for the pairs
+apply -- gives the same apply result bit for bit (each output is the same
 operations in the same order whatever the tiling), the tuner keeps a shape
 that launches, and operators created later for the same (degree, dim) start
 with the tuned shape."""
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+SHAPES = [(2, 1), (4, 1), (8, 1), (2, 2), (4, 2)]
 
 
 @pytest.fixture(scope="module")
@@ -33,16 +36,29 @@ def test_every_tile_shape_gives_identical_applies(sipg, torch, p, d):
             assert p == 8 and rows == 8
             return None
 
-    for rows in (2, 4, 8):
-        for kind in ("f64", "f32", "pairs"):
-            op.set_tile(kind, rows)
-            assert op.get_tile(kind) == rows
-        outs[rows] = (run(op.apply, x64), run(op.apply, x32), run(op.apply_pairs, xp))
-    for rows in (4, 8):
+    for rows, tpe in SHAPES:
+        kinds = ("pairs",) if tpe == 2 else ("f64", "f32", "pairs")
+        for kind in kinds:
+            op.set_tile(kind, rows, tpe)
+            assert op.get_tile(kind) == (rows, tpe)
+        if tpe == 2:
+            outs[(rows, tpe)] = (None, None, run(op.apply_pairs, xp))
+        else:
+            outs[(rows, tpe)] = (run(op.apply, x64), run(op.apply, x32), run(op.apply_pairs, xp))
+    base = outs[(2, 1)]
+    for shape in SHAPES[1:]:
         for k in range(3):
-            a, b = outs[2][k], outs[rows][k]
+            a, b = base[k], outs[shape][k]
             if a is not None and b is not None:
-                assert torch.equal(a, b), (rows, k)
+                assert torch.equal(a, b), (shape, k)
+    op.close()
+
+
+def test_two_threads_per_element_rejected_where_not_compiled(sipg):
+    op = sipg.Operator(8, 3, 9.0)
+    for kind, rows in (("f64", 4), ("f32", 4), ("pairs", 8)):
+        with pytest.raises(sipg.SipgError):
+            op.set_tile(kind, rows, 2)
     op.close()
 
 
@@ -50,22 +66,28 @@ def test_autotune_picks_a_launchable_shape_and_is_remembered(sipg, torch):
     p, d = 6, 96
     op = sipg.Operator(d, p, 36.0)
     choice = op.autotune()
-    for kind, (rows, ms) in choice.items():
-        assert rows in (2, 4, 8) and ms > 0, (kind, rows, ms)
-        assert op.get_tile(kind) == rows
+    for kind, (rows, tpe, ms) in choice.items():
+        assert (rows, tpe) in SHAPES and ms > 0, (kind, rows, tpe, ms)
+        assert tpe == 1 or kind == "pairs"
+        assert op.get_tile(kind) == (rows, tpe)
     # a later operator of the same degree and size starts from the tuned shapes
     op2 = sipg.Operator(d, p, 36.0)
-    for kind, (rows, _) in choice.items():
-        assert op2.get_tile(kind) == rows
+    for kind, (rows, tpe, _) in choice.items():
+        assert op2.get_tile(kind) == (rows, tpe)
     # and a CG solve after re-tuning re-captures its graphs and still converges
     b = op.rhs("sinsin")
     x = torch.zeros_like(b)
     st, res = op.cg(x, b, 1e-10, relative=True)
     assert st == 0 and res.converged == 1
-    op.set_tile("f64", 2 if op.get_tile("f64") != 2 else 4)
+    op.set_tile("f64", 2 if op.get_tile("f64")[0] != 2 else 4)
     x2 = torch.zeros_like(b)
     st, res2 = op.cg(x2, b, 1e-10, relative=True)
     assert st == 0 and abs(res2.iterations - res.iterations) <= 1
     assert (x2 - x).abs().max().item() <= 1e-8 * x.abs().max().item()
+    # the pairs mixed solve with two threads per element
+    op.set_tile("pairs", 4, 2)
+    xm = torch.zeros_like(b)
+    st, rm = op.solve_mixed(xm, b, inner="pairs")
+    assert st == 0 and rm.rel_residual <= 1e-10
     op.close()
     op2.close()
