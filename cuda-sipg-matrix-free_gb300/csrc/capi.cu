@@ -461,6 +461,7 @@ sipg_status sipg_op_destroy(sipg_op* op) {
   ws_free(op->ws64);
   ws_free(op->ws32);
   if (op->mixed_free) op->mixed_free(op->mixed);
+  if (op->pcg_free) op->pcg_free(op->pcg);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
   delete op;

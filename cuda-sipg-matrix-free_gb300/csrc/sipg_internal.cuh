@@ -83,6 +83,8 @@ struct CgState {
   int pad;
   T rr_prev;  // r.r before the last update (beta after a forced correction)
   T pad2;
+  T rres;     // preconditioned CG: r.r of the residual (its stop test; rr holds r.z)
+  T pad3;
 };
 
 // Deterministic grid reduction scratch: per-block partials, reduced in a fixed
@@ -205,4 +207,6 @@ struct sipg_op {
   double* stage_out = nullptr;
   void* mixed = nullptr;  // the mixed-precision solver's cached workspace
   void (*mixed_free)(void*) = nullptr;
+  void* pcg = nullptr;  // the block-Jacobi preconditioner and PCG workspace
+  void (*pcg_free)(void*) = nullptr;
 };

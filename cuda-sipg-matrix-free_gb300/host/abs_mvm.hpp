@@ -21,4 +21,7 @@ class fused_cg_operator {
   virtual ~fused_cg_operator() {}
   // absolute tolerance on sqrt(r.r), max_it = DoF, as conjugate_gradient
   virtual int fused_cg(mode_vector<FLOAT_TYPE, int> x, mode_vector<FLOAT_TYPE, int> b, FLOAT_TYPE tol) const = 0;
+  // the same with the operator's block-Jacobi preconditioner, as
+  // preconditioned_conjugate_gradient; -1 where the operator has none
+  virtual int fused_pcg(mode_vector<FLOAT_TYPE, int>, mode_vector<FLOAT_TYPE, int>, FLOAT_TYPE) const { return -1; }
 };

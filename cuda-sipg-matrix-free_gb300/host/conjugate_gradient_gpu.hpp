@@ -7,7 +7,8 @@
 // scalars, graph-captured iterations; any other abs_mvm runs the reference's
 // loop with the library's vector steps (sipg_dot / sipg_cg_step / sipg_xpby).
 // preconditioned_conjugate_gradient: the reference's PCG loop
-// (conjugate_gradient_gpu.hpp:116-213) with problem._prec_mvm.
+// (conjugate_gradient_gpu.hpp:116-213) with problem._prec_mvm; on an operator
+// of this library, its fused, graph-driven form (sipg_pcg_f64).
 #pragma once
 
 #include <cmath>
@@ -70,6 +71,10 @@ template <typename FLOAT_TYPE>
 int preconditioned_conjugate_gradient(const abs_mvm<FLOAT_TYPE>& problem, mode_vector<FLOAT_TYPE, int> x,
                                       mode_vector<FLOAT_TYPE, int> b, FLOAT_TYPE tol) {
   using namespace sipg_host;
+  if (auto* fused = dynamic_cast<const fused_cg_operator<FLOAT_TYPE>*>(&problem)) {
+    const int it = fused->fused_pcg(x, b, tol);
+    if (it >= 0) return it;
+  }
   const int noe = x.get_noe(), nompe = x.get_nompe();
   const size_t n = (size_t)b.size();
   mode_vector<FLOAT_TYPE, int> r(noe, nompe), p(noe, nompe), Ap(noe, nompe), z(noe, nompe);

@@ -9,8 +9,11 @@
 // norms are computed on the host in FLOAT_TYPE, as the reference does
 // (compute_rhs :232-305, err_norms :311-370).  With a built-in problem id
 // (FP64) both run on the device (sipg_rhs_f64, sipg_err_norms_f64).
-// _prec_mvm is the identity (the block-Jacobi preconditioner of the reference
-// is not part of this library).
+// As in the reference, defining USE_PRECONDITIONER before including this
+// header makes the solve the block-Jacobi preconditioned CG and _prec_mvm the
+// block-Jacobi preconditioner (sipg_apply_prec_f64 / sipg_pcg_f64; FP64);
+// without it _prec_mvm copies its input (the reference's leaves the output
+// untouched).
 #pragma once
 
 #include <cmath>
@@ -48,7 +51,11 @@ class sipg_sem_2d : public abs_mvm<FLOAT_TYPE>, public fused_cg_operator<FLOAT_T
 
   void solve(FLOAT_TYPE tol) {
     system_solution_time.start();
+#ifdef USE_PRECONDITIONER
+    iterations = preconditioned_conjugate_gradient(*this, d_u, d_rhs, tol);
+#else
     iterations = conjugate_gradient(*this, d_u, d_rhs, tol);
+#endif
     system_solution_time.stop();
     copy(d_u, solution);
   }
@@ -100,8 +107,27 @@ class sipg_sem_2d : public abs_mvm<FLOAT_TYPE>, public fused_cg_operator<FLOAT_T
   }
 
   int _prec_mvm(mode_vector<FLOAT_TYPE, int> input, mode_vector<FLOAT_TYPE, int> output) const override {
+#ifdef USE_PRECONDITIONER
+    if (std::is_same<FLOAT_TYPE, double>::value)
+      return (int)sipg_apply_prec_f64(op, (const double*)input.data(), (double*)output.data(), nullptr);
+#endif
     return (int)cudaMemcpy(output.data(), input.data(), sizeof(FLOAT_TYPE) * (size_t)input.size(),
                            cudaMemcpyDeviceToDevice);
+  }
+
+  int fused_pcg(mode_vector<FLOAT_TYPE, int> x, mode_vector<FLOAT_TYPE, int> b, FLOAT_TYPE tol) const override {
+#ifdef USE_PRECONDITIONER
+    if (std::is_same<FLOAT_TYPE, double>::value) {
+      sipg_cg_result r;
+      const sipg_status s = sipg_pcg_f64(op, (double*)x.data(), (const double*)b.data(), (double)tol, 0, 0, &r, nullptr);
+      if (s != SIPG_OK && s != SIPG_ERR_NOT_CONVERGED) sipg_host::check(s, "sipg_pcg_f64");
+      return r.iterations;
+    }
+#endif
+    (void)x;
+    (void)b;
+    (void)tol;
+    return -1;
   }
 
   int fused_cg(mode_vector<FLOAT_TYPE, int> x, mode_vector<FLOAT_TYPE, int> b, FLOAT_TYPE tol) const override {

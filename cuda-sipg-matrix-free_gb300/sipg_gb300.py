@@ -107,6 +107,8 @@ _SIGS = {
     "sipg_apply_host_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_cg_f64": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
     "sipg_cg_f32": (C.c_int, [_VP, _VP, _VP, C.c_float, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
+    "sipg_pcg_f64": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
+    "sipg_apply_prec_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), C.POINTER(MixedResult), _VP]),
     "sipg_rhs_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP]),
     "sipg_err_norms_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP, _VP]),
@@ -317,6 +319,30 @@ class Operator:
         if st not in (0, 3, 4):
             _check(st, "cg")
         return st, res
+
+    def pcg(self, x, b, tol, relative=False, max_it=0, stream=None):
+        """Block-Jacobi preconditioned CG (FP64) from x (in place): the
+        reference's USE_PRECONDITIONER solve.  Returns (status, CgResult)."""
+        import torch
+
+        self._vec(x, torch.float64)
+        self._vec(b, torch.float64)
+        res = CgResult()
+        st = lib().sipg_pcg_f64(self._h, _ptr(x), _ptr(b), float(tol), int(bool(relative)), int(max_it),
+                                C.byref(res), _stream(stream))
+        if st not in (0, 3, 4):
+            _check(st, "pcg")
+        return st, res
+
+    def apply_prec(self, x, out=None, stream=None):
+        """out = M x, the block-Jacobi preconditioner (FP64)."""
+        import torch
+
+        self._vec(x, torch.float64)
+        if out is None:
+            out = torch.empty_like(x)
+        _check(lib().sipg_apply_prec_f64(self._h, _ptr(x), _ptr(out), _stream(stream)), "apply_prec")
+        return out
 
     def solve_mixed(self, x, b, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, inner="auto",
                     stream=None):

@@ -179,6 +179,22 @@ sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol,
 sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
                         sipg_cg_result* res, void* stream);
 
+/* Block-Jacobi preconditioner (the reference's USE_PRECONDITIONER path):
+ * d_out = M d_in, M the inverse of an interior element's diagonal block kept
+ * on the (i1,.) / (.,i2) cross pattern, the same for every element, penalty
+ * truncated to an integer as the reference does.  Replaces
+ * sipg_sem_2d<T>::_prec_mvm (sipg_sem_2d.hpp:205-224) with
+ * host_preconditioner_matrix (mode_matrix.hpp:474-522) and
+ * block_diagonal_preconditioner_2d (laplacian_operator.hpp:95-186). */
+sipg_status sipg_apply_prec_f64(sipg_op* op, const double* d_in, double* d_out, void* stream);
+/* Preconditioned CG with that M: stops when sqrt(r.r) <= tol (absolute, as
+ * the reference, or tol*||b|| with tol_relative = 1) or after max_it
+ * iterations (<= 0: DoF); the first iteration always runs, as the
+ * reference's.  res->rr is the final r.r.  Replaces
+ * preconditioned_conjugate_gradient (conjugate_gradient_gpu.hpp:116-213). */
+sipg_status sipg_pcg_f64(sipg_op* op, double* d_x, const double* d_b, double tol, int tol_relative, int max_it,
+                         sipg_cg_result* res, void* stream);
+
 /* Mixed precision: the operator and CG run on the FP32 pipes (FP32 values,
  * or double-float pairs, see sipg_inner_kind) inside FP64 defect correction
  * with reliable updates -- whenever the inner residual has fallen by

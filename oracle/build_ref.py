@@ -14,7 +14,9 @@ what the GPU computes.  This recipe:
    (the only change; written to a temporary directory under oracle/_ref/
    that is deleted after the compile);
 3. compiles oracle/ref_emul.cpp with oracle/cuda_emul.h against them with
-   g++ -O2 -ffp-contract=off into oracle/_ref/libref_emul.so;
+   g++ -O2 -ffp-contract=off into oracle/_ref/libref_emul.so, and again with
+   -DUSE_PRECONDITIONER (the block-Jacobi path; LAPACK, absent here, replaced
+   by oracle/lapacke_emul/lapacke.h) into oracle/_ref/libref_emul_pcg.so;
 4. compiles the reference's FP64 kernels, unchanged, for sm_103a into
    oracle/_ref/ref_kernels.cubin (oracle/ref_gpu_kernels.cu holds only their
    explicit instantiations).  The cubin is device code and travels with the
@@ -61,7 +63,7 @@ def build(ref_dir=None, verbose=False):
             dst = os.path.join(tmp, sub)
             os.makedirs(dst, exist_ok=True)
             for name in os.listdir(src):
-                if name.endswith(".hpp"):
+                if name.endswith(".hpp") or (sub == "include" and name.endswith(".cpp")):
                     with open(os.path.join(src, name)) as f:
                         text = f.read()
                     with open(os.path.join(dst, name), "w") as f:
@@ -74,6 +76,13 @@ def build(ref_dir=None, verbose=False):
         if verbose:
             print(" ".join(cmd))
         subprocess.check_call(cmd)
+        # the same with the block-Jacobi preconditioner (USE_PRECONDITIONER),
+        # LAPACK replaced by oracle/lapacke_emul/lapacke.h
+        cmd_pcg = cmd[:-2] + ["-DUSE_PRECONDITIONER", "-I", os.path.join(HERE, "lapacke_emul"), "-o",
+                              os.path.join(OUT_DIR, "libref_emul_pcg.so")]
+        if verbose:
+            print(" ".join(cmd_pcg))
+        subprocess.check_call(cmd_pcg)
         cubin = os.path.join(OUT_DIR, "ref_kernels.cubin")
         cmd = [os.environ.get("NVCC", "nvcc"), "-std=c++14", "-O3", "-cubin", "-gencode",
                "arch=compute_103a,code=sm_103a", "-w", "-I", inc, os.path.join(HERE, "ref_gpu_kernels.cu"),

@@ -225,4 +225,34 @@ int ref_rhs(int p, int dim, double pen, int sol, double* b) {
   mesh.device_info.free();
   return 0;
 }
+
+#ifdef USE_PRECONDITIONER
+/* Built a second time with -DUSE_PRECONDITIONER into libref_emul_pcg.so:
+ * the block-Jacobi path.  ref_solve above then runs the preconditioned CG
+ * (sipg_sem_2d.hpp:121-134).  ref_prec_block: the block the reference builds
+ * (laplacian_operator.hpp:133-186) before, and its inverse after, the LAPACK
+ * calls (lapacke_emul/lapacke.h stands in for LAPACK).  ref_prec_rows: the
+ * (2p+1) entries per row of host_preconditioner_matrix (mode_matrix.hpp:
+ * 474-522), rows[((i1*(p+1)+i2)*(2p+1)) + r]. */
+int ref_prec_block(int p, double pen, double* block, double* inverse) {
+  block_diagonal_preconditioner_2d prec(p, pen);
+  const size_t nn = (size_t)(p + 1) * (p + 1);
+  const std::vector<double>& a0 = lapacke_emul::last_factored();
+  if (a0.size() != nn * nn) return -1;
+  for (size_t i = 0; i < nn * nn; ++i) {
+    block[i] = a0[i];
+    inverse[i] = prec.a[i];
+  }
+  return 0;
+}
+
+int ref_prec_rows(int p, double pen, double* rows) {
+  host_preconditioner_matrix<double, int> m(1, p, pen);
+  const int n = p + 1, R = 2 * p + 1;
+  for (int i1 = 0; i1 < n; ++i1)
+    for (int i2 = 0; i2 < n; ++i2)
+      for (int r = 0; r < R; ++r) rows[(size_t)(i1 * n + i2) * R + r] = m(i1, i2, r, 0);
+  return 0;
+}
+#endif
 }

@@ -329,6 +329,213 @@ int sipg_oracle_cg(int p, int dim, double pen, double* x, const double* b, doubl
 }
 
 /* ------------------------------------------------------------------------- */
+/* Block-Jacobi preconditioner and preconditioned CG (USE_PRECONDITIONER).     */
+/* ------------------------------------------------------------------------- */
+/* laplace_2d::operator() (laplacian_operator.hpp:67-88), one entry */
+static double lap_entry(int n, const double* w, const double* D, int i1, int i2, int j1, int j2) {
+  double result = 0;
+  if (i2 == j2)
+    for (int k = 0; k < n; ++k) result += w[k] * w[i2] * D[i1 * n + k] * D[j1 * n + k];
+  if (i1 == j1)
+    for (int k = 0; k < n; ++k) result += w[k] * w[i1] * D[i2 * n + k] * D[j2 * n + k];
+  return result;
+}
+
+/* block_diagonal_preconditioner_2d::build_diagonal_block
+ * (laplacian_operator.hpp:133-186): the element Laplacian, the consistency
+ * terms of its four faces with the interior factor 1/2, the penalty on the
+ * face nodes */
+int sipg_oracle_prec_block(int p, double pen_in, double* a) {
+  const int N = p, n = p + 1, nn = n * n;
+  double nodes[ORACLE_MAX_N], w[ORACLE_MAX_N], D[ORACLE_MAX_N * ORACLE_MAX_N];
+  if (p < 1 || n > ORACLE_MAX_N) return -1;
+  lgl_d(n, nodes, w);
+  dphi_d(p, D);
+  const double pen = (double)(int)pen_in; /* the constructor takes `int _pen` (:116) */
+#define IDX(i1, i2, j1, j2) (nn * (n * (i2) + (i1)) + (n * (j2) + (j1)))
+  for (int i1 = 0; i1 <= N; ++i1)
+    for (int i2 = 0; i2 <= N; ++i2)
+      for (int j1 = 0; j1 <= N; ++j1)
+        for (int j2 = 0; j2 <= N; ++j2) a[IDX(i1, i2, j1, j2)] = lap_entry(n, w, D, i1, i2, j1, j2);
+  for (int j = 0; j <= N; ++j)
+    for (int i = 0; i <= N; ++i) {
+      const double d0 = D[i * n + 0], dN = D[i * n + N];
+      a[IDX(i, j, 0, j)] -= -1 * w[j] * d0 * .5; /* LEFT */
+      a[IDX(0, j, i, j)] -= -1 * w[j] * d0 * .5;
+      a[IDX(i, j, N, j)] -= w[j] * dN * .5; /* RIGHT */
+      a[IDX(N, j, i, j)] -= w[j] * dN * .5;
+      a[IDX(j, i, j, 0)] -= -1 * w[j] * d0 * .5; /* DOWN */
+      a[IDX(j, 0, j, i)] -= -1 * w[j] * d0 * .5;
+      a[IDX(j, i, j, N)] -= w[j] * dN * .5; /* UP */
+      a[IDX(j, N, j, i)] -= w[j] * dN * .5;
+    }
+  for (int i = 0; i <= N; ++i) {
+    a[IDX(N, i, N, i)] += pen * w[i];
+    a[IDX(i, N, i, N)] += pen * w[i];
+    a[IDX(0, i, 0, i)] += pen * w[i];
+    a[IDX(i, 0, i, 0)] += pen * w[i];
+  }
+#undef IDX
+  return 0;
+}
+
+/* The inverse as LAPACK's dgetrf + dgetri compute it (lapack_wrapper.cpp:
+ * 29-42): LU with partial pivoting (unit lower triangle, row interchanges in
+ * order), then each column of the inverse by forward and back substitution of
+ * the interchanged unit vector.  Row-major. */
+int sipg_oracle_invert(int n, double* A) {
+  int* piv = (int*)malloc(sizeof(int) * n);
+  double* inv = (double*)malloc(sizeof(double) * n * n);
+  double* col = (double*)malloc(sizeof(double) * n);
+  int rc = 0;
+  if (!piv || !inv || !col) {
+    rc = -1;
+    goto out;
+  }
+  for (int c = 0; c < n; ++c) {
+    int pr = c;
+    for (int r = c + 1; r < n; ++r)
+      if (fabs(A[r * n + c]) > fabs(A[pr * n + c])) pr = r;
+    piv[c] = pr;
+    if (A[pr * n + c] == 0) {
+      rc = -1;
+      goto out;
+    }
+    if (pr != c)
+      for (int k = 0; k < n; ++k) {
+        const double t = A[c * n + k];
+        A[c * n + k] = A[pr * n + k];
+        A[pr * n + k] = t;
+      }
+    for (int r = c + 1; r < n; ++r) {
+      const double l = A[r * n + c] / A[c * n + c];
+      A[r * n + c] = l;
+      for (int k = c + 1; k < n; ++k) A[r * n + k] -= l * A[c * n + k];
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < n; ++i) col[i] = (i == j) ? 1.0 : 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double t = col[i];
+      col[i] = col[piv[i]];
+      col[piv[i]] = t;
+    }
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < i; ++k) col[i] -= A[i * n + k] * col[k];
+    for (int i = n - 1; i >= 0; --i) {
+      for (int k = i + 1; k < n; ++k) col[i] -= A[i * n + k] * col[k];
+      col[i] /= A[i * n + i];
+    }
+    for (int i = 0; i < n; ++i) inv[i * n + j] = col[i];
+  }
+  memcpy(A, inv, sizeof(double) * n * n);
+out:
+  free(piv);
+  free(inv);
+  free(col);
+  return rc;
+}
+
+/* host_preconditioner_matrix (mode_matrix.hpp:474-522): per row (i1,i2) of
+ * the inverse, the diagonal, then the same-i1 entries, then the same-i2 ones */
+int sipg_oracle_prec_rows(int p, double pen, double* rows) {
+  const int n = p + 1, nn = n * n, R = 2 * p + 1;
+  double* a = (double*)malloc(sizeof(double) * nn * nn);
+  if (!a) return -1;
+  if (sipg_oracle_prec_block(p, pen, a) || sipg_oracle_invert(nn, a)) {
+    free(a);
+    return -1;
+  }
+#define PREC(i1, i2, j1, j2) a[nn * (n * (i2) + (i1)) + (n * (j2) + (j1))]
+  for (int i1 = 0; i1 < n; ++i1)
+    for (int i2 = 0; i2 < n; ++i2) {
+      double* row = rows + (size_t)(i1 * n + i2) * R;
+      int r = 0;
+      row[r] = PREC(i1, i2, i1, i2);
+      for (int j = 0; j < n; ++j)
+        if (j != i2) row[++r] = PREC(i1, i2, i1, j);
+      for (int j = 0; j < n; ++j)
+        if (j != i1) row[++r] = PREC(i1, i2, j, i2);
+    }
+#undef PREC
+  free(a);
+  return 0;
+}
+
+/* volume_mvm<T, 1> (mode_matrix_kernels.hpp:7-65) with the rows above */
+int sipg_oracle_prec_apply(int p, int dim, const double* rows, const double* in, double* out) {
+  const int n = p + 1, R = 2 * p + 1;
+  const long noe = (long)dim * dim;
+  for (int i1 = 0; i1 < n; ++i1)
+    for (int i2 = 0; i2 < n; ++i2) {
+      const double* row = rows + (size_t)(i1 * n + i2) * R;
+      for (long e = 0; e < noe; ++e) {
+        int r = 0;
+        double result = 0.;
+        result += row[r] * in[(long)(i1 * n + i2) * noe + e];
+        for (int i = 0; i < n; ++i)
+          if (i != i2) result += row[++r] * in[(long)(i1 * n + i) * noe + e];
+        for (int i = 0; i < n; ++i)
+          if (i != i1) result += row[++r] * in[(long)(i * n + i2) * noe + e];
+        out[(long)(i1 * n + i2) * noe + e] = result;
+      }
+    }
+  return 0;
+}
+
+/* preconditioned_conjugate_gradient (conjugate_gradient_gpu.hpp:116-213) */
+int sipg_oracle_pcg(int p, int dim, double pen, double* x, const double* b, double tol, int rel, int max_it_in,
+                    double* rr_out, int nthreads) {
+  const int n1 = p + 1, R = 2 * p + 1;
+  const long n = (long)dim * dim * n1 * n1;
+  double* rows = (double*)malloc(sizeof(double) * n1 * n1 * R);
+  double* r = (double*)malloc(sizeof(double) * n);
+  double* pv = (double*)malloc(sizeof(double) * n);
+  double* Ap = (double*)malloc(sizeof(double) * n);
+  double* z = (double*)malloc(sizeof(double) * n);
+  int it = -1;
+  if (!rows || !r || !pv || !Ap || !z || sipg_oracle_prec_rows(p, pen, rows)) goto out;
+  {
+    const double norm_b = sqrt(or_dot(b, b, n, nthreads));
+    axpy_ctx c = {x, pv, r, Ap, b, 0, 0, 0};
+    apply_d(p, dim, pen, x, r, nthreads); /* r = b - A x */
+    c.which = 2;
+    c.beta = -1;
+    or_parallel_for(nthreads, n, axpy_task, &c);
+    sipg_oracle_prec_apply(p, dim, rows, r, z);
+    memcpy(pv, z, sizeof(double) * n); /* p = z */
+    double rr_old = or_dot(r, z, n, nthreads);
+    const double stop = rel ? tol * norm_b : tol;
+    const long max_it = max_it_in > 0 ? max_it_in : n;
+    double rr = 1;
+    it = 0;
+    while (sqrt(rr) > stop && it < max_it) {
+      apply_d(p, dim, pen, pv, Ap, nthreads);
+      const double pAp = or_dot(pv, Ap, n, nthreads);
+      c.alpha = rr_old / pAp;
+      c.which = 0;
+      or_parallel_for(nthreads, n, axpy_task, &c);
+      rr = or_dot(r, r, n, nthreads);
+      sipg_oracle_prec_apply(p, dim, rows, r, z);
+      const double rr_new = or_dot(z, r, n, nthreads);
+      /* beta_kernel(p, z, beta): p = z + beta p */
+      c.beta = rr_new / rr_old;
+      for (long i = 0; i < n; ++i) pv[i] = z[i] + c.beta * pv[i];
+      rr_old = rr_new;
+      ++it;
+    }
+    if (rr_out) *rr_out = rr;
+  }
+out:
+  free(rows);
+  free(r);
+  free(pv);
+  free(Ap);
+  free(z);
+  return it;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Test problems (validation_tests/analytical_solutions.hpp:7-94 for A..E).   */
 /* ------------------------------------------------------------------------- */
 static void eval_problem(int sol, const or_modes* m, double x, double y, double* u, double* f, double* dx,

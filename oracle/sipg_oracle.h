@@ -67,6 +67,31 @@ int sipg_oracle_flux_y(int p, int dim, double pen, const double* in, double* out
 int sipg_oracle_cg(int p, int dim, double pen, double* x, const double* b, double tol, int rel,
                    int max_it, double* rr_out, int nthreads);
 
+/* Block-Jacobi preconditioner of the reference's USE_PRECONDITIONER path.
+ * sipg_oracle_prec_block: the interior element's diagonal block of the SIPG
+ * matrix, (p+1)^2 x (p+1)^2, row (p+1)*i2+i1, column (p+1)*j2+j1
+ * (laplacian_operator.hpp:104-186; the penalty is truncated to an int as the
+ * reference's constructor parameter does, :116).
+ * sipg_oracle_invert: the inverse in place by LU with partial pivoting and
+ * substitution, the computation of LAPACK's dgetrf + dgetri that the
+ * reference calls (lapack_wrapper.cpp:29-42; another LAPACK build agrees to
+ * rounding).  Returns -1 for a singular matrix.
+ * sipg_oracle_prec_rows: the inverse kept on the "cross" pattern of the
+ * stored-operator kernel, 2p+1 entries per row in that kernel's order --
+ * (i1,i2), then (i1,j) j != i2, then (j,i2) j != i1 -- at
+ * rows[((i1*(p+1)+i2)*(2p+1)) + r] (mode_matrix.hpp:491-518).
+ * sipg_oracle_prec_apply: out = M in with those rows, element by element
+ * (volume_mvm<T,1>, mode_matrix_kernels.hpp:7-65).
+ * sipg_oracle_pcg: preconditioned CG of conjugate_gradient_gpu.hpp:116-213
+ * (stop on sqrt(r.r) <= tol, absolute, or tol*||b|| if rel; the first
+ * iteration always runs, as the reference's rr starts at 1). */
+int sipg_oracle_prec_block(int p, double pen, double* A);
+int sipg_oracle_invert(int n, double* A);
+int sipg_oracle_prec_rows(int p, double pen, double* rows);
+int sipg_oracle_prec_apply(int p, int dim, const double* rows, const double* in, double* out);
+int sipg_oracle_pcg(int p, int dim, double pen, double* x, const double* b, double tol, int rel, int max_it,
+                    double* rr_out, int nthreads);
+
 /* compute_rhs (sipg_sem_2d.hpp:232-305) for test problem `sol`. */
 int sipg_oracle_rhs(int p, int dim, double pen, int sol, const or_modes* modes, double* b);
 /* err_norms (sipg_sem_2d.hpp:311-370): out[0]=L2, out[1]=H1, out[2]=max. */

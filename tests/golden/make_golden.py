@@ -4,7 +4,9 @@
 Runs oracle/_ref/libref_emul.so -- paogor/CUDA-SIPG-matrix-free's headers
 (LGL_quadrature_table, sem_function, volume, flux_term6a/6b, volume_mvm,
 sipg_sem_2d, conjugate_gradient) compiled for a CPU by oracle/build_ref.py --
-on small seeded inputs and stores inputs and outputs.  Run it where the
+on small seeded inputs and stores inputs and outputs; and
+oracle/_ref/libref_emul_pcg.so, the same built with USE_PRECONDITIONER, for
+the block-Jacobi preconditioner and the preconditioned CG.  Run it where the
 reference checkout exists:
 
     python3 oracle/build_ref.py && python3 tests/golden/make_golden.py
@@ -22,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 LIB = os.path.join(ROOT, "oracle", "_ref", "libref_emul.so")
+LIB_PCG = os.path.join(ROOT, "oracle", "_ref", "libref_emul_pcg.so")
 OUT = os.path.join(HERE, "reference_golden.npz")
 
 dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -43,6 +46,15 @@ def load():
     return ref
 
 
+def load_pcg():
+    ref = C.CDLL(LIB_PCG)
+    ref.ref_prec_block.argtypes = [C.c_int, C.c_double, dp, dp]
+    ref.ref_prec_rows.argtypes = [C.c_int, C.c_double, dp]
+    ref.ref_solve.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp]
+    ref.ref_rhs.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, dp]
+    return ref
+
+
 # (p, dim) cases for the matvec: every supported degree on tiny meshes (1x1 is
 # all boundary; 2x2 has every face kind), plus odd, non-tile-multiple sizes.
 APPLY_CASES = [(p, d) for p in range(1, 9) for d in (1, 2, 3, 5)] + [(4, 16), (4, 33), (8, 12), (6, 7)]
@@ -50,6 +62,16 @@ APPLY_CASES = [(p, d) for p in range(1, 9) for d in (1, 2, 3, 5)] + [(4, 16), (4
 SOLVE_CASES = [
     (5, 2, 4, 4.0, 1e-12), (5, 4, 4, 16.0, 1e-12), (5, 3, 8, 9.0, 1e-12), (1, 2, 4, 4.0, 1e-13),
     (2, 3, 4, 9.0, 1e-12), (3, 2, 2, 4.0, 1e-13), (4, 1, 3, 1.0, 1e-13), (5, 2, 8, 400.0, 1e-15),
+]
+
+
+# the block-Jacobi preconditioner: every degree, the drivers' penalties (p^2,
+# 100 p^2) and one that the reference's int parameter truncates (37.9 -> 37)
+PREC_PENS = lambda p: (float(p * p), 100.0 * p * p, 37.9)
+# preconditioned solves (USE_PRECONDITIONER): (solution, p, dim, pen, absolute tol)
+PCG_CASES = [
+    (5, 2, 4, 400.0, 1e-15), (5, 3, 8, 900.0, 1e-15), (6, 4, 16, 16.0, 1e-12), (5, 4, 8, 1600.0, 1e-14),
+    (1, 6, 6, 36.0, 1e-13),
 ]
 
 
@@ -120,6 +142,27 @@ def main():
     ref.ref_solve(p, d, pen, tol, 6, u, st)
     g["poisson16_rhs"], g["poisson16_u"] = b, u
     g["poisson16_stats"] = np.array([p, d, pen, tol] + list(st))
+    pref = load_pcg()
+    for p in range(1, 9):
+        nn = (p + 1) ** 2
+        for k, pen in enumerate(PREC_PENS(p)):
+            rows = np.zeros(nn * (2 * p + 1))
+            pref.ref_prec_rows(p, pen, rows)
+            g["prec_rows_%d_%d" % (p, k)] = rows
+            if k == 0 and p in (3, 8):
+                blk, inv = np.zeros(nn * nn), np.zeros(nn * nn)
+                pref.ref_prec_block(p, pen, blk, inv)
+                g["prec_block_%d" % p], g["prec_inverse_%d" % p] = blk, inv
+    pcg = []
+    for i, (sol, p, d, pen, tol) in enumerate(PCG_CASES):
+        n = d * d * (p + 1) ** 2
+        u, st = np.zeros(n), np.zeros(4)
+        pref.ref_solve(p, d, pen, tol, sol, u, st)
+        b = np.zeros(n)
+        pref.ref_rhs(p, d, pen, sol, b)
+        g["pcg_u_%d" % i], g["pcg_rhs_%d" % i] = u, b
+        pcg.append([sol, p, d, pen, tol] + list(st))
+    g["pcg_table"] = np.array(pcg)
     np.savez_compressed(OUT, **g)
     print("wrote %s (%d arrays, %.1f KB)" % (OUT, len(g), os.path.getsize(OUT) / 1024))
     return 0

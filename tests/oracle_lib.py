@@ -33,6 +33,12 @@ class Oracle:
         L.sipg_oracle_err_norms.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, dp, dp]
         L.sipg_oracle_u_exact.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double]
         L.sipg_oracle_u_exact.restype = C.c_double
+        L.sipg_oracle_prec_block.argtypes = [C.c_int, C.c_double, dp]
+        L.sipg_oracle_invert.argtypes = [C.c_int, dp]
+        L.sipg_oracle_prec_rows.argtypes = [C.c_int, C.c_double, dp]
+        L.sipg_oracle_prec_apply.argtypes = [C.c_int, C.c_int, dp, dp, dp]
+        L.sipg_oracle_pcg.argtypes = [C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, C.c_int,
+                                      C.POINTER(C.c_double), C.c_int]
         self.nthreads = max(1, min(16, os.cpu_count() or 1))
 
     def lgl(self, n):
@@ -77,6 +83,36 @@ class Oracle:
         rr = C.c_double()
         it = self.L.sipg_oracle_cg(p, dim, pen, x, np.ascontiguousarray(b), tol, int(rel), max_it, C.byref(rr),
                                    nthreads)
+        return it, x, rr.value
+
+    def prec_block(self, p, pen):
+        nn = (p + 1) ** 2
+        a = np.zeros(nn * nn)
+        assert self.L.sipg_oracle_prec_block(p, pen, a) == 0
+        return a
+
+    def invert(self, a):
+        n = int(round(np.sqrt(a.size)))
+        b = np.array(a, dtype=np.float64)
+        assert self.L.sipg_oracle_invert(n, b) == 0
+        return b
+
+    def prec_rows(self, p, pen):
+        rows = np.zeros((p + 1) ** 2 * (2 * p + 1))
+        assert self.L.sipg_oracle_prec_rows(p, pen, rows) == 0
+        return rows
+
+    def prec_apply(self, p, dim, rows, x):
+        y = np.zeros_like(x)
+        assert self.L.sipg_oracle_prec_apply(p, dim, np.ascontiguousarray(rows), np.ascontiguousarray(x), y) == 0
+        return y
+
+    def pcg(self, p, dim, pen, b, tol, rel=False, max_it=0, x0=None, nthreads=1):
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        rr = C.c_double()
+        it = self.L.sipg_oracle_pcg(p, dim, pen, x, np.ascontiguousarray(b), tol, int(rel), max_it, C.byref(rr),
+                                    nthreads)
+        assert it >= 0
         return it, x, rr.value
 
     @staticmethod

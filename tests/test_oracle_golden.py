@@ -183,3 +183,48 @@ def test_convergence_rates_h(oracle):
     r_l2 = np.log2(errs[1][0] / errs[2][0])
     assert r_h1 == pytest.approx(p, abs=0.25)
     assert r_l2 > p + 0.8
+
+
+# ---- block-Jacobi preconditioner and preconditioned CG (USE_PRECONDITIONER) ----
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_prec_rows_match_reference(oracle, golden, p):
+    # the reference's penalty parameter is an int: 37.9 acts as 37
+    for k, pen in enumerate((float(p * p), 100.0 * p * p, 37.9)):
+        assert np.array_equal(oracle.prec_rows(p, pen), golden["prec_rows_%d_%d" % (p, k)]), (p, k)
+
+
+@pytest.mark.parametrize("p", [3, 8])
+def test_prec_block_and_inverse_match_reference(oracle, golden, p):
+    blk = oracle.prec_block(p, float(p * p))
+    assert np.array_equal(blk, golden["prec_block_%d" % p])
+    assert np.array_equal(oracle.invert(blk), golden["prec_inverse_%d" % p])
+    # and it is an inverse
+    nn = (p + 1) ** 2
+    prod = blk.reshape(nn, nn) @ golden["prec_inverse_%d" % p].reshape(nn, nn)
+    assert np.max(np.abs(prod - np.eye(nn))) < 1e-12
+
+
+def test_pcg_matches_reference_solves(oracle, golden):
+    for i, row in enumerate(golden["pcg_table"]):
+        sol, p, d, pen, tol = int(row[0]), int(row[1]), int(row[2]), float(row[3]), float(row[4])
+        b = oracle.rhs(p, d, pen, sol)
+        assert np.array_equal(b, golden["pcg_rhs_%d" % i])
+        it, x, _ = oracle.pcg(p, d, pen, b, tol)
+        assert it == int(row[5]), (i, it, row[5])
+        assert np.array_equal(x, golden["pcg_u_%d" % i]), i
+        l2, h1, mx = oracle.err_norms(p, d, sol, x)
+        assert (l2, h1, mx) == (row[6], row[7], row[8])
+
+
+def test_pcg_reproduces_thesis_rows(oracle, golden):
+    # solution E, penalty 100 p^2, tolerance 1e-15: the h-adaptivity driver's
+    # preconditioned solves give the thesis's Table 4.10 errors
+    seen = 0
+    for row in golden["pcg_table"]:
+        sol, p, d, pen, tol = int(row[0]), int(row[1]), int(row[2]), float(row[3]), float(row[4])
+        if sol == 5 and pen == 100.0 * p * p and (p, d) in THESIS_T4_10:
+            H1, L2, _ = THESIS_T4_10[(p, d)]
+            assert row[7] == pytest.approx(H1, rel=1e-5) and row[6] == pytest.approx(L2, rel=1e-5)
+            seen += 1
+    assert seen >= 3
