@@ -140,6 +140,32 @@ __device__ __forceinline__ double prec_value(const double* __restrict__ rows, co
   return v;
 }
 
+// The stored-operator apply of volume_mvm<T, same> (mode_matrix_kernels.hpp:
+// 7-65): value r of row (i1,i2) of element e's operator at
+// mat[((i1*n + i2)*(2p+1) + r)*mat_noe + (mat_noe == 1 ? 0 : e)] -- the
+// reference's mode_matrix layout -- one operator for every element
+// (mat_noe = 1) or one per element (mat_noe = noe).
+__global__ void __launch_bounds__(kVecThreads) k_stored_apply(const double* __restrict__ mat, size_t mat_noe,
+                                                              const double* __restrict__ in, double* __restrict__ out,
+                                                              size_t n, size_t noe, int p) {
+  const int nn1 = p + 1, R = 2 * p + 1;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int k = (int)(i / noe);
+    const size_t e = i - (size_t)k * noe;
+    const int i1 = k / nn1, i2 = k - i1 * nn1;
+    const double* row = mat + (size_t)k * R * mat_noe + (mat_noe == 1 ? 0 : e);
+    int q = 0;
+    double v = 0.0;
+    v += __ldg(row) * in[i];
+    for (int j = 0; j < nn1; ++j)
+      if (j != i2) v += __ldg(row + (size_t)(++q) * mat_noe) * in[(size_t)(i1 * nn1 + j) * noe + e];
+    for (int j = 0; j < nn1; ++j)
+      if (j != i1) v += __ldg(row + (size_t)(++q) * mat_noe) * in[(size_t)(j * nn1 + i2) * noe + e];
+    out[i] = v;
+  }
+}
+
 __global__ void __launch_bounds__(kVecThreads) k_prec_apply(const double* __restrict__ rows,
                                                             const double* __restrict__ in, double* __restrict__ out,
                                                             size_t n, size_t noe, int p) {
@@ -360,6 +386,21 @@ sipg_status sipg_apply_prec_f64(sipg_op* op, const double* d_in, double* d_out, 
   const size_t n = (size_t)op->ndof;
   k_prec_apply<<<vec_grid(n), kVecThreads, 0, (cudaStream_t)stream>>>(c->rows, d_in, d_out, n, (size_t)op->noe,
                                                                        op->p);
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+sipg_status sipg_volume_mvm_f64(int dim, int degree, const double* d_mat, int mat_noe, const double* d_in,
+                                double* d_out, void* stream) {
+  if (dim < 1 || degree < 1 || degree > SIPG_MAX_DEGREE || !d_mat || !d_in || !d_out || d_in == d_out ||
+      !(mat_noe == 1 || (long long)mat_noe == (long long)dim * dim)) {
+    set_error("sipg_volume_mvm_f64: need dim >= 1, degree 1..8, mat_noe 1 or dim*dim, distinct non-null vectors");
+    return SIPG_ERR_INVALID;
+  }
+  const size_t noe = (size_t)dim * dim, n = noe * (size_t)(degree + 1) * (degree + 1);
+  k_stored_apply<<<vec_grid(n), kVecThreads, 0, (cudaStream_t)stream>>>(d_mat, (size_t)mat_noe, d_in, d_out, n,
+                                                                         noe, degree);
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
   return SIPG_OK;

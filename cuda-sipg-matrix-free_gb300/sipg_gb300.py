@@ -109,6 +109,7 @@ _SIGS = {
     "sipg_cg_f32": (C.c_int, [_VP, _VP, _VP, C.c_float, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
     "sipg_pcg_f64": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_int, C.POINTER(CgResult), _VP]),
     "sipg_apply_prec_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_volume_mvm_f64": (C.c_int, [C.c_int, C.c_int, _VP, C.c_int, _VP, _VP, _VP]),
     "sipg_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), C.POINTER(MixedResult), _VP]),
     "sipg_rhs_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP]),
     "sipg_err_norms_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP, _VP]),
@@ -164,6 +165,21 @@ def _stream(stream=None):
     import torch
 
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def volume_mvm(dim, degree, mat, x, out=None, stream=None):
+    """out = M x for a stored operator in the reference's mode_matrix layout
+    (float64 CUDA tensors; mat holds one operator, or one per element)."""
+    import torch
+
+    n1 = degree + 1
+    per = n1 * n1 * (2 * degree + 1)
+    mat_noe = mat.numel() // per
+    if out is None:
+        out = torch.empty_like(x)
+    _check(lib().sipg_volume_mvm_f64(int(dim), int(degree), _ptr(mat), int(mat_noe), _ptr(x), _ptr(out),
+                                     _stream(stream)), "volume_mvm")
+    return out
 
 
 def to_pairs(x64):

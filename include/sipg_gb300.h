@@ -179,6 +179,17 @@ sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol,
 sipg_status sipg_cg_f32(sipg_op* op, float* d_x, const float* d_b, float tol, int tol_relative, int max_it,
                         sipg_cg_result* res, void* stream);
 
+/* The stored-operator apply of the reference's USE_MODE_MATRIX path:
+ * d_out = M d_in with M stored per node row on the (i1,.) / (.,i2) cross
+ * pattern, 2p+1 values per row in the reference's mode_matrix layout
+ * (value r of row (i1,i2) of element e at ((i1*(p+1)+i2)*(2p+1) + r)*mat_noe
+ * + e), one operator for all elements (mat_noe = 1) or one per element
+ * (mat_noe = dim*dim).  A mode_matrix::data() pointer is a valid d_mat.
+ * Replaces volume_mvm<T, 1> and volume_mvm<T, 0>
+ * (mode_matrix_kernels.hpp:7-65). */
+sipg_status sipg_volume_mvm_f64(int dim, int degree, const double* d_mat, int mat_noe, const double* d_in,
+                                double* d_out, void* stream);
+
 /* Block-Jacobi preconditioner (the reference's USE_PRECONDITIONER path):
  * d_out = M d_in, M the inverse of an interior element's diagonal block kept
  * on the (i1,.) / (.,i2) cross pattern, the same for every element, penalty

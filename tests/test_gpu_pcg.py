@@ -111,3 +111,46 @@ def test_host_api_with_use_preconditioner(pcg_driver_output, oracle):
     assert seen >= 6
     gen = next(r for r in pcg_driver_output if r["case"] == "generic")
     assert abs(gen["it_generic"] - gen["it_fused"]) <= 1 and gen["rel_diff"] <= 1e-9
+
+
+def _laplacian_rows(oracle, p):
+    """host_laplacian_matrix (mode_matrix.hpp:419-466) rows from the oracle's
+    element Laplacian: the diagonal, then (i1, j != i2), then (j != i1, i2)."""
+    n = p + 1
+    L = oracle.laplace2d(p).reshape(n, n, n, n)  # [i1, i2, j1, j2]
+    rows = []
+    for i1 in range(n):
+        for i2 in range(n):
+            rows.append(L[i1, i2, i1, i2])
+            rows += [L[i1, i2, i1, j] for j in range(n) if j != i2]
+            rows += [L[i1, i2, j, i2] for j in range(n) if j != i1]
+    return np.array(rows)
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_stored_operator_apply_matches_reference(sipg, oracle, golden, torch, p):
+    # the reference's volume_mvm<T,1> with the Laplacian mode matrix, on the
+    # golden inputs (tests/golden: its outputs, from the reference's code)
+    rows = torch.from_numpy(_laplacian_rows(oracle, p)).cuda()
+    for d in (1, 2, 3):
+        x = golden["apply_in_%d_%d" % (p, d)]
+        y = sipg.volume_mvm(d, p, rows, torch.from_numpy(x).cuda()).cpu().numpy()
+        ref = golden["volume_mvm_out_%d_%d" % (p, d)]
+        assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref)), (p, d)
+
+
+def test_stored_operator_per_element(sipg, torch):
+    # volume_mvm<T,0>: a different operator per element, mode_matrix layout
+    p, d = 3, 5
+    n, R, noe = p + 1, 2 * p + 1, d * d
+    rng = np.random.default_rng(7)
+    mat = rng.normal(size=(n * n, R, noe))  # [row k][entry r][element e]
+    x = rng.normal(size=(n * n, noe))
+    ref = np.zeros_like(x)
+    for i1 in range(n):
+        for i2 in range(n):
+            k = i1 * n + i2
+            cols = [k] + [i1 * n + j for j in range(n) if j != i2] + [j * n + i2 for j in range(n) if j != i1]
+            ref[k] = sum(mat[k, r] * x[c] for r, c in enumerate(cols))
+    y = sipg.volume_mvm(d, p, torch.from_numpy(mat.ravel()).cuda(), torch.from_numpy(x.ravel()).cuda())
+    assert np.max(np.abs(y.cpu().numpy().reshape(n * n, noe) - ref)) <= 1e-13 * np.max(np.abs(ref))
