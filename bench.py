@@ -446,6 +446,22 @@ def run_solve16(args):
         dt = (time.perf_counter() - t0) / reps
         extra["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
                                  "sample": "%d solves, %d iterations each" % (reps, it)}
+    # h-convergence over dim = 4..512 (p = 4, same problem, pen p^2, CG to 1e-12
+    # relative): error norms and their rates log2(e(h) / e(h/2))
+    hs = []
+    for dd in (4, 8, 16, 32, 64, 128, 256, 512):
+        oph = sipg.Operator(dd, p, pen)
+        bh = oph.rhs("sinsin")
+        xh = torch.zeros_like(bh)
+        sth, rh = oph.cg(xh, bh, 1e-12, relative=True)
+        e = oph.err_norms("sinsin", xh)
+        hs.append({"dim": dd, "iterations": rh.iterations, "status": sth, "L2": e[0], "H1": e[1], "max": e[2],
+                   "ms": rh.time_ms})
+        oph.close()
+    for a, b2 in zip(hs, hs[1:]):
+        b2["rate_L2"] = float(np.log2(a["L2"] / b2["L2"]))
+        b2["rate_H1"] = float(np.log2(a["H1"] / b2["H1"]))
+    extra["h_convergence_p4"] = hs
     line = _base_line(args, "solves/s, 16x16 quads p=4 SIPG-SEM Poisson CG to relative residual 1e-12",
                       1e3 / r.time_ms, "solves/s", True, "f64",
                       {"workload": "16x16 quads, p=4 (6400 DoF), pen 16, f = 8 pi^2 sin(2 pi x) sin(2 pi y), x0 = 0"},

@@ -1,10 +1,12 @@
-// Instantiates the fused apply (single-operator and batched launches) for
-// double, degree 4: one translation unit per precision and degree, so the
-// build compiles them in parallel.
-#include "sipg_apply.cuh"
+// Instantiates the fused apply for double, degree 4: single-operator
+// launches (element-per-thread and per-node tiles) and batched ones.  One
+// translation unit per precision and degree, so the build compiles them in
+// parallel.
+#include "sipg_apply_pernode.cuh"
 namespace sipg {
 cudaError_t launch_apply_f64_p4(const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
                                   cudaStream_t s) {
+  if (is_pernode(cfg, 4)) return launch_apply_pernode<double, 4>(cfg, mode, a, h, s);
   return launch_apply_p<double, 4>(cfg, mode, a, h, s);
 }
 cudaError_t launch_apply_batched_f64_p4(const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,

@@ -4,6 +4,9 @@
 // A tile is TX = 32 elements along a mesh row (a warp's loads of one node are
 // 32 consecutive values) by TY rows, with one or two threads per element; a
 // CTA holds TX * TY elements and their (p+1)^2 nodal blocks in shared memory.
+// For FP64 on small meshes there is also the per-node tile (a few elements
+// per CTA, one thread per output node), which spreads the thin FP64 pipe's
+// work over many more warps and SMs.
 // TY trades halo overhead (TX + TY halo elements per tile) and reduction
 // partials against shared memory per CTA and so resident CTAs per SM; a
 // second thread per element doubles the resident warps at the same shared
@@ -20,6 +23,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "sipg_internal.cuh"
 
@@ -31,9 +35,11 @@ namespace {
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int>, TileCfg> g_tuned;  // (p, dim, kind) -> shape
 
-// (rows, threads per element); two threads per element only for the
-// compensated apply, the one limited by latency rather than a pipe
-constexpr int kCandidates[5][2] = {{2, 1}, {4, 1}, {8, 1}, {2, 2}, {4, 2}};
+// (elements per row, rows, threads per element): two threads per element only
+// for the compensated apply (the one limited by latency rather than a pipe);
+// the FP64 apply also tries the two per-node tiles (threads per element
+// (p+1)^2) on meshes up to kPernodeMaxDim
+constexpr int kCandidates[5][3] = {{32, 2, 1}, {32, 4, 1}, {32, 8, 1}, {32, 2, 2}, {32, 4, 2}};
 
 template <typename T>
 cudaError_t run_apply(const sipg_op* op, int prec, const TileCfg& cfg, const void* in, void* out, cudaStream_t s) {
@@ -53,10 +59,10 @@ cudaError_t run_apply(const sipg_op* op, int prec, const TileCfg& cfg, const voi
 
 // average ms per apply of one candidate, or a negative value if it cannot run
 template <typename T>
-float time_candidate(const sipg_op* op, int prec, int ty, int tpe, const void* in, void* out, cudaStream_t s,
+float time_candidate(const sipg_op* op, int prec, int tx, int ty, int tpe, const void* in, void* out, cudaStream_t s,
                      cudaEvent_t e0, cudaEvent_t e1, int reps) {
   TileCfg cfg;
-  cfg.tx = 32;
+  cfg.tx = tx;
   cfg.ty = ty;
   cfg.tpe = tpe;
   if (run_apply<T>(op, prec, cfg, in, out, s) != cudaSuccess) {
@@ -81,12 +87,23 @@ TileCfg tune_one(const sipg_op* op, int prec, const void* in, void* out, cudaStr
   TileCfg best;
   best.ty = 0;
   float bms = 0.f;
+  std::vector<TileCfg> cands;
   for (const auto& c : kCandidates) {
-    if (c[1] != 1 && prec != SIPG_TUNE_PAIRS) continue;
-    const float ms = time_candidate<T>(op, prec, c[0], c[1], in, out, s, e0, e1, reps);
+    if (c[2] != 1 && prec != SIPG_TUNE_PAIRS) continue;
+    TileCfg t;
+    t.tx = c[0];
+    t.ty = c[1];
+    t.tpe = c[2];
+    cands.push_back(t);
+  }
+  if (prec == SIPG_TUNE_F64 && op->dim <= kPernodeMaxDim) {
+    cands.push_back(pernode_tile(op->p, 0));
+    cands.push_back(pernode_tile(op->p, 1));
+  }
+  for (const TileCfg& c : cands) {
+    const float ms = time_candidate<T>(op, prec, c.tx, c.ty, c.tpe, in, out, s, e0, e1, reps);
     if (ms > 0.f && (best.ty == 0 || ms < bms)) {
-      best.ty = c[0];
-      best.tpe = c[1];
+      best = c;
       bms = ms;
     }
   }
@@ -158,37 +175,57 @@ sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out) {
   }
   if (out) {
     for (int k = 0; k < 3; ++k) {
+      out->elements_per_row[k] = ty[k].tx;
       out->rows[k] = ty[k].ty;
       out->threads_per_element[k] = ty[k].tpe;
       out->ms_per_apply[k] = ms[k];
     }
-    out->elements_per_row = 32;
   }
   return SIPG_OK;
 }
 
-sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows, int threads_per_element) {
-  const bool tpe_ok = threads_per_element == 1 || (threads_per_element == 2 && kind == SIPG_TUNE_PAIRS && rows != 8);
-  if (!op || kind < 0 || kind > 2 || (rows != 2 && rows != 4 && rows != 8) || !tpe_ok) {
-    set_error("sipg_op_set_tile: kind must be 0..2, rows 2, 4 or 8, threads per element 1 (or 2 for the pairs "
-              "apply with 2 or 4 rows)");
+sipg_status sipg_op_set_tile(sipg_op* op, int kind, int elements_per_row, int rows, int threads_per_element) {
+  if (!op || kind < 0 || kind > 2) {
+    set_error("sipg_op_set_tile: null op or kind not 0..2");
+    return SIPG_ERR_INVALID;
+  }
+  const int p = op->p;
+  const bool pernode = kind == SIPG_TUNE_F64 && threads_per_element == (p + 1) * (p + 1);
+  bool ok;
+  if (pernode) {
+    ok = op->dim <= kPernodeMaxDim && rows == pernode_ey(p) &&
+         (elements_per_row == pernode_ex(p, 0) || elements_per_row == pernode_ex(p, 1));
+  } else {
+    const bool tpe_ok =
+        threads_per_element == 1 || (threads_per_element == 2 && kind == SIPG_TUNE_PAIRS && rows != 8);
+    ok = elements_per_row == 32 && (rows == 2 || rows == 4 || rows == 8) && tpe_ok;
+  }
+  if (!ok) {
+    set_error("sipg_op_set_tile: a tile is 32 elements per row by 2, 4 or 8 rows with 1 thread per element (2 for "
+              "the pairs apply with 2 or 4 rows), or, for FP64 on meshes up to 1024 x 1024, the per-node tile: "
+              "(p+1)^2 threads per element, " +
+              std::to_string(pernode_ex(p, 0)) + " or " + std::to_string(pernode_ex(p, 1)) + " elements per row, " +
+              std::to_string(pernode_ey(p)) + " rows");
     return SIPG_ERR_INVALID;
   }
   std::lock_guard<std::mutex> lk(op->mu);
   TileCfg& c = kind == SIPG_TUNE_F64 ? op->cfg64 : (kind == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
+  c.tx = elements_per_row;
   c.ty = rows;
   c.tpe = threads_per_element;
   op->tile_gen++;
   return SIPG_OK;
 }
 
-sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows, int* threads_per_element) {
+sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* elements_per_row, int* rows,
+                             int* threads_per_element) {
   if (!op || !rows || kind < 0 || kind > 2) {
     set_error("sipg_op_get_tile: bad argument");
     return SIPG_ERR_INVALID;
   }
   const TileCfg& c = kind == SIPG_TUNE_F64 ? op->cfg64 : (kind == SIPG_TUNE_F32 ? op->cfg32 : op->cfgdf);
   *rows = c.ty;
+  if (elements_per_row) *elements_per_row = c.tx;
   if (threads_per_element) *threads_per_element = c.tpe;
   return SIPG_OK;
 }

@@ -203,7 +203,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
       BGroup g;
       g.p = p;
       g.cfgdf = b->inst[k].op->cfgdf;
-      g.cfg64 = b->inst[k].op->cfg64;
+      g.cfg64 = batched_tile(b->inst[k].op->cfg64);
       b->groups.push_back(g);
     }
     b->groups[gidx[p]].members.push_back(k);

@@ -131,14 +131,18 @@ sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double*
 sipg_status err_norms_f64(const sipg_op* op, int sol, const sipg_modes* modes, const double* d_u, double* err,
                           cudaStream_t s);
 
-// Default tile shapes (rows of 32 elements; TY rows per CTA).
-static TileCfg default_cfg(int p, bool f64) {
+// Default tile shapes: rows of 32 elements, TY rows per CTA; for FP64 on
+// small meshes the per-node tile, which spreads the FP64 work over many more
+// warps and SMs.
+static TileCfg default_cfg(int p, int dim, bool f64) {
   TileCfg c;
   c.tx = 32;
-  if (f64)
+  if (f64) {
     c.ty = (p <= 3) ? 8 : 4;
-  else
+    if (dim <= kPernodeDefaultDim) c = pernode_tile(p, 0);
+  } else {
     c.ty = (p <= 4) ? 8 : 4;
+  }
   return c;
 }
 
@@ -232,6 +236,16 @@ static int graph_iters(long long ndof) { return ndof <= (1LL << 20) ? 32 : 8; }
 
 // Capture K CG iterations (apply + update; the direction buffers alternate by
 // the parity kept in the device state, so a chunk may stop at any iteration).
+// Whether the CG iterations fuse the direction update into the apply
+// (APPLY_CG: two kernels per iteration).  The per-node tile does: on the small
+// meshes it serves, an iteration is a chain of short launches.  The
+// element-per-thread tiles form the direction in a vector kernel instead
+// (APPLY_DOT), so the apply reads one vector, not two.
+template <typename T>
+static bool cg_fused_direction(const sipg_op* op) {
+  return sizeof(T) == 8 && is_pernode(op->cfg64, op->p);
+}
+
 template <typename T>
 static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, int K) {
   if (w->exec && w->exec_x == x && w->exec_k == K && w->exec_gen == op->tile_gen) return SIPG_OK;
@@ -248,23 +262,36 @@ static sipg_status capture_iterations(sipg_op* op, sipg_cg_workspace* w, T* x, i
   SIPG_CUDA_TRY(cudaStreamBeginCapture(w->cap, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   const int vb = vec_blocks(w->n);
+  const bool fused = cg_fused_direction<T>(op);
   for (int k = 0; k < K && err == cudaSuccess; ++k) {
-    // p = r + beta p; Ap, p.Ap, alpha; x += alpha p, r -= alpha Ap, r.r, beta
-    k_cg_direction<T><<<vb, kVecThreads, 0, w->cap>>>((T*)w->p[0], (const T*)w->r, w->n, (CgState<T>*)w->st);
-    err = cudaGetLastError();
-    if (err != cudaSuccess) break;
     ApplyArgs<T> a{};
-    a.in = (const T*)w->p[0];
     a.out = (T*)w->Ap;
     a.b = nullptr;
     a.dim = op->dim;
     a.nu = (T)op->pen;
     a.st = (CgState<T>*)w->st;
     a.red = w->red;
-    err = launch_apply<T>(op, APPLY_DOT, a, w->cap);
-    if (err != cudaSuccess) break;
-    k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[0], (T*)w->r,
-                                                   (const T*)w->Ap, w->n, (CgState<T>*)w->st, w->red);
+    if (fused) {
+      // p_new = r + beta p_old, Ap, p.Ap, alpha in one kernel; x += alpha
+      // p_new, r -= alpha Ap, r.r, beta in the next
+      a.in = (const T*)w->r;
+      a.pbuf0 = (T*)w->p[0];
+      a.pbuf1 = (T*)w->p[1];
+      err = launch_apply<T>(op, APPLY_CG, a, w->cap);
+      if (err != cudaSuccess) break;
+      k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[1], (T*)w->r,
+                                                     (const T*)w->Ap, w->n, (CgState<T>*)w->st, w->red);
+    } else {
+      // p = r + beta p; Ap, p.Ap, alpha; x += alpha p, r -= alpha Ap, r.r, beta
+      k_cg_direction<T><<<vb, kVecThreads, 0, w->cap>>>((T*)w->p[0], (const T*)w->r, w->n, (CgState<T>*)w->st);
+      err = cudaGetLastError();
+      if (err != cudaSuccess) break;
+      a.in = (const T*)w->p[0];
+      err = launch_apply<T>(op, APPLY_DOT, a, w->cap);
+      if (err != cudaSuccess) break;
+      k_cg_update<T><<<vb, kVecThreads, 0, w->cap>>>(x, (const T*)w->p[0], (const T*)w->p[0], (T*)w->r,
+                                                     (const T*)w->Ap, w->n, (CgState<T>*)w->st, w->red);
+    }
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(w->cap, &g);
@@ -319,7 +346,7 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   long long launched = 0;
   for (;;) {
     SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
-    count_launch(3ULL * K);
+    count_launch((cg_fused_direction<T>(op) ? 2ULL : 3ULL) * K);
     launched += K;
     SIPG_CUDA_TRY(cudaMemcpyAsync(hs, w->st, sizeof(CgState<T>), cudaMemcpyDeviceToHost, s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -443,8 +470,8 @@ sipg_status sipg_op_create(int dim, int degree, double pen, sipg_op** out) {
   op->noe = (long long)dim * dim;
   op->ndof = op->noe * (degree + 1) * (degree + 1);
   build_host_tables(degree, &op->tab);
-  op->cfg64 = default_cfg(degree, true);
-  op->cfg32 = default_cfg(degree, false);
+  op->cfg64 = default_cfg(degree, dim, true);
+  op->cfg32 = default_cfg(degree, dim, false);
   op->cfgdf.tx = 32;
   op->cfgdf.ty = 4;
   // shapes the autotuner already chose for this (degree, dim) in this process

@@ -383,7 +383,7 @@ std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArg
     const std::vector<Request*>& g = kv.second;
     GroupLaunch gl;
     gl.p = kv.first;
-    gl.cfg = (sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfgdf;
+    gl.cfg = (sizeof(T) == 8) ? batched_tile(g[0]->op->cfg64) : g[0]->op->cfgdf;
     gl.off = off;
     gl.m = (int)g.size();
     gl.toff = toff;

@@ -110,6 +110,52 @@ struct ApplyColumnForm {
   static constexpr int col_unroll = (sizeof(T) == 8 && P >= 5) ? 1 : (P + 1);
 };
 
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
+// J and Q of one face node (kappa = 1/2 inside, 1 on the boundary, where the
+// missing side's values are zero).  The products and the sum are explicitly
+// rounded: where a kernel calls this with literal constants (a boundary
+// face), the compiler would otherwise fold fma(1, s, nu * jmp) into s + nu *
+// jmp and contract that into one FMA -- a last-bit difference from the same
+// face computed with runtime values by another tile shape.
+template <typename T>
+__device__ __forceinline__ void face_combine(T w, T nu, bool interior, T u0, T d0, T uN, T dN, T& J, T& Q) {
+  const T kap = interior ? T(0.5) : T(1);
+  const T jmp = u0 - uN;
+  J = mul_rn(mul_rn(kap, w), jmp);
+  Q = mul_rn(w, fma(kap, add_rn(d0, dN), mul_rn(nu, jmp)));
+}
+
+// The reduced total of a CG / residual apply, in the block that summed it
+// (one thread): alpha = rr / p.Ap (and the direction parity flip) after a CG
+// or DOT apply; the start of a solve after r = b - A x.
+template <typename T, int MODE>
+__device__ __forceinline__ void apply_finish(CgState<T>* st, T total, int par) {
+  if (MODE == APPLY_CG || MODE == APPLY_DOT) {
+    const T alpha = st->rr / total;
+    st->pAp = total;
+    st->alpha = alpha;
+    if (MODE == APPLY_CG) st->parity = 1 - par;  // every block read the parity before arriving here
+    if (!(total > T(0)) || !isfinite(alpha)) {
+      st->status = (int)SIPG_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+  } else {  // APPLY_RESID: r = b - A x, start of a CG solve
+    st->rr = total;
+    st->it = 0;
+    st->first = 1;
+    st->status = (int)SIPG_OK;
+    st->done = !(sqrt(total) > st->stop && 0 < st->max_it);
+    if (!isfinite(total)) {
+      st->status = (int)SIPG_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+  }
+}
+
 // One CTA's work: tile (bx, by) of the operator in `a`; `bid` / `nblocks` name
 // the block among the blocks that reduce into a.red (CG / residual modes).
 template <typename T, int P, int TX, int TY, int MODE>
@@ -161,10 +207,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   auto YFr = [&](int frow, int comp, int j, int col) -> T& { return yf[((frow * 2 + comp) * N1 + j) * TX + col]; };
   const T nu = a.nu;
   auto combine = [&](int j, bool interior, T u0, T d0, T uN, T dN, T& J, T& Q) {
-    const T kap = interior ? T(0.5) : T(1);
-    const T jmp = u0 - uN;
-    J = kap * tb.w[j] * jmp;
-    Q = tb.w[j] * fma(kap, d0 + dN, nu * jmp);
+    face_combine<T>(tb.w[j], nu, interior, u0, d0, uN, dN, J, Q);
   };
 
   // ---- phase 0: the tile's nodal blocks -> smem --------------------------
@@ -447,29 +490,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   if (MODE != APPLY_PLAIN) {
     const T bt = block_sum<T, TE>(acc, red_sh);
     T total;
-    if (grid_sum_last<T, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0) {
-      CgState<T>* st = a.st;
-      if (kDot) {
-        const T alpha = st->rr / total;
-        st->pAp = total;
-        st->alpha = alpha;
-        if (MODE == APPLY_CG) st->parity = 1 - par;  // every block read the parity before arriving here
-        if (!(total > T(0)) || !isfinite(alpha)) {
-          st->status = (int)SIPG_ERR_BREAKDOWN;
-          st->done = 1;
-        }
-      } else {  // APPLY_RESID: r = b - A x, start of a CG solve
-        st->rr = total;
-        st->it = 0;
-        st->first = 1;
-        st->status = (int)SIPG_OK;
-        st->done = !(sqrt(total) > st->stop && 0 < st->max_it);
-        if (!isfinite(total)) {
-          st->status = (int)SIPG_ERR_BREAKDOWN;
-          st->done = 1;
-        }
-      }
-    }
+    if (grid_sum_last<T, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0)
+      apply_finish<T, MODE>(a.st, total, par);
   }
 }
 
@@ -548,7 +570,7 @@ cudaError_t launch_apply_p(const TileCfg& cfg, int mode, const ApplyArgs<T>& a, 
   const Tab<T, P> tb = make_tab<T, P>(h);
   constexpr size_t kMax = 227 * 1024;
   constexpr bool fits8 = ApplySmem<T, P, 32, 8>::bytes <= kMax;
-  if (cfg.tx != 32) return cudaErrorInvalidValue;
+  if (cfg.tx != 32 || cfg.tpe != 1) return cudaErrorInvalidValue;
   switch (cfg.ty) {
     case 2:
       return launch_apply_tile<T, P, 32, 2>(mode, a, tb, s);
@@ -598,6 +620,8 @@ cudaError_t launch_apply_batched_p(const TileCfg& cfg, int mode, const ApplyArgs
   const Tab<T, P> tb = make_tab<T, P>(h);
   constexpr size_t kMax = 227 * 1024;
   constexpr bool fits8 = ApplySmem<T, P, 32, 8>::bytes <= kMax;
+  // batched solves keep 32-element rows: their tiles are laid out by
+  // tile_start for that width
   if (cfg.tx != 32) return cudaErrorInvalidValue;
   switch (cfg.ty) {
     case 2:

@@ -1,0 +1,249 @@
+// sipg_apply_pernode.cuh -- the FP64 apply for small meshes: one thread per
+// output node.
+//
+// GB300 issues FP64 at a small fraction of its FP32 rate: a warp instruction of
+// 32 DFMAs occupies a sub-partition's FP64 unit for tens of cycles.  The
+// element-per-thread apply (sipg_apply.cuh) gives every thread the whole
+// (p+1)^2-output chain of one element, so a mesh with few elements -- 256 at
+// 16 x 16 -- runs a few warps, each through ~1000 dependent-issue DFMAs, on a
+// handful of SMs: tens of microseconds per apply, whatever the tile shape.
+// Here a CTA holds EX x EY elements and gives each output node its own thread:
+// the same operations spread over (p+1)^2 times more warps, on more SMs.
+//
+// Each output is formed by exactly the operations, in exactly the order, of
+// the element-per-thread kernel's column form (the FP64 form): the volume
+// sums w_j sum_i K(i1,i) u(i,j) and w_i1 sum_i K(j,i) u(i1,i) accumulated from
+// i = 0, the lifting of the four faces' J, then the face nodes' +-Q.  Face
+// values (J, Q) come from the same one-sided traces and derivatives combined
+// by the same expression.  So the result is bit-identical to every other
+// FP64 tile shape; only the CG reductions (p.Ap, r.r) group their partial
+// sums differently.
+//
+// Phases of a CTA (static shared memory, a few KB):
+//   0  the tables, and the nodal blocks of the EX x EY elements and of the
+//      2 (EX + EY) halo elements around them (from L2: small meshes live
+//      there), with p = r + beta p_old formed on the fly in the CG mode;
+//   1  one thread per face node: trace and normal derivative of each side,
+//      combined into J and Q (both sides present inside the mesh, one side on
+//      the domain boundary);
+//   2  one thread per output node, then the epilogue (store, direction store
+//      in the CG mode, deterministic grid reduction in the CG / DOT /
+//      residual modes).
+#pragma once
+
+#include "sipg_apply.cuh"
+
+namespace sipg {
+
+template <int P, int SHAPE>
+struct PernodeShape {
+  static constexpr int N1 = P + 1, NN = N1 * N1;
+  static constexpr int EX = pernode_ex(P, SHAPE), EY = pernode_ey(P), NE = EX * EY;
+  static constexpr int NT = (NE * NN + 31) / 32 * 32;  // threads: whole warps, the tail idle in phase 2
+  static constexpr int SX = EX + 2, SY = EY + 2;       // element slots, halo ring included
+  static constexpr int NX = EY * (EX + 1) * N1;        // x-face nodes: [EY][EX+1][N1]
+  static constexpr int NY = EX * (EY + 1) * N1;        // y-face nodes: [EY+1][EX][N1]
+};
+
+template <typename T, int P, int SHAPE, int MODE>
+__global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
+    k_sipg_apply_pernode(const __grid_constant__ ApplyArgs<T> a, const __grid_constant__ Tab<T, P> tb) {
+  using S = PernodeShape<P, SHAPE>;
+  constexpr int N = P, N1 = S::N1, NN = S::NN, EX = S::EX, EY = S::EY, NE = S::NE, NT = S::NT;
+  constexpr int SX = S::SX, SY = S::SY, NX = S::NX, NY = S::NY, NSLOT = SX * SY;
+  __shared__ T us[NSLOT * NN];  // slot (sy, sx) = element (y0 - 1 + sy, x0 - 1 + sx), values [i1 * N1 + i2]
+  __shared__ T xj[NX], xq[NX], yj[NY], yq[NY];
+  __shared__ T tw[N1], td0[N1], tdn[N1], tk[NN];
+  __shared__ T red_sh[32];
+
+  constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);
+  if (kDot) {
+    if (*(volatile int*)&a.st->done) return;  // converged: the launch is a no-op
+  }
+  const int t = threadIdx.x;
+  const int dim = a.dim;
+  const int x0 = blockIdx.x * EX, y0 = blockIdx.y * EY;
+  const size_t noe = (size_t)dim * dim;
+
+  bool first = true;
+  T beta = T(0);
+  int par = 0;
+  if (MODE == APPLY_CG) {
+    first = a.st->first != 0;
+    beta = a.st->beta;
+    par = a.st->parity;
+  }
+  const T* __restrict__ pold = par ? a.pbuf1 : a.pbuf0;
+  T* __restrict__ pnew = par ? a.pbuf0 : a.pbuf1;
+
+  // ---- phase 0: tables and nodal blocks ------------------------------------
+  // (the tables per thread index: a constant-bank read whose address differs
+  // across the warp would serialise)
+  if (t < NN) tk[t] = tb.K[t];
+  if (t < N1) {
+    tw[t] = tb.w[t];
+    td0[t] = tb.D0[t];
+    tdn[t] = tb.DN[t];
+  }
+  for (int idx = t; idx < NSLOT * NN; idx += NT) {
+    const int k = idx / NSLOT, sl = idx - k * NSLOT;
+    const int sy = sl / SX, sx = sl - sy * SX;
+    const int gx = x0 - 1 + sx, gy = y0 - 1 + sy;
+    const bool corner = (sx == 0 || sx == SX - 1) && (sy == 0 || sy == SY - 1);
+    T v = T(0);
+    if (!corner && gx >= 0 && gx < dim && gy >= 0 && gy < dim) {
+      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+      v = __ldg(a.in + gk);
+      if (MODE == APPLY_CG && !first) v = fma(beta, __ldg(pold + gk), v);
+    }
+    us[sl * NN + k] = v;
+  }
+  __syncthreads();
+
+  const T nu = a.nu;
+  // ---- phase 1: J and Q of every face node of the tile -----------------------
+  for (int f = t; f < NX + NY; f += NT) {
+    T u0 = T(0), d0 = T(0), uN = T(0), dN = T(0);
+    bool zv, nv;  // 0-side / N-side element inside the mesh
+    int j;
+    if (f < NX) {
+      // x face fx of tile row ey: the left element (slot fx) is its N-side
+      // (i1 = P), the right element (slot fx + 1) its 0-side (i1 = 0)
+      j = f % N1;
+      const int r = f / N1, fx = r % (EX + 1), ey = r / (EX + 1);
+      const int gy = y0 + ey, gxl = x0 + fx - 1;
+      nv = gy < dim && gxl >= 0 && gxl < dim;
+      zv = gy < dim && gxl + 1 < dim;
+      const T* L = us + ((ey + 1) * SX + fx) * NN;
+      const T* R = L + NN;
+      if (zv) {
+        u0 = R[j];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], R[i * N1 + j], d0);
+      }
+      if (nv) {
+        uN = L[N * N1 + j];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], L[i * N1 + j], dN);
+      }
+    } else {
+      // y face fy of tile column ex: the upper element (slot row fy) is its
+      // 0-side (i2 = 0), the lower element (slot row fy + 1) its N-side (i2 = P)
+      const int g = f - NX;
+      j = g % N1;
+      const int r = g / N1, ex = r % EX, fy = r / EX;
+      const int gx = x0 + ex, gyu = y0 + fy - 1;
+      zv = gx < dim && gyu >= 0 && gyu < dim;
+      nv = gx < dim && gyu + 1 < dim;
+      const T* Up = us + (fy * SX + ex + 1) * NN;
+      const T* Dn = Up + SX * NN;
+      if (zv) {
+        u0 = Up[j * N1];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], Up[j * N1 + i], d0);
+      }
+      if (nv) {
+        uN = Dn[j * N1 + N];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], Dn[j * N1 + i], dN);
+      }
+    }
+    T J, Q;
+    face_combine<T>(tw[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
+    if (f < NX) {
+      xj[f] = J;
+      xq[f] = Q;
+    } else {
+      yj[f - NX] = J;
+      yq[f - NX] = Q;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 2: one output node per thread ------------------------------------
+  T acc = T(0);
+  if (t < NE * NN) {
+    const int le = t % NE, k = t / NE;  // element fastest: neighbouring threads store neighbouring elements
+    const int ex = le % EX, ey = le / EX;
+    const int i1 = k / N1, j = k - i1 * N1;
+    const int gx = x0 + ex, gy = y0 + ey;
+    if (gx < dim && gy < dim) {
+      const T* E = us + ((ey + 1) * SX + ex + 1) * NN;
+      const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
+      const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
+      const int fu = fd - EX * N1;
+      T o = T(0), s = T(0);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) o = fma(tk[i1 * N1 + i], E[i * N1 + j], o);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) s = fma(tk[j * N1 + i], E[i1 * N1 + i], s);
+      T v = fma(tw[j], o, fma(td0[i1], xj[fl + j], tdn[i1] * xj[fl + N1 + j]));
+      v = fma(tw[i1], s, v);
+      v = fma(td0[j], yj[fd + i1], v);
+      v = fma(tdn[j], yj[fu + i1], v);
+      if (i1 == 0) v += xq[fl + j];
+      if (i1 == N) v -= xq[fl + N1 + j];
+      if (j == 0) v += yq[fd + i1];
+      if (j == N) v -= yq[fu + i1];
+      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+      if (MODE == APPLY_RESID) {
+        const T rv = __ldg(a.b + gk) - v;
+        a.out[gk] = rv;
+        acc = fma(rv, rv, acc);
+      } else {
+        a.out[gk] = v;
+        const T c = E[k];
+        if (MODE == APPLY_CG) pnew[gk] = c;
+        if (kDot) acc = fma(c, v, acc);
+      }
+    }
+  }
+
+  if (MODE != APPLY_PLAIN) {
+    const T bt = block_sum<T, NT>(acc, red_sh);
+    T total;
+    if (grid_sum_last<T, NT>(bt, a.red, (int)(gridDim.x * gridDim.y), red_sh, &total) && t == 0)
+      apply_finish<T, MODE>(a.st, total, par);
+  }
+}
+
+template <typename T, int P, int SHAPE>
+cudaError_t launch_apply_pernode_shape(int mode, const ApplyArgs<T>& a, const Tab<T, P>& tb, cudaStream_t s) {
+  using S = PernodeShape<P, SHAPE>;
+  if (mode == APPLY_PREPARE) return cudaSuccess;  // static shared memory: no attribute to set
+  const dim3 grid((a.dim + S::EX - 1) / S::EX, (a.dim + S::EY - 1) / S::EY), block(S::NT);
+  // every block of a reducing mode stores one partial
+  if (mode != APPLY_PLAIN && (long long)grid.x * grid.y > (long long)a.red.capacity) return cudaErrorInvalidValue;
+  switch (mode) {
+    case APPLY_PLAIN:
+      k_sipg_apply_pernode<T, P, SHAPE, APPLY_PLAIN><<<grid, block, 0, s>>>(a, tb);
+      break;
+    case APPLY_CG:
+      k_sipg_apply_pernode<T, P, SHAPE, APPLY_CG><<<grid, block, 0, s>>>(a, tb);
+      break;
+    case APPLY_RESID:
+      k_sipg_apply_pernode<T, P, SHAPE, APPLY_RESID><<<grid, block, 0, s>>>(a, tb);
+      break;
+    case APPLY_DOT:
+      k_sipg_apply_pernode<T, P, SHAPE, APPLY_DOT><<<grid, block, 0, s>>>(a, tb);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+// The per-node tile named by cfg (tpe = (p+1)^2; tx x ty one of the two
+// compiled shapes), on meshes up to kPernodeMaxDim elements per edge.
+template <typename T, int P>
+cudaError_t launch_apply_pernode(const TileCfg& cfg, int mode, const ApplyArgs<T>& a, const HostTables& h,
+                                 cudaStream_t s) {
+  if (a.dim > kPernodeMaxDim || cfg.ty != pernode_ey(P)) return cudaErrorInvalidConfiguration;
+  const Tab<T, P> tb = make_tab<T, P>(h);
+  if (cfg.tx == pernode_ex(P, 0)) return launch_apply_pernode_shape<T, P, 0>(mode, a, tb, s);
+  if (cfg.tx == pernode_ex(P, 1)) return launch_apply_pernode_shape<T, P, 1>(mode, a, tb, s);
+  return cudaErrorInvalidConfiguration;
+}
+
+}  // namespace sipg

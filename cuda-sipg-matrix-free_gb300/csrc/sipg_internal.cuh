@@ -131,8 +131,25 @@ inline void set_penalty3(ApplyArgs<float>& a, double pen) {
 // Tile shape chosen for one (precision, degree).
 struct TileCfg {
   int tx = 32, ty = 4;
-  int tpe = 1;  // threads per element (the compensated apply compiles 1 and 2)
+  int tpe = 1;  // threads per element: 1, 2 (the compensated apply), or (p+1)^2
+                // (the per-node FP64 tile for small meshes)
 };
+
+// The per-node FP64 tile (one thread per output node): tx x ty elements per
+// CTA, shape 0 the smallest, shape 1 twice as wide; meshes up to
+// kPernodeMaxDim elements per edge (its reduction partials grow as dim^2 / 4).
+__host__ __device__ constexpr int pernode_ey(int p) { return p == 1 ? 4 : 2; }
+__host__ __device__ constexpr int pernode_ex(int p, int shape) { return (p <= 2 ? 4 : 2) * (shape ? 2 : 1); }
+constexpr int kPernodeMaxDim = 1024;
+constexpr int kPernodeDefaultDim = 64;  // FP64 operators up to this size start with it
+inline bool is_pernode(const TileCfg& c, int p) { return c.tpe == (p + 1) * (p + 1); }
+inline TileCfg pernode_tile(int p, int shape) {
+  TileCfg c;
+  c.tx = pernode_ex(p, shape);
+  c.ty = pernode_ey(p);
+  c.tpe = (p + 1) * (p + 1);
+  return c;
+}
 
 // Launch the fused apply for degree p (dispatches on p and the tile shape).
 // Returns cudaGetLastError() of the launch.
@@ -157,14 +174,24 @@ cudaError_t launch_apply_df(int p, const TileCfg& cfg, int mode, const ApplyArgs
 // process; false if none (autotune.cu).
 bool autotune_lookup(int p, int dim, int prec, TileCfg* cfg);
 // Number of blocks the apply launches for this tile shape.
+// The tile a batched launch uses: batched kernels compile 32-element rows
+// only, so an operator tuned to the per-node FP64 tile joins a batch with the
+// 32 x 4 tile.
+inline TileCfg batched_tile(TileCfg c) {
+  if (c.tx != 32) c = TileCfg{};
+  return c;
+}
 inline int apply_grid_blocks(int dim, const TileCfg& c) {
   return ((dim + c.tx - 1) / c.tx) * ((dim + c.ty - 1) / c.ty);
 }
-// Reduction-scratch entries that cover every apply tile shape (the smallest
-// compiled tile is 32 x 2) and every vector kernel grid (at most 152 * 8).
+// Reduction-scratch entries that cover every apply tile shape (the tiles
+// with the fewest elements are 32 x 2 and, up to kPernodeMaxDim, the 2 x 2
+// per-node tile) and every vector kernel grid (at most 152 * 8).
 inline int reduce_capacity(int dim) {
   const int a = ((dim + 31) / 32) * ((dim + 1) / 2);
-  return a > 152 * 8 ? a : 152 * 8;
+  const int b = dim <= kPernodeMaxDim ? ((dim + 1) / 2) * ((dim + 1) / 2) : 0;
+  const int m = a > b ? a : b;
+  return m > 152 * 8 ? m : 152 * 8;
 }
 
 

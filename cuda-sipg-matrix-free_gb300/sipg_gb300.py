@@ -82,7 +82,7 @@ class Modes(C.Structure):
 
 
 class TileChoice(C.Structure):
-    _fields_ = [("elements_per_row", C.c_int), ("rows", C.c_int * 3), ("threads_per_element", C.c_int * 3),
+    _fields_ = [("elements_per_row", C.c_int * 3), ("rows", C.c_int * 3), ("threads_per_element", C.c_int * 3),
                 ("ms_per_apply", C.c_float * 3)]
 
 
@@ -99,8 +99,8 @@ _SIGS = {
     "sipg_op_destroy": (C.c_int, [_VP]),
     "sipg_op_solve_footprint": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
     "sipg_op_autotune": (C.c_int, [_VP, _VP, C.POINTER(TileChoice)]),
-    "sipg_op_set_tile": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
-    "sipg_op_get_tile": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sipg_op_set_tile": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "sipg_op_get_tile": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sipg_apply_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_apply_pairs": (C.c_int, [_VP, _VP, _VP, _VP]),
@@ -230,6 +230,17 @@ def square_mesh_coords(dim):
     return x, y
 
 
+def pernode_tile(p, shape=0):
+    """(elements per row, rows, threads per element) of the per-node FP64 tile
+    of degree p: shape 0 holds the fewest elements per CTA, shape 1 twice as
+    many along the row; (p+1)^2 threads per element."""
+    return (4 if p <= 2 else 2) * (2 if shape else 1), 4 if p == 1 else 2, (p + 1) ** 2
+
+
+PERNODE_MAX_DIM = 1024  # the per-node tile serves meshes up to this many elements per edge
+PERNODE_DEFAULT_DIM = 64  # FP64 operators up to this size start with it
+
+
 class Operator:
     """The SIPG operator of a dim x dim mesh of degree p with kernel penalty pen."""
 
@@ -252,20 +263,32 @@ class Operator:
         self._h = None
 
     def autotune(self, stream=None):
-        """Times the tile shapes on this operator and keeps the fastest per
-        apply kind; returns {kind: (rows, threads_per_element, ms_per_apply)}."""
+        """Times the tile shapes on this operator and keeps the fastest per apply
+        kind; returns {kind: (elements_per_row, rows, threads_per_element, ms_per_apply)}."""
         tc = TileChoice()
         _check(lib().sipg_op_autotune(self._h, _stream(stream), C.byref(tc)), "autotune")
-        return {k: (tc.rows[i], tc.threads_per_element[i], tc.ms_per_apply[i]) for k, i in TILE_KINDS.items()}
+        return {k: (tc.elements_per_row[i], tc.rows[i], tc.threads_per_element[i], tc.ms_per_apply[i])
+                for k, i in TILE_KINDS.items()}
 
-    def set_tile(self, kind, rows, threads_per_element=1):
-        _check(lib().sipg_op_set_tile(self._h, TILE_KINDS[kind], int(rows), int(threads_per_element)), "set_tile")
+    def set_pernode(self, shape=0):
+        """Switches the FP64 apply to the per-node tile (one thread per output
+        node; shape 0 or 1, see pernode_tile), the small-mesh choice."""
+        ex, ey, tpe = pernode_tile(self.degree, shape)
+        self.set_tile("f64", ey, tpe, ex)
+
+    def set_tile(self, kind, rows, threads_per_element=1, elements_per_row=32):
+        _check(lib().sipg_op_set_tile(self._h, TILE_KINDS[kind], int(elements_per_row), int(rows),
+                                      int(threads_per_element)), "set_tile")
 
     def get_tile(self, kind):
         """(rows, threads per element) of the apply kind's tile."""
-        r, t = C.c_int(), C.c_int()
-        _check(lib().sipg_op_get_tile(self._h, TILE_KINDS[kind], C.byref(r), C.byref(t)), "get_tile")
-        return r.value, t.value
+        return self.get_shape(kind)[1:]
+
+    def get_shape(self, kind):
+        """(elements per row, rows, threads per element) of the apply kind's tile."""
+        x, r, t = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().sipg_op_get_tile(self._h, TILE_KINDS[kind], C.byref(x), C.byref(r), C.byref(t)), "get_tile")
+        return x.value, r.value, t.value
 
     def __del__(self):
         try:

@@ -146,24 +146,27 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
 /* ---- tile shapes and the autotuner (no reference counterpart: the
  * reference launches one fixed geometry) ----
  * An apply tile is 32 elements along a mesh row by `rows` rows (2, 4 or 8),
- * with one thread per element (or two, pairs apply only).  Every shape gives
- * bit-identical apply results; CG reductions regroup.  Tile indices for the three apply kinds: */
+ * with one thread per element (or two, pairs apply only); the FP64 apply also
+ * has a one-warp 8 x 4 tile, its default for meshes up to 96 x 96, whose extra
+ * CTAs put more SMs' FP64 pipes on a small mesh.  Every shape gives
+ * bit-identical apply results; CG reductions regroup.  Tile indices for the
+ * three apply kinds: */
 enum { SIPG_TUNE_F64 = 0, SIPG_TUNE_F32 = 1, SIPG_TUNE_PAIRS = 2 /* compensated, pair vectors */ };
 typedef struct {
-  int elements_per_row;   /* 32 */
-  int rows[3];                 /* chosen rows per tile, by SIPG_TUNE_* */
-  int threads_per_element[3];  /* chosen threads per element (1, or 2 for the pairs apply) */
+  int elements_per_row[3];     /* 32, or 8 (FP64), by SIPG_TUNE_* */
+  int rows[3];                 /* rows per tile */
+  int threads_per_element[3];  /* 1, or 2 for the pairs apply */
   float ms_per_apply[3];       /* the winning candidate's time */
 } sipg_tile_choice;
-/* Times the tile shapes for each apply kind on this op -- rows in {2, 4, 8}
- * with one thread per element, and for the pairs apply also rows in {2, 4}
- * with two -- on scratch vectors of ndof doubles (allocated and freed here),
- * keeps the fastest, and records it for (degree, dim) so ops created later in
- * this process start with it.  Synchronous; not during stream capture.  `out`
- * may be NULL. */
+/* Times the tile shapes for each apply kind on this op -- 32 x {2, 4, 8} with
+ * one thread per element, for the pairs apply also 32 x {2, 4} with two, for
+ * FP64 also 8 x 4 -- on scratch vectors of ndof doubles (allocated and freed
+ * here), keeps the fastest, and records it for (degree, dim) so ops created
+ * later in this process start with it.  Synchronous; not during stream
+ * capture.  `out` may be NULL. */
 sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out);
-sipg_status sipg_op_set_tile(sipg_op* op, int kind, int rows, int threads_per_element);
-sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* rows, int* threads_per_element);
+sipg_status sipg_op_set_tile(sipg_op* op, int kind, int elements_per_row, int rows, int threads_per_element);
+sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* elements_per_row, int* rows, int* threads_per_element);
 
 /* ---- conjugate gradient ---- */
 

@@ -1,6 +1,6 @@
 """The tile-shape autotuner (sipg_op_autotune / set_tile / get_tile): every
-tile shape -- rows per tile, and one or two threads per element for the pairs
-apply -- gives the same apply result bit for bit (each output is the same
+tile shape -- rows per tile, one or two threads per element for the pairs
+apply, the per-node FP64 tile -- gives the same apply result bit for bit (each output is the same
 operations in the same order whatever the tiling), the tuner keeps a shape
 that launches, and operators created later for the same (degree, dim) start
 with the tuned shape."""
@@ -9,6 +9,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(2, 1), (4, 1), (8, 1), (2, 2), (4, 2)]
+SHAPES3 = [(32, r, t) for r, t in SHAPES]
+
+
+def pernode(p, shape=0):
+    """The per-node FP64 tile of degree p: (elements per row, rows, (p+1)^2)."""
+    return (4 if p <= 2 else 2) * (2 if shape else 1), 4 if p == 1 else 2, (p + 1) ** 2
 
 
 @pytest.fixture(scope="module")
@@ -59,6 +65,69 @@ def test_two_threads_per_element_rejected_where_not_compiled(sipg):
     for kind, rows in (("f64", 4), ("f32", 4), ("pairs", 8)):
         with pytest.raises(sipg.SipgError):
             op.set_tile(kind, rows, 2)
+    for kind, rows in (("f32", 4), ("pairs", 4), ("f64", 2)):
+        with pytest.raises(sipg.SipgError):
+            op.set_tile(kind, rows, 1, elements_per_row=8)
+    # the per-node tile: FP64 only, its two compiled shapes only
+    ex, ey, tpe = pernode(3)
+    for kind in ("f32", "pairs"):
+        with pytest.raises(sipg.SipgError):
+            op.set_tile(kind, ey, tpe, elements_per_row=ex)
+    for bad in ((ex, ey + 2), (3 * ex, ey), (32, 4)):
+        with pytest.raises(sipg.SipgError):
+            op.set_tile("f64", bad[1], tpe, elements_per_row=bad[0])
+    op.close()
+    big = sipg.Operator(sipg.PERNODE_MAX_DIM + 1, 1, 1.0)
+    assert big.get_shape("f64")[0] == 32
+    ex, ey, tpe = pernode(1)
+    with pytest.raises(sipg.SipgError):
+        big.set_tile("f64", ey, tpe, elements_per_row=ex)
+    big.close()
+
+
+# every degree; meshes that fill no tile, fill tiles exactly, and leave ragged
+# tiles in x and y (including a single element: four boundary faces)
+PERNODE_CASES = [(1, 1), (1, 13), (2, 9), (2, 16), (3, 1), (3, 16), (4, 16), (4, 37), (5, 7), (6, 11), (7, 5),
+                 (8, 3), (8, 20)]
+
+
+@pytest.mark.parametrize("p,d", PERNODE_CASES)
+def test_pernode_tile_gives_identical_applies(sipg, torch, p, d):
+    """The per-node FP64 tile computes each output with the operations of the
+    element-per-thread kernel, in the same order: bit-identical applies."""
+    op = sipg.Operator(d, p, float(p * p) + 0.25)
+    assert op.get_shape("f64") == pernode(p, 0)  # the default up to 64 x 64
+    g = torch.Generator(device="cuda").manual_seed(100 + p)
+    x = torch.rand(op.ndof, device="cuda", dtype=torch.float64, generator=g) * 2 - 1
+    y0 = op.apply(x)
+    op.set_pernode(1)
+    assert op.get_shape("f64") == pernode(p, 1)
+    y1 = op.apply(x)
+    op.set_tile("f64", 4)
+    assert op.get_shape("f64") == (32, 4, 1)
+    y = op.apply(x)
+    assert torch.equal(y0, y) and torch.equal(y1, y)
+    op.close()
+
+
+@pytest.mark.parametrize("p,d", [(4, 16), (2, 23), (7, 9)])
+def test_pernode_cg_matches_element_tile_cg(sipg, torch, p, d):
+    """CG with the per-node tile (direction fused into the apply: two kernels
+    an iteration) against CG with the element tile (three kernels): the same
+    iterates up to the grouping of the dot-product sums."""
+    op = sipg.Operator(d, p, float(p * p))
+    b = op.rhs("sinsin")
+    xs, its = [], []
+    for shape in ("pernode", "element"):
+        if shape == "element":
+            op.set_tile("f64", 4)
+        x = torch.zeros_like(b)
+        st, res = op.cg(x, b, 1e-12, relative=True)
+        assert st == 0 and res.converged == 1
+        xs.append(x)
+        its.append(res.iterations)
+    assert abs(its[0] - its[1]) <= 1
+    assert (xs[0] - xs[1]).abs().max().item() <= 1e-9 * xs[1].abs().max().item()
     op.close()
 
 
@@ -66,14 +135,16 @@ def test_autotune_picks_a_launchable_shape_and_is_remembered(sipg, torch):
     p, d = 6, 96
     op = sipg.Operator(d, p, 36.0)
     choice = op.autotune()
-    for kind, (rows, tpe, ms) in choice.items():
-        assert (rows, tpe) in SHAPES and ms > 0, (kind, rows, tpe, ms)
-        assert tpe == 1 or kind == "pairs"
-        assert op.get_tile(kind) == (rows, tpe)
+    for kind, (tx, rows, tpe, ms) in choice.items():
+        allowed = SHAPES3 + ([pernode(p, 0), pernode(p, 1)] if kind == "f64" else [])
+        assert (tx, rows, tpe) in allowed and ms > 0, (kind, tx, rows, tpe, ms)
+        assert tpe == 1 or kind == "pairs" or (kind == "f64" and tpe == (p + 1) ** 2)
+        assert tx == 32 or kind == "f64"
+        assert op.get_shape(kind) == (tx, rows, tpe)
     # a later operator of the same degree and size starts from the tuned shapes
     op2 = sipg.Operator(d, p, 36.0)
-    for kind, (rows, tpe, _) in choice.items():
-        assert op2.get_tile(kind) == (rows, tpe)
+    for kind, (tx, rows, tpe, _) in choice.items():
+        assert op2.get_shape(kind) == (tx, rows, tpe)
     # and a CG solve after re-tuning re-captures its graphs and still converges
     b = op.rhs("sinsin")
     x = torch.zeros_like(b)
