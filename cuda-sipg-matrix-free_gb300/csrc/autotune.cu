@@ -38,7 +38,7 @@ std::map<std::tuple<int, int, int>, TileCfg> g_tuned;  // (p, dim, kind) -> shap
 // (elements per row, rows, threads per element): two threads per element only
 // for the compensated apply (the one limited by latency rather than a pipe);
 // the FP64 apply also tries the two per-node tiles (threads per element
-// (p+1)^2) on meshes up to kPernodeMaxDim
+// (p+1)^2)
 constexpr int kCandidates[5][3] = {{32, 2, 1}, {32, 4, 1}, {32, 8, 1}, {32, 2, 2}, {32, 4, 2}};
 
 template <typename T>
@@ -96,7 +96,7 @@ TileCfg tune_one(const sipg_op* op, int prec, const void* in, void* out, cudaStr
     t.tpe = c[2];
     cands.push_back(t);
   }
-  if (prec == SIPG_TUNE_F64 && op->dim <= kPernodeMaxDim) {
+  if (prec == SIPG_TUNE_F64) {
     cands.push_back(pernode_tile(op->p, 0));
     cands.push_back(pernode_tile(op->p, 1));
   }
@@ -193,8 +193,7 @@ sipg_status sipg_op_set_tile(sipg_op* op, int kind, int elements_per_row, int ro
   const bool pernode = kind == SIPG_TUNE_F64 && threads_per_element == (p + 1) * (p + 1);
   bool ok;
   if (pernode) {
-    ok = op->dim <= kPernodeMaxDim && rows == pernode_ey(p) &&
-         (elements_per_row == pernode_ex(p, 0) || elements_per_row == pernode_ex(p, 1));
+    ok = rows == pernode_ey(p) && (elements_per_row == pernode_ex(p, 0) || elements_per_row == pernode_ex(p, 1));
   } else {
     const bool tpe_ok =
         threads_per_element == 1 || (threads_per_element == 2 && kind == SIPG_TUNE_PAIRS && rows != 8);
@@ -202,7 +201,7 @@ sipg_status sipg_op_set_tile(sipg_op* op, int kind, int elements_per_row, int ro
   }
   if (!ok) {
     set_error("sipg_op_set_tile: a tile is 32 elements per row by 2, 4 or 8 rows with 1 thread per element (2 for "
-              "the pairs apply with 2 or 4 rows), or, for FP64 on meshes up to 1024 x 1024, the per-node tile: "
+              "the pairs apply with 2 or 4 rows), or, for FP64, the per-node tile: "
               "(p+1)^2 threads per element, " +
               std::to_string(pernode_ex(p, 0)) + " or " + std::to_string(pernode_ex(p, 1)) + " elements per row, " +
               std::to_string(pernode_ey(p)) + " rows");

@@ -125,7 +125,7 @@ template <typename T>
 __device__ __forceinline__ void face_combine(T w, T nu, bool interior, T u0, T d0, T uN, T dN, T& J, T& Q) {
   const T kap = interior ? T(0.5) : T(1);
   const T jmp = u0 - uN;
-  J = mul_rn(mul_rn(kap, w), jmp);
+  J = mul_rn(kap * w, jmp);  // kap * w is exact
   Q = mul_rn(w, fma(kap, add_rn(d0, dN), mul_rn(nu, jmp)));
 }
 
@@ -367,6 +367,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   // ---- phase 2: outputs ---------------------------------------------------
   // Row form: w_j sum_i K(i1,i) u(i,j) + D[i1][0] J_L,j + D[i1][P] J_R,j.
   // Column form: w_i1 sum_i K(i2,i) u(i1,i) + D[i2][0] J_D,i1 + D[i2][P] J_U,i1.
+  // (The column form reads w_b K(a,i) from KW and accumulates every term
+  // into one chain per output.)
   // Then the face nodes get +Q (0-side) / -Q (N-side).  kCols computes one
   // output column at a time (n live accumulators; the row contractions read
   // smem n times) -- the register-light form; otherwise all n^2 outputs stay in
@@ -383,24 +385,24 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll(ApplyColumnForm<T, P>::col_unroll)
       for (int i1 = 0; i1 < N1; ++i1) {
         T o[N1], c[N1];
+        // each output starts from its x-face lifting, then takes the
+        // weighted volume sums (w folded into KW) and the y-face lifting:
+        // 2n + 4 FP64 operations
 #pragma unroll
-        for (int j = 0; j < N1; ++j) o[j] = T(0);
+        for (int j = 0; j < N1; ++j) o[j] = fma(tb.D0[i1], eJ[j], tb.DN[i1] * fJ[j]);
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
-          const T k = tb.K[i1 * N1 + i];
 #pragma unroll
-          for (int j = 0; j < N1; ++j) o[j] = fma(k, Uv(i, j), o[j]);
+          for (int j = 0; j < N1; ++j) o[j] = fma(tb.KW[(i1 * N1 + i) * N1 + j], Uv(i, j), o[j]);
         }
 #pragma unroll
         for (int i = 0; i < N1; ++i) c[i] = U(i1, i);
         const T gj = YFr(ty + 1, 0, i1, tx), hj = YFr(ty, 0, i1, tx);
 #pragma unroll
         for (int j = 0; j < N1; ++j) {
-          T s = T(0);
+          T v = o[j];
 #pragma unroll
-          for (int i = 0; i < N1; ++i) s = fma(tb.K[j * N1 + i], c[i], s);
-          T v = fma(tb.w[j], o[j], fma(tb.D0[i1], eJ[j], tb.DN[i1] * fJ[j]));
-          v = fma(tb.w[i1], s, v);
+          for (int i = 0; i < N1; ++i) v = fma(tb.KW[(j * N1 + i) * N1 + i1], c[i], v);
           v = fma(tb.D0[j], gj, v);
           o[j] = fma(tb.DN[j], hj, v);
         }

@@ -11,15 +11,19 @@
 // the same operations spread over (p+1)^2 times more warps, on more SMs.
 //
 // Each output is formed by exactly the operations, in exactly the order, of
-// the element-per-thread kernel's column form (the FP64 form): the volume
-// sums w_j sum_i K(i1,i) u(i,j) and w_i1 sum_i K(j,i) u(i1,i) accumulated from
-// i = 0, the lifting of the four faces' J, then the face nodes' +-Q.  Face
+// the element-per-thread kernel's column form (the FP64 form): one chain
+// from the x-face lifting through the weighted volume sums sum_i w_j K(i1,i)
+// u(i,j) and sum_i w_i1 K(j,i) u(i1,i) to the y-face lifting, then the face
+// nodes' +-Q.  Face
 // values (J, Q) come from the same one-sided traces and derivatives combined
 // by the same expression.  So the result is bit-identical to every other
 // FP64 tile shape; only the CG reductions (p.Ap, r.r) group their partial
 // sums differently.
 //
-// Phases of a CTA (static shared memory, a few KB):
+// A CTA works through tiles blockIdx.x, blockIdx.x + gridDim.x, ... with the
+// grid at most the resident CTAs, so a mesh of any size has at most a few
+// thousand reduction partials.  Phases per tile (static shared memory, a few
+// KB):
 //   0  the tables, and the nodal blocks of the EX x EY elements and of the
 //      2 (EX + EY) halo elements around them (from L2: small meshes live
 //      there), with p = r + beta p_old formed on the fly in the CG mode;
@@ -30,6 +34,9 @@
 //      in the CG mode, deterministic grid reduction in the CG / DOT /
 //      residual modes).
 #pragma once
+
+#include <algorithm>
+#include <atomic>
 
 #include "sipg_apply.cuh"
 
@@ -53,7 +60,7 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   constexpr int SX = S::SX, SY = S::SY, NX = S::NX, NY = S::NY, NSLOT = SX * SY;
   __shared__ T us[NSLOT * NN];  // slot (sy, sx) = element (y0 - 1 + sy, x0 - 1 + sx), values [i1 * N1 + i2]
   __shared__ T xj[NX], xq[NX], yj[NY], yq[NY];
-  __shared__ T tw[N1], td0[N1], tdn[N1], tk[NN];
+  __shared__ T tw[N1], td0[N1], tdn[N1], tkw[NN * N1];
   __shared__ T red_sh[32];
 
   constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);
@@ -62,8 +69,8 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   }
   const int t = threadIdx.x;
   const int dim = a.dim;
-  const int x0 = blockIdx.x * EX, y0 = blockIdx.y * EY;
   const size_t noe = (size_t)dim * dim;
+  const int tiles_x = (dim + EX - 1) / EX, ntiles = tiles_x * ((dim + EY - 1) / EY);
 
   bool first = true;
   T beta = T(0);
@@ -76,157 +83,196 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   const T* __restrict__ pold = par ? a.pbuf1 : a.pbuf0;
   T* __restrict__ pnew = par ? a.pbuf0 : a.pbuf1;
 
-  // ---- phase 0: tables and nodal blocks ------------------------------------
-  // (the tables per thread index: a constant-bank read whose address differs
-  // across the warp would serialise)
-  if (t < NN) tk[t] = tb.K[t];
+  // the tables, indexed per thread below (a constant-bank read whose address
+  // differs across the warp would serialise)
+  for (int k = t; k < NN * N1; k += NT) tkw[k] = tb.KW[k];
   if (t < N1) {
     tw[t] = tb.w[t];
     td0[t] = tb.D0[t];
     tdn[t] = tb.DN[t];
   }
-  for (int idx = t; idx < NSLOT * NN; idx += NT) {
-    const int k = idx / NSLOT, sl = idx - k * NSLOT;
-    const int sy = sl / SX, sx = sl - sy * SX;
-    const int gx = x0 - 1 + sx, gy = y0 - 1 + sy;
-    const bool corner = (sx == 0 || sx == SX - 1) && (sy == 0 || sy == SY - 1);
-    T v = T(0);
-    if (!corner && gx >= 0 && gx < dim && gy >= 0 && gy < dim) {
-      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
-      v = __ldg(a.in + gk);
-      if (MODE == APPLY_CG && !first) v = fma(beta, __ldg(pold + gk), v);
-    }
-    us[sl * NN + k] = v;
-  }
-  __syncthreads();
-
   const T nu = a.nu;
-  // ---- phase 1: J and Q of every face node of the tile -----------------------
-  for (int f = t; f < NX + NY; f += NT) {
-    T u0 = T(0), d0 = T(0), uN = T(0), dN = T(0);
-    bool zv, nv;  // 0-side / N-side element inside the mesh
-    int j;
-    if (f < NX) {
-      // x face fx of tile row ey: the left element (slot fx) is its N-side
-      // (i1 = P), the right element (slot fx + 1) its 0-side (i1 = 0)
-      j = f % N1;
-      const int r = f / N1, fx = r % (EX + 1), ey = r / (EX + 1);
-      const int gy = y0 + ey, gxl = x0 + fx - 1;
-      nv = gy < dim && gxl >= 0 && gxl < dim;
-      zv = gy < dim && gxl + 1 < dim;
-      const T* L = us + ((ey + 1) * SX + fx) * NN;
-      const T* R = L + NN;
-      if (zv) {
-        u0 = R[j];
-#pragma unroll
-        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], R[i * N1 + j], d0);
-      }
-      if (nv) {
-        uN = L[N * N1 + j];
-#pragma unroll
-        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], L[i * N1 + j], dN);
-      }
-    } else {
-      // y face fy of tile column ex: the upper element (slot row fy) is its
-      // 0-side (i2 = 0), the lower element (slot row fy + 1) its N-side (i2 = P)
-      const int g = f - NX;
-      j = g % N1;
-      const int r = g / N1, ex = r % EX, fy = r / EX;
-      const int gx = x0 + ex, gyu = y0 + fy - 1;
-      zv = gx < dim && gyu >= 0 && gyu < dim;
-      nv = gx < dim && gyu + 1 < dim;
-      const T* Up = us + (fy * SX + ex + 1) * NN;
-      const T* Dn = Up + SX * NN;
-      if (zv) {
-        u0 = Up[j * N1];
-#pragma unroll
-        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], Up[j * N1 + i], d0);
-      }
-      if (nv) {
-        uN = Dn[j * N1 + N];
-#pragma unroll
-        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], Dn[j * N1 + i], dN);
-      }
-    }
-    T J, Q;
-    face_combine<T>(tw[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
-    if (f < NX) {
-      xj[f] = J;
-      xq[f] = Q;
-    } else {
-      yj[f - NX] = J;
-      yq[f - NX] = Q;
-    }
-  }
-  __syncthreads();
-
-  // ---- phase 2: one output node per thread ------------------------------------
   T acc = T(0);
-  if (t < NE * NN) {
-    const int le = t % NE, k = t / NE;  // element fastest: neighbouring threads store neighbouring elements
-    const int ex = le % EX, ey = le / EX;
-    const int i1 = k / N1, j = k - i1 * N1;
-    const int gx = x0 + ex, gy = y0 + ey;
-    if (gx < dim && gy < dim) {
-      const T* E = us + ((ey + 1) * SX + ex + 1) * NN;
-      const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
-      const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
-      const int fu = fd - EX * N1;
-      T o = T(0), s = T(0);
+
+  // the CTA's tiles: blockIdx.x, + gridDim.x, ... (the grid is at most the
+  // resident CTAs, so the reduction has few partials on any mesh)
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int x0 = (tile % tiles_x) * EX, y0 = (tile / tiles_x) * EY;
+
+    // ---- phase 0: nodal blocks ------------------------------------------------
+    for (int idx = t; idx < NSLOT * NN; idx += NT) {
+      const int k = idx / NSLOT, sl = idx - k * NSLOT;
+      const int sy = sl / SX, sx = sl - sy * SX;
+      const int gx = x0 - 1 + sx, gy = y0 - 1 + sy;
+      const bool corner = (sx == 0 || sx == SX - 1) && (sy == 0 || sy == SY - 1);
+      T v = T(0);
+      if (!corner && gx >= 0 && gx < dim && gy >= 0 && gy < dim) {
+        const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+        v = __ldg(a.in + gk);
+        if (MODE == APPLY_CG && !first) v = fma(beta, __ldg(pold + gk), v);
+      }
+      us[sl * NN + k] = v;
+    }
+    __syncthreads();
+
+    // ---- phase 1: J and Q of every face node of the tile -----------------------
+    for (int f = t; f < NX + NY; f += NT) {
+      T u0 = T(0), d0 = T(0), uN = T(0), dN = T(0);
+      bool zv, nv;  // 0-side / N-side element inside the mesh
+      int j;
+      if (f < NX) {
+        // x face fx of tile row ey: the left element (slot fx) is its N-side
+        // (i1 = P), the right element (slot fx + 1) its 0-side (i1 = 0)
+        j = f % N1;
+        const int r = f / N1, fx = r % (EX + 1), ey = r / (EX + 1);
+        const int gy = y0 + ey, gxl = x0 + fx - 1;
+        nv = gy < dim && gxl >= 0 && gxl < dim;
+        zv = gy < dim && gxl + 1 < dim;
+        const T* L = us + ((ey + 1) * SX + fx) * NN;
+        const T* R = L + NN;
+        if (zv) {
+          u0 = R[j];
 #pragma unroll
-      for (int i = 0; i < N1; ++i) o = fma(tk[i1 * N1 + i], E[i * N1 + j], o);
+          for (int i = 0; i < N1; ++i) d0 = fma(td0[i], R[i * N1 + j], d0);
+        }
+        if (nv) {
+          uN = L[N * N1 + j];
 #pragma unroll
-      for (int i = 0; i < N1; ++i) s = fma(tk[j * N1 + i], E[i1 * N1 + i], s);
-      T v = fma(tw[j], o, fma(td0[i1], xj[fl + j], tdn[i1] * xj[fl + N1 + j]));
-      v = fma(tw[i1], s, v);
-      v = fma(td0[j], yj[fd + i1], v);
-      v = fma(tdn[j], yj[fu + i1], v);
-      if (i1 == 0) v += xq[fl + j];
-      if (i1 == N) v -= xq[fl + N1 + j];
-      if (j == 0) v += yq[fd + i1];
-      if (j == N) v -= yq[fu + i1];
-      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
-      if (MODE == APPLY_RESID) {
-        const T rv = __ldg(a.b + gk) - v;
-        a.out[gk] = rv;
-        acc = fma(rv, rv, acc);
+          for (int i = 0; i < N1; ++i) dN = fma(tdn[i], L[i * N1 + j], dN);
+        }
       } else {
-        a.out[gk] = v;
-        const T c = E[k];
-        if (MODE == APPLY_CG) pnew[gk] = c;
-        if (kDot) acc = fma(c, v, acc);
+        // y face fy of tile column ex: the upper element (slot row fy) is its
+        // 0-side (i2 = 0), the lower element (slot row fy + 1) its N-side (i2 = P)
+        const int g = f - NX;
+        j = g % N1;
+        const int r = g / N1, ex = r % EX, fy = r / EX;
+        const int gx = x0 + ex, gyu = y0 + fy - 1;
+        zv = gx < dim && gyu >= 0 && gyu < dim;
+        nv = gx < dim && gyu + 1 < dim;
+        const T* Up = us + (fy * SX + ex + 1) * NN;
+        const T* Dn = Up + SX * NN;
+        if (zv) {
+          u0 = Up[j * N1];
+#pragma unroll
+          for (int i = 0; i < N1; ++i) d0 = fma(td0[i], Up[j * N1 + i], d0);
+        }
+        if (nv) {
+          uN = Dn[j * N1 + N];
+#pragma unroll
+          for (int i = 0; i < N1; ++i) dN = fma(tdn[i], Dn[j * N1 + i], dN);
+        }
+      }
+      T J, Q;
+      face_combine<T>(tw[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
+      if (f < NX) {
+        xj[f] = J;
+        xq[f] = Q;
+      } else {
+        yj[f - NX] = J;
+        yq[f - NX] = Q;
       }
     }
-  }
+    __syncthreads();
+
+    // ---- phase 2: one output node per thread ------------------------------------
+    if (t < NE * NN) {
+      const int le = t % NE, k = t / NE;  // element fastest: neighbouring threads store neighbouring elements
+      const int ex = le % EX, ey = le / EX;
+      const int i1 = k / N1, j = k - i1 * N1;
+      const int gx = x0 + ex, gy = y0 + ey;
+      if (gx < dim && gy < dim) {
+        const T* E = us + ((ey + 1) * SX + ex + 1) * NN;
+        const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
+        const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
+        const int fu = fd - EX * N1;
+        T v = fma(td0[i1], xj[fl + j], tdn[i1] * xj[fl + N1 + j]);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) v = fma(tkw[(i1 * N1 + i) * N1 + j], E[i * N1 + j], v);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) v = fma(tkw[(j * N1 + i) * N1 + i1], E[i1 * N1 + i], v);
+        v = fma(td0[j], yj[fd + i1], v);
+        v = fma(tdn[j], yj[fu + i1], v);
+        if (i1 == 0) v += xq[fl + j];
+        if (i1 == N) v -= xq[fl + N1 + j];
+        if (j == 0) v += yq[fd + i1];
+        if (j == N) v -= yq[fu + i1];
+        const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+        if (MODE == APPLY_RESID) {
+          const T rv = __ldg(a.b + gk) - v;
+          a.out[gk] = rv;
+          acc = fma(rv, rv, acc);
+        } else {
+          a.out[gk] = v;
+          const T c = E[k];
+          if (MODE == APPLY_CG) pnew[gk] = c;
+          if (kDot) acc = fma(c, v, acc);
+        }
+      }
+    }
+    __syncthreads();  // the next tile overwrites the shared memory
+  }  // tiles
 
   if (MODE != APPLY_PLAIN) {
     const T bt = block_sum<T, NT>(acc, red_sh);
     T total;
-    if (grid_sum_last<T, NT>(bt, a.red, (int)(gridDim.x * gridDim.y), red_sh, &total) && t == 0)
+    if (grid_sum_last<T, NT>(bt, a.red, (int)blockIdx.x, (int)gridDim.x, red_sh, &total) && t == 0)
       apply_finish<T, MODE>(a.st, total, par);
   }
+}
+
+// Resident CTAs of a per-node kernel on the current device (occupancy x SMs),
+// computed once per kernel.
+template <typename K>
+int pernode_resident_blocks(K kernel, int threads) {
+  static std::atomic<int> cached{0};
+  int v = cached.load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return 152;  // one CTA per SM of a GB300
+  }
+  v = sms * per_sm;
+  cached.store(v, std::memory_order_relaxed);
+  return v;
 }
 
 template <typename T, int P, int SHAPE>
 cudaError_t launch_apply_pernode_shape(int mode, const ApplyArgs<T>& a, const Tab<T, P>& tb, cudaStream_t s) {
   using S = PernodeShape<P, SHAPE>;
   if (mode == APPLY_PREPARE) return cudaSuccess;  // static shared memory: no attribute to set
-  const dim3 grid((a.dim + S::EX - 1) / S::EX, (a.dim + S::EY - 1) / S::EY), block(S::NT);
-  // every block of a reducing mode stores one partial
-  if (mode != APPLY_PLAIN && (long long)grid.x * grid.y > (long long)a.red.capacity) return cudaErrorInvalidValue;
+  const long long ntiles = (long long)((a.dim + S::EX - 1) / S::EX) * ((a.dim + S::EY - 1) / S::EY);
+  // at most the resident CTAs, and in a reducing mode at most one partial per
+  // scratch entry
+  auto grid_for = [&](auto kernel, bool reduces) {
+    long long g = std::min<long long>(ntiles, pernode_resident_blocks(kernel, S::NT));
+    if (reduces) g = std::min<long long>(g, a.red.capacity);
+    return (int)std::max<long long>(g, 1);
+  };
+  const dim3 block(S::NT);
   switch (mode) {
-    case APPLY_PLAIN:
-      k_sipg_apply_pernode<T, P, SHAPE, APPLY_PLAIN><<<grid, block, 0, s>>>(a, tb);
+    case APPLY_PLAIN: {
+      auto k = k_sipg_apply_pernode<T, P, SHAPE, APPLY_PLAIN>;
+      k<<<grid_for(k, false), block, 0, s>>>(a, tb);
       break;
-    case APPLY_CG:
-      k_sipg_apply_pernode<T, P, SHAPE, APPLY_CG><<<grid, block, 0, s>>>(a, tb);
+    }
+    case APPLY_CG: {
+      auto k = k_sipg_apply_pernode<T, P, SHAPE, APPLY_CG>;
+      k<<<grid_for(k, true), block, 0, s>>>(a, tb);
       break;
-    case APPLY_RESID:
-      k_sipg_apply_pernode<T, P, SHAPE, APPLY_RESID><<<grid, block, 0, s>>>(a, tb);
+    }
+    case APPLY_RESID: {
+      auto k = k_sipg_apply_pernode<T, P, SHAPE, APPLY_RESID>;
+      k<<<grid_for(k, true), block, 0, s>>>(a, tb);
       break;
-    case APPLY_DOT:
-      k_sipg_apply_pernode<T, P, SHAPE, APPLY_DOT><<<grid, block, 0, s>>>(a, tb);
+    }
+    case APPLY_DOT: {
+      auto k = k_sipg_apply_pernode<T, P, SHAPE, APPLY_DOT>;
+      k<<<grid_for(k, true), block, 0, s>>>(a, tb);
       break;
+    }
     default:
       return cudaErrorInvalidValue;
   }
@@ -235,11 +281,11 @@ cudaError_t launch_apply_pernode_shape(int mode, const ApplyArgs<T>& a, const Ta
 }
 
 // The per-node tile named by cfg (tpe = (p+1)^2; tx x ty one of the two
-// compiled shapes), on meshes up to kPernodeMaxDim elements per edge.
+// compiled shapes).
 template <typename T, int P>
 cudaError_t launch_apply_pernode(const TileCfg& cfg, int mode, const ApplyArgs<T>& a, const HostTables& h,
                                  cudaStream_t s) {
-  if (a.dim > kPernodeMaxDim || cfg.ty != pernode_ey(P)) return cudaErrorInvalidConfiguration;
+  if (cfg.ty != pernode_ey(P)) return cudaErrorInvalidConfiguration;
   const Tab<T, P> tb = make_tab<T, P>(h);
   if (cfg.tx == pernode_ex(P, 0)) return launch_apply_pernode_shape<T, P, 0>(mode, a, tb, s);
   if (cfg.tx == pernode_ex(P, 1)) return launch_apply_pernode_shape<T, P, 1>(mode, a, tb, s);

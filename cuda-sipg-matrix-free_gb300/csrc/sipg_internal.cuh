@@ -32,6 +32,7 @@ struct Tab {
   T D0[N1];
   T DN[N1];
   T K[N1 * N1];
+  T KW[N1 * N1 * N1];  // KW[(a * N1 + i) * N1 + b] = w_b K[a][i]: the weighted stiffness of the column form
 };
 
 // Host-side double tables for one degree (filled by tables.cpp).
@@ -57,6 +58,9 @@ inline Tab<T, P> make_tab(const HostTables& h) {
     t.DN[i] = (T)h.D[i * n + P];
   }
   for (int i = 0; i < n * n; ++i) t.K[i] = (T)h.K[i];
+  for (int a = 0; a < n; ++a)
+    for (int i = 0; i < n; ++i)
+      for (int b = 0; b < n; ++b) t.KW[(a * n + i) * n + b] = (T)(h.w[b] * h.K[a * n + i]);
   return t;
 }
 
@@ -136,12 +140,14 @@ struct TileCfg {
 };
 
 // The per-node FP64 tile (one thread per output node): tx x ty elements per
-// CTA, shape 0 the smallest, shape 1 twice as wide; meshes up to
-// kPernodeMaxDim elements per edge (its reduction partials grow as dim^2 / 4).
+// CTA, shape 0 the smallest, shape 1 twice as wide.
 __host__ __device__ constexpr int pernode_ey(int p) { return p == 1 ? 4 : 2; }
 __host__ __device__ constexpr int pernode_ex(int p, int shape) { return (p <= 2 ? 4 : 2) * (shape ? 2 : 1); }
-constexpr int kPernodeMaxDim = 1024;
-constexpr int kPernodeDefaultDim = 64;  // FP64 operators up to this size start with it
+// FP64 operators up to kPernodeDefaultDim elements per edge start with the
+// per-node tile (measured faster than 32-element rows up to there), shape 1
+// above kPernodeWideDim
+constexpr int kPernodeDefaultDim = 128;
+constexpr int kPernodeWideDim = 32;
 inline bool is_pernode(const TileCfg& c, int p) { return c.tpe == (p + 1) * (p + 1); }
 inline TileCfg pernode_tile(int p, int shape) {
   TileCfg c;
@@ -184,14 +190,13 @@ inline TileCfg batched_tile(TileCfg c) {
 inline int apply_grid_blocks(int dim, const TileCfg& c) {
   return ((dim + c.tx - 1) / c.tx) * ((dim + c.ty - 1) / c.ty);
 }
-// Reduction-scratch entries that cover every apply tile shape (the tiles
-// with the fewest elements are 32 x 2 and, up to kPernodeMaxDim, the 2 x 2
-// per-node tile) and every vector kernel grid (at most 152 * 8).
+// Reduction-scratch entries that cover every element-per-thread tile shape
+// (the one with the fewest elements is 32 x 2), every vector kernel grid (at
+// most 152 * 8) and 16 resident per-node CTAs per SM (the per-node apply caps
+// its grid at the scratch).
 inline int reduce_capacity(int dim) {
   const int a = ((dim + 31) / 32) * ((dim + 1) / 2);
-  const int b = dim <= kPernodeMaxDim ? ((dim + 1) / 2) * ((dim + 1) / 2) : 0;
-  const int m = a > b ? a : b;
-  return m > 152 * 8 ? m : 152 * 8;
+  return a > 152 * 16 ? a : 152 * 16;
 }
 
 

@@ -237,8 +237,8 @@ def pernode_tile(p, shape=0):
     return (4 if p <= 2 else 2) * (2 if shape else 1), 4 if p == 1 else 2, (p + 1) ** 2
 
 
-PERNODE_MAX_DIM = 1024  # the per-node tile serves meshes up to this many elements per edge
-PERNODE_DEFAULT_DIM = 64  # FP64 operators up to this size start with it
+PERNODE_DEFAULT_DIM = 128  # FP64 operators up to this size start with the per-node tile,
+PERNODE_WIDE_DIM = 32  # shape 1 above this size
 
 
 class Operator:
@@ -272,7 +272,7 @@ class Operator:
 
     def set_pernode(self, shape=0):
         """Switches the FP64 apply to the per-node tile (one thread per output
-        node; shape 0 or 1, see pernode_tile), the small-mesh choice."""
+        node; shape 0 or 1, see pernode_tile)."""
         ex, ey, tpe = pernode_tile(self.degree, shape)
         self.set_tile("f64", ey, tpe, ex)
 

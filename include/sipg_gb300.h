@@ -146,24 +146,27 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
 /* ---- tile shapes and the autotuner (no reference counterpart: the
  * reference launches one fixed geometry) ----
  * An apply tile is 32 elements along a mesh row by `rows` rows (2, 4 or 8),
- * with one thread per element (or two, pairs apply only); the FP64 apply also
- * has a one-warp 8 x 4 tile, its default for meshes up to 96 x 96, whose extra
- * CTAs put more SMs' FP64 pipes on a small mesh.  Every shape gives
- * bit-identical apply results; CG reductions regroup.  Tile indices for the
- * three apply kinds: */
+ * with one thread per element (or two, pairs apply only).  The FP64 apply also
+ * has the per-node tile: (p+1)^2 threads per element, one per output node,
+ * over ex x ey elements per CTA -- ey = 4 at p = 1, else 2; ex = 4 (p <= 2) or
+ * 2 (p >= 3), or twice that -- its default for meshes up to 128 x 128, where
+ * 32-element rows leave most of GB300's thin FP64 pipes idle.  Every shape
+ * gives bit-identical apply results; CG reductions regroup.  Tile indices for
+ * the three apply kinds: */
 enum { SIPG_TUNE_F64 = 0, SIPG_TUNE_F32 = 1, SIPG_TUNE_PAIRS = 2 /* compensated, pair vectors */ };
 typedef struct {
-  int elements_per_row[3];     /* 32, or 8 (FP64), by SIPG_TUNE_* */
+  int elements_per_row[3];     /* 32, or ex of the per-node tile (FP64), by SIPG_TUNE_* */
   int rows[3];                 /* rows per tile */
-  int threads_per_element[3];  /* 1, or 2 for the pairs apply */
+  int threads_per_element[3];  /* 1, 2 (pairs apply) or (p+1)^2 (per-node FP64 tile) */
   float ms_per_apply[3];       /* the winning candidate's time */
 } sipg_tile_choice;
 /* Times the tile shapes for each apply kind on this op -- 32 x {2, 4, 8} with
  * one thread per element, for the pairs apply also 32 x {2, 4} with two, for
- * FP64 also 8 x 4 -- on scratch vectors of ndof doubles (allocated and freed
- * here), keeps the fastest, and records it for (degree, dim) so ops created
- * later in this process start with it.  Synchronous; not during stream
- * capture.  `out` may be NULL. */
+ * FP64 also both per-node tiles -- on scratch vectors of ndof doubles
+ * (allocated and freed here), keeps the fastest, and records it for (degree,
+ * dim) so ops created later in this process start with it.  Synchronous; not
+ * during stream capture.  `out` may be NULL.  sipg_op_set_tile returns
+ * SIPG_ERR_INVALID for a shape that is not compiled. */
 sipg_status sipg_op_autotune(sipg_op* op, void* stream, sipg_tile_choice* out);
 sipg_status sipg_op_set_tile(sipg_op* op, int kind, int elements_per_row, int rows, int threads_per_element);
 sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* elements_per_row, int* rows, int* threads_per_element);

@@ -77,18 +77,14 @@ def test_two_threads_per_element_rejected_where_not_compiled(sipg):
         with pytest.raises(sipg.SipgError):
             op.set_tile("f64", bad[1], tpe, elements_per_row=bad[0])
     op.close()
-    big = sipg.Operator(sipg.PERNODE_MAX_DIM + 1, 1, 1.0)
-    assert big.get_shape("f64")[0] == 32
-    ex, ey, tpe = pernode(1)
-    with pytest.raises(sipg.SipgError):
-        big.set_tile("f64", ey, tpe, elements_per_row=ex)
-    big.close()
 
 
 # every degree; meshes that fill no tile, fill tiles exactly, and leave ragged
-# tiles in x and y (including a single element: four boundary faces)
+# tiles in x and y (including a single element: four boundary faces); and
+# meshes with more tiles than resident CTAs, where each CTA works through
+# several tiles
 PERNODE_CASES = [(1, 1), (1, 13), (2, 9), (2, 16), (3, 1), (3, 16), (4, 16), (4, 37), (5, 7), (6, 11), (7, 5),
-                 (8, 3), (8, 20)]
+                 (8, 3), (8, 20), (1, 1025), (4, 301), (8, 150)]
 
 
 @pytest.mark.parametrize("p,d", PERNODE_CASES)
@@ -96,7 +92,11 @@ def test_pernode_tile_gives_identical_applies(sipg, torch, p, d):
     """The per-node FP64 tile computes each output with the operations of the
     element-per-thread kernel, in the same order: bit-identical applies."""
     op = sipg.Operator(d, p, float(p * p) + 0.25)
-    assert op.get_shape("f64") == pernode(p, 0)  # the default up to 64 x 64
+    if d <= sipg.PERNODE_DEFAULT_DIM:
+        assert op.get_shape("f64") == pernode(p, 0 if d <= sipg.PERNODE_WIDE_DIM else 1)
+    else:
+        assert op.get_shape("f64") == (32, 8 if p <= 3 else (4 if p <= 7 else 2), 1)
+    op.set_pernode(0)
     g = torch.Generator(device="cuda").manual_seed(100 + p)
     x = torch.rand(op.ndof, device="cuda", dtype=torch.float64, generator=g) * 2 - 1
     y0 = op.apply(x)
@@ -110,7 +110,7 @@ def test_pernode_tile_gives_identical_applies(sipg, torch, p, d):
     op.close()
 
 
-@pytest.mark.parametrize("p,d", [(4, 16), (2, 23), (7, 9)])
+@pytest.mark.parametrize("p,d", [(4, 16), (2, 23), (7, 9), (4, 128)])
 def test_pernode_cg_matches_element_tile_cg(sipg, torch, p, d):
     """CG with the per-node tile (direction fused into the apply: two kernels
     an iteration) against CG with the element tile (three kernels): the same
@@ -121,6 +121,8 @@ def test_pernode_cg_matches_element_tile_cg(sipg, torch, p, d):
     for shape in ("pernode", "element"):
         if shape == "element":
             op.set_tile("f64", 4)
+        else:
+            op.set_pernode(0)
         x = torch.zeros_like(b)
         st, res = op.cg(x, b, 1e-12, relative=True)
         assert st == 0 and res.converged == 1
