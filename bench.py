@@ -35,10 +35,11 @@ PEN = float(DEGREE * DEGREE)
 NDOF = DIM * DIM * (DEGREE + 1) ** 2
 APPLIES_PER_STEP = 100
 BYTES_PER_DOF = 16  # read u once, write y once (FP64)
-# DFMA-pipe instructions per DoF issued by the fused FP64 kernel (column form):
-# one chain per output of 2n + 4 (weighted volume sums and the four liftings),
-# face derivatives 4, face combine and corrections ~ 16/n
-FP64_FLOPS_PER_DOF = 2.0 * (2 * (DEGREE + 1) + 8 + 16.0 / (DEGREE + 1))
+# FP64-pipe operations per DoF issued by the fused FP64 kernel (column form),
+# counted as two flops each: one chain per output of 2n + 4 (face corrections
+# as its seed, weighted volume sums, the four liftings), face derivatives 4,
+# face combines 12/n, corner additions 4/n^2
+FP64_FLOPS_PER_DOF = 2.0 * (2 * (DEGREE + 1) + 8 + 12.0 / (DEGREE + 1) + 4.0 / (DEGREE + 1) ** 2)
 THESIS_K20X_GDOFS = 1.031  # Thesis_TEXT.pdf p.54 T4.15: 1024^2, p=4, volume+flux on a K20X
 METRIC = "GDoF/s per SIPG apply (FP64, 1024x1024 elements, p=4)"
 CONFIG = {

@@ -122,11 +122,27 @@ __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, 
 // jmp and contract that into one FMA -- a last-bit difference from the same
 // face computed with runtime values by another tile shape.
 template <typename T>
-__device__ __forceinline__ void face_combine(T w, T nu, bool interior, T u0, T d0, T uN, T dN, T& J, T& Q) {
+__device__ __forceinline__ void face_combine(T w, T wh, T nu, bool interior, T u0, T d0, T uN, T dN, T& J,
+                                             T& Q) {
   const T kap = interior ? T(0.5) : T(1);
   const T jmp = u0 - uN;
-  J = mul_rn(kap * w, jmp);  // kap * w is exact
+  J = mul_rn(interior ? wh : w, jmp);  // kappa w from the table: wh = w / 2
   Q = mul_rn(w, fma(kap, add_rn(d0, dN), mul_rn(nu, jmp)));
+}
+
+// The face corrections of output (i1, j) as the start of its chain: +Q of
+// the x face it is the 0-side of (i1 = 0), -Q of the one it is the N-side of
+// (i1 = P), then likewise for the y faces (j = 0, j = P); zero elsewhere.
+// qx0 / qxN / qy0 / qyN are those four faces' Q at this node.
+template <typename T, int N>
+__device__ __forceinline__ T face_seed(int i1, int j, T qx0, T qxN, T qy0, T qyN) {
+  T s = T(0);
+  if (i1 == 0) s = qx0;
+  if (i1 == N) s = -qxN;
+  const bool xface = (i1 == 0) || (i1 == N);
+  if (j == 0) s = xface ? s + qy0 : qy0;
+  if (j == N) s = xface ? s - qyN : -qyN;
+  return s;
 }
 
 // The reduced total of a CG / residual apply, in the block that summed it
@@ -207,7 +223,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   auto YFr = [&](int frow, int comp, int j, int col) -> T& { return yf[((frow * 2 + comp) * N1 + j) * TX + col]; };
   const T nu = a.nu;
   auto combine = [&](int j, bool interior, T u0, T d0, T uN, T dN, T& J, T& Q) {
-    face_combine<T>(tb.w[j], nu, interior, u0, d0, uN, dN, J, Q);
+    face_combine<T>(tb.w[j], tb.WH[j], nu, interior, u0, d0, uN, dN, J, Q);
   };
 
   // ---- phase 0: the tile's nodal blocks -> smem --------------------------
@@ -385,11 +401,16 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll(ApplyColumnForm<T, P>::col_unroll)
       for (int i1 = 0; i1 < N1; ++i1) {
         T o[N1], c[N1];
-        // each output starts from its x-face lifting, then takes the
-        // weighted volume sums (w folded into KW) and the y-face lifting:
-        // 2n + 4 FP64 operations
+        // each output starts from its face corrections (+-Q) and x-face
+        // lifting, then takes the weighted volume sums (w folded into KW)
+        // and the y-face lifting: 2n + 4 FP64 operations (+1 at corners)
 #pragma unroll
-        for (int j = 0; j < N1; ++j) o[j] = fma(tb.D0[i1], eJ[j], tb.DN[i1] * fJ[j]);
+        for (int j = 0; j < N1; ++j) {
+          const bool xf = (i1 == 0) || (i1 == N);
+          const T seed = face_seed<T, N>(i1, j, xf ? XFr(ty, 1, j, tx) : T(0), xf ? XFr(ty, 1, j, tx + 1) : T(0),
+                                         (j == 0) ? YFr(ty + 1, 1, i1, tx) : T(0), (j == N) ? YFr(ty, 1, i1, tx) : T(0));
+          o[j] = fma(tb.D0[i1], eJ[j], fma(tb.DN[i1], fJ[j], seed));
+        }
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
 #pragma unroll
@@ -406,16 +427,6 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
           v = fma(tb.D0[j], gj, v);
           o[j] = fma(tb.DN[j], hj, v);
         }
-        if (i1 == 0) {
-#pragma unroll
-          for (int j = 0; j < N1; ++j) o[j] += XFr(ty, 1, j, tx);
-        }
-        if (i1 == N) {
-#pragma unroll
-          for (int j = 0; j < N1; ++j) o[j] -= XFr(ty, 1, j, tx + 1);
-        }
-        o[0] += YFr(ty + 1, 1, i1, tx);
-        o[N] -= YFr(ty, 1, i1, tx);
 #pragma unroll
         for (int j = 0; j < N1; ++j) {
           const int k = i1 * N1 + j;

@@ -12,9 +12,9 @@
 //
 // Each output is formed by exactly the operations, in exactly the order, of
 // the element-per-thread kernel's column form (the FP64 form): one chain
-// from the x-face lifting through the weighted volume sums sum_i w_j K(i1,i)
-// u(i,j) and sum_i w_i1 K(j,i) u(i1,i) to the y-face lifting, then the face
-// nodes' +-Q.  Face
+// from the face nodes' +-Q and the x-face lifting through the weighted volume
+// sums sum_i w_j K(i1,i) u(i,j) and sum_i w_i1 K(j,i) u(i1,i) to the y-face
+// lifting.  Face
 // values (J, Q) come from the same one-sided traces and derivatives combined
 // by the same expression.  So the result is bit-identical to every other
 // FP64 tile shape; only the CG reductions (p.Ap, r.r) group their partial
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   constexpr int SX = S::SX, SY = S::SY, NX = S::NX, NY = S::NY, NSLOT = SX * SY;
   __shared__ T us[NSLOT * NN];  // slot (sy, sx) = element (y0 - 1 + sy, x0 - 1 + sx), values [i1 * N1 + i2]
   __shared__ T xj[NX], xq[NX], yj[NY], yq[NY];
-  __shared__ T tw[N1], td0[N1], tdn[N1], tkw[NN * N1];
+  __shared__ T tw[N1], twh[N1], td0[N1], tdn[N1], tkw[NN * N1];
   __shared__ T red_sh[32];
 
   constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);
@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   for (int k = t; k < NN * N1; k += NT) tkw[k] = tb.KW[k];
   if (t < N1) {
     tw[t] = tb.w[t];
+    twh[t] = tb.WH[t];
     td0[t] = tb.D0[t];
     tdn[t] = tb.DN[t];
   }
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
         }
       }
       T J, Q;
-      face_combine<T>(tw[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
+      face_combine<T>(tw[j], twh[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
       if (f < NX) {
         xj[f] = J;
         xq[f] = Q;
@@ -185,17 +186,16 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
         const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
         const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
         const int fu = fd - EX * N1;
-        T v = fma(td0[i1], xj[fl + j], tdn[i1] * xj[fl + N1 + j]);
+        const bool xf = (i1 == 0) || (i1 == N);
+        const T seed = face_seed<T, N>(i1, j, xf ? xq[fl + j] : T(0), xf ? xq[fl + N1 + j] : T(0),
+                                       (j == 0) ? yq[fd + i1] : T(0), (j == N) ? yq[fu + i1] : T(0));
+        T v = fma(td0[i1], xj[fl + j], fma(tdn[i1], xj[fl + N1 + j], seed));
 #pragma unroll
         for (int i = 0; i < N1; ++i) v = fma(tkw[(i1 * N1 + i) * N1 + j], E[i * N1 + j], v);
 #pragma unroll
         for (int i = 0; i < N1; ++i) v = fma(tkw[(j * N1 + i) * N1 + i1], E[i1 * N1 + i], v);
         v = fma(td0[j], yj[fd + i1], v);
         v = fma(tdn[j], yj[fu + i1], v);
-        if (i1 == 0) v += xq[fl + j];
-        if (i1 == N) v -= xq[fl + N1 + j];
-        if (j == 0) v += yq[fd + i1];
-        if (j == N) v -= yq[fu + i1];
         const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
         if (MODE == APPLY_RESID) {
           const T rv = __ldg(a.b + gk) - v;

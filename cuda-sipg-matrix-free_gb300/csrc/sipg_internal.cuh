@@ -29,6 +29,7 @@ template <typename T, int P>
 struct Tab {
   static constexpr int N1 = P + 1;
   T w[N1];
+  T WH[N1];  // w / 2 (exact): the lifted jump's weight on an interior face
   T D0[N1];
   T DN[N1];
   T K[N1 * N1];
@@ -54,6 +55,7 @@ inline Tab<T, P> make_tab(const HostTables& h) {
   const int n = P + 1;
   for (int i = 0; i < n; ++i) {
     t.w[i] = (T)h.w[i];
+    t.WH[i] = (T)(0.5 * h.w[i]);
     t.D0[i] = (T)h.D[i * n + 0];
     t.DN[i] = (T)h.D[i * n + P];
   }
