@@ -59,6 +59,28 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def copy_bound_ms(torch, h_in, h_out, reps=10):
+    """ms to move one step's input host->device and output device->host at
+    once (two streams, pinned buffers): the floor of an end-to-end step."""
+    d_a = torch.empty(h_in.numel(), dtype=h_in.dtype, device="cuda")
+    d_b = torch.empty(h_out.numel(), dtype=h_out.dtype, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_a.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_b, non_blocking=True)
+
+    both()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        both()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps * 1e3
+
+
 def traffic_per_launch():
     """DRAM bytes per apply launch from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "apply_f64_1024_p4_traffic.json")
@@ -266,6 +288,7 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = world * e2e_steps * NDOF / e2e_s / 1e9
     ok = bool(np.array_equal(h_out.numpy(), y.cpu().numpy()))
+    copy_ms = copy_bound_ms(torch, h_in, h_out)
 
     peak, peak_src = measured_peaks()
     dur = ms * 1e-3 / (args.steps * APPLIES_PER_STEP)
@@ -282,7 +305,9 @@ def run_ours(args):
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": NDOF * 8, "d2h_bytes_per_step": NDOF * 8,
                 "steps": e2e_steps, "api": "sipg_apply_host_f64 (pinned host buffers, one apply per step)",
-                "matches_device_result": ok},
+                "matches_device_result": ok,
+                "copy_bound": {"ms_per_step": copy_ms, "gdofs": NDOF / (copy_ms * 1e-3) / 1e9,
+                               "what": "the step's H2D and D2H run at once on two streams (torch copies), no apply"}},
         "gpu_launches": launches,
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -1,6 +1,8 @@
 // capi.cu -- the C ABI (include/sipg_gb300.h): operator lifetime, the fused
 // apply, the graph-driven conjugate gradient, host-buffer apply, tables.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -494,6 +496,10 @@ sipg_status sipg_op_destroy(sipg_op* op) {
   if (op->pcg_free) op->pcg_free(op->pcg);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
+  for (cudaStream_t h : op->hs)
+    if (h) cudaStreamDestroy(h);
+  for (cudaEvent_t e : op->hev)
+    if (e) cudaEventDestroy(e);
   delete op;
   return SIPG_OK;
 }
@@ -548,22 +554,84 @@ sipg_status sipg_apply_pairs(const sipg_op* op, const float* d_in, float* d_out,
   return SIPG_OK;
 }
 
+// Copies element rows [r0, r1) of every node plane between a host and a
+// device vector (node-major layout: plane k of noe values at k * noe): one
+// strided copy where the plane pitch allows it, else one copy per plane.
+static cudaError_t copy_rows(double* dst, const double* src, const sipg_op* op, int r0, int r1, cudaMemcpyKind kind,
+                             cudaStream_t s) {
+  const size_t pitch = (size_t)op->noe * sizeof(double);
+  const size_t off = (size_t)r0 * op->dim, width = (size_t)(r1 - r0) * op->dim * sizeof(double);
+  const int planes = (op->p + 1) * (op->p + 1);
+  if (pitch <= (size_t)INT32_MAX)
+    return cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch, width, planes, kind, s);
+  for (int k = 0; k < planes; ++k) {
+    const cudaError_t e =
+        cudaMemcpyAsync(dst + (size_t)k * op->noe + off, src + (size_t)k * op->noe + off, width, kind, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// y = A x with host buffers, pipelined over bands of element rows: the
+// copy-in of band b + 1, the apply of band b (two compute streams, so one
+// band's tail overlaps the next band's start) and the copy-out of band b - 1
+// run at once.  Band b's apply waits for its own rows and for the first row
+// of band b + 1 (its halo below; the row above arrived with band b - 1).
+// Synchronous: returns when h_out is written.
 sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream) {
   if (!op || !h_in || !h_out) {
     set_error("sipg_apply_host_f64: null argument");
     return SIPG_ERR_INVALID;
   }
+  SIPG_CUDA_TRY(cudaSetDevice(op->device));
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = (size_t)op->ndof * sizeof(double);
-  {
-    std::lock_guard<std::mutex> lk(op->mu);
-    if (!op->stage_in) SIPG_CUDA_TRY(cudaMalloc(&op->stage_in, bytes));
-    if (!op->stage_out) SIPG_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
+  constexpr int kMaxBands = 16;
+  // bands of a multiple of 8 rows (every tile's rows divide 8), ~64 rows
+  // each: measured at 1024^2, p = 4, 8 bands reach 15.3 GDoF/s end to end,
+  // 16 bands 16.7, 32 bands 11.7 (per-copy overheads)
+  const int nb = std::max(1, std::min(kMaxBands, op->dim / 64));
+  const int band_rows = ((op->dim + nb - 1) / nb + 7) / 8 * 8;
+  std::lock_guard<std::mutex> lk(op->mu);  // the staging buffers and streams are per op
+  if (!op->stage_in) SIPG_CUDA_TRY(cudaMalloc(&op->stage_in, bytes));
+  if (!op->stage_out) SIPG_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
+  if (!op->hs[0]) {
+    for (cudaStream_t& h : op->hs) SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : op->hev) SIPG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
-  SIPG_CUDA_TRY(cudaMemcpyAsync(op->stage_in, h_in, bytes, cudaMemcpyHostToDevice, s));
-  sipg_status st = sipg_apply_f64(op, op->stage_in, op->stage_out, stream);
-  if (st != SIPG_OK) return st;
-  SIPG_CUDA_TRY(cudaMemcpyAsync(h_out, op->stage_out, bytes, cudaMemcpyDeviceToHost, s));
+  cudaStream_t s_in = op->hs[0], s_out = op->hs[1];
+  cudaEvent_t* ev_in = op->hev;              // [kMaxBands]: band b's rows are on the device
+  cudaEvent_t* ev_done = op->hev + kMaxBands;  // [kMaxBands]: band b's outputs are written
+  cudaEvent_t ev_start = op->hev[2 * kMaxBands], ev_end = op->hev[2 * kMaxBands + 1];
+  // everything starts after the work already queued on the caller's stream
+  SIPG_CUDA_TRY(cudaEventRecord(ev_start, s));
+  for (int k = 0; k < 4; ++k) SIPG_CUDA_TRY(cudaStreamWaitEvent(op->hs[k], ev_start, 0));
+  int r0 = 0;
+  for (int b = 0; r0 < op->dim; ++b, r0 += band_rows) {
+    const int r1 = std::min(op->dim, r0 + band_rows);
+    SIPG_CUDA_TRY(copy_rows(op->stage_in, h_in, op, r0, r1, cudaMemcpyHostToDevice, s_in));
+    SIPG_CUDA_TRY(cudaEventRecord(ev_in[b], s_in));
+  }
+  r0 = 0;
+  for (int b = 0; r0 < op->dim; ++b, r0 += band_rows) {
+    const int r1 = std::min(op->dim, r0 + band_rows);
+    cudaStream_t cs = op->hs[2 + (b & 1)];
+    const bool last = r1 >= op->dim;
+    SIPG_CUDA_TRY(cudaStreamWaitEvent(cs, ev_in[last ? b : b + 1], 0));  // rows r0 .. r1 (inclusive)
+    ApplyArgs<double> a{};
+    a.in = op->stage_in;
+    a.out = op->stage_out;
+    a.dim = op->dim;
+    a.nu = op->pen;
+    a.row0 = r0;
+    a.nrows = r1 - r0;
+    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_PLAIN, a, op->tab, cs));
+    SIPG_CUDA_TRY(cudaEventRecord(ev_done[b], cs));
+    SIPG_CUDA_TRY(cudaStreamWaitEvent(s_out, ev_done[b], 0));
+    SIPG_CUDA_TRY(copy_rows(h_out, op->stage_out, op, r0, r1, cudaMemcpyDeviceToHost, s_out));
+  }
+  SIPG_CUDA_TRY(cudaEventRecord(ev_end, s_out));
+  SIPG_CUDA_TRY(cudaStreamWaitEvent(s, ev_end, 0));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
   return SIPG_OK;
 }

@@ -193,7 +193,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
   const int dim = a.dim;
-  const int x0 = bx * TX, y0 = by * TY;
+  const int x0 = bx * TX, y0 = a.row0 + by * TY;
   const int gx = x0 + tx, gy = y0 + ty;
   const bool act = (gx < dim) && (gy < dim);
   const size_t noe = (size_t)dim * dim;
@@ -539,7 +539,8 @@ __global__ void __launch_bounds__(TX* TY)
 template <typename T, int P, int TX, int TY>
 cudaError_t launch_apply_tile(int mode, const ApplyArgs<T>& a, const Tab<T, P>& tb, cudaStream_t s) {
   using S = ApplySmem<T, P, TX, TY>;
-  const dim3 grid((a.dim + TX - 1) / TX, (a.dim + TY - 1) / TY), block(TX, TY);
+  const int rows = a.nrows > 0 ? a.nrows : a.dim;
+  const dim3 grid((a.dim + TX - 1) / TX, (rows + TY - 1) / TY), block(TX, TY);
   const size_t smem = S::bytes;
   // the dynamic shared memory opt-in, for all three modes (outside any capture)
   cudaError_t err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_PLAIN>,

@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   const int t = threadIdx.x;
   const int dim = a.dim;
   const size_t noe = (size_t)dim * dim;
-  const int tiles_x = (dim + EX - 1) / EX, ntiles = tiles_x * ((dim + EY - 1) / EY);
+  const int rows = a.nrows > 0 ? a.nrows : dim;  // a band of element rows from a.row0
+  const int tiles_x = (dim + EX - 1) / EX, ntiles = tiles_x * ((rows + EY - 1) / EY);
 
   bool first = true;
   T beta = T(0);
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   // the CTA's tiles: blockIdx.x, + gridDim.x, ... (the grid is at most the
   // resident CTAs, so the reduction has few partials on any mesh)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int x0 = (tile % tiles_x) * EX, y0 = (tile / tiles_x) * EY;
+    const int x0 = (tile % tiles_x) * EX, y0 = a.row0 + (tile / tiles_x) * EY;
 
     // ---- phase 0: nodal blocks ------------------------------------------------
     for (int idx = t; idx < NSLOT * NN; idx += NT) {
@@ -243,7 +244,8 @@ template <typename T, int P, int SHAPE>
 cudaError_t launch_apply_pernode_shape(int mode, const ApplyArgs<T>& a, const Tab<T, P>& tb, cudaStream_t s) {
   using S = PernodeShape<P, SHAPE>;
   if (mode == APPLY_PREPARE) return cudaSuccess;  // static shared memory: no attribute to set
-  const long long ntiles = (long long)((a.dim + S::EX - 1) / S::EX) * ((a.dim + S::EY - 1) / S::EY);
+  const int rows = a.nrows > 0 ? a.nrows : a.dim;
+  const long long ntiles = (long long)((a.dim + S::EX - 1) / S::EX) * ((rows + S::EY - 1) / S::EY);
   // at most the resident CTAs, and in a reducing mode at most one partial per
   // scratch entry
   auto grid_for = [&](auto kernel, bool reduces) {

@@ -124,6 +124,10 @@ struct ApplyArgs {
   CgState<T>* st;  // CG / RESID
   ReduceScratch red;
   CgState<double>* stp;  // compensated apply, CG mode: the inner state (FP64 scalars)
+  // a band of element rows [row0, row0 + nrows) (nrows = 0: the whole mesh),
+  // row0 a multiple of the tile's rows; the FP64 applies (element and
+  // per-node tiles) honour it
+  int row0, nrows;
 };
 
 // The penalty of a compensated apply as three floats (nu + nu_lo + nu_lo2).
@@ -239,6 +243,10 @@ struct sipg_op {
   sipg_cg_workspace* ws32 = nullptr;
   double* stage_in = nullptr;  // host-buffer apply staging (device)
   double* stage_out = nullptr;
+  // the host-buffer apply's pipeline: copy-in, copy-out and two compute
+  // streams, and per band events
+  cudaStream_t hs[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t hev[2 * 16 + 2] = {};
   void* mixed = nullptr;  // the mixed-precision solver's cached workspace
   void (*mixed_free)(void*) = nullptr;
   void* pcg = nullptr;  // the block-Jacobi preconditioner and PCG workspace
