@@ -88,13 +88,24 @@ __device__ __forceinline__ bool grid_sum_last(A block_total, const ReduceScratch
   return grid_sum_last<A, NT>(block_total, red, (int)(blockIdx.y * gridDim.x + blockIdx.x), nblocks, sh, total);
 }
 
+// Where the column form reads its weighted stiffness KW (n^3 values): from
+// the kernel parameters (constant bank), or from shared memory where the
+// table read with a per-row index overflows the constant cache.  Measured
+// for FP64 at ~16 M DoF: shared memory pays at p = 8 (5.8 KB; 15.8 -> 17.0
+// GDoF/s), not at p = 6 or 7 (2.7 and 4 KB).
+template <typename T, int P>
+struct KwInSmem {
+  static constexpr bool value = P >= 8;
+};
+
 template <typename T, int P, int TX, int TY>
 struct ApplySmem {
   static constexpr int N1 = P + 1, NN = N1 * N1, TE = TX * TY;
   static constexpr int US = NN * TE;                 // nodal values of the tile
   static constexpr int XF = TY * 2 * N1 * (TX + 1);  // x faces [TY][2][N1][TX+1]
   static constexpr int YF = (TY + 1) * 2 * N1 * TX;  // y faces [TY+1][2][N1][TX]
-  static constexpr size_t bytes = (size_t)(US + XF + YF) * sizeof(T);
+  static constexpr int KW = KwInSmem<T, P>::value ? N1 * N1 * N1 : 0;
+  static constexpr size_t bytes = (size_t)(US + XF + YF + KW) * sizeof(T);
 };
 
 // Phase-2 form per (precision, degree): the column form for FP64 (whose n^2
@@ -185,6 +196,9 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   T* __restrict__ us = reinterpret_cast<T*>(smem_raw);
   T* __restrict__ xf = us + S::US;
   T* __restrict__ yf = xf + S::XF;
+  T* __restrict__ kws = yf + S::YF;  // KW, when KwInSmem
+  constexpr bool kKwSmem = KwInSmem<T, P>::value;
+  auto KWv = [&](int k) -> T { return kKwSmem ? kws[k] : tb.KW[k]; };
 
   constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);  // p.Ap -> alpha
   if (kDot) {
@@ -229,6 +243,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   // ---- phase 0: the tile's nodal blocks -> smem --------------------------
   // (loads only: CG mode writes the new direction in phase 2, so that no
   // store sits between loads the compiler could otherwise batch)
+  if (kKwSmem)
+    for (int k = t; k < N1 * N1 * N1; k += TE) kws[k] = tb.KW[k];
 #pragma unroll(ApplyColumnForm<T, P>::load_unroll)
   for (int k = 0; k < NN; ++k) {
     const T v = act ? ld(k, e) : T(0);
@@ -414,7 +430,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
 #pragma unroll
-          for (int j = 0; j < N1; ++j) o[j] = fma(tb.KW[(i1 * N1 + i) * N1 + j], Uv(i, j), o[j]);
+          for (int j = 0; j < N1; ++j) o[j] = fma(KWv((i1 * N1 + i) * N1 + j), Uv(i, j), o[j]);
         }
 #pragma unroll
         for (int i = 0; i < N1; ++i) c[i] = U(i1, i);
@@ -423,7 +439,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         for (int j = 0; j < N1; ++j) {
           T v = o[j];
 #pragma unroll
-          for (int i = 0; i < N1; ++i) v = fma(tb.KW[(j * N1 + i) * N1 + i1], c[i], v);
+          for (int i = 0; i < N1; ++i) v = fma(KWv((j * N1 + i) * N1 + i1), c[i], v);
           v = fma(tb.D0[j], gj, v);
           o[j] = fma(tb.DN[j], hj, v);
         }

@@ -29,10 +29,22 @@
 
 namespace sipg {
 
+// The phase-2 form per degree: up to p = 4 the weighted stiffness KW[(a *
+// N1 + i) * N1 + b] = w_b K[a][i] (n^3 three-float coefficients, 1.5 KB at
+// p = 4) saves the two weight multiplications per output; from p = 5 on the
+// table read with a per-row index overflows the constant cache and K with
+// the weights applied afterwards is faster (measured: 68.7 against 59.8
+// GDoF/s at p = 4, 800^2; 28.7 against 35.8 at p = 6, 512^2).
+template <int P>
+struct DfKwForm {
+  static constexpr bool value = P <= 4;
+};
+
 template <int P>
 struct TabDF {
   static constexpr int N1 = P + 1;
   cf w[N1], D0[N1], DN[N1], K[N1 * N1];
+  cf KW[DfKwForm<P>::value ? N1 * N1 * N1 : 1];
 };
 
 // a double as three floats, h + m + l (exact to ~2^-72 relative)
@@ -55,6 +67,12 @@ inline TabDF<P> make_tab_df(const HostTables& h) {
     t.DN[i] = split_cf(h.D[i * n + P]);
   }
   for (int i = 0; i < n * n; ++i) t.K[i] = split_cf(h.K[i]);
+  // w_b K[a][i] to 72 bits: the product of two doubles, rounded once more
+  // than either factor (2^-53 relative, far below the pairs' 2^-48)
+  if (DfKwForm<P>::value)
+    for (int a = 0; a < n; ++a)
+      for (int i = 0; i < n; ++i)
+        for (int b = 0; b < n; ++b) t.KW[(a * n + i) * n + b] = split_cf(h.w[b] * h.K[a * n + i]);
   return t;
 }
 
@@ -325,36 +343,65 @@ __device__ __forceinline__ void apply_tile_df(const ApplyArgs<float>& a, const T
   if (act) {
 #pragma unroll 1
     for (int i1 = s; i1 < N1; i1 += TPE) {
+      constexpr bool kKw = DfKwForm<P>::value;
+      const bool xf = (i1 == 0) || (i1 == N);
+      // the node's face corrections (+-Q) as the seed of its chain: no
+      // separate additions except at the corners
+      auto seed_of = [&](int j) -> df {
+        df seed = df_zero();
+        if (i1 == 0) seed = XF2(ty, 2, j, tx);
+        if (i1 == N) seed = df_neg(XF2(ty, 2, j, tx + 1));
+        if (j == 0) seed = xf ? df_add(seed, YF2(ty + 1, 2, i1, tx)) : YF2(ty + 1, 2, i1, tx);
+        if (j == N) seed = xf ? df_add(seed, df_neg(YF2(ty, 2, i1, tx))) : df_neg(YF2(ty, 2, i1, tx));
+        return seed;
+      };
+      const cf d0i = tb.D0[i1], dni = tb.DN[i1], wi = tb.w[i1];
       df o[N1];
+      if (kKw) {
+        // KW form: seed, x-face lifting, sum_i w_j K(i1,i) u(i,j), then (below)
+        // sum_i w_i1 K(j,i) u(i1,i) and the y-face lifting
 #pragma unroll
-      for (int j = 0; j < N1; ++j) o[j] = df_zero();
+        for (int j = 0; j < N1; ++j)
+          o[j] = df_macc(df_macc(seed_of(j), dni, XF2(ty, 0, j, tx + 1)), d0i, XF2(ty, 0, j, tx));
 #pragma unroll
-      for (int i = 0; i < N1; ++i) {
-        const cf kc = tb.K[i1 * N1 + i];
+        for (int i = 0; i < N1; ++i) {
 #pragma unroll
-        for (int j = 0; j < N1; ++j) o[j] = df_macc(o[j], kc, Uv(i, j));
+          for (int j = 0; j < N1; ++j) o[j] = df_macc(o[j], tb.KW[kKw ? (i1 * N1 + i) * N1 + j : 0], Uv(i, j));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < N1; ++j) o[j] = df_zero();
+#pragma unroll
+        for (int i = 0; i < N1; ++i) {
+          const cf kc = tb.K[i1 * N1 + i];
+#pragma unroll
+          for (int j = 0; j < N1; ++j) o[j] = df_macc(o[j], kc, Uv(i, j));
+        }
       }
       df c[N1];
 #pragma unroll
       for (int i = 0; i < N1; ++i) c[i] = U(i1, i);
       const df gJ = YF2(ty + 1, 0, i1, tx);
       const df hJ = YF2(ty, 0, i1, tx);
-      const cf d0i = tb.D0[i1], dni = tb.DN[i1], wi = tb.w[i1];
 #pragma unroll
       for (int j = 0; j < N1; ++j) {
-        df s = df_zero();
+        df v;
+        if (kKw) {
+          v = o[j];
 #pragma unroll
-        for (int i = 0; i < N1; ++i) s = df_macc(s, tb.K[j * N1 + i], c[i]);
-        df v = df_mulc(tb.w[j], o[j]);
-        v = df_macc(v, d0i, XF2(ty, 0, j, tx));
-        v = df_macc(v, dni, XF2(ty, 0, j, tx + 1));
-        v = df_macc(v, wi, s);
+          for (int i = 0; i < N1; ++i) v = df_macc(v, tb.KW[kKw ? (j * N1 + i) * N1 + i1 : 0], c[i]);
+        } else {
+          // K form: w_j (K u)_j on the seed, the x-face lifting, w_i1 (K u)_i1
+          df s = df_zero();
+#pragma unroll
+          for (int i = 0; i < N1; ++i) s = df_macc(s, tb.K[j * N1 + i], c[i]);
+          v = df_macc(seed_of(j), tb.w[j], o[j]);
+          v = df_macc(v, d0i, XF2(ty, 0, j, tx));
+          v = df_macc(v, dni, XF2(ty, 0, j, tx + 1));
+          v = df_macc(v, wi, s);
+        }
         v = df_macc(v, tb.D0[j], gJ);
         v = df_macc(v, tb.DN[j], hJ);
-        if (i1 == 0) v = df_add(v, XF2(ty, 2, j, tx));
-        if (i1 == N) v = df_add(v, df_neg(XF2(ty, 2, j, tx + 1)));
-        if (j == 0) v = df_add(v, YF2(ty + 1, 2, i1, tx));
-        if (j == N) v = df_add(v, df_neg(YF2(ty, 2, i1, tx)));
         v = df_norm(v);
         const size_t oi = (size_t)(i1 * N1 + j) * noe + e;
         a.out[oi] = v.hi;
