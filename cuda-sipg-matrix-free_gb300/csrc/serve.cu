@@ -21,6 +21,16 @@
 // Retired requests free their vectors at once (their results stay until the
 // caller releases them), so memory and slots turn over while others run.
 // Meshes/operators are cached and shared; all solver state stays on the device.
+//
+// Requests run in three lanes by size (up to 2^18 DoF, up to 2^22, larger),
+// each with its own stream -- the smaller the solves, the higher the stream
+// priority -- its own descriptor staging and its own host mirror of the
+// states.  A lane's round is steps 2-3 for its requests; sipg_server_step
+// finishes every lane whose round has ended and starts its next one, so a
+// lane of small solves turns rounds over (and retires requests) while a lane
+// of large ones is mid-round, instead of advancing one iteration per large
+// solve's iteration.  The step blocks only when every lane with work is
+// mid-round.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -185,23 +195,18 @@ struct Request {
 struct Slots {
   CgState<double>* d32 = nullptr;  // mixed requests' inner states
   CgState<double>* d64 = nullptr;
-  CgState<double>* h32 = nullptr;
-  CgState<double>* h64 = nullptr;
 };
 
-}  // namespace
-
-struct sipg_server {
-  sipg_server_opts opts{};
+// One size class of requests (see the file comment).
+struct Lane {
   cudaStream_t s = nullptr;
-  Slots slots;
-  std::vector<int> free_slots;
-  std::deque<Request*> queue;
-  std::vector<Request*> active;
-  std::unordered_map<unsigned long long, Request*> all;
-  std::map<std::tuple<int, int, double>, sipg_op*> ops;
-  unsigned long long next_id = 1;
-  size_t used = 0;
+  cudaEvent_t ev = nullptr;      // the end of the lane's round in flight
+  bool busy = false;
+  std::vector<Request*> active;  // started requests
+  std::vector<Request*> fresh;   // admitted; started at the lane's next round
+  // pinned mirrors of the slot states, written by this lane's copies only
+  CgState<double>* h32 = nullptr;
+  CgState<double>* h64 = nullptr;
   // pinned staging and device descriptor arrays (capacity max_active; tile
   // starts max_active + 16): FP32 CG applies, FP64 CG applies, FP64 residuals
   ApplyArgs<float>* h_a32 = nullptr;
@@ -226,6 +231,24 @@ struct sipg_server {
   double* d_tol = nullptr;
   const double** h_bptr = nullptr;
   const double** d_bptr = nullptr;
+};
+
+constexpr int kLanes = 3;
+int lane_of(size_t n) { return n <= (size_t(1) << 18) ? 0 : (n <= (size_t(1) << 22) ? 1 : 2); }
+
+}  // namespace
+
+struct sipg_server {
+  sipg_server_opts opts{};
+  cudaStream_t s = nullptr;  // solution copies and releases
+  Slots slots;
+  std::vector<int> free_slots;
+  std::deque<Request*> queue;
+  std::unordered_map<unsigned long long, Request*> all;
+  std::map<std::tuple<int, int, double>, sipg_op*> ops;
+  unsigned long long next_id = 1;
+  size_t used = 0;
+  Lane lanes[kLanes];
   unsigned long long completed = 0, rejected = 0;
 };
 
@@ -257,10 +280,10 @@ sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
 }
 
 // carve one pool allocation into the request's vectors
-sipg_status admit(sipg_server* sv, Request* r) {
+sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
   r->x_bytes = r->n * sizeof(double);
-  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->x64, r->x_bytes, sv->s));
-  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->mem, r->footprint - r->x_bytes, sv->s));
+  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->x64, r->x_bytes, s));
+  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->mem, r->footprint - r->x_bytes, s));
   char* p = r->mem;
   auto take = [&](size_t bytes) {
     char* q = p;
@@ -287,10 +310,10 @@ sipg_status admit(sipg_server* sv, Request* r) {
   r->red64.partials = (double*)take(sizeof(double) * cap);
   r->red64.counter = (unsigned int*)take(256);
   r->red64.capacity = cap;
-  SIPG_CUDA_TRY(cudaMemsetAsync(r->red32.counter, 0, 4, sv->s));
-  SIPG_CUDA_TRY(cudaMemsetAsync(r->red64.counter, 0, 4, sv->s));
+  SIPG_CUDA_TRY(cudaMemsetAsync(r->red32.counter, 0, 4, s));
+  SIPG_CUDA_TRY(cudaMemsetAsync(r->red64.counter, 0, 4, s));
   const sipg_modes* modes = (r->req.sol == SIPG_SOL_MODES) ? &r->req.modes : nullptr;
-  sipg_status st = rhs_f64(r->op, r->req.sol, modes, r->b64, sv->s);
+  sipg_status st = rhs_f64(r->op, r->req.sol, modes, r->b64, s);
   if (st != SIPG_OK) return st;
   r->slot = sv->free_slots.back();
   sv->free_slots.pop_back();
@@ -301,7 +324,7 @@ sipg_status admit(sipg_server* sv, Request* r) {
   return SIPG_OK;
 }
 
-void retire(sipg_server* sv, Request* r, sipg_status status, int iterations, double rel) {
+void retire(sipg_server* sv, Request* r, cudaStream_t s, sipg_status status, int iterations, double rel) {
   r->t_done = Clock::now();
   r->result.status = status;
   r->result.iterations = iterations;
@@ -310,7 +333,7 @@ void retire(sipg_server* sv, Request* r, sipg_status status, int iterations, dou
   r->result.queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
   r->result.latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
   r->result.done = 1;
-  cudaFreeAsync(r->mem, sv->s);
+  cudaFreeAsync(r->mem, s);
   r->mem = nullptr;
   sv->used -= r->footprint - r->x_bytes;  // the solution stays until release
   sv->free_slots.push_back(r->slot);
@@ -432,36 +455,46 @@ sipg_status server_alloc(sipg_server* sv) {
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d64, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMemset(sv->slots.d64, 0, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h32, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->slots.h64, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_a32, sizeof(ApplyArgs<float>) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_a32, sizeof(ApplyArgs<float>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_a64, sizeof(ApplyArgs<double>) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_a64, sizeof(ApplyArgs<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_r64, sizeof(ApplyArgs<double>) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_r64, sizeof(ApplyArgs<double>) * cap));
-  int** tiles_h[3] = {&sv->h_t32, &sv->h_t64, &sv->h_tr};
-  int** tiles_d[3] = {&sv->d_t32, &sv->d_t64, &sv->d_tr};
-  for (int k = 0; k < 3; ++k) {
-    SIPG_CUDA_TRY(cudaMallocHost(tiles_h[k], sizeof(int) * (cap + 16)));
-    SIPG_CUDA_TRY(cudaMalloc(tiles_d[k], sizeof(int) * (cap + 16)));
+  int least = 0, greatest = 0;  // numerically: greatest priority is the lowest value
+  SIPG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  for (int k = 0; k < kLanes; ++k) {
+    Lane& L = sv->lanes[k];
+    const int prio = greatest + (least - greatest) * k / (kLanes - 1);
+    SIPG_CUDA_TRY(cudaStreamCreateWithPriority(&L.s, cudaStreamNonBlocking, prio));
+    SIPG_CUDA_TRY(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h32, sizeof(CgState<double>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h64, sizeof(CgState<double>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_a32, sizeof(ApplyArgs<float>) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_a32, sizeof(ApplyArgs<float>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_a64, sizeof(ApplyArgs<double>) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_a64, sizeof(ApplyArgs<double>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_r64, sizeof(ApplyArgs<double>) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_r64, sizeof(ApplyArgs<double>) * cap));
+    int** tiles_h[3] = {&L.h_t32, &L.h_t64, &L.h_tr};
+    int** tiles_d[3] = {&L.d_t32, &L.d_t64, &L.d_tr};
+    for (int t = 0; t < 3; ++t) {
+      SIPG_CUDA_TRY(cudaMallocHost(tiles_h[t], sizeof(int) * (cap + 16)));
+      SIPG_CUDA_TRY(cudaMalloc(tiles_d[t], sizeof(int) * (cap + 16)));
+    }
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_v32, sizeof(PairInst) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_v32, sizeof(PairInst) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_v64, sizeof(VecInst<double>) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_v64, sizeof(VecInst<double>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_m, sizeof(ServeMixed) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_m, sizeof(ServeMixed) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_tol, sizeof(double) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_tol, sizeof(double) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_bptr, sizeof(double*) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_bptr, sizeof(double*) * cap));
   }
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v32, sizeof(PairInst) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v32, sizeof(PairInst) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_v64, sizeof(VecInst<double>) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_v64, sizeof(VecInst<double>) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_m, sizeof(ServeMixed) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_m, sizeof(ServeMixed) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_tol, sizeof(double) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_tol, sizeof(double) * cap));
-  SIPG_CUDA_TRY(cudaMallocHost(&sv->h_bptr, sizeof(double*) * cap));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->d_bptr, sizeof(double*) * cap));
   for (int k = cap - 1; k >= 0; --k) sv->free_slots.push_back(k);
   return SIPG_OK;
 }
 
 void server_free(sipg_server* sv) {
   if (!sv) return;
+  for (Lane& L : sv->lanes)
+    if (L.s) cudaStreamSynchronize(L.s);
   if (sv->s) cudaStreamSynchronize(sv->s);
   for (auto& kv : sv->all) {
     if (kv.second->mem) cudaFreeAsync(kv.second->mem, sv->s);
@@ -473,33 +506,259 @@ void server_free(sipg_server* sv) {
   if (sv->s) cudaStreamSynchronize(sv->s);
   cudaFree(sv->slots.d32);
   cudaFree(sv->slots.d64);
-  cudaFreeHost(sv->slots.h32);
-  cudaFreeHost(sv->slots.h64);
-  cudaFreeHost(sv->h_a32);
-  cudaFree(sv->d_a32);
-  cudaFreeHost(sv->h_a64);
-  cudaFree(sv->d_a64);
-  cudaFreeHost(sv->h_r64);
-  cudaFree(sv->d_r64);
-  cudaFreeHost(sv->h_t32);
-  cudaFree(sv->d_t32);
-  cudaFreeHost(sv->h_t64);
-  cudaFree(sv->d_t64);
-  cudaFreeHost(sv->h_tr);
-  cudaFree(sv->d_tr);
-  cudaFreeHost(sv->h_v32);
-  cudaFree(sv->d_v32);
-  cudaFreeHost(sv->h_v64);
-  cudaFree(sv->d_v64);
-  cudaFreeHost(sv->h_m);
-  cudaFree(sv->d_m);
-  cudaFreeHost(sv->h_tol);
-  cudaFree(sv->d_tol);
-  cudaFreeHost(sv->h_bptr);
-  cudaFree(sv->d_bptr);
+  for (Lane& L : sv->lanes) {
+    cudaFreeHost(L.h32);
+    cudaFreeHost(L.h64);
+    cudaFreeHost(L.h_a32);
+    cudaFree(L.d_a32);
+    cudaFreeHost(L.h_a64);
+    cudaFree(L.d_a64);
+    cudaFreeHost(L.h_r64);
+    cudaFree(L.d_r64);
+    cudaFreeHost(L.h_t32);
+    cudaFree(L.d_t32);
+    cudaFreeHost(L.h_t64);
+    cudaFree(L.d_t64);
+    cudaFreeHost(L.h_tr);
+    cudaFree(L.d_tr);
+    cudaFreeHost(L.h_v32);
+    cudaFree(L.d_v32);
+    cudaFreeHost(L.h_v64);
+    cudaFree(L.d_v64);
+    cudaFreeHost(L.h_m);
+    cudaFree(L.d_m);
+    cudaFreeHost(L.h_tol);
+    cudaFree(L.d_tol);
+    cudaFreeHost(L.h_bptr);
+    cudaFree(L.d_bptr);
+    if (L.ev) cudaEventDestroy(L.ev);
+    if (L.s) cudaStreamDestroy(L.s);
+  }
   for (auto& kv : sv->ops) sipg_op_destroy(kv.second);
   if (sv->s) cudaStreamDestroy(sv->s);
   delete sv;
+}
+
+int active_count(const sipg_server* sv) {
+  int n = 0;
+  for (const Lane& L : sv->lanes) n += (int)(L.active.size() + L.fresh.size());
+  return n;
+}
+
+// Starts the lane's admitted requests (x = 0, r = b; one batched launch per
+// precision) and moves them to its active list.  Synchronous on the lane's
+// stream (its staging is reused for the round that follows).
+sipg_status lane_start(sipg_server* sv, Lane& L) {
+  int m32 = 0, m64 = 0;
+  size_t nmax32 = 0, nmax64 = 0;
+  for (Request* r : L.fresh) {
+    if (r->req.precision == SIPG_F64) {
+      VecInst<double> v;
+      v.x = r->x64;
+      v.pb0 = r->p64[0];
+      v.pb1 = r->p64[1];
+      v.r = r->r64;
+      v.Ap = r->Ap64;
+      v.n = r->n;
+      v.st = sv->slots.d64 + r->slot;
+      v.red = r->red64;
+      v.nblk = inst_blocks(r->n);
+      v.pad = 0;
+      L.h_v64[m64] = v;
+      L.h_tol[m64] = r->req.tol;
+      L.h_bptr[m64] = r->b64;
+      nmax64 = std::max(nmax64, r->n);
+      ++m64;
+    } else {
+      L.h_m[m32++] = mixed_of(r, sv, 1);
+      nmax32 = std::max(nmax32, r->n);
+    }
+  }
+  if (m64) {
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v64, L.h_v64, sizeof(VecInst<double>) * m64, cudaMemcpyHostToDevice, L.s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_tol, L.h_tol, sizeof(double) * m64, cudaMemcpyHostToDevice, L.s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_bptr, L.h_bptr, sizeof(double*) * m64, cudaMemcpyHostToDevice, L.s));
+    k_serve_init_f64<<<dim3(vec_bpi(nmax64, m64), m64), kVecThreads, 0, L.s>>>(L.d_v64, L.d_tol, L.d_bptr);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+  }
+  if (m32) {
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m32, cudaMemcpyHostToDevice, L.s));
+    k_serve_init_mixed<<<dim3(vec_bpi(nmax32, m32), m32), kVecThreads, 0, L.s>>>(L.d_m);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+  }
+  SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
+  L.active.insert(L.active.end(), L.fresh.begin(), L.fresh.end());
+  L.fresh.clear();
+  return SIPG_OK;
+}
+
+// Queues a round for the lane: iters_per_step CG iterations of its active
+// requests (per precision: one batched launch per degree and kernel), the
+// copy of the slot states into the lane's mirrors, and the lane's event.
+sipg_status lane_launch(sipg_server* sv, Lane& L) {
+  std::vector<Request*> a32, a64;
+  for (Request* r : L.active) (r->req.precision == SIPG_F64 ? a64 : a32).push_back(r);
+  size_t nmax32 = 0, nmax64 = 0;
+  for (int j = 0; j < (int)a32.size(); ++j) {
+    Request* r = a32[j];
+    PairInst v;
+    v.x = r->e32;
+    v.pb0 = r->p32[0];
+    v.pb1 = r->p32[0];
+    v.r = r->r32;
+    v.Ap = r->Ap32;
+    v.n = r->n;
+    v.st = sv->slots.d32 + r->slot;
+    v.red = r->red32;
+    v.nblk = inst_blocks(r->n);
+    v.pad = 0;
+    L.h_v32[j] = v;
+    nmax32 = std::max(nmax32, r->n);
+  }
+  for (int j = 0; j < (int)a64.size(); ++j) {
+    Request* r = a64[j];
+    VecInst<double> v;
+    v.x = r->x64;
+    v.pb0 = r->p64[0];
+    v.pb1 = r->p64[1];
+    v.r = r->r64;
+    v.Ap = r->Ap64;
+    v.n = r->n;
+    v.st = sv->slots.d64 + r->slot;
+    v.red = r->red64;
+    v.nblk = inst_blocks(r->n);
+    v.pad = 0;
+    L.h_v64[j] = v;
+    nmax64 = std::max(nmax64, r->n);
+  }
+  if (!a32.empty())
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v32, L.h_v32, sizeof(PairInst) * a32.size(), cudaMemcpyHostToDevice, L.s));
+  if (!a64.empty())
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v64, L.h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, L.s));
+  const std::vector<GroupLaunch> g32 =
+      pack_groups<float>(a32, L.h_a32, L.h_t32, [&](const Request* r) { return cg_args32(r, sv); });
+  const std::vector<GroupLaunch> g64 =
+      pack_groups<double>(a64, L.h_a64, L.h_t64, [&](const Request* r) { return cg_args64(r, sv); });
+  {
+    sipg_status st = upload_groups<float>(g32, L.h_a32, L.d_a32, L.h_t32, L.d_t32, L.s);
+    if (st == SIPG_OK) st = upload_groups<double>(g64, L.h_a64, L.d_a64, L.h_t64, L.d_t64, L.s);
+    if (st != SIPG_OK) return st;
+  }
+  for (int k = 0; k < sv->opts.iters_per_step; ++k) {
+    if (!a32.empty()) {
+      const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
+      k_cg_direction_pairs_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+      sipg_status st = launch_groups<float>(g32, APPLY_DOT, L.d_a32, L.d_t32, L.s);
+      if (st != SIPG_OK) return st;
+      k_cg_update_pairs_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+    if (!a64.empty()) {
+      sipg_status st = launch_groups<double>(g64, APPLY_CG, L.d_a64, L.d_t64, L.s);
+      if (st != SIPG_OK) return st;
+      k_cg_update_batched<double><<<dim3(vec_bpi(nmax64, (int)a64.size()), (unsigned)a64.size()), kVecThreads, 0,
+                                    L.s>>>(L.d_v64);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  const int cap = sv->opts.max_active;
+  SIPG_CUDA_TRY(cudaMemcpyAsync(L.h32, sv->slots.d32, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
+  SIPG_CUDA_TRY(cudaEventRecord(L.ev, L.s));
+  L.busy = true;
+  return SIPG_OK;
+}
+
+// After a lane's round: FP64 requests that are done retire; mixed requests
+// due a reliable update get x += e and their FP64 residual (batched FP64
+// applies, synchronously on the lane's stream), then retire or restart.
+sipg_status lane_finish(sipg_server* sv, Lane& L) {
+  std::vector<Request*> keep, fix;
+  for (Request* r : L.active) {
+    if (r->req.precision == SIPG_F64) {
+      const CgState<double>& h = L.h64[r->slot];
+      if (h.done) {
+        const bool conv = !(std::sqrt(h.rr) > h.stop);
+        const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
+        retire(sv, r, L.s,
+               h.status == (int)SIPG_ERR_BREAKDOWN ? SIPG_ERR_BREAKDOWN : (conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED),
+               h.it, rel);
+      } else {
+        keep.push_back(r);
+      }
+    } else {
+      if (L.h32[r->slot].done) fix.push_back(r);
+      else keep.push_back(r);
+    }
+  }
+  if (!fix.empty()) {
+    int m = 0;
+    size_t nmax = 0;
+    for (Request* r : fix) {
+      L.h_m[m++] = mixed_of(r, sv, 0);
+      nmax = std::max(nmax, r->n);
+    }
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, L.s));
+    k_serve_fold<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, L.s>>>(L.d_m);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    const std::vector<GroupLaunch> gr = pack_groups<double>(fix, L.h_r64, L.h_tr, [&](const Request* r) {
+      ApplyArgs<double> a{};
+      a.in = r->x64;
+      a.out = r->r64;
+      a.b = r->b64;
+      a.dim = r->req.dim;
+      a.nu = r->req.pen;
+      a.st = sv->slots.d64 + r->slot;
+      a.red = r->red64;
+      return a;
+    });
+    sipg_status st = upload_groups<double>(gr, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
+    if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, L.d_r64, L.d_tr, L.s);
+    if (st != SIPG_OK) return st;
+    const int cap = sv->opts.max_active;
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
+    std::vector<Request*> cont;
+    for (Request* r : fix) {
+      r->corrections++;
+      const CgState<double>& h = L.h64[r->slot];
+      const CgState<double>& h32 = L.h32[r->slot];
+      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
+      if (!std::isfinite(rel) || h32.status == (int)SIPG_ERR_BREAKDOWN) {
+        retire(sv, r, L.s, SIPG_ERR_BREAKDOWN, h32.it, rel);
+      } else if (rel <= r->req.tol || h.rr == 0.0) {
+        retire(sv, r, L.s, SIPG_OK, h32.it, rel);
+      } else if (r->corrections >= 1000) {
+        retire(sv, r, L.s, SIPG_ERR_NOT_CONVERGED, h32.it, rel);
+      } else {
+        cont.push_back(r);
+      }
+    }
+    if (!cont.empty()) {
+      m = 0;
+      nmax = 0;
+      for (Request* r : cont) {
+        L.h_m[m++] = mixed_of(r, sv, 0);
+        nmax = std::max(nmax, r->n);
+      }
+      SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, L.s));
+      k_serve_restart<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, L.s>>>(L.d_m);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+      for (Request* r : cont) keep.push_back(r);
+    }
+    // the pinned staging (h_m) is rewritten by the lane's next round
+    SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
+  }
+  L.active = keep;
+  return SIPG_OK;
 }
 
 }  // namespace
@@ -564,224 +823,54 @@ sipg_status sipg_server_submit(sipg_server* sv, const sipg_request* req, unsigne
 sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   if (!sv) return SIPG_ERR_INVALID;
   const unsigned long long done_before = sv->completed;
-  // 1. admission
-  std::vector<Request*> fresh;
+  // 1. admission, FIFO over all lanes
   while (!sv->queue.empty() && !sv->free_slots.empty()) {
     Request* r = sv->queue.front();
     if (sv->used + r->footprint > sv->opts.budget_bytes) break;  // FIFO: wait for memory
     sipg_status st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &r->op);
     if (st != SIPG_OK) return st;
-    st = admit(sv, r);
+    Lane& L = sv->lanes[lane_of(r->n)];
+    st = admit(sv, r, L.s);
     if (st != SIPG_OK) return st;
     sv->queue.pop_front();
-    sv->active.push_back(r);
-    fresh.push_back(r);
+    L.fresh.push_back(r);
   }
-  if (!fresh.empty()) {
-    // start the new requests (x = 0, r = b), one batched launch per precision
-    int m32 = 0, m64 = 0;
-    size_t nmax32 = 0, nmax64 = 0;
-    for (Request* r : fresh) {
-      if (r->req.precision == SIPG_F64) {
-        VecInst<double> v;
-        v.x = r->x64;
-        v.pb0 = r->p64[0];
-        v.pb1 = r->p64[1];
-        v.r = r->r64;
-        v.Ap = r->Ap64;
-        v.n = r->n;
-        v.st = sv->slots.d64 + r->slot;
-        v.red = r->red64;
-        v.nblk = inst_blocks(r->n);
-        v.pad = 0;
-        sv->h_v64[m64] = v;
-        sv->h_tol[m64] = r->req.tol;
-        sv->h_bptr[m64] = r->b64;
-        nmax64 = std::max(nmax64, r->n);
-        ++m64;
-      } else {
-        sv->h_m[m32++] = mixed_of(r, sv, 1);
-        nmax32 = std::max(nmax32, r->n);
+  // 2. every lane whose round has ended: its results, then its next round;
+  // if every lane with work is mid-round, wait for the one of the smallest
+  // solves and take it
+  for (int pass = 0; pass < 2; ++pass) {
+    bool progressed = false;
+    for (Lane& L : sv->lanes) {
+      if (L.busy) {
+        const cudaError_t q = cudaEventQuery(L.ev);
+        if (q == cudaErrorNotReady) continue;
+        SIPG_CUDA_TRY(q);
+        L.busy = false;
+        sipg_status st = lane_finish(sv, L);
+        if (st != SIPG_OK) return st;
+        progressed = true;
+      }
+      if (!L.fresh.empty()) {
+        sipg_status st = lane_start(sv, L);
+        if (st != SIPG_OK) return st;
+        progressed = true;
+      }
+      if (!L.active.empty()) {
+        sipg_status st = lane_launch(sv, L);
+        if (st != SIPG_OK) return st;
       }
     }
-    if (m64) {
-      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v64, sv->h_v64, sizeof(VecInst<double>) * m64, cudaMemcpyHostToDevice, sv->s));
-      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_tol, sv->h_tol, sizeof(double) * m64, cudaMemcpyHostToDevice, sv->s));
-      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_bptr, sv->h_bptr, sizeof(double*) * m64, cudaMemcpyHostToDevice, sv->s));
-      k_serve_init_f64<<<dim3(vec_bpi(nmax64, m64), m64), kVecThreads, 0, sv->s>>>(sv->d_v64, sv->d_tol, sv->d_bptr);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-    }
-    if (m32) {
-      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m32, cudaMemcpyHostToDevice, sv->s));
-      k_serve_init_mixed<<<dim3(vec_bpi(nmax32, m32), m32), kVecThreads, 0, sv->s>>>(sv->d_m);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-    }
-    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
-  }
-  if (sv->active.empty()) {
-    if (n_active) *n_active = 0;
-    if (n_completed) *n_completed = (int)(sv->completed - done_before);
-    return SIPG_OK;
-  }
-  // 2. K iterations of every active request
-  std::vector<Request*> a32, a64;
-  for (Request* r : sv->active) (r->req.precision == SIPG_F64 ? a64 : a32).push_back(r);
-  size_t nmax32 = 0, nmax64 = 0;
-  for (int j = 0; j < (int)a32.size(); ++j) {
-    Request* r = a32[j];
-    PairInst v;
-    v.x = r->e32;
-    v.pb0 = r->p32[0];
-    v.pb1 = r->p32[0];
-    v.r = r->r32;
-    v.Ap = r->Ap32;
-    v.n = r->n;
-    v.st = sv->slots.d32 + r->slot;
-    v.red = r->red32;
-    v.nblk = inst_blocks(r->n);
-    v.pad = 0;
-    sv->h_v32[j] = v;
-    nmax32 = std::max(nmax32, r->n);
-  }
-  for (int j = 0; j < (int)a64.size(); ++j) {
-    Request* r = a64[j];
-    VecInst<double> v;
-    v.x = r->x64;
-    v.pb0 = r->p64[0];
-    v.pb1 = r->p64[1];
-    v.r = r->r64;
-    v.Ap = r->Ap64;
-    v.n = r->n;
-    v.st = sv->slots.d64 + r->slot;
-    v.red = r->red64;
-    v.nblk = inst_blocks(r->n);
-    v.pad = 0;
-    sv->h_v64[j] = v;
-    nmax64 = std::max(nmax64, r->n);
-  }
-  if (!a32.empty())
-    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v32, sv->h_v32, sizeof(PairInst) * a32.size(), cudaMemcpyHostToDevice,
-                                  sv->s));
-  if (!a64.empty())
-    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_v64, sv->h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, sv->s));
-  const std::vector<GroupLaunch> g32 =
-      pack_groups<float>(a32, sv->h_a32, sv->h_t32, [&](const Request* r) { return cg_args32(r, sv); });
-  const std::vector<GroupLaunch> g64 =
-      pack_groups<double>(a64, sv->h_a64, sv->h_t64, [&](const Request* r) { return cg_args64(r, sv); });
-  {
-    sipg_status st = upload_groups<float>(g32, sv->h_a32, sv->d_a32, sv->h_t32, sv->d_t32, sv->s);
-    if (st == SIPG_OK) st = upload_groups<double>(g64, sv->h_a64, sv->d_a64, sv->h_t64, sv->d_t64, sv->s);
-    if (st != SIPG_OK) return st;
-  }
-  for (int k = 0; k < sv->opts.iters_per_step; ++k) {
-    if (!a32.empty()) {
-      const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
-      k_cg_direction_pairs_batched<<<vg, kVecThreads, 0, sv->s>>>(sv->d_v32);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-      sipg_status st = launch_groups<float>(g32, APPLY_DOT, sv->d_a32, sv->d_t32, sv->s);
-      if (st != SIPG_OK) return st;
-      k_cg_update_pairs_batched<<<dim3(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size()), kVecThreads, 0,
-                                  sv->s>>>(sv->d_v32);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-    }
-    if (!a64.empty()) {
-      sipg_status st = launch_groups<double>(g64, APPLY_CG, sv->d_a64, sv->d_t64, sv->s);
-      if (st != SIPG_OK) return st;
-      k_cg_update_batched<double><<<dim3(vec_bpi(nmax64, (int)a64.size()), (unsigned)a64.size()), kVecThreads, 0, sv->s>>>(
-          sv->d_v64);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-    }
-  }
-  // 3. states, corrections, retirements
-  const int cap = sv->opts.max_active;
-  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h32, sv->slots.d32, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost,
-                                sv->s));
-  SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, sv->s));
-  SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
-  std::vector<Request*> keep, fix;
-  for (Request* r : a64) {
-    const CgState<double>& h = sv->slots.h64[r->slot];
-    if (h.done) {
-      const bool conv = !(std::sqrt(h.rr) > h.stop);
-      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
-      retire(sv, r, h.status == (int)SIPG_ERR_BREAKDOWN ? SIPG_ERR_BREAKDOWN : (conv ? SIPG_OK : SIPG_ERR_NOT_CONVERGED),
-             h.it, rel);
-    } else {
-      keep.push_back(r);
-    }
-  }
-  for (Request* r : a32) {
-    const CgState<double>& h = sv->slots.h32[r->slot];
-    if (h.done) fix.push_back(r);
-    else keep.push_back(r);
-  }
-  if (!fix.empty()) {
-    // x += e and the FP64 residual of the mixed requests due an update
-    int m = 0;
-    size_t nmax = 0;
-    for (Request* r : fix) {
-      sv->h_m[m++] = mixed_of(r, sv, 0);
-      nmax = std::max(nmax, r->n);
-    }
-    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, sv->s));
-    k_serve_fold<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, sv->s>>>(sv->d_m);
-    count_launch();
-    SIPG_CUDA_TRY(cudaGetLastError());
-    const std::vector<GroupLaunch> gr = pack_groups<double>(fix, sv->h_r64, sv->h_tr, [&](const Request* r) {
-      ApplyArgs<double> a{};
-      a.in = r->x64;
-      a.out = r->r64;
-      a.b = r->b64;
-      a.dim = r->req.dim;
-      a.nu = r->req.pen;
-      a.st = sv->slots.d64 + r->slot;
-      a.red = r->red64;
-      return a;
-    });
-    sipg_status st = upload_groups<double>(gr, sv->h_r64, sv->d_r64, sv->h_tr, sv->d_tr, sv->s);
-    if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, sv->d_r64, sv->d_tr, sv->s);
-    if (st != SIPG_OK) return st;
-    SIPG_CUDA_TRY(cudaMemcpyAsync(sv->slots.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, sv->s));
-    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
-    std::vector<Request*> cont;
-    for (Request* r : fix) {
-      r->corrections++;
-      const CgState<double>& h = sv->slots.h64[r->slot];
-      const CgState<double>& h32 = sv->slots.h32[r->slot];
-      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
-      if (!std::isfinite(rel) || h32.status == (int)SIPG_ERR_BREAKDOWN) {
-        retire(sv, r, SIPG_ERR_BREAKDOWN, h32.it, rel);
-      } else if (rel <= r->req.tol || h.rr == 0.0) {
-        retire(sv, r, SIPG_OK, h32.it, rel);
-      } else if (r->corrections >= 1000) {
-        retire(sv, r, SIPG_ERR_NOT_CONVERGED, h32.it, rel);
-      } else {
-        cont.push_back(r);
+    if (progressed) break;
+    bool waited = false;
+    for (Lane& L : sv->lanes)
+      if (L.busy) {
+        SIPG_CUDA_TRY(cudaEventSynchronize(L.ev));
+        waited = true;
+        break;
       }
-    }
-    if (!cont.empty()) {
-      m = 0;
-      nmax = 0;
-      for (Request* r : cont) {
-        sv->h_m[m++] = mixed_of(r, sv, 0);
-        nmax = std::max(nmax, r->n);
-      }
-      SIPG_CUDA_TRY(cudaMemcpyAsync(sv->d_m, sv->h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, sv->s));
-      k_serve_restart<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, sv->s>>>(sv->d_m);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-      for (Request* r : cont) keep.push_back(r);
-    }
-    // the pinned staging (h_m) is rewritten in the next step
-    SIPG_CUDA_TRY(cudaStreamSynchronize(sv->s));
+    if (!waited) break;
   }
-  sv->active = keep;
-  if (n_active) *n_active = (int)sv->active.size();
+  if (n_active) *n_active = active_count(sv);
   if (n_completed) *n_completed = (int)(sv->completed - done_before);
   return SIPG_OK;
 }
@@ -829,7 +918,7 @@ sipg_status sipg_server_solution(sipg_server* sv, unsigned long long id, double*
 sipg_status sipg_server_stats(const sipg_server* sv, sipg_server_stats_t* out) {
   if (!sv || !out) return SIPG_ERR_INVALID;
   out->queued = (int)sv->queue.size();
-  out->active = (int)sv->active.size();
+  out->active = active_count(sv);
   out->completed = sv->completed;
   out->rejected = sv->rejected;
   out->bytes_in_use = sv->used;

@@ -325,8 +325,13 @@ sipg_status sipg_server_destroy(sipg_server* server);
 /* Queues a request (FIFO); returns SIPG_ERR_REJECTED (and a retired result)
  * when its device footprint alone exceeds the budget. */
 sipg_status sipg_server_submit(sipg_server* server, const sipg_request* req, unsigned long long* id);
-/* One scheduling step: admit what fits, run iters_per_step CG iterations of
- * every active request in batched launches, correct / retire.  Synchronous. */
+/* One scheduling step: admit what fits (FIFO), then for each of three
+ * size-class lanes (up to 2^18 DoF, up to 2^22, larger; each on its own
+ * stream, the smaller the higher its priority) whose previous round has
+ * ended: correct / retire its requests and queue its next round of
+ * iters_per_step CG iterations in batched launches.  Returns once at least
+ * one lane has made progress (it waits only when every lane with work is
+ * mid-round); n_active counts admitted, unfinished requests. */
 sipg_status sipg_server_step(sipg_server* server, int* n_active, int* n_completed);
 sipg_status sipg_server_poll(sipg_server* server, unsigned long long id, sipg_request_result* result);
 /* Copies a retired request's solution (n = its DoF) to host memory; the
