@@ -110,3 +110,25 @@ def test_server_budget_admission_and_rejection(sipg, torch):
     assert peak <= 64 << 20
     assert all(sv.poll(i).status == 0 for i in ids)
     sv.close()
+
+
+def test_server_small_request_not_held_behind_a_large_one(sipg, torch):
+    """Requests run in size-class lanes stepped independently: a small solve
+    submitted after a large one retires while the large one is still running
+    (in lockstep it would advance one iteration per large-solve iteration)."""
+    sv = sipg.Server(max_active=8, iters_per_step=8)
+    modes = sipg.Modes.make([1.0, 0.5], [1, 3], [2, 1])
+    big, _ = sv.submit(400, 8, 64.0, 1e-10, modes=modes)  # ~13 M DoF: the large lane
+    sv.step()
+    small, _ = sv.submit(16, 3, 9.0, 1e-10, modes=modes)  # 4096 DoF: the small lane
+    for _ in range(100000):
+        sv.step()
+        if sv.poll(small).done:
+            break
+    rs, rb = sv.poll(small), sv.poll(big)
+    assert rs.done == 1 and rs.status == 0 and rs.rel_residual <= 1e-10
+    assert rb.done == 0, "the small request waited for the large one"
+    x = sv.solution(small, 16 * 16 * 16)
+    ref = _reference(sipg, torch, 16, 3, 9.0, modes)
+    assert np.max(np.abs(x - ref)) <= 1e-6 * np.max(np.abs(ref))
+    sv.close()  # the large request is dropped unfinished
