@@ -410,6 +410,33 @@ sipg_status sipg_dphi_table(int degree, double* D) {
   return SIPG_OK;
 }
 
+sipg_status sipg_laplacian_rows_f64(int degree, double* rows) {
+  if (degree < 1 || degree > SIPG_MAX_DEGREE || !rows) {
+    set_error("sipg_laplacian_rows_f64: degree must be in 1..SIPG_MAX_DEGREE and rows non-null");
+    return SIPG_ERR_INVALID;
+  }
+  HostTables t;
+  if (build_host_tables(degree, &t) != 0) {
+    set_error("sipg_laplacian_rows_f64: table construction failed");
+    return SIPG_ERR_INVALID;
+  }
+  // lap(i1,i2,j1,j2) = [i2 == j2] w_i2 K(i1,j1) + [i1 == j1] w_i1 K(i2,j2) on
+  // the reference element; row (i1,i2) keeps its cross pattern: the
+  // diagonal, then (i1, j != i2), then (j != i1, i2)
+  const int n = degree + 1, R = 2 * degree + 1;
+  for (int i1 = 0; i1 < n; ++i1)
+    for (int i2 = 0; i2 < n; ++i2) {
+      double* row = rows + (size_t)(i1 * n + i2) * R;
+      int r = 0;
+      row[r++] = t.w[i2] * t.K[i1 * n + i1] + t.w[i1] * t.K[i2 * n + i2];
+      for (int j = 0; j < n; ++j)
+        if (j != i2) row[r++] = t.w[i1] * t.K[i2 * n + j];
+      for (int j = 0; j < n; ++j)
+        if (j != i1) row[r++] = t.w[i2] * t.K[i1 * n + j];
+    }
+  return SIPG_OK;
+}
+
 sipg_status sipg_square_mesh_coords(int dim, double* x, double* y) {
   if (dim < 1 || !x || !y) {
     set_error("sipg_square_mesh_coords: dim >= 1 and non-null pointers required");

@@ -9,6 +9,11 @@
 // norms are computed on the host in FLOAT_TYPE, as the reference does
 // (compute_rhs :232-305, err_norms :311-370).  With a built-in problem id
 // (FP64) both run on the device (sipg_rhs_f64, sipg_err_norms_f64).
+// Defining USE_MODE_MATRIX (the reference's stored-operator volume kernel,
+// volume_mvm<T,1> with host_laplacian_matrix) changes nothing here: the
+// stored Laplacian is the volume term the fused apply computes, so both
+// settings solve the same system (the stored form is available as
+// sipg_laplacian_rows_f64 + sipg_volume_mvm_f64).
 // As in the reference, defining USE_PRECONDITIONER before including this
 // header makes the solve the block-Jacobi preconditioned CG and _prec_mvm the
 // block-Jacobi preconditioner (sipg_apply_prec_f64 / sipg_pcg_f64; FP64);

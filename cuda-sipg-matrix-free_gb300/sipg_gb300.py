@@ -94,6 +94,7 @@ _VP = C.c_void_p
 _SIGS = {
     "sipg_lgl_table": (C.c_int, [C.c_int, _VP, _VP]),
     "sipg_dphi_table": (C.c_int, [C.c_int, _VP]),
+    "sipg_laplacian_rows_f64": (C.c_int, [C.c_int, _VP]),
     "sipg_square_mesh_coords": (C.c_int, [C.c_int, _VP, _VP]),
     "sipg_op_create": (C.c_int, [C.c_int, C.c_int, C.c_double, C.POINTER(_VP)]),
     "sipg_op_destroy": (C.c_int, [_VP]),
@@ -165,6 +166,16 @@ def _stream(stream=None):
     import torch
 
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def laplacian_rows(degree):
+    """The element Laplacian's stored rows (numpy, (p+1)^2 * (2p+1) values):
+    the mode_matrix of the reference's host_laplacian_matrix(1, p), for
+    volume_mvm."""
+    n, R = degree + 1, 2 * degree + 1
+    rows = np.zeros(n * n * R)
+    _check(lib().sipg_laplacian_rows_f64(int(degree), rows.ctypes.data), "laplacian_rows")
+    return rows
 
 
 def volume_mvm(dim, degree, mat, x, out=None, stream=None):

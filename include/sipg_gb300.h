@@ -109,6 +109,14 @@ sipg_status sipg_lgl_table(int npts, double* nodes, double* weights);
  * degree 1..63.
  * Replaces sem_function<T>::d_phi / DbaseVALUES (sem_function.hpp:86-110, device_const.hpp:115-127). */
 sipg_status sipg_dphi_table(int degree, double* D);
+/* The element Laplacian as stored rows: (p+1)^2 rows of 2p+1 values on the
+ * (i1,.) / (.,i2) cross pattern (the diagonal, then (i1, j != i2), then
+ * (j != i1, i2)), in the mode_matrix layout of one shared operator -- value r
+ * of row (i1,i2) at (i1*(p+1)+i2)*(2p+1) + r -- the d_mat of
+ * sipg_volume_mvm_f64 with mat_noe = 1.  Host memory.
+ * Replaces host_laplacian_matrix<T>(1, p) (mode_matrix.hpp:419-466) with
+ * laplace_2d<T> (laplacian_operator.hpp:67-88). */
+sipg_status sipg_laplacian_rows_f64(int degree, double* rows);
 /* Element corner coordinates x[c*noe+e], y[c*noe+e], c=0..3.
  * Replaces square_mesh<T>::compute_coordinates (build_square_mesh.hpp:250-288). */
 sipg_status sipg_square_mesh_coords(int dim, double* x, double* y);

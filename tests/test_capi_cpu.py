@@ -60,6 +60,30 @@ def test_host_tables_match_reference(built_lib, golden):
         assert np.max(np.abs(D - ref)) <= 2e-14 * np.max(np.abs(ref)), p
 
 
+def _rows_from_laplace2d(L, p):
+    """The mode_matrix rows of host_laplacian_matrix (mode_matrix.hpp:428-463)
+    from the reference's laplace_2d values L[i1, i2, j1, j2]."""
+    n = p + 1
+    L = L.reshape(n, n, n, n)
+    rows = []
+    for i1 in range(n):
+        for i2 in range(n):
+            rows.append(L[i1, i2, i1, i2])
+            rows += [L[i1, i2, i1, j] for j in range(n) if j != i2]
+            rows += [L[i1, i2, j, i2] for j in range(n) if j != i1]
+    return np.array(rows)
+
+
+def test_laplacian_rows_match_reference(built_lib, golden):
+    # the stored element Laplacian against the reference's own laplace_2d
+    # values (tests/golden, from its code)
+    for p in range(1, 9):
+        rows = built_lib.laplacian_rows(p)
+        ref = _rows_from_laplace2d(golden["laplace2d_%d" % p], p)
+        assert rows.shape == ref.shape
+        assert np.max(np.abs(rows - ref)) <= 1e-13 * np.max(np.abs(ref)), p
+
+
 def test_mesh_coords_match_reference(built_lib, golden):
     for d in (1, 2, 3, 16):
         x, y = built_lib.square_mesh_coords(d)

@@ -131,7 +131,8 @@ def _laplacian_rows(oracle, p):
 def test_stored_operator_apply_matches_reference(sipg, oracle, golden, torch, p):
     # the reference's volume_mvm<T,1> with the Laplacian mode matrix, on the
     # golden inputs (tests/golden: its outputs, from the reference's code)
-    rows = torch.from_numpy(_laplacian_rows(oracle, p)).cuda()
+    rows = torch.from_numpy(sipg.laplacian_rows(p)).cuda()  # the product's builder
+    assert np.max(np.abs(rows.cpu().numpy() - _laplacian_rows(oracle, p))) <= 1e-13 * rows.abs().max().item()
     for d in (1, 2, 3):
         x = golden["apply_in_%d_%d" % (p, d)]
         y = sipg.volume_mvm(d, p, rows, torch.from_numpy(x).cuda()).cpu().numpy()
