@@ -602,9 +602,10 @@ static cudaError_t copy_rows(double* dst, const double* src, const sipg_op* op, 
 // y = A x with host buffers, pipelined over bands of element rows: the
 // copy-in of band b + 1, the apply of band b (two compute streams, so one
 // band's tail overlaps the next band's start) and the copy-out of band b - 1
-// run at once.  Band b's apply waits for its own rows and for the first row
-// of band b + 1 (its halo below; the row above arrived with band b - 1).
-// Synchronous: returns when h_out is written.
+// run at once.  Band b's copy-in carries one row more -- the first row of
+// band b + 1, its halo below (the row above arrived with band b - 1) -- so its
+// apply waits for its own copy only.  Synchronous: returns when h_out is
+// written.
 sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream) {
   if (!op || !h_in || !h_out) {
     set_error("sipg_apply_host_f64: null argument");
@@ -614,11 +615,18 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = (size_t)op->ndof * sizeof(double);
   constexpr int kMaxBands = 16;
-  // bands of a multiple of 8 rows (every tile's rows divide 8), ~64 rows
-  // each: measured at 1024^2, p = 4, 8 bands reach 15.3 GDoF/s end to end,
-  // 16 bands 16.7, 32 bands 11.7 (per-copy overheads)
-  const int nb = std::max(1, std::min(kMaxBands, op->dim / 64));
-  const int band_rows = ((op->dim + nb - 1) / nb + 7) / 8 * 8;
+  // equal bands of a multiple of 8 rows (every tile's rows divide 8), ~64
+  // rows each.  Measured at 1024^2, p = 4, end to end: 8 bands 15.3 GDoF/s,
+  // 16 bands 16.9, 32 bands 11.7; 16-row first and last bands (a faster fill
+  // and drain on paper) 11.5
+  int bounds[kMaxBands + 1];
+  int nb = 0;
+  {
+    const int n = std::max(1, std::min(kMaxBands, op->dim / 64));
+    const int rows = ((op->dim + n - 1) / n + 7) / 8 * 8;
+    for (int r = 0; r < op->dim; r += rows) bounds[nb++] = r;
+    bounds[nb] = op->dim;
+  }
   std::lock_guard<std::mutex> lk(op->mu);  // the staging buffers and streams are per op
   if (!op->stage_in) SIPG_CUDA_TRY(cudaMalloc(&op->stage_in, bytes));
   if (!op->stage_out) SIPG_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
@@ -627,24 +635,21 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
     for (cudaEvent_t& e : op->hev) SIPG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   cudaStream_t s_in = op->hs[0], s_out = op->hs[1];
-  cudaEvent_t* ev_in = op->hev;              // [kMaxBands]: band b's rows are on the device
+  cudaEvent_t* ev_in = op->hev;                // [kMaxBands]: band b's rows (and its halo row) are on the device
   cudaEvent_t* ev_done = op->hev + kMaxBands;  // [kMaxBands]: band b's outputs are written
   cudaEvent_t ev_start = op->hev[2 * kMaxBands], ev_end = op->hev[2 * kMaxBands + 1];
   // everything starts after the work already queued on the caller's stream
   SIPG_CUDA_TRY(cudaEventRecord(ev_start, s));
   for (int k = 0; k < 4; ++k) SIPG_CUDA_TRY(cudaStreamWaitEvent(op->hs[k], ev_start, 0));
-  int r0 = 0;
-  for (int b = 0; r0 < op->dim; ++b, r0 += band_rows) {
-    const int r1 = std::min(op->dim, r0 + band_rows);
+  for (int b = 0; b < nb; ++b) {
+    const int r0 = bounds[b], r1 = std::min(op->dim, bounds[b + 1] + 1);  // + the halo row below
     SIPG_CUDA_TRY(copy_rows(op->stage_in, h_in, op, r0, r1, cudaMemcpyHostToDevice, s_in));
     SIPG_CUDA_TRY(cudaEventRecord(ev_in[b], s_in));
   }
-  r0 = 0;
-  for (int b = 0; r0 < op->dim; ++b, r0 += band_rows) {
-    const int r1 = std::min(op->dim, r0 + band_rows);
+  for (int b = 0; b < nb; ++b) {
+    const int r0 = bounds[b], r1 = bounds[b + 1];
     cudaStream_t cs = op->hs[2 + (b & 1)];
-    const bool last = r1 >= op->dim;
-    SIPG_CUDA_TRY(cudaStreamWaitEvent(cs, ev_in[last ? b : b + 1], 0));  // rows r0 .. r1 (inclusive)
+    SIPG_CUDA_TRY(cudaStreamWaitEvent(cs, ev_in[b], 0));
     ApplyArgs<double> a{};
     a.in = op->stage_in;
     a.out = op->stage_out;
