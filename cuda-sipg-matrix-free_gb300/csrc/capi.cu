@@ -140,9 +140,10 @@ static TileCfg default_cfg(int p, int dim, bool f64) {
   TileCfg c;
   c.tx = 32;
   if (f64) {
-    // 32 x TY tiles by measurement at ~16 M DoF, p = 1..8; TY = 2 at p = 6
-    // and 8, where a 32 x 4 tile's shared memory leaves too few CTAs per SM
-    static const int kRows[9] = {4, 8, 8, 8, 4, 4, 2, 4, 2};
+    // 32 x TY tiles by measurement at ~16 M DoF, p = 1..8 (p = 4: 1024^2,
+    // 24.5 GDoF/s with 8 rows against 23.9 with 4); TY = 2 at p = 6 and 8,
+    // where a 32 x 4 tile's shared memory leaves too few CTAs per SM
+    static const int kRows[9] = {4, 8, 8, 8, 8, 4, 2, 4, 2};
     c.ty = kRows[p >= 1 && p <= 8 ? p : 0];
     if (dim <= kPernodeDefaultDim) c = pernode_tile(p, dim <= kPernodeWideDim ? 0 : 1);
   } else {

@@ -95,7 +95,7 @@ def test_pernode_tile_gives_identical_applies(sipg, torch, p, d):
     if d <= sipg.PERNODE_DEFAULT_DIM:
         assert op.get_shape("f64") == pernode(p, 0 if d <= sipg.PERNODE_WIDE_DIM else 1)
     else:
-        assert op.get_shape("f64") == (32, {1: 8, 2: 8, 3: 8, 4: 4, 5: 4, 6: 2, 7: 4, 8: 2}[p], 1)
+        assert op.get_shape("f64") == (32, {1: 8, 2: 8, 3: 8, 4: 8, 5: 4, 6: 2, 7: 4, 8: 2}[p], 1)
     op.set_pernode(0)
     g = torch.Generator(device="cuda").manual_seed(100 + p)
     x = torch.rand(op.ndof, device="cuda", dtype=torch.float64, generator=g) * 2 - 1
