@@ -168,6 +168,7 @@ struct sipg_cg_workspace {
   void* r = nullptr;
   void* p[2] = {nullptr, nullptr};
   void* Ap = nullptr;
+  void* bar = nullptr;     // the persistent small-mesh CG's barrier counter and abort flag
   void* st = nullptr;      // CgState<T>
   void* st_host = nullptr; // pinned mirror
   ReduceScratch red;
@@ -186,6 +187,7 @@ static void ws_free(sipg_cg_workspace* w) {
   cudaFree(w->p[0]);
   cudaFree(w->p[1]);
   cudaFree(w->Ap);
+  cudaFree(w->bar);
   cudaFree(w->st);
   cudaFreeHost(w->st_host);
   cudaFree(w->red.partials);
@@ -333,8 +335,15 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   const long long mx = (max_it > 0) ? max_it : op->ndof;
   const int max_i = (int)std::min<long long>(mx, 2000000000LL);
   const int K = graph_iters(op->ndof);
-  st = capture_iterations<T>(op, w, x, K);
-  if (st != SIPG_OK) return st;
+  // small FP64 meshes on the per-node tile: one persistent kernel runs every
+  // iteration (cg_small.cu); otherwise graphs of K iterations
+  const bool small = sizeof(T) == 8 && is_pernode(op->cfg64, op->p) && op->dim <= kPernodeDefaultDim;
+  if (!small) {
+    st = capture_iterations<T>(op, w, x, K);
+    if (st != SIPG_OK) return st;
+  } else if (!w->bar) {
+    SIPG_CUDA_TRY(cudaMalloc(&w->bar, 256));
+  }
   SIPG_CUDA_TRY(cudaEventRecord(w->ev0, s));
   k_cg_init<T><<<vec_blocks(w->n), kVecThreads, 0, s>>>(b, w->n, (CgState<T>*)w->st, tol, rel, max_i, w->red);
   count_launch();
@@ -350,7 +359,30 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   SIPG_CUDA_TRY(launch_apply<T>(op, APPLY_RESID, a, s));
   CgState<T>* hs = (CgState<T>*)w->st_host;
   long long launched = 0;
-  for (;;) {
+  if (small) {
+    SIPG_CUDA_TRY(cudaMemsetAsync(w->bar, 0, 256, s));
+    SmallCgArgs g;
+    g.x = (double*)x;
+    g.r = (double*)w->r;
+    g.p0 = (double*)w->p[0];
+    g.p1 = (double*)w->p[1];
+    g.Ap = (double*)w->Ap;
+    g.st = (CgState<double>*)w->st;
+    g.part_a = w->red.partials;
+    g.part_b = w->red.partials + kSmallCgMaxBlocks;
+    g.bar = (unsigned long long*)w->bar;
+    g.abort = (int*)((char*)w->bar + 128);
+    g.dim = op->dim;
+    g.nu = op->pen;
+    SIPG_CUDA_TRY(launch_cg_small(op->p, op->cfg64, g, op->tab, s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(hs, w->st, sizeof(CgState<T>), cudaMemcpyDeviceToHost, s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs->status == (int)SIPG_ERR_CUDA) {
+      set_error("sipg_cg: a grid barrier of the persistent CG gave up waiting");
+      return SIPG_ERR_CUDA;
+    }
+  }
+  for (; !small;) {
     SIPG_CUDA_TRY(cudaGraphLaunch(w->exec, s));
     count_launch((cg_fused_direction<T>(op) ? 2ULL : 3ULL) * K);
     launched += K;

@@ -52,15 +52,178 @@ struct PernodeShape {
   static constexpr int NY = EX * (EY + 1) * N1;        // y-face nodes: [EY+1][EX][N1]
 };
 
+// The CTA's shared memory: the nodal blocks of its tile and halo ring, the
+// face values, and the tables.
+template <typename T, int P, int SHAPE>
+struct PernodeSmem {
+  using S = PernodeShape<P, SHAPE>;
+  T us[S::SX * S::SY * S::NN];  // slot (sy, sx) = element (y0 - 1 + sy, x0 - 1 + sx), values [i1 * N1 + i2]
+  T xj[S::NX], xq[S::NX], yj[S::NY], yq[S::NY];
+  T tw[S::N1], twh[S::N1], td0[S::N1], tdn[S::N1], tkw[S::NN * S::N1];
+};
+
+// The tables into shared memory (indexed per thread below: a constant-bank
+// read whose address differs across the warp would serialise).  The caller
+// synchronises before their first use.
+template <typename T, int P, int SHAPE>
+__device__ __forceinline__ void pernode_tables(PernodeSmem<T, P, SHAPE>& sm, const Tab<T, P>& tb) {
+  using S = PernodeShape<P, SHAPE>;
+  const int t = threadIdx.x;
+  for (int k = t; k < S::NN * S::N1; k += S::NT) sm.tkw[k] = tb.KW[k];
+  if (t < S::N1) {
+    sm.tw[t] = tb.w[t];
+    sm.twh[t] = tb.WH[t];
+    sm.td0[t] = tb.D0[t];
+    sm.tdn[t] = tb.DN[t];
+  }
+}
+
+// One tile (origin x0, y0): phases 0-2, returning this thread's share of the
+// reduction (p.Ap in the CG / DOT modes, r.r in the residual mode).
+// kCoherent: read a.in and pold through L2 only -- for a caller that runs
+// while other CTAs of the same grid write them (the persistent CG).
+template <typename T, int P, int SHAPE, int MODE, bool kCoherent>
+__device__ __forceinline__ T pernode_tile(const ApplyArgs<T>& a, PernodeSmem<T, P, SHAPE>& sm, int x0, int y0,
+                                          bool first, T beta, const T* __restrict__ pold, T* __restrict__ pnew) {
+  using S = PernodeShape<P, SHAPE>;
+  constexpr int N = P, N1 = S::N1, NN = S::NN, EX = S::EX, NE = S::NE, NT = S::NT;
+  constexpr int SX = S::SX, SY = S::SY, NX = S::NX, NY = S::NY, NSLOT = SX * SY;
+  constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);
+  T* __restrict__ us = sm.us;
+  T* __restrict__ xj = sm.xj;
+  T* __restrict__ xq = sm.xq;
+  T* __restrict__ yj = sm.yj;
+  T* __restrict__ yq = sm.yq;
+  const T* __restrict__ tw = sm.tw;
+  const T* __restrict__ twh = sm.twh;
+  const T* __restrict__ td0 = sm.td0;
+  const T* __restrict__ tdn = sm.tdn;
+  const T* __restrict__ tkw = sm.tkw;
+  const int t = threadIdx.x;
+  const int dim = a.dim;
+  const size_t noe = (size_t)dim * dim;
+  const T nu = a.nu;
+  auto ldin = [&](const T* p) -> T { return kCoherent ? __ldcg(p) : __ldg(p); };
+  T acc = T(0);
+  // ---- phase 0: nodal blocks ------------------------------------------------
+  for (int idx = t; idx < NSLOT * NN; idx += NT) {
+    const int k = idx / NSLOT, sl = idx - k * NSLOT;
+    const int sy = sl / SX, sx = sl - sy * SX;
+    const int gx = x0 - 1 + sx, gy = y0 - 1 + sy;
+    const bool corner = (sx == 0 || sx == SX - 1) && (sy == 0 || sy == SY - 1);
+    T v = T(0);
+    if (!corner && gx >= 0 && gx < dim && gy >= 0 && gy < dim) {
+      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+      v = ldin(a.in + gk);
+      if (MODE == APPLY_CG && !first) v = fma(beta, ldin(pold + gk), v);
+    }
+    us[sl * NN + k] = v;
+  }
+  __syncthreads();
+
+  // ---- phase 1: J and Q of every face node of the tile -----------------------
+  for (int f = t; f < NX + NY; f += NT) {
+    T u0 = T(0), d0 = T(0), uN = T(0), dN = T(0);
+    bool zv, nv;  // 0-side / N-side element inside the mesh
+    int j;
+    if (f < NX) {
+      // x face fx of tile row ey: the left element (slot fx) is its N-side
+      // (i1 = P), the right element (slot fx + 1) its 0-side (i1 = 0)
+      j = f % N1;
+      const int r = f / N1, fx = r % (EX + 1), ey = r / (EX + 1);
+      const int gy = y0 + ey, gxl = x0 + fx - 1;
+      nv = gy < dim && gxl >= 0 && gxl < dim;
+      zv = gy < dim && gxl + 1 < dim;
+      const T* L = us + ((ey + 1) * SX + fx) * NN;
+      const T* R = L + NN;
+      if (zv) {
+        u0 = R[j];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], R[i * N1 + j], d0);
+      }
+      if (nv) {
+        uN = L[N * N1 + j];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], L[i * N1 + j], dN);
+      }
+    } else {
+      // y face fy of tile column ex: the upper element (slot row fy) is its
+      // 0-side (i2 = 0), the lower element (slot row fy + 1) its N-side (i2 = P)
+      const int g = f - NX;
+      j = g % N1;
+      const int r = g / N1, ex = r % EX, fy = r / EX;
+      const int gx = x0 + ex, gyu = y0 + fy - 1;
+      zv = gx < dim && gyu >= 0 && gyu < dim;
+      nv = gx < dim && gyu + 1 < dim;
+      const T* Up = us + (fy * SX + ex + 1) * NN;
+      const T* Dn = Up + SX * NN;
+      if (zv) {
+        u0 = Up[j * N1];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) d0 = fma(td0[i], Up[j * N1 + i], d0);
+      }
+      if (nv) {
+        uN = Dn[j * N1 + N];
+#pragma unroll
+        for (int i = 0; i < N1; ++i) dN = fma(tdn[i], Dn[j * N1 + i], dN);
+      }
+    }
+    T J, Q;
+    face_combine<T>(tw[j], twh[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
+    if (f < NX) {
+      xj[f] = J;
+      xq[f] = Q;
+    } else {
+      yj[f - NX] = J;
+      yq[f - NX] = Q;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 2: one output node per thread ------------------------------------
+  if (t < NE * NN) {
+    const int le = t % NE, k = t / NE;  // element fastest: neighbouring threads store neighbouring elements
+    const int ex = le % EX, ey = le / EX;
+    const int i1 = k / N1, j = k - i1 * N1;
+    const int gx = x0 + ex, gy = y0 + ey;
+    if (gx < dim && gy < dim) {
+      const T* E = us + ((ey + 1) * SX + ex + 1) * NN;
+      const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
+      const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
+      const int fu = fd - EX * N1;
+      const bool xf = (i1 == 0) || (i1 == N);
+      const T seed = face_seed<T, N>(i1, j, xf ? xq[fl + j] : T(0), xf ? xq[fl + N1 + j] : T(0),
+                                     (j == 0) ? yq[fd + i1] : T(0), (j == N) ? yq[fu + i1] : T(0));
+      T v = fma(td0[i1], xj[fl + j], fma(tdn[i1], xj[fl + N1 + j], seed));
+#pragma unroll
+      for (int i = 0; i < N1; ++i) v = fma(tkw[(i1 * N1 + i) * N1 + j], E[i * N1 + j], v);
+#pragma unroll
+      for (int i = 0; i < N1; ++i) v = fma(tkw[(j * N1 + i) * N1 + i1], E[i1 * N1 + i], v);
+      v = fma(td0[j], yj[fd + i1], v);
+      v = fma(tdn[j], yj[fu + i1], v);
+      const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
+      if (MODE == APPLY_RESID) {
+        const T rv = __ldg(a.b + gk) - v;
+        a.out[gk] = rv;
+        acc = fma(rv, rv, acc);
+      } else {
+        a.out[gk] = v;
+        const T c = E[k];
+        if (MODE == APPLY_CG) pnew[gk] = c;
+        if (kDot) acc = fma(c, v, acc);
+      }
+    }
+  }
+  __syncthreads();  // the next tile overwrites the shared memory
+  return acc;
+}
+
 template <typename T, int P, int SHAPE, int MODE>
 __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
     k_sipg_apply_pernode(const __grid_constant__ ApplyArgs<T> a, const __grid_constant__ Tab<T, P> tb) {
   using S = PernodeShape<P, SHAPE>;
-  constexpr int N = P, N1 = S::N1, NN = S::NN, EX = S::EX, EY = S::EY, NE = S::NE, NT = S::NT;
-  constexpr int SX = S::SX, SY = S::SY, NX = S::NX, NY = S::NY, NSLOT = SX * SY;
-  __shared__ T us[NSLOT * NN];  // slot (sy, sx) = element (y0 - 1 + sy, x0 - 1 + sx), values [i1 * N1 + i2]
-  __shared__ T xj[NX], xq[NX], yj[NY], yq[NY];
-  __shared__ T tw[N1], twh[N1], td0[N1], tdn[N1], tkw[NN * N1];
+  constexpr int EX = S::EX, EY = S::EY, NT = S::NT;
+  __shared__ PernodeSmem<T, P, SHAPE> sm;
   __shared__ T red_sh[32];
 
   constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);
@@ -69,7 +232,6 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   }
   const int t = threadIdx.x;
   const int dim = a.dim;
-  const size_t noe = (size_t)dim * dim;
   const int rows = a.nrows > 0 ? a.nrows : dim;  // a band of element rows from a.row0
   const int tiles_x = (dim + EX - 1) / EX, ntiles = tiles_x * ((rows + EY - 1) / EY);
 
@@ -83,135 +245,14 @@ __global__ void __launch_bounds__(PernodeShape<P, SHAPE>::NT)
   }
   const T* __restrict__ pold = par ? a.pbuf1 : a.pbuf0;
   T* __restrict__ pnew = par ? a.pbuf0 : a.pbuf1;
-
-  // the tables, indexed per thread below (a constant-bank read whose address
-  // differs across the warp would serialise)
-  for (int k = t; k < NN * N1; k += NT) tkw[k] = tb.KW[k];
-  if (t < N1) {
-    tw[t] = tb.w[t];
-    twh[t] = tb.WH[t];
-    td0[t] = tb.D0[t];
-    tdn[t] = tb.DN[t];
-  }
-  const T nu = a.nu;
+  pernode_tables<T, P, SHAPE>(sm, tb);
   T acc = T(0);
-
   // the CTA's tiles: blockIdx.x, + gridDim.x, ... (the grid is at most the
   // resident CTAs, so the reduction has few partials on any mesh)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int x0 = (tile % tiles_x) * EX, y0 = a.row0 + (tile / tiles_x) * EY;
-
-    // ---- phase 0: nodal blocks ------------------------------------------------
-    for (int idx = t; idx < NSLOT * NN; idx += NT) {
-      const int k = idx / NSLOT, sl = idx - k * NSLOT;
-      const int sy = sl / SX, sx = sl - sy * SX;
-      const int gx = x0 - 1 + sx, gy = y0 - 1 + sy;
-      const bool corner = (sx == 0 || sx == SX - 1) && (sy == 0 || sy == SY - 1);
-      T v = T(0);
-      if (!corner && gx >= 0 && gx < dim && gy >= 0 && gy < dim) {
-        const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
-        v = __ldg(a.in + gk);
-        if (MODE == APPLY_CG && !first) v = fma(beta, __ldg(pold + gk), v);
-      }
-      us[sl * NN + k] = v;
-    }
-    __syncthreads();
-
-    // ---- phase 1: J and Q of every face node of the tile -----------------------
-    for (int f = t; f < NX + NY; f += NT) {
-      T u0 = T(0), d0 = T(0), uN = T(0), dN = T(0);
-      bool zv, nv;  // 0-side / N-side element inside the mesh
-      int j;
-      if (f < NX) {
-        // x face fx of tile row ey: the left element (slot fx) is its N-side
-        // (i1 = P), the right element (slot fx + 1) its 0-side (i1 = 0)
-        j = f % N1;
-        const int r = f / N1, fx = r % (EX + 1), ey = r / (EX + 1);
-        const int gy = y0 + ey, gxl = x0 + fx - 1;
-        nv = gy < dim && gxl >= 0 && gxl < dim;
-        zv = gy < dim && gxl + 1 < dim;
-        const T* L = us + ((ey + 1) * SX + fx) * NN;
-        const T* R = L + NN;
-        if (zv) {
-          u0 = R[j];
-#pragma unroll
-          for (int i = 0; i < N1; ++i) d0 = fma(td0[i], R[i * N1 + j], d0);
-        }
-        if (nv) {
-          uN = L[N * N1 + j];
-#pragma unroll
-          for (int i = 0; i < N1; ++i) dN = fma(tdn[i], L[i * N1 + j], dN);
-        }
-      } else {
-        // y face fy of tile column ex: the upper element (slot row fy) is its
-        // 0-side (i2 = 0), the lower element (slot row fy + 1) its N-side (i2 = P)
-        const int g = f - NX;
-        j = g % N1;
-        const int r = g / N1, ex = r % EX, fy = r / EX;
-        const int gx = x0 + ex, gyu = y0 + fy - 1;
-        zv = gx < dim && gyu >= 0 && gyu < dim;
-        nv = gx < dim && gyu + 1 < dim;
-        const T* Up = us + (fy * SX + ex + 1) * NN;
-        const T* Dn = Up + SX * NN;
-        if (zv) {
-          u0 = Up[j * N1];
-#pragma unroll
-          for (int i = 0; i < N1; ++i) d0 = fma(td0[i], Up[j * N1 + i], d0);
-        }
-        if (nv) {
-          uN = Dn[j * N1 + N];
-#pragma unroll
-          for (int i = 0; i < N1; ++i) dN = fma(tdn[i], Dn[j * N1 + i], dN);
-        }
-      }
-      T J, Q;
-      face_combine<T>(tw[j], twh[j], nu, zv && nv, u0, d0, uN, dN, J, Q);
-      if (f < NX) {
-        xj[f] = J;
-        xq[f] = Q;
-      } else {
-        yj[f - NX] = J;
-        yq[f - NX] = Q;
-      }
-    }
-    __syncthreads();
-
-    // ---- phase 2: one output node per thread ------------------------------------
-    if (t < NE * NN) {
-      const int le = t % NE, k = t / NE;  // element fastest: neighbouring threads store neighbouring elements
-      const int ex = le % EX, ey = le / EX;
-      const int i1 = k / N1, j = k - i1 * N1;
-      const int gx = x0 + ex, gy = y0 + ey;
-      if (gx < dim && gy < dim) {
-        const T* E = us + ((ey + 1) * SX + ex + 1) * NN;
-        const int fl = (ey * (EX + 1) + ex) * N1;  // left x face; the right one is fl + N1
-        const int fd = ((ey + 1) * EX + ex) * N1;  // down y face; the up one is fd - EX * N1
-        const int fu = fd - EX * N1;
-        const bool xf = (i1 == 0) || (i1 == N);
-        const T seed = face_seed<T, N>(i1, j, xf ? xq[fl + j] : T(0), xf ? xq[fl + N1 + j] : T(0),
-                                       (j == 0) ? yq[fd + i1] : T(0), (j == N) ? yq[fu + i1] : T(0));
-        T v = fma(td0[i1], xj[fl + j], fma(tdn[i1], xj[fl + N1 + j], seed));
-#pragma unroll
-        for (int i = 0; i < N1; ++i) v = fma(tkw[(i1 * N1 + i) * N1 + j], E[i * N1 + j], v);
-#pragma unroll
-        for (int i = 0; i < N1; ++i) v = fma(tkw[(j * N1 + i) * N1 + i1], E[i1 * N1 + i], v);
-        v = fma(td0[j], yj[fd + i1], v);
-        v = fma(tdn[j], yj[fu + i1], v);
-        const size_t gk = (size_t)k * noe + (size_t)gy * dim + gx;
-        if (MODE == APPLY_RESID) {
-          const T rv = __ldg(a.b + gk) - v;
-          a.out[gk] = rv;
-          acc = fma(rv, rv, acc);
-        } else {
-          a.out[gk] = v;
-          const T c = E[k];
-          if (MODE == APPLY_CG) pnew[gk] = c;
-          if (kDot) acc = fma(c, v, acc);
-        }
-      }
-    }
-    __syncthreads();  // the next tile overwrites the shared memory
-  }  // tiles
+    acc += pernode_tile<T, P, SHAPE, MODE, false>(a, sm, x0, y0, first, beta, pold, pnew);
+  }
 
   if (MODE != APPLY_PLAIN) {
     const T bt = block_sum<T, NT>(acc, red_sh);

@@ -182,6 +182,26 @@ cudaError_t launch_apply_batched_f32(int p, const TileCfg& cfg, int mode, const 
 // degree-p operators; modes APPLY_PREPARE / PLAIN / CG.
 cudaError_t launch_apply_df(int p, const TileCfg& cfg, int mode, const ApplyArgs<float>& a, const ApplyArgs<float>* insts,
                             const int* tile_start, int ninst, int total_tiles, const HostTables& h, cudaStream_t s);
+// The persistent CG of small FP64 meshes (cg_small.cu): operands, and its
+// launch for an operator whose FP64 tile is a per-node one.  At most
+// kSmallCgMaxBlocks CTAs (two partial slots each in the reduction scratch).
+struct SmallCgArgs {
+  double* x;
+  double* r;
+  double* p0;
+  double* p1;
+  double* Ap;
+  CgState<double>* st;  // read at the start (after the residual kernel), written back at the end
+  double* part_a;       // [gridDim.x] p.Ap partials
+  double* part_b;       // [gridDim.x] r.r partials
+  unsigned long long* bar;  // barrier arrivals (zero at launch)
+  int* abort;           // raised when a barrier wait gives up (zero at launch)
+  int dim;
+  double nu;
+};
+constexpr int kSmallCgMaxBlocks = 152 * 8;
+cudaError_t launch_cg_small(int p, const TileCfg& cfg, const SmallCgArgs& g, const HostTables& h, cudaStream_t s);
+
 // Tile shapes the autotuner chose for (degree, dim, precision) in this
 // process; false if none (autotune.cu).
 bool autotune_lookup(int p, int dim, int prec, TileCfg* cfg);
