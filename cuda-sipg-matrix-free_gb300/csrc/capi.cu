@@ -336,8 +336,11 @@ static sipg_status cg_solve(sipg_op* op, T* x, const T* b, T tol, int rel, int m
   const int max_i = (int)std::min<long long>(mx, 2000000000LL);
   const int K = graph_iters(op->ndof);
   // small FP64 meshes on the per-node tile: one persistent kernel runs every
-  // iteration (cg_small.cu); otherwise graphs of K iterations
-  const bool small = sizeof(T) == 8 && is_pernode(op->cfg64, op->p) && op->dim <= kPernodeDefaultDim;
+  // iteration (cg_small.cu); otherwise graphs of K iterations.  Measured at
+  // p = 4: the persistent kernel is faster up to 32 x 32 (16^2: 1.80 against
+  // 2.2 ms), slower at 64 x 64 (12.2 against 9.9 ms: hundreds of CTAs meet at
+  // each grid barrier)
+  const bool small = sizeof(T) == 8 && is_pernode(op->cfg64, op->p) && op->dim <= kSmallCgDim;
   if (!small) {
     st = capture_iterations<T>(op, w, x, K);
     if (st != SIPG_OK) return st;

@@ -1,4 +1,5 @@
-// cg_small.cu -- CG on small FP64 meshes as one persistent kernel.
+// cg_small.cu -- CG on small FP64 meshes (up to kSmallCgDim elements per
+// edge) as one persistent kernel.
 //
 // On a mesh of a few hundred elements an iteration of the graph-driven CG
 // (capi.cu) is two short kernels whose cost is launch and reduction latency:

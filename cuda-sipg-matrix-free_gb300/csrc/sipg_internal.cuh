@@ -200,6 +200,7 @@ struct SmallCgArgs {
   double nu;
 };
 constexpr int kSmallCgMaxBlocks = 152 * 8;
+constexpr int kSmallCgDim = 32;  // meshes up to this many elements per edge use it
 cudaError_t launch_cg_small(int p, const TileCfg& cfg, const SmallCgArgs& g, const HostTables& h, cudaStream_t s);
 
 // Tile shapes the autotuner chose for (degree, dim, precision) in this
