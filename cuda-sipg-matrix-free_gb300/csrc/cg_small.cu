@@ -28,7 +28,10 @@
 
 namespace sipg {
 
-constexpr unsigned kBarrierSpins = 1u << 22;  // x ~32 ns sleeps between polls: well under a second
+// polls of the arrival count (an L2 round trip, ~0.7 us, and a 32 ns sleep
+// each): a wait gives up after about a second; a barrier that completes
+// takes tens of polls
+constexpr unsigned kBarrierSpins = 1u << 20;
 
 // Grid barrier: every CTA arrives once; the barrier is complete when the
 // arrival count reaches `target` (the count only grows: target = barrier
@@ -199,6 +202,15 @@ cudaError_t launch_cg_small_p(const TileCfg& cfg, const SmallCgArgs& g, const Ho
   return cudaErrorInvalidConfiguration;
 }
 
+// The barrier's give-up path, for the self-test: every CTA waits for one
+// arrival more than the grid has, so each wait runs out (bounded), raises
+// the abort flag and returns; out[blockIdx.x] = 1 where the barrier reported
+// failure.
+__global__ void k_barrier_selftest(unsigned long long* bar, int* abort, int* out) {
+  const bool ok = grid_barrier(bar, abort, (unsigned long long)gridDim.x + 1ull);
+  if (threadIdx.x == 0) out[blockIdx.x] = ok ? 0 : 1;
+}
+
 cudaError_t launch_cg_small(int p, const TileCfg& cfg, const SmallCgArgs& g, const HostTables& h, cudaStream_t s) {
   switch (p) {
     case 1: return launch_cg_small_p<1>(cfg, g, h, s);
@@ -214,3 +226,35 @@ cudaError_t launch_cg_small(int p, const TileCfg& cfg, const SmallCgArgs& g, con
 }
 
 }  // namespace sipg
+
+using namespace sipg;
+
+extern "C" sipg_status sipg_selftest_barrier_timeout(int* gave_up) {
+  if (!gave_up) return SIPG_ERR_INVALID;
+  *gave_up = 0;
+  constexpr int kBlocks = 4;
+  void* mem = nullptr;
+  SIPG_CUDA_TRY(cudaMalloc(&mem, 512));
+  unsigned long long* bar = (unsigned long long*)mem;
+  int* abort = (int*)((char*)mem + 128);
+  int* out = (int*)((char*)mem + 256);
+  cudaError_t e = cudaMemset(mem, 0, 512);
+  if (e == cudaSuccess) {
+    void* args[] = {(void*)&bar, (void*)&abort, (void*)&out};
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(kBlocks), dim3(32), args, 0, nullptr);
+    count_launch();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int h_out[kBlocks] = {0, 0, 0, 0}, h_abort = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(h_out, out, sizeof(h_out), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&h_abort, abort, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(mem);
+  if (e != cudaSuccess) {
+    set_error(std::string("sipg_selftest_barrier_timeout: ") + cudaGetErrorString(e));
+    return SIPG_ERR_CUDA;
+  }
+  int n = 0;
+  for (int v : h_out) n += v;
+  *gave_up = (n == kBlocks && h_abort == 1) ? 1 : 0;
+  return SIPG_OK;
+}

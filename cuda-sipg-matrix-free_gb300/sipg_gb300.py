@@ -95,6 +95,7 @@ _SIGS = {
     "sipg_lgl_table": (C.c_int, [C.c_int, _VP, _VP]),
     "sipg_dphi_table": (C.c_int, [C.c_int, _VP]),
     "sipg_laplacian_rows_f64": (C.c_int, [C.c_int, _VP]),
+    "sipg_selftest_barrier_timeout": (C.c_int, [C.POINTER(C.c_int)]),
     "sipg_square_mesh_coords": (C.c_int, [C.c_int, _VP, _VP]),
     "sipg_op_create": (C.c_int, [C.c_int, C.c_int, C.c_double, C.POINTER(_VP)]),
     "sipg_op_destroy": (C.c_int, [_VP]),
@@ -166,6 +167,14 @@ def _stream(stream=None):
     import torch
 
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def selftest_barrier_timeout():
+    """True when the persistent CG's grid barrier gives up on a wait that
+    cannot complete (the abort path) and the device stays usable."""
+    g = C.c_int(0)
+    _check(lib().sipg_selftest_barrier_timeout(C.byref(g)), "selftest_barrier_timeout")
+    return bool(g.value)
 
 
 def laplacian_rows(degree):

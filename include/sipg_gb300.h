@@ -349,6 +349,13 @@ sipg_status sipg_server_solution(sipg_server* server, unsigned long long id, dou
 sipg_status sipg_server_release(sipg_server* server, unsigned long long id);
 sipg_status sipg_server_stats(const sipg_server* server, sipg_server_stats_t* stats);
 
+/* Self-test of the bounded waits of the persistent small-mesh CG: runs its
+ * grid barrier with a target that no arrival count reaches, on 4 CTAs.  Every
+ * wait gives up (well under a second), raises the abort flag and returns;
+ * *gave_up = 1 when all four did and the context is still usable.  No
+ * reference counterpart. */
+sipg_status sipg_selftest_barrier_timeout(int* gave_up);
+
 /* ---- either side of the solve ---- */
 
 /* d_b = the right-hand side of test problem `sol` (f term + Nitsche terms of

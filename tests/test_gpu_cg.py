@@ -194,3 +194,16 @@ def test_mixed_auto_picks_f32_for_well_conditioned(sipg, torch):
     st, rm = op.solve_mixed(x, b)
     assert st == 0 and rm.inner_kind == 1 and rm.rel_residual <= 1e-10
     op.close()
+
+
+def test_persistent_cg_barrier_gives_up_and_device_stays_usable(sipg, torch):
+    """The persistent small-mesh CG's grid barrier with a target no arrival
+    count reaches: every CTA's bounded wait runs out and reports it (no fault,
+    no hang), and the next solve runs normally."""
+    assert sipg.selftest_barrier_timeout()
+    op = sipg.Operator(16, 4, 16.0)
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    st, res = op.cg(x, b, 1e-12, relative=True)
+    assert st == 0 and res.converged == 1 and abs(res.iterations - 136) <= 1
+    op.close()
