@@ -146,6 +146,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The largest of `value` over the ranks of the process group (a timing:
+    the slowest rank's), or `value` itself in a single process."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, units_per_step, ms):
+    """Whole-job units per second of `world` replicas that each processed
+    steps x units_per_step in the slowest replica's `ms` milliseconds."""
+    return world * steps * units_per_step / (ms * 1e-3)
+
+
 def cpu_apply_rate(seconds=10.0, max_reps=20):
     """The oracle (CPU restatement of the reference matvec) on all host threads."""
     import numpy as np
@@ -251,14 +269,11 @@ def run_ours(args):
     e1.synchronize()
     launches = sipg.launch_count() - n0
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), pg, "cuda")
     if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
         pg.barrier()
     ms_per_step = ms / args.steps
-    value = world * args.steps * APPLIES_PER_STEP * NDOF / (ms * 1e-3) / 1e9
+    value = replica_throughput(world, args.steps, APPLIES_PER_STEP * NDOF, ms) / 1e9
 
     # end to end through the public C ABI with pinned host buffers: every step
     # copies the input to the device, applies once, copies the result back
@@ -281,12 +296,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         host_apply()
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * e2e_steps * NDOF / e2e_s / 1e9
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg, "cuda")
+    e2e_value = replica_throughput(world, e2e_steps, NDOF, e2e_s * 1e3) / 1e9
     ok = bool(np.array_equal(h_out.numpy(), y.cpu().numpy()))
     copy_ms = copy_bound_ms(torch, h_in, h_out)
 
