@@ -101,3 +101,15 @@ def test_invalid_arguments_are_errors_not_crashes(built_lib):
     assert b"degree" in L.sipg_last_error()
     assert L.sipg_op_destroy(None) == 0
     assert L.sipg_op_solve_footprint(1024, 4, 0) > 6 * 26214400 * 8 - 1
+
+
+@pytest.mark.parametrize("std,defines", [("c++14", []), ("c++14", ["-DUSE_PRECONDITIONER"]),
+                                         ("c++14", ["-DUSE_MODE_MATRIX"]), ("c++17", [])])
+def test_host_api_compiles_with_the_reference_flags(tmp_path, std, defines):
+    # the reference's drivers build as C++14 with these switches; the host API
+    # headers over the C ABI must accept the same (compile only: no GPU here)
+    drv = os.path.join(ROOT, "tests", "cpp",
+                       "host_api_pcg_driver.cpp" if "-DUSE_PRECONDITIONER" in defines else "host_api_driver.cpp")
+    subprocess.check_call(["nvcc", "-std=" + std, "-O0", *defines, "-I", os.path.join(ROOT, "include"), "-I",
+                           os.path.join(ROOT, "cuda-sipg-matrix-free_gb300", "host"), "-c", drv, "-o",
+                           str(tmp_path / "drv.o")])
