@@ -147,7 +147,7 @@ static TileCfg default_cfg(int p, int dim, bool f64) {
     c.ty = kRows[p >= 1 && p <= 8 ? p : 0];
     if (dim <= kPernodeDefaultDim) c = pernode_tile(p, dim <= kPernodeWideDim ? 0 : 1);
   } else {
-    c.ty = (p <= 4) ? 8 : 4;
+    c.ty = (p == 1) ? 8 : 4;  // measured at ~16 M DoF (p = 4, 1024^2: 492 GDoF/s with 4 rows, 474 with 8)
   }
   return c;
 }

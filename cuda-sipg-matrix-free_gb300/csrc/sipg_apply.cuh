@@ -98,10 +98,20 @@ struct KwInSmem {
   static constexpr bool value = P >= 8;
 };
 
+// Where a thread keeps its element's nodal block: only the owning thread
+// reads it (halo elements come from global memory, neighbours exchange face
+// values only), so where the n^2 values fit in registers -- FP32 up to p = 4
+// (the row form, fully unrolled) -- they stay there, and the tile's shared
+// memory holds the faces alone.
+template <typename T, int P>
+struct NodalInRegs {
+  static constexpr bool value = sizeof(T) == 4 && P <= 4;
+};
+
 template <typename T, int P, int TX, int TY>
 struct ApplySmem {
   static constexpr int N1 = P + 1, NN = N1 * N1, TE = TX * TY;
-  static constexpr int US = NN * TE;                 // nodal values of the tile
+  static constexpr int US = NodalInRegs<T, P>::value ? 0 : NN * TE;  // nodal values of the tile
   static constexpr int XF = TY * 2 * N1 * (TX + 1);  // x faces [TY][2][N1][TX+1]
   static constexpr int YF = (TY + 1) * 2 * N1 * TX;  // y faces [TY+1][2][N1][TX]
   static constexpr int KW = KwInSmem<T, P>::value ? N1 * N1 * N1 : 0;
@@ -229,7 +239,10 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
     if (MODE == APPLY_CG) return first ? r : fma(beta, __ldg(pold + (size_t)k * noe + ee), r);
     return r;
   };
-  auto U = [&](int i1, int i2) -> T& { return us[(i1 * N1 + i2) * TE + t]; };
+  constexpr bool kRegs = NodalInRegs<T, P>::value;
+  static_assert(!kRegs || !kCols, "register-resident nodal blocks: row form only");
+  T ureg[kRegs ? NN : 1];  // the element's nodal block, when kRegs
+  auto U = [&](int i1, int i2) -> T& { return kRegs ? ureg[kRegs ? i1 * N1 + i2 : 0] : us[(i1 * N1 + i2) * TE + t]; };
   // a read that the compiler may not hoist out of the column loop (keeps the
   // column form's register footprint at O(n) instead of O(n^2))
   auto Uv = [&](int i1, int i2) -> T { return ((volatile T*)us)[(i1 * N1 + i2) * TE + t]; };
@@ -248,7 +261,8 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll(ApplyColumnForm<T, P>::load_unroll)
   for (int k = 0; k < NN; ++k) {
     const T v = act ? ld(k, e) : T(0);
-    us[k * TE + t] = v;
+    if (kRegs) ureg[kRegs ? k : 0] = v;
+    else us[k * TE + t] = v;
   }
   __syncthreads();
 
@@ -507,7 +521,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         } else {
           a.out[gk] = o[k];
           if (kDot) {
-            const T pk = us[k * TE + t];
+            const T pk = kRegs ? ureg[kRegs ? k : 0] : us[k * TE + t];
             if (MODE == APPLY_CG) pnew[gk] = pk;
             acc = fma(pk, o[k], acc);
           }
