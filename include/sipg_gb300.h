@@ -186,7 +186,9 @@ sipg_status sipg_op_get_tile(const sipg_op* op, int kind, int* elements_per_row,
  * conjugate_gradient_gpu.hpp:63-69) or <= tol*||b|| (tol_relative = 1), or
  * after max_it iterations (max_it <= 0: DoF, as the reference).  Replaces
  * conjugate_gradient<T> (conjugate_gradient_gpu.hpp:18-109).  Scalars stay on
- * the device; iterations run as CUDA graphs.  Returns SIPG_OK,
+ * the device; iterations run as CUDA graphs, or, for FP64 meshes up to 32 x 32
+ * on the per-node tile, as one persistent cooperative kernel whose grid
+ * barriers give up after about a second (SIPG_ERR_CUDA).  Returns SIPG_OK,
  * SIPG_ERR_NOT_CONVERGED or SIPG_ERR_BREAKDOWN; `res` may be NULL. */
 sipg_status sipg_cg_f64(sipg_op* op, double* d_x, const double* d_b, double tol, int tol_relative, int max_it,
                         sipg_cg_result* res, void* stream);
