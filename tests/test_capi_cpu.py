@@ -113,3 +113,12 @@ def test_host_api_compiles_with_the_reference_flags(tmp_path, std, defines):
     subprocess.check_call(["nvcc", "-std=" + std, "-O0", *defines, "-I", os.path.join(ROOT, "include"), "-I",
                            os.path.join(ROOT, "cuda-sipg-matrix-free_gb300", "host"), "-c", drv, "-o",
                            str(tmp_path / "drv.o")])
+
+
+def test_integration_binding_example_compiles(tmp_path):
+    # INTEGRATION.md's reference-side abs_mvm over the C ABI, against the host
+    # headers with the reference's class names (compile only)
+    subprocess.check_call(["nvcc", "-std=c++14", "-O0", "-I", os.path.join(ROOT, "include"), "-I",
+                           os.path.join(ROOT, "cuda-sipg-matrix-free_gb300", "host"), "-c",
+                           os.path.join(ROOT, "tests", "cpp", "integration_binding.cpp"), "-o",
+                           str(tmp_path / "binding.o")])
