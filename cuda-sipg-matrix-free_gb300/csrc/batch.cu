@@ -2,21 +2,23 @@
 // reference): many right-hand sides on one mesh, or uneven (dim, p) problems.
 //
 // Every instance keeps its own operator (shared between instances with the
-// same dim, p and penalty), inner CG vectors (double-float pairs: the inner
-// kind SIPG_INNER_PAIRS of mixed.cu, which converges at every condition
-// number), FP64 residual, device CG states and reduction scratch, resident on
-// the device for the life of the batch.  One inner iteration of the whole
-// batch is one batched compensated apply launch per degree present
-// (k_sipg_apply_df_batched: the instances' tiles concatenated into one grid)
-// plus a batched direction launch before it and a batched update launch after
-// it (k_cg_direction_pairs_batched, k_cg_update_pairs_batched); K iterations are
-// captured once as a CUDA graph and replayed.  The mixed-precision scheme is
-// the reliable-update one of mixed.cu, per instance: an instance whose inner
-// residual has fallen by inner_tol stops iterating (its blocks return at once)
-// until the host, between graph replays, folds its correction into x in FP64,
-// recomputes its FP64 residual (batched FP64 applies over the instances that
-// need it) and restarts it -- or retires it once ||b - Ax|| <= outer_tol
-// ||b||.  Converged instances retire mid-batch while the others go on.
+// same dim, p and penalty), FP64 residual, direction and A d, FP32 inner CG
+// vectors, device states and reduction scratch, resident on the device for
+// the life of the batch.  The scheme is the flexible one of mixed.cu, per
+// instance (sipg_fcg.cuh): flexible CG in FP64 around an FP32 inner CG (FP32
+// values and accumulation) that restarts from zero on the scaled residual.
+//
+// One inner iteration of the whole batch is one batched FP32 apply launch
+// per degree present (k_sipg_apply_batched in APPLY_DOT mode: the instances'
+// tiles concatenated into one grid), with a batched direction launch before
+// it and a batched update launch after it; K iterations are captured once as
+// a CUDA graph and replayed.  An instance whose inner solve has finished
+// skips the replays (its blocks return at once) until the host, between
+// replays, runs its FP64 outer step together with every other instance due
+// one (batched gamma / direction / FP64 apply / update launches over that
+// selection) and restarts its inner solve -- or, once its FP64 residual
+// b - A x (recomputed in FP64 before it may stop) is under outer_tol ||b||,
+// retires it.  Converged instances retire mid-batch while the others go on.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -24,90 +26,59 @@
 #include <tuple>
 #include <vector>
 
-#include "sipg_cg_df.cuh"
+#include "sipg_fcg.cuh"
 
 using namespace sipg;
 
 namespace sipg {
 
-struct MixedInst {
-  double* x64;
-  const double* b64;
-  double* r64;
-  float* r32;  // pair vectors
-  float* e;
-  CgState<double>* st32;  // the inner state (FP64 scalars)
-  CgState<double>* st64;
-  ReduceScratch red32;
-  ReduceScratch red64;
-  size_t n;
-  int first;
-  double delta;
-  double stop;  // the outer target in inner residual units
-  int max_it;
-  int nblk;  // blocks this instance uses (see VecInst)
-};
-
-// ||b||^2 of every listed instance into its FP64 state
-__global__ void __launch_bounds__(kVecThreads) k_batch_norm_b(const MixedInst* __restrict__ insts) {
-  const MixedInst m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
-  cg_init_body<double>(m.b64, m.n, m.st64, 0.0, 0, 1, m.red64, blockIdx.x, m.nblk);
-}
-
-// inner residual = r64 as pairs, e = 0, inner CG state for the next run (see
-// inner_restart_body)
-__global__ void __launch_bounds__(kVecThreads) k_batch_restart(const MixedInst* __restrict__ insts) {
-  const MixedInst m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
-  inner_restart_body<INNER_PAIRS>(m.r64, m.r32, m.e, m.n, m.st32, m.red32, m.first, m.delta, m.stop, m.max_it,
-                                  blockIdx.x, m.nblk);
-}
-
-// x64 += e
-__global__ void __launch_bounds__(kVecThreads) k_batch_fold(const MixedInst* __restrict__ insts) {
-  const MixedInst m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
-  inner_fold_body<INNER_PAIRS>(m.x64, m.e, m.n, blockIdx.x, m.nblk);
+// ||b||^2 and the stop threshold outer_tol ||b|| of every listed instance
+__global__ void __launch_bounds__(kVecThreads) k_batch_init(const FcgInst* __restrict__ insts, double tol) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  cg_init_body<double>(v.b, v.n, v.st64, tol, 1, 1 << 30, v.red64, blockIdx.x, v.nblk);
 }
 
 // park instances: the FP32 iterations skip them
-__global__ void k_batch_park(const MixedInst* __restrict__ insts, int n) {
+__global__ void k_batch_park(const FcgInst* __restrict__ insts, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    insts[i].st32->done = 1;
-    insts[i].st32->need_update = 0;
-  }
+  if (i < n) insts[i].st32->done = 1;
 }
 
 }  // namespace sipg
 
 namespace {
 
+// inner iterations one preconditioner solve may take
+constexpr int kInnerCap = 4000;
+
 struct BInst {
   int dim = 0, p = 0;
   double pen = 0;
   sipg_op* op = nullptr;
   size_t n = 0;
-  double* r64 = nullptr;
-  float* r32 = nullptr;  // pair vectors (2 n floats) from here
-  float* e = nullptr;
-  float* p0 = nullptr;
-  float* Ap = nullptr;
-  CgState<double>* st32 = nullptr;  // inner state
+  double* r64 = nullptr;  // FP64: residual, direction, A d
+  double* d64 = nullptr;
+  double* q64 = nullptr;
+  float* r32 = nullptr;   // FP32 inner: residual, solution, direction, A p
+  float* e32 = nullptr;
+  float* p32 = nullptr;
+  float* Ap32 = nullptr;
+  CgState<float>* st32 = nullptr;   // (in the batch's contiguous state arrays)
   CgState<double>* st64 = nullptr;
+  FcgState* fs = nullptr;
   ReduceScratch red32, red64;
-  int tilesdf = 0, tiles64 = 0;
+  int tiles32 = 0, tiles64 = 0;
 };
 
 struct BGroup {
   int p = 0;
   std::vector<int> members;
-  TileCfg cfgdf, cfg64;
-  ApplyArgs<float>* d_cg = nullptr;  // all members, compensated FP32 CG mode
-  int* d_tilesdf = nullptr;
-  int totaldf = 0;
-  ApplyArgs<double>* d_res = nullptr;  // a subset, FP64 residual mode (rebuilt per round)
+  TileCfg cfg32, cfg64;
+  ApplyArgs<float>* d_cg = nullptr;  // all members, FP32 inner CG (APPLY_DOT)
+  int* d_tiles32 = nullptr;
+  int total32 = 0;
+  ApplyArgs<double>* d_sub = nullptr;  // a selection, FP64 residual or step (rebuilt per use)
   int* d_tiles64 = nullptr;
 };
 
@@ -120,12 +91,15 @@ struct sipg_batch {
   std::vector<BInst> inst;
   std::vector<BGroup> groups;
   std::vector<sipg_op*> owned;
-  PairInst* d_vec = nullptr;
-  MixedInst* d_sel = nullptr;  // selection list (capacity n)
-  MixedInst* h_sel = nullptr;  // pinned
-  ApplyArgs<double>* h_res = nullptr;  // pinned staging for FP64 residual args
+  CgState<float>* st32 = nullptr;   // n inner states
+  CgState<double>* st64 = nullptr;  // n outer states
+  FcgState* fs = nullptr;           // n flexible-step scalars
+  FcgInst* d_vec = nullptr;         // every instance (the inner graph)
+  FcgInst* d_sel = nullptr;         // a selection (capacity n)
+  FcgInst* h_sel = nullptr;         // pinned
+  ApplyArgs<double>* h_sub = nullptr;  // pinned staging for FP64 apply args
   int* h_tiles = nullptr;              // pinned staging for tile starts
-  CgState<double>* h_st32 = nullptr;   // pinned mirrors, n each
+  CgState<float>* h_st32 = nullptr;    // pinned mirrors, n each
   CgState<double>* h_st64 = nullptr;
   cudaStream_t cap = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -139,12 +113,12 @@ static void batch_free(sipg_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   for (BInst& i : b->inst) {
     cudaFree(i.r64);
+    cudaFree(i.d64);
+    cudaFree(i.q64);
     cudaFree(i.r32);
-    cudaFree(i.e);
-    cudaFree(i.p0);
-    cudaFree(i.Ap);
-    cudaFree(i.st32);
-    cudaFree(i.st64);
+    cudaFree(i.e32);
+    cudaFree(i.p32);
+    cudaFree(i.Ap32);
     cudaFree(i.red32.partials);
     cudaFree(i.red32.counter);
     cudaFree(i.red64.partials);
@@ -152,14 +126,17 @@ static void batch_free(sipg_batch* b) {
   }
   for (BGroup& g : b->groups) {
     cudaFree(g.d_cg);
-    cudaFree(g.d_tilesdf);
-    cudaFree(g.d_res);
+    cudaFree(g.d_tiles32);
+    cudaFree(g.d_sub);
     cudaFree(g.d_tiles64);
   }
+  cudaFree(b->st32);
+  cudaFree(b->st64);
+  cudaFree(b->fs);
   cudaFree(b->d_vec);
   cudaFree(b->d_sel);
   cudaFreeHost(b->h_sel);
-  cudaFreeHost(b->h_res);
+  cudaFreeHost(b->h_sub);
   cudaFreeHost(b->h_tiles);
   cudaFreeHost(b->h_st32);
   cudaFreeHost(b->h_st64);
@@ -170,22 +147,55 @@ static void batch_free(sipg_batch* b) {
   delete b;
 }
 
+// One instance's operands (x, rhs: the caller's vectors of this solve).
+static FcgInst inst_of(const sipg_batch* b, int k, double* x, const double* rhs, int first, float stop) {
+  const BInst& i = b->inst[k];
+  FcgInst v;
+  v.x = x;
+  v.b = rhs;
+  v.r64 = i.r64;
+  v.d64 = i.d64;
+  v.q64 = i.q64;
+  v.r32 = i.r32;
+  v.e32 = i.e32;
+  v.p32 = i.p32;
+  v.Ap32 = i.Ap32;
+  v.st32 = i.st32;
+  v.st64 = i.st64;
+  v.fs = i.fs;
+  v.red32 = i.red32;
+  v.red64 = i.red64;
+  v.n = i.n;
+  v.nblk = inst_blocks(i.n);
+  v.first = first;
+  v.stop = stop;
+  v.max_it = kInnerCap;
+  return v;
+}
+
 static sipg_status batch_alloc(sipg_batch* b) {
   const int n = b->n;
   b->bpi = 1;
   for (const BInst& i : b->inst) b->bpi = std::max(b->bpi, inst_blocks(i.n));
-  for (BInst& i : b->inst) {
+  SIPG_CUDA_TRY(cudaMalloc(&b->st32, sizeof(CgState<float>) * n));
+  SIPG_CUDA_TRY(cudaMalloc(&b->st64, sizeof(CgState<double>) * n));
+  SIPG_CUDA_TRY(cudaMalloc(&b->fs, sizeof(FcgState) * n));
+  SIPG_CUDA_TRY(cudaMemset(b->st32, 0, sizeof(CgState<float>) * n));
+  SIPG_CUDA_TRY(cudaMemset(b->st64, 0, sizeof(CgState<double>) * n));
+  SIPG_CUDA_TRY(cudaMemset(b->fs, 0, sizeof(FcgState) * n));
+  for (int k = 0; k < n; ++k) {
+    BInst& i = b->inst[k];
     const int cap = reduce_capacity(i.dim);
-    const size_t pair_bytes = 2 * i.n * sizeof(float);
     SIPG_CUDA_TRY(cudaMalloc(&i.r64, i.n * sizeof(double)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.r32, pair_bytes));
-    SIPG_CUDA_TRY(cudaMalloc(&i.e, pair_bytes));
-    SIPG_CUDA_TRY(cudaMalloc(&i.p0, pair_bytes));
-    SIPG_CUDA_TRY(cudaMalloc(&i.Ap, pair_bytes));
-    SIPG_CUDA_TRY(cudaMalloc(&i.st32, sizeof(CgState<double>)));
-    SIPG_CUDA_TRY(cudaMalloc(&i.st64, sizeof(CgState<double>)));
-    SIPG_CUDA_TRY(cudaMemset(i.st32, 0, sizeof(CgState<double>)));
-    SIPG_CUDA_TRY(cudaMemset(i.st64, 0, sizeof(CgState<double>)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.d64, i.n * sizeof(double)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.q64, i.n * sizeof(double)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.r32, i.n * sizeof(float)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.e32, i.n * sizeof(float)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.p32, i.n * sizeof(float)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.Ap32, i.n * sizeof(float)));
+    i.st32 = b->st32 + k;
+    i.st64 = b->st64 + k;
+    i.fs = b->fs + k;
     ReduceScratch* reds[2] = {&i.red32, &i.red64};
     for (ReduceScratch* r : reds) {
       SIPG_CUDA_TRY(cudaMalloc(&r->partials, sizeof(double) * cap));
@@ -202,7 +212,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
       gidx[p] = (int)b->groups.size();
       BGroup g;
       g.p = p;
-      g.cfgdf = b->inst[k].op->cfgdf;
+      g.cfg32 = batched_tile(b->inst[k].op->cfg32);
       g.cfg64 = batched_tile(b->inst[k].op->cfg64);
       b->groups.push_back(g);
     }
@@ -214,50 +224,35 @@ static sipg_status batch_alloc(sipg_batch* b) {
     std::vector<int> ts(m + 1, 0);
     for (int j = 0; j < m; ++j) {
       BInst& i = b->inst[g.members[j]];
-      i.tilesdf = tiles_of(i.dim, g.cfgdf);
+      i.tiles32 = tiles_of(i.dim, g.cfg32);
       i.tiles64 = tiles_of(i.dim, g.cfg64);
       ApplyArgs<float> a{};
-      a.in = i.p0;  // the direction, formed by k_cg_direction_pairs_batched
-      a.out = i.Ap;
+      a.in = i.p32;  // the direction, formed by k_fcg_inner_direction_batched
+      a.out = i.Ap32;
       a.dim = i.dim;
       a.nu = (float)i.pen;
-      set_penalty3(a, i.pen);
-      a.stp = i.st32;
+      a.st = i.st32;
       a.red = i.red32;
       args[j] = a;
-      ts[j + 1] = ts[j] + i.tilesdf;
+      ts[j + 1] = ts[j] + i.tiles32;
     }
-    g.totaldf = ts[m];
+    g.total32 = ts[m];
     SIPG_CUDA_TRY(cudaMalloc(&g.d_cg, sizeof(ApplyArgs<float>) * m));
-    SIPG_CUDA_TRY(cudaMalloc(&g.d_tilesdf, sizeof(int) * (m + 1)));
-    SIPG_CUDA_TRY(cudaMalloc(&g.d_res, sizeof(ApplyArgs<double>) * m));
+    SIPG_CUDA_TRY(cudaMalloc(&g.d_tiles32, sizeof(int) * (m + 1)));
+    SIPG_CUDA_TRY(cudaMalloc(&g.d_sub, sizeof(ApplyArgs<double>) * m));
     SIPG_CUDA_TRY(cudaMalloc(&g.d_tiles64, sizeof(int) * (m + 1)));
     SIPG_CUDA_TRY(cudaMemcpy(g.d_cg, args.data(), sizeof(ApplyArgs<float>) * m, cudaMemcpyHostToDevice));
-    SIPG_CUDA_TRY(cudaMemcpy(g.d_tilesdf, ts.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+    SIPG_CUDA_TRY(cudaMemcpy(g.d_tiles32, ts.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
   }
-  std::vector<PairInst> vec(n);
-  for (int k = 0; k < n; ++k) {
-    BInst& i = b->inst[k];
-    PairInst v;
-    v.x = i.e;
-    v.pb0 = i.p0;
-    v.pb1 = i.p0;
-    v.r = i.r32;
-    v.Ap = i.Ap;
-    v.n = i.n;
-    v.st = i.st32;
-    v.red = i.red32;
-    v.nblk = inst_blocks(i.n);
-    v.pad = 0;
-    vec[k] = v;
-  }
-  SIPG_CUDA_TRY(cudaMalloc(&b->d_vec, sizeof(PairInst) * n));
-  SIPG_CUDA_TRY(cudaMemcpy(b->d_vec, vec.data(), sizeof(PairInst) * n, cudaMemcpyHostToDevice));
-  SIPG_CUDA_TRY(cudaMalloc(&b->d_sel, sizeof(MixedInst) * n));
-  SIPG_CUDA_TRY(cudaMallocHost(&b->h_sel, sizeof(MixedInst) * n));
-  SIPG_CUDA_TRY(cudaMallocHost(&b->h_res, sizeof(ApplyArgs<double>) * n));
+  std::vector<FcgInst> vec(n);
+  for (int k = 0; k < n; ++k) vec[k] = inst_of(b, k, nullptr, nullptr, 1, 0.f);
+  SIPG_CUDA_TRY(cudaMalloc(&b->d_vec, sizeof(FcgInst) * n));
+  SIPG_CUDA_TRY(cudaMemcpy(b->d_vec, vec.data(), sizeof(FcgInst) * n, cudaMemcpyHostToDevice));
+  SIPG_CUDA_TRY(cudaMalloc(&b->d_sel, sizeof(FcgInst) * n));
+  SIPG_CUDA_TRY(cudaMallocHost(&b->h_sel, sizeof(FcgInst) * n));
+  SIPG_CUDA_TRY(cudaMallocHost(&b->h_sub, sizeof(ApplyArgs<double>) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_tiles, sizeof(int) * (n + 1)));
-  SIPG_CUDA_TRY(cudaMallocHost(&b->h_st32, sizeof(CgState<double>) * n));
+  SIPG_CUDA_TRY(cudaMallocHost(&b->h_st32, sizeof(CgState<float>) * n));
   SIPG_CUDA_TRY(cudaMallocHost(&b->h_st64, sizeof(CgState<double>) * n));
   SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   SIPG_CUDA_TRY(cudaEventCreate(&b->ev0));
@@ -268,27 +263,27 @@ static sipg_status batch_alloc(sipg_batch* b) {
   return SIPG_OK;
 }
 
-// K FP32 CG iterations of every instance: per degree a batched apply, then one
-// batched update; captured once.
+// K FP32 CG iterations of every instance: per degree a batched apply, with a
+// batched direction before and a batched update after; captured once.
 static sipg_status batch_capture(sipg_batch* b) {
   if (b->exec) return SIPG_OK;
   for (BGroup& g : b->groups)
-    SIPG_CUDA_TRY(launch_apply_df(g.p, g.cfgdf, APPLY_PREPARE, ApplyArgs<float>{}, nullptr, nullptr, 0, 0,
-                                  b->inst[g.members[0]].op->tab, b->cap));
+    SIPG_CUDA_TRY(launch_apply_batched_f32(g.p, g.cfg32, APPLY_PREPARE, nullptr, nullptr, 0, 0,
+                                           b->inst[g.members[0]].op->tab, b->cap));
   cudaGraph_t graph = nullptr;
   SIPG_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
+  const dim3 vg(b->bpi, b->n);
   for (int k = 0; k < b->K && err == cudaSuccess; ++k) {
-    k_cg_direction_pairs_batched<<<dim3(b->bpi, b->n), kVecThreads, 0, b->cap>>>(b->d_vec);
+    k_fcg_inner_direction_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
     err = cudaGetLastError();
     for (BGroup& g : b->groups) {
       if (err != cudaSuccess) break;
-      err = launch_apply_df(g.p, g.cfgdf, APPLY_DOT, ApplyArgs<float>{}, g.d_cg, g.d_tilesdf, (int)g.members.size(),
-                            g.totaldf, b->inst[g.members[0]].op->tab, b->cap);
-      if (err != cudaSuccess) break;
+      err = launch_apply_batched_f32(g.p, g.cfg32, APPLY_DOT, g.d_cg, g.d_tiles32, (int)g.members.size(), g.total32,
+                                     b->inst[g.members[0]].op->tab, b->cap);
     }
     if (err != cudaSuccess) break;
-    k_cg_update_pairs_batched<<<dim3(b->bpi, b->n), kVecThreads, 0, b->cap>>>(b->d_vec);
+    k_fcg_inner_update_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
     err = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamEndCapture(b->cap, &graph);
@@ -307,9 +302,10 @@ static sipg_status batch_capture(sipg_batch* b) {
   return SIPG_OK;
 }
 
-// FP64 residual r = b - A x of the selected instances (batched per degree)
-static sipg_status batch_residuals(sipg_batch* b, const std::vector<int>& sel, double* const* d_x,
-                                   const double* const* d_b, cudaStream_t s) {
+// FP64 applies of the selected instances, batched per degree: APPLY_RESID
+// (r64 = b - A x, r.r) or APPLY_DOT (q = A d, alpha = d.r / d.q).
+static sipg_status batch_apply64(sipg_batch* b, const std::vector<int>& sel, int mode, double* const* d_x,
+                                 const double* const* d_b, cudaStream_t s) {
   for (BGroup& g : b->groups) {
     int m = 0;
     b->h_tiles[0] = 0;
@@ -317,21 +313,26 @@ static sipg_status batch_residuals(sipg_batch* b, const std::vector<int>& sel, d
       BInst& i = b->inst[k];
       if (i.p != g.p) continue;
       ApplyArgs<double> a{};
-      a.in = d_x[k];
-      a.out = i.r64;
-      a.b = d_b[k];
+      if (mode == APPLY_RESID) {
+        a.in = d_x[k];
+        a.out = i.r64;
+        a.b = d_b[k];
+      } else {
+        a.in = i.d64;
+        a.out = i.q64;
+      }
       a.dim = i.dim;
       a.nu = i.pen;
       a.st = i.st64;
       a.red = i.red64;
-      b->h_res[m] = a;
+      b->h_sub[m] = a;
       b->h_tiles[m + 1] = b->h_tiles[m] + i.tiles64;
       ++m;
     }
     if (!m) continue;
-    SIPG_CUDA_TRY(cudaMemcpyAsync(g.d_res, b->h_res, sizeof(ApplyArgs<double>) * m, cudaMemcpyHostToDevice, s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(g.d_sub, b->h_sub, sizeof(ApplyArgs<double>) * m, cudaMemcpyHostToDevice, s));
     SIPG_CUDA_TRY(cudaMemcpyAsync(g.d_tiles64, b->h_tiles, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, s));
-    SIPG_CUDA_TRY(launch_apply_batched_f64(g.p, g.cfg64, APPLY_RESID, g.d_res, g.d_tiles64, m, b->h_tiles[m],
+    SIPG_CUDA_TRY(launch_apply_batched_f64(g.p, g.cfg64, mode, g.d_sub, g.d_tiles64, m, b->h_tiles[m],
                                            b->inst[g.members[0]].op->tab, s));
     // the pinned staging is reused by the next group: wait for the copies
     SIPG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -339,30 +340,22 @@ static sipg_status batch_residuals(sipg_batch* b, const std::vector<int>& sel, d
   return SIPG_OK;
 }
 
-static int fill_sel(sipg_batch* b, const std::vector<int>& sel, double* const* d_x, const double* const* d_b,
-                    int first, double delta, const std::vector<double>& stop, int max_it) {
+// Uploads the selection `sel` (with each instance's first-step flag) into d_sel.
+static sipg_status upload_sel(sipg_batch* b, const std::vector<int>& sel, double* const* d_x, const double* const* d_b,
+                              const std::vector<int>& first, float stop, cudaStream_t s) {
   int m = 0;
-  for (int k : sel) {
-    BInst& i = b->inst[k];
-    MixedInst mi;
-    mi.x64 = d_x[k];
-    mi.b64 = d_b[k];
-    mi.r64 = i.r64;
-    mi.e = i.e;
-    mi.r32 = i.r32;
-    mi.st32 = i.st32;
-    mi.st64 = i.st64;
-    mi.red32 = i.red32;
-    mi.red64 = i.red64;
-    mi.n = i.n;
-    mi.first = first;
-    mi.delta = delta;
-    mi.stop = stop[k];
-    mi.max_it = max_it;
-    mi.nblk = inst_blocks(i.n);
-    b->h_sel[m++] = mi;
-  }
-  return m;
+  for (int k : sel) b->h_sel[m++] = inst_of(b, k, d_x[k], d_b[k], first[k], stop);
+  SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(FcgInst) * m, cudaMemcpyHostToDevice, s));
+  return SIPG_OK;
+}
+
+static sipg_status read_states(sipg_batch* b, cudaStream_t s, bool inner, bool outer) {
+  if (inner)
+    SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st32, b->st32, sizeof(CgState<float>) * b->n, cudaMemcpyDeviceToHost, s));
+  if (outer)
+    SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st64, b->st64, sizeof(CgState<double>) * b->n, cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+  return SIPG_OK;
 }
 
 extern "C" {
@@ -426,7 +419,9 @@ sipg_status sipg_batch_op(const sipg_batch* b, int i, sipg_op** op) {
 size_t sipg_batch_footprint(const sipg_batch* b) {
   if (!b) return 0;
   size_t bytes = 0;
-  for (const BInst& i : b->inst) bytes += i.n * (8 + 4 * 8) + 2 * sizeof(double) * reduce_capacity(i.dim);
+  for (const BInst& i : b->inst)
+    bytes += i.n * (3 * 8 + 4 * 4) + 2 * sizeof(double) * reduce_capacity(i.dim) + sizeof(CgState<double>) +
+             sizeof(CgState<float>) + sizeof(FcgState);
   return bytes;
 }
 
@@ -441,10 +436,15 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
       set_error("sipg_batch_solve_mixed: null vector");
       return SIPG_ERR_INVALID;
     }
-  sipg_mixed_opts o = {0.1, 1e-10, 200, 0};
+  sipg_mixed_opts o = {1e-2, 1e-10, 200, 0, SIPG_INNER_AUTO, SIPG_OUTER_AUTO};
   if (opts) o = *opts;
   if (!(o.inner_tol > 0) || !(o.inner_tol < 1) || !(o.outer_tol > 0) || o.max_outer < 1) {
     set_error("sipg_batch_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1");
+    return SIPG_ERR_INVALID;
+  }
+  if ((o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32) ||
+      (o.outer != SIPG_OUTER_AUTO && o.outer != SIPG_OUTER_FLEXIBLE)) {
+    set_error("sipg_batch_solve_mixed: batches run the flexible outer kind with an FP32 inner CG");
     return SIPG_ERR_INVALID;
   }
   cudaStream_t s = (cudaStream_t)stream;
@@ -452,100 +452,120 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
   sipg_status st = batch_capture(b);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(cudaEventRecord(b->ev0, s));
-  std::vector<int> all(n);
+  const float stop_in = (float)o.inner_tol;
+  std::vector<int> all(n), first(n, 1), steps(n, 0), fp64(n, 0), retired(n, 0), conv(n, 0);
   for (int k = 0; k < n; ++k) all[k] = k;
-  std::vector<int> corrections(n, 0), retired(n, 0), conv(n, 0);
   std::vector<double> bnorm(n, 0.0), rel(n, INFINITY);
-  std::vector<long long> max_inner(n);
+  std::vector<long long> inner_total(n, 0), max_inner(n);
   for (int k = 0; k < n; ++k) max_inner[k] = o.max_inner > 0 ? o.max_inner : (long long)b->inst[k].n;
+  sipg_status status = SIPG_OK;
+  auto retire = [&](int k, sipg_status why) {
+    retired[k] = 1;
+    if (why == SIPG_OK) conv[k] = 1;
+    else if (status == SIPG_OK || why == SIPG_ERR_BREAKDOWN) status = why;
+  };
 
-  // ||b|| of every instance, and park every FP32 state
-  std::vector<double> stop(n, 0.0);
-  int m = fill_sel(b, all, d_x, d_b, 1, o.inner_tol, stop, 0);
-  SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
-  k_batch_norm_b<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
-  k_batch_park<<<(m + 127) / 128, 128, 0, s>>>(b->d_sel, m);
+  // ||b||, the stop thresholds, every inner state parked; r = b - A x
+  st = upload_sel(b, all, d_x, d_b, first, stop_in, s);
+  if (st != SIPG_OK) return st;
+  k_batch_init<<<dim3(b->bpi, n), kVecThreads, 0, s>>>(b->d_sel, o.outer_tol);
+  k_batch_park<<<(n + 127) / 128, 128, 0, s>>>(b->d_sel, n);
   count_launch(2);
   SIPG_CUDA_TRY(cudaGetLastError());
-  for (int k = 0; k < n; ++k)
-    SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st64 + k, b->inst[k].st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
-  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+  st = batch_apply64(b, all, APPLY_RESID, d_x, d_b, s);
+  if (st != SIPG_OK) return st;
+  st = read_states(b, s, false, true);
+  if (st != SIPG_OK) return st;
+  std::vector<int> cont;
   for (int k = 0; k < n; ++k) {
+    fp64[k] = 1;
     bnorm[k] = std::sqrt(b->h_st64[k].bb);
-    stop[k] = 0.5 * o.outer_tol * (bnorm[k] > 0 ? bnorm[k] : 1.0);
+    const double rr = b->h_st64[k].rr;
+    rel[k] = bnorm[k] > 0 ? std::sqrt(rr) / bnorm[k] : std::sqrt(rr);
+    if (!std::isfinite(rel[k])) retire(k, SIPG_ERR_BREAKDOWN);
+    else if (rel[k] <= o.outer_tol || rr == 0.0) retire(k, SIPG_OK);
+    else cont.push_back(k);
   }
-
-  std::vector<int> sel = all;
-  bool first_round = true;
-  sipg_status status = SIPG_OK;
   for (;;) {
-    if (!sel.empty()) {
-      // FP64 residuals of the selected instances; retire or restart them
-      st = batch_residuals(b, sel, d_x, d_b, s);
+    // inner restarts of the instances that go on
+    if (!cont.empty()) {
+      st = upload_sel(b, cont, d_x, d_b, first, stop_in, s);
       if (st != SIPG_OK) return st;
-      for (int k : sel)
-        SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st64 + k, b->inst[k].st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
-      SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-      std::vector<int> restart_first, restart_cont;
-      for (int k : sel) {
-        const double rr = b->h_st64[k].rr;
-        rel[k] = bnorm[k] > 0 ? std::sqrt(rr) / bnorm[k] : std::sqrt(rr);
-        const long long its = first_round ? 0 : b->h_st32[k].it;
-        if (!std::isfinite(rel[k])) {
-          retired[k] = 1;
-          status = SIPG_ERR_BREAKDOWN;
-        } else if (rel[k] <= o.outer_tol || rr == 0.0) {
-          retired[k] = 1;
-          conv[k] = 1;
-        } else if (corrections[k] >= o.max_outer || its >= max_inner[k]) {
-          retired[k] = 1;
-          if (status == SIPG_OK) status = SIPG_ERR_NOT_CONVERGED;
-        } else if (first_round) {
-          restart_first.push_back(k);
-        } else {
-          restart_cont.push_back(k);
-        }
-      }
-      for (int pass = 0; pass < 2; ++pass) {
-        const std::vector<int>& list = pass ? restart_cont : restart_first;
-        if (list.empty()) continue;
-        m = fill_sel(b, list, d_x, d_b, pass ? 0 : 1, o.inner_tol, stop, 1000);
-        SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
-        k_batch_restart<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
-        count_launch();
-        SIPG_CUDA_TRY(cudaGetLastError());
-        SIPG_CUDA_TRY(cudaStreamSynchronize(s));  // h_sel is reused
-      }
-      first_round = false;
+      k_fcg_restart_batched<<<dim3(b->bpi, (unsigned)cont.size()), kVecThreads, 0, s>>>(b->d_sel);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
+      SIPG_CUDA_TRY(cudaStreamSynchronize(s));  // h_sel is reused
     }
     bool active = false;
     for (int k = 0; k < n; ++k) active = active || !retired[k];
     if (!active) break;
-    // FP32 iterations of every active instance
+    // FP32 inner iterations of every instance still in an inner solve
     SIPG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
-    unsigned long long per_iter = (unsigned long long)b->groups.size() + 2;
-    count_launch(per_iter * b->K);
-    for (int k = 0; k < n; ++k)
-      SIPG_CUDA_TRY(cudaMemcpyAsync(b->h_st32 + k, b->inst[k].st32, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
-    SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-    sel.clear();
+    count_launch((unsigned long long)(b->groups.size() + 2) * b->K);
+    st = read_states(b, s, true, false);
+    if (st != SIPG_OK) return st;
+    std::vector<int> sel;
     for (int k = 0; k < n; ++k) {
       if (retired[k] || !b->h_st32[k].done) continue;
-      if (b->h_st32[k].status == (int)SIPG_ERR_BREAKDOWN) {
-        retired[k] = 1;
-        status = SIPG_ERR_BREAKDOWN;
-        continue;
-      }
-      sel.push_back(k);
+      inner_total[k] += b->h_st32[k].it;
+      if (b->h_st32[k].it == 0) retire(k, SIPG_ERR_BREAKDOWN);  // no inner step: no direction
+      else sel.push_back(k);
     }
-    if (!sel.empty()) {
-      m = fill_sel(b, sel, d_x, d_b, 0, o.inner_tol, stop, 0);
-      SIPG_CUDA_TRY(cudaMemcpyAsync(b->d_sel, b->h_sel, sizeof(MixedInst) * m, cudaMemcpyHostToDevice, s));
-      k_batch_fold<<<dim3(b->bpi, m), kVecThreads, 0, s>>>(b->d_sel);
-      count_launch();
-      SIPG_CUDA_TRY(cudaGetLastError());
-      SIPG_CUDA_TRY(cudaStreamSynchronize(s));  // h_sel is reused
-      for (int k : sel) corrections[k] += 1;
+    cont.clear();
+    if (sel.empty()) continue;
+    // the FP64 outer step of every instance whose inner solve finished
+    st = upload_sel(b, sel, d_x, d_b, first, stop_in, s);
+    if (st != SIPG_OK) return st;
+    const dim3 sg(b->bpi, (unsigned)sel.size());
+    k_fcg_gamma_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
+    k_fcg_direction_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
+    count_launch(2);
+    SIPG_CUDA_TRY(cudaGetLastError());
+    st = batch_apply64(b, sel, APPLY_DOT, d_x, d_b, s);
+    if (st != SIPG_OK) return st;
+    k_fcg_update_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    st = read_states(b, s, false, true);
+    if (st != SIPG_OK) return st;
+    std::vector<int> chk;
+    for (int k : sel) {
+      steps[k] += 1;
+      fp64[k] += 1;
+      first[k] = 0;
+      const CgState<double>& h = b->h_st64[k];
+      const double r = bnorm[k] > 0 ? std::sqrt(h.rr) / bnorm[k] : std::sqrt(h.rr);
+      if (h.status == (int)SIPG_ERR_BREAKDOWN || !std::isfinite(r)) {
+        rel[k] = r;
+        retire(k, SIPG_ERR_BREAKDOWN);
+      } else if (r <= o.outer_tol) {
+        chk.push_back(k);
+      } else if (steps[k] >= o.max_outer || inner_total[k] >= max_inner[k]) {
+        rel[k] = r;
+        retire(k, SIPG_ERR_NOT_CONVERGED);
+      } else {
+        cont.push_back(k);
+      }
+    }
+    if (!chk.empty()) {
+      // the recursion says done: b - A x in FP64 decides
+      st = batch_apply64(b, chk, APPLY_RESID, d_x, d_b, s);
+      if (st != SIPG_OK) return st;
+      st = read_states(b, s, false, true);
+      if (st != SIPG_OK) return st;
+      for (int k : chk) {
+        fp64[k] += 1;
+        const double rr = b->h_st64[k].rr;
+        rel[k] = bnorm[k] > 0 ? std::sqrt(rr) / bnorm[k] : std::sqrt(rr);
+        if (rel[k] <= o.outer_tol) {
+          retire(k, SIPG_OK);
+        } else if (steps[k] >= o.max_outer || inner_total[k] >= max_inner[k]) {
+          retire(k, SIPG_ERR_NOT_CONVERGED);
+        } else {
+          first[k] = 1;  // a fresh direction history from the true residual
+          cont.push_back(k);
+        }
+      }
     }
   }
   SIPG_CUDA_TRY(cudaEventRecord(b->ev1, s));
@@ -554,11 +574,14 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
   cudaEventElapsedTime(&ms, b->ev0, b->ev1);
   if (res)
     for (int k = 0; k < n; ++k) {
-      res[k].outer_iterations = corrections[k];
-      res[k].inner_iterations = b->h_st32[k].it;
+      res[k].outer_iterations = steps[k];
+      res[k].inner_iterations = (int)inner_total[k];
       res[k].rel_residual = rel[k];
       res[k].time_ms = ms;
       res[k].converged = conv[k];
+      res[k].inner_kind = SIPG_INNER_F32;
+      res[k].outer_kind = SIPG_OUTER_FLEXIBLE;
+      res[k].fp64_applies = fp64[k];
     }
   return status;
 }

@@ -23,11 +23,28 @@
 // with its search direction* (beta = r_new.r_new / r_prev.r_prev): the
 // reliable-update scheme of Sleijpen & van der Vorst (1996), as used for
 // mixed-precision CG on GPUs by Clark et al. (2010).
+//
+// The flexible outer kind (SIPG_OUTER_FLEXIBLE) replaces the unit-step
+// correction by flexible CG in FP64 (Notay, SIAM J. Sci. Comput. 22, 2000;
+// FCG(1): each direction A-orthogonal to the previous one) whose
+// preconditioner is the FP32 inner CG, run from zero on r / ||r|| until its
+// residual fell by inner_tol.  One outer step:
+//   z = ||r|| e                      (e: the FP32 inner solution)
+//   gamma = z.q_prev / d_prev.q_prev,  d = z - gamma d_prev,  d.r
+//   q = A d (FP64 apply),  alpha = d.r / d.q
+//   x += alpha d,  r -= alpha q,  r.r           (all FP64)
+// and, once ||r|| reaches the target, r = b - A x recomputed in FP64 (the
+// recursion's drift) before the solve may stop.  Why FP32 suffices here but
+// not for the unit step: the line search measures the correction in the
+// energy norm, in which rounding a smooth correction to FP32 is an error of
+// relative size ~sqrt(kappa) eps_32 (3e-4 at kappa = 2e7), while the residual
+// norm sees ~kappa eps_32 (~1).
 #include <cmath>
 #include <new>
 
 #include "sipg_apply_df.cuh"
 #include "sipg_cg_df.cuh"
+#include "sipg_fcg.cuh"
 
 using namespace sipg;
 
@@ -131,7 +148,15 @@ struct MixedCache {
   int exec_k[4] = {0, 0, 0, 0};
   int exec_gen[4] = {-1, -1, -1, -1};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // flexible outer kind (allocated on its first use): the FP64 direction d and
+  // q = A d, and its scalars
+  double* d64 = nullptr;
+  double* q64 = nullptr;
+  FcgState* fs = nullptr;
   ~MixedCache() {
+    cudaFree(d64);
+    cudaFree(q64);
+    cudaFree(fs);
     for (cudaGraphExec_t g : exec)
       if (g) cudaGraphExecDestroy(g);
     if (cap) cudaStreamDestroy(cap);
@@ -157,6 +182,15 @@ struct MixedCache {
 };
 
 void mixed_cache_free(void* p) { delete static_cast<MixedCache*>(p); }
+
+sipg_status fcg_alloc(MixedCache& m) {
+  if (m.fs) return SIPG_OK;
+  SIPG_CUDA_TRY(cudaMalloc(&m.d64, m.n * sizeof(double)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.q64, m.n * sizeof(double)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.fs, sizeof(FcgState)));
+  SIPG_CUDA_TRY(cudaMemset(m.fs, 0, sizeof(FcgState)));
+  return SIPG_OK;
+}
 
 int vec_grid(size_t n) {
   return (int)std::max<size_t>(1, std::min<size_t>((n + kVecThreads - 1) / kVecThreads, 152 * 8));
@@ -293,23 +327,217 @@ sipg_status capture(sipg_op* op, MixedCache& m, int kind, int K) {
 }
 }  // namespace
 
+namespace {
+// What both outer kinds share for one solve.
+struct Solve {
+  sipg_op* op;
+  MixedCache* m;
+  double* x;
+  const double* b;
+  cudaStream_t s;
+  size_t n;
+  int vb;    // vector-kernel grid
+  int K;     // inner iterations per graph launch
+  double bnorm;
+  // results
+  int outer = 0;
+  long long inner_total = 0;
+  int fp64_applies = 0;
+  double rel = INFINITY;
+};
+
+// r64 = b - A x in FP64 (APPLY_RESID: r.r into st64, it = 0), read back.
+sipg_status true_residual(Solve& v, double* rr_out) {
+  MixedCache& m = *v.m;
+  ApplyArgs<double> a{};
+  a.in = v.x;
+  a.out = m.r64;
+  a.b = v.b;
+  a.dim = v.op->dim;
+  a.nu = v.op->pen;
+  a.st = m.st64;
+  a.red = m.red64;
+  SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_RESID, a, v.op->tab, v.s));
+  ++v.fp64_applies;
+  SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, v.s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
+  *rr_out = m.st64_host->rr;
+  return SIPG_OK;
+}
+
+// Replays the inner K-iteration graph until the inner state says done.
+template <typename StT>
+sipg_status run_inner(Solve& v, int kind, StT* st_dev, StT* st_host) {
+  for (;;) {
+    SIPG_CUDA_TRY(cudaGraphLaunch(v.m->exec[kind], v.s));
+    count_launch(3ULL * v.K);
+    SIPG_CUDA_TRY(cudaMemcpyAsync(st_host, st_dev, sizeof(StT), cudaMemcpyDeviceToHost, v.s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
+    if (st_host->done) return SIPG_OK;
+  }
+}
+
+// Defect correction with reliable updates (see the top of this file).
+sipg_status solve_reliable(Solve& v, int kind, const sipg_mixed_opts& o, long long max_inner) {
+  MixedCache& m = *v.m;
+  const size_t n = v.n;
+  const int vb = v.vb;
+  cudaStream_t s = v.s;
+  // the inner loop may also stop once its own residual is under the target
+  const double stop_in = 0.5 * o.outer_tol * (v.bnorm > 0 ? v.bnorm : 1.0);
+  // the inner state as the host last read it
+  const bool st_double = kind != SIPG_INNER_F32;  // pairs and FP64 keep FP64 scalars in stp
+  auto inner_it = [&]() { return st_double ? m.stp_host->it : m.st32_host->it; };
+  auto inner_status = [&]() { return st_double ? m.stp_host->status : m.st32_host->status; };
+  for (;;) {
+    double rr = 0;
+    sipg_status st = true_residual(v, &rr);
+    if (st != SIPG_OK) return st;
+    v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
+    if (!std::isfinite(v.rel)) {
+      set_error("sipg_solve_mixed: non-finite residual");
+      return SIPG_ERR_BREAKDOWN;
+    }
+    if (v.rel <= o.outer_tol || rr == 0.0) return SIPG_OK;
+    if (v.outer >= o.max_outer || v.inner_total >= max_inner) return SIPG_ERR_NOT_CONVERGED;
+    // the inner residual and CG state; after the first update the direction is kept
+    const int first = v.outer == 0;
+    if (kind == SIPG_INNER_F64)
+      k_mixed_restart_f64<<<vb, kVecThreads, 0, s>>>(m.r64, (double*)m.r, (double*)m.e, n, m.stp, m.red32, first,
+                                                     o.inner_tol, stop_in, kCorrectEvery);
+    else if (kind == SIPG_INNER_PAIRS)
+      k_mixed_restart<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.stp, m.red32, first,
+                                                               o.inner_tol, stop_in, kCorrectEvery);
+    else
+      k_mixed_restart<INNER_F32><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.st32, m.red32, first, o.inner_tol,
+                                                             stop_in, kCorrectEvery);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    const int it_before = first ? 0 : inner_it();
+    // inner iterations until an update is due (at most kCorrectEvery)
+    st = st_double ? run_inner(v, kind, m.stp, m.stp_host) : run_inner(v, kind, m.st32, m.st32_host);
+    if (st != SIPG_OK) return st;
+    v.inner_total += inner_it() - it_before;
+    if (inner_status() == (int)SIPG_ERR_BREAKDOWN) {
+      set_error("sipg_solve_mixed: inner CG breakdown");
+      return SIPG_ERR_BREAKDOWN;
+    }
+    if (kind == SIPG_INNER_F64)
+      k_mixed_fold_f64<<<vb, kVecThreads, 0, s>>>(v.x, (const double*)m.e, n);
+    else if (kind == SIPG_INNER_PAIRS)
+      k_mixed_fold<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(v.x, m.e, n);
+    else
+      k_mixed_fold<INNER_F32><<<vb, kVecThreads, 0, s>>>(v.x, m.e, n);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    ++v.outer;
+  }
+}
+
+// inner iterations one preconditioner solve of the flexible kind may take
+constexpr int kFlexibleInnerCap = 4000;
+
+// Flexible CG in FP64 with the FP32 inner CG as its preconditioner (see the
+// top of this file).
+sipg_status solve_flexible(Solve& v, const sipg_mixed_opts& o, long long max_inner) {
+  MixedCache& m = *v.m;
+  const size_t n = v.n;
+  const int vb = v.vb;
+  cudaStream_t s = v.s;
+  sipg_status st = fcg_alloc(m);
+  if (st != SIPG_OK) return st;
+  double rr = 0;
+  st = true_residual(v, &rr);
+  if (st != SIPG_OK) return st;
+  v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
+  int first = 1;
+  for (;;) {
+    if (!std::isfinite(v.rel)) {
+      set_error("sipg_solve_mixed: non-finite residual");
+      return SIPG_ERR_BREAKDOWN;
+    }
+    if (v.rel <= o.outer_tol || rr == 0.0) return SIPG_OK;
+    if (v.outer >= o.max_outer || v.inner_total >= max_inner) return SIPG_ERR_NOT_CONVERGED;
+    // z ~ A^-1 r: the FP32 inner CG from zero on r / ||r||
+    k_fcg_restart<<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.st64, m.fs, m.st32, m.red32, (float)o.inner_tol,
+                                             kFlexibleInnerCap);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    st = run_inner(v, SIPG_INNER_F32, m.st32, m.st32_host);
+    if (st != SIPG_OK) return st;
+    v.inner_total += m.st32_host->it;
+    if (m.st32_host->it == 0) {
+      // not one inner step (a breakdown at the first direction): no direction to search along
+      set_error("sipg_solve_mixed: the FP32 inner CG made no step");
+      return SIPG_ERR_BREAKDOWN;
+    }
+    // (an inner breakdown after some steps still leaves a usable direction)
+    // d = z - gamma d_prev, q = A d, alpha = d.r / d.q, x += alpha d, r -= alpha q
+    if (!first) {
+      k_fcg_gamma<<<vb, kVecThreads, 0, s>>>(m.e, m.q64, n, m.st64, m.fs, m.red64);
+      count_launch();
+    }
+    k_fcg_direction<<<vb, kVecThreads, 0, s>>>(m.e, m.d64, m.r64, n, m.st64, m.fs, m.red64, first);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    ApplyArgs<double> a{};
+    a.in = m.d64;
+    a.out = m.q64;
+    a.dim = v.op->dim;
+    a.nu = v.op->pen;
+    a.st = m.st64;
+    a.red = m.red64;
+    SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_DOT, a, v.op->tab, s));
+    ++v.fp64_applies;
+    k_cg_update<double><<<vb, kVecThreads, 0, s>>>(v.x, m.d64, m.d64, m.r64, m.q64, n, m.st64, m.red64);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+    ++v.outer;
+    if (m.st64_host->status == (int)SIPG_ERR_BREAKDOWN) {
+      set_error("sipg_solve_mixed: flexible CG breakdown (d.Ad <= 0 or a non-finite scalar)");
+      return SIPG_ERR_BREAKDOWN;
+    }
+    rr = m.st64_host->rr;
+    v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
+    first = 0;
+    if (v.rel <= o.outer_tol) {
+      // the recursion says done: recompute b - A x in FP64; continue (a
+      // fresh direction history) if the drift left it above the target
+      st = true_residual(v, &rr);
+      if (st != SIPG_OK) return st;
+      v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
+      first = 1;
+    }
+  }
+}
+}  // namespace
+
 extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
                                         sipg_mixed_result* res, void* stream) {
   if (!op || !d_x || !d_b) {
     set_error("sipg_solve_mixed: null argument");
     return SIPG_ERR_INVALID;
   }
-  sipg_mixed_opts o = {0.1, 1e-10, 200, 0, SIPG_INNER_AUTO, 0};
+  sipg_mixed_opts o = {0.1, 1e-10, 200, 0, SIPG_INNER_AUTO, SIPG_OUTER_AUTO};
   if (opts) o = *opts;
   if (!(o.inner_tol > 0) || !(o.inner_tol < 1) || !(o.outer_tol > 0) || o.max_outer < 1 || o.inner < 0 ||
-      o.inner > 3) {
-    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1, inner in 0..3");
+      o.inner > 3 || o.outer < 0 || o.outer > 2) {
+    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1, inner in 0..3, outer in 0..2");
     return SIPG_ERR_INVALID;
   }
+  int outer = o.outer;
+  if (outer == SIPG_OUTER_AUTO)
+    outer = (o.inner == SIPG_INNER_PAIRS || o.inner == SIPG_INNER_F64) ? SIPG_OUTER_RELIABLE : SIPG_OUTER_FLEXIBLE;
+  if (outer == SIPG_OUTER_FLEXIBLE && o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32) {
+    set_error("sipg_solve_mixed: the flexible outer kind runs an FP32 inner CG (inner = AUTO or F32)");
+    return SIPG_ERR_INVALID;
+  }
+  const int kind = outer == SIPG_OUTER_FLEXIBLE ? (int)SIPG_INNER_F32 : choose_inner(o.inner, op->p, op->dim, op->pen);
   cudaStream_t s = (cudaStream_t)stream;
   SIPG_CUDA_TRY(cudaSetDevice(op->device));
   const size_t n = (size_t)op->ndof;
-  const int kind = choose_inner(o.inner, op->p, op->dim, op->pen);
   MixedCache* mp = nullptr;
   sipg_status st = cache_get(op, &mp);
   if (st != SIPG_OK) return st;
@@ -318,104 +546,31 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   st = capture(op, m, kind, K);
   if (st != SIPG_OK) return st;
   const long long max_inner = o.max_inner > 0 ? o.max_inner : op->ndof;
-  const int vb = vec_grid(n);
+  Solve v{op, &m, d_x, d_b, s, n, vec_grid(n), K, 0.0};
   SIPG_CUDA_TRY(cudaEventRecord(m.ev0, s));
-
-  // ||b|| in FP64
-  k_cg_init<double><<<vb, kVecThreads, 0, s>>>(d_b, n, m.st64, 0.0, 0, 1, m.red64);
+  // ||b|| in FP64; the FP64 state's stop threshold outer_tol ||b||
+  k_cg_init<double><<<v.vb, kVecThreads, 0, s>>>(d_b, n, m.st64, o.outer_tol, 1, 1 << 30, m.red64);
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
   SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-  const double bnorm = std::sqrt(m.st64_host->bb);
-  // the inner loop may also stop once its own residual is under the target
-  const double stop_in = 0.5 * o.outer_tol * (bnorm > 0 ? bnorm : 1.0);
-  // the inner state as the host last read it
-  const bool st_double = kind != SIPG_INNER_F32;  // pairs and FP64 keep FP64 scalars in stp
-  auto inner_done = [&]() { return st_double ? m.stp_host->done : m.st32_host->done; };
-  auto inner_it = [&]() { return st_double ? m.stp_host->it : m.st32_host->it; };
-  auto inner_status = [&]() { return st_double ? m.stp_host->status : m.st32_host->status; };
-
-  int updates = 0;
-  long long inner_total = 0;
-  double rel = INFINITY;
-  sipg_status status = SIPG_OK;
-  for (;;) {
-    // the true residual in FP64
-    ApplyArgs<double> a{};
-    a.in = d_x;
-    a.out = m.r64;
-    a.b = d_b;
-    a.dim = op->dim;
-    a.nu = op->pen;
-    a.st = m.st64;
-    a.red = m.red64;
-    SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_RESID, a, op->tab, s));
-    SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
-    SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-    const double rr = m.st64_host->rr;
-    rel = (bnorm > 0) ? std::sqrt(rr) / bnorm : std::sqrt(rr);
-    if (!std::isfinite(rel)) {
-      set_error("sipg_solve_mixed: non-finite residual");
-      status = SIPG_ERR_BREAKDOWN;
-      break;
-    }
-    if (rel <= o.outer_tol || rr == 0.0) break;
-    if (updates >= o.max_outer || inner_total >= max_inner) {
-      status = SIPG_ERR_NOT_CONVERGED;
-      break;
-    }
-    // the inner residual and CG state; after the first update the direction is kept
-    if (kind == SIPG_INNER_F64)
-      k_mixed_restart_f64<<<vb, kVecThreads, 0, s>>>(m.r64, (double*)m.r, (double*)m.e, n, m.stp, m.red32,
-                                                     updates == 0, o.inner_tol, stop_in, kCorrectEvery);
-    else if (kind == SIPG_INNER_PAIRS)
-      k_mixed_restart<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.stp, m.red32, updates == 0,
-                                                               o.inner_tol, stop_in, kCorrectEvery);
-    else
-      k_mixed_restart<INNER_F32><<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.st32, m.red32, updates == 0,
-                                                             o.inner_tol, stop_in, kCorrectEvery);
-    count_launch();
-    SIPG_CUDA_TRY(cudaGetLastError());
-    const int it_before = (updates == 0) ? 0 : inner_it();
-    // inner iterations until an update is due (at most kCorrectEvery)
-    for (;;) {
-      SIPG_CUDA_TRY(cudaGraphLaunch(m.exec[kind], s));
-      count_launch(3ULL * K);
-      if (st_double)
-        SIPG_CUDA_TRY(cudaMemcpyAsync(m.stp_host, m.stp, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
-      else
-        SIPG_CUDA_TRY(cudaMemcpyAsync(m.st32_host, m.st32, sizeof(CgState<float>), cudaMemcpyDeviceToHost, s));
-      SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-      if (inner_done()) break;
-    }
-    inner_total += inner_it() - it_before;
-    if (inner_status() == (int)SIPG_ERR_BREAKDOWN) {
-      set_error("sipg_solve_mixed: inner CG breakdown");
-      status = SIPG_ERR_BREAKDOWN;
-      break;
-    }
-    if (kind == SIPG_INNER_F64)
-      k_mixed_fold_f64<<<vb, kVecThreads, 0, s>>>(d_x, (const double*)m.e, n);
-    else if (kind == SIPG_INNER_PAIRS)
-      k_mixed_fold<INNER_PAIRS><<<vb, kVecThreads, 0, s>>>(d_x, m.e, n);
-    else
-      k_mixed_fold<INNER_F32><<<vb, kVecThreads, 0, s>>>(d_x, m.e, n);
-    count_launch();
-    SIPG_CUDA_TRY(cudaGetLastError());
-    ++updates;
-  }
+  v.bnorm = std::sqrt(m.st64_host->bb);
+  const sipg_status status = outer == SIPG_OUTER_FLEXIBLE ? solve_flexible(v, o, max_inner)
+                                                          : solve_reliable(v, kind, o, max_inner);
+  if (status == SIPG_ERR_CUDA || status == SIPG_ERR_NOMEM) return status;
   SIPG_CUDA_TRY(cudaEventRecord(m.ev1, s));
   SIPG_CUDA_TRY(cudaEventSynchronize(m.ev1));
   float ms = 0;
   cudaEventElapsedTime(&ms, m.ev0, m.ev1);
   if (res) {
-    res->outer_iterations = updates;
-    res->inner_iterations = (int)inner_total;
-    res->rel_residual = rel;
+    res->outer_iterations = v.outer;
+    res->inner_iterations = (int)v.inner_total;
+    res->rel_residual = v.rel;
     res->time_ms = ms;
     res->converged = (status == SIPG_OK) ? 1 : 0;
     res->inner_kind = kind;
+    res->outer_kind = outer;
+    res->fp64_applies = v.fp64_applies;
   }
   return status;
 }

@@ -9,15 +9,17 @@
 //      pool allocator, its right-hand side built on the device, x = 0, and a
 //      slot in the device state arrays;
 //   2. runs K CG iterations of every active request together: per degree one
-//      batched apply launch for the mixed requests (inner CG on double-float
-//      pair vectors with the compensated apply, k_sipg_apply_df_batched, the
-//      requests' tiles concatenated) and one for the FP64 ones
-//      (k_sipg_apply_batched), then one batched update per precision --
+//      batched apply launch for the mixed requests (the FP32 inner CG of the
+//      flexible mixed-precision solve, sipg_fcg.cuh: FP32 vectors and the
+//      FP32 apply, the requests' tiles concatenated) and one for the FP64
+//      ones (k_sipg_apply_batched), then one batched update per precision --
 //      requests admitted while others are mid-solve simply join the next
 //      launches;
-//   3. reads all active states with one copy; mixed requests due for a
-//      reliable update get x += e and their FP64 residual (batched FP64
-//      applies), then retire or continue; FP64 requests that converged retire.
+//   3. reads all active states with one copy; mixed requests whose inner
+//      solve has finished take their FP64 flexible-CG step (batched gamma,
+//      direction, FP64 apply and update launches; a batched FP64 residual
+//      b - A x before one may stop), then retire or restart their inner
+//      solve; FP64 requests that converged retire.
 // Retired requests free their vectors at once (their results stay until the
 // caller releases them), so memory and slots turn over while others run.
 // Meshes/operators are cached and shared; all solver state stays on the device.
@@ -41,30 +43,12 @@
 #include <unordered_map>
 #include <vector>
 
-#include "sipg_cg_df.cuh"
+#include "sipg_fcg.cuh"
 
 using namespace sipg;
 
 namespace sipg {
 sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, cudaStream_t s);
-
-struct ServeMixed {  // one mixed request's operands for the vector kernels
-  double* x64;
-  const double* b64;
-  double* r64;
-  float* r32;  // pair vectors
-  float* e;
-  CgState<double>* st32;  // the inner state (FP64 scalars)
-  CgState<double>* st64;
-  ReduceScratch red32;
-  ReduceScratch red64;
-  size_t n;
-  int first;
-  double delta;
-  double tol;  // relative FP64 tolerance
-  int nblk;    // blocks this request uses (see VecInst)
-  int pad;
-};
 
 // FP64 request start: r = b (x = 0), stop = tol ||b||, p = r on the first iteration
 __global__ void __launch_bounds__(kVecThreads) k_serve_init_f64(const VecInst<double>* __restrict__ insts,
@@ -101,61 +85,38 @@ __global__ void __launch_bounds__(kVecThreads) k_serve_init_f64(const VecInst<do
   }
 }
 
-// mixed request start: ||b||, r64 = b (x = 0), then the FP32 state (first run)
-__global__ void __launch_bounds__(kVecThreads) k_serve_init_mixed(const ServeMixed* __restrict__ insts) {
+// mixed request start: x = 0, r64 = b, ||b||^2 and the FP64 state (stop =
+// tol ||b||); the inner restart (k_fcg_restart_batched) follows on the stream
+__global__ void __launch_bounds__(kVecThreads) k_serve_init_fcg(const FcgInst* __restrict__ insts,
+                                                                const double* __restrict__ tols) {
   __shared__ double sh[32];
-  const ServeMixed m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
   double acc = 0.0;
-  const size_t stride = (size_t)m.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += stride) {
-    const double bi = m.b64[i];
-    m.x64[i] = 0.0;
-    m.r64[i] = bi;
-    const float v = (float)bi;
-    m.r32[i] = v;
-    m.r32[m.n + i] = (float)(bi - (double)v);
-    m.e[i] = 0.f;
-    m.e[m.n + i] = 0.f;
+  const size_t stride = (size_t)v.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += stride) {
+    const double bi = v.b[i];
+    v.x[i] = 0.0;
+    v.r64[i] = bi;
     acc = fma(bi, bi, acc);
   }
   const double bt = block_sum<double, kVecThreads>(acc, sh);
   double total;
-  if (grid_sum_last<double, kVecThreads>(bt, m.red64, blockIdx.x, m.nblk, sh, &total) && threadIdx.x == 0) {
-    m.st64->bb = total;
-    m.st64->rr = total;
-    CgState<double>* st = m.st32;
-    st->first = 1;
-    st->it = 0;
-    st->parity = 0;
-    st->beta = 0.0;
-    st->status = (int)SIPG_OK;
+  if (grid_sum_last<double, kVecThreads>(bt, v.red64, blockIdx.x, v.nblk, sh, &total) && threadIdx.x == 0) {
+    CgState<double>* st = v.st64;
+    st->bb = total;
     st->rr = total;
-    st->rmax = sqrt(total);
-    st->delta = m.delta;
-    // the inner loop also stops under the request's target, for the FP64 check
-    st->stop = 0.5 * m.tol * sqrt(total);
-    st->max_it = 1000;  // an FP64 update is forced after 1000 inner iterations
+    st->stop = tols[blockIdx.y] * sqrt(total);
+    st->max_it = 1 << 30;
+    st->it = 0;
+    st->first = 1;
+    st->parity = 0;
+    st->status = (int)SIPG_OK;
     st->need_update = 0;
-    st->done = (total == 0.0) ? 1 : 0;
+    st->delta = 0.0;
+    st->rmax = 0.0;
+    st->done = !(sqrt(total) > st->stop);
   }
-}
-
-// x64 += e for every listed mixed request
-__global__ void __launch_bounds__(kVecThreads) k_serve_fold(const ServeMixed* __restrict__ insts) {
-  const ServeMixed m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
-  inner_fold_body<INNER_PAIRS>(m.x64, m.e, m.n, blockIdx.x, m.nblk);
-}
-
-// after an FP64 update: the inner residual = r64 as pairs, e = 0, beta =
-// r_new.r_new / r_prev.r_prev, and the inner iterations continue with the
-// kept search direction
-__global__ void __launch_bounds__(kVecThreads) k_serve_restart(const ServeMixed* __restrict__ insts) {
-  const ServeMixed m = insts[blockIdx.y];
-  if ((int)blockIdx.x >= m.nblk) return;
-  const double stop = 0.5 * m.tol * sqrt(m.st64->bb);  // as at the start
-  inner_restart_body<INNER_PAIRS>(m.r64, m.r32, m.e, m.n, m.st32, m.red32, 0, m.delta, stop, 1000, blockIdx.x, m.nblk);
 }
 
 }  // namespace sipg
@@ -178,14 +139,18 @@ struct Request {
   size_t x_bytes = 0;
   double* b64 = nullptr;
   double* r64 = nullptr;     // mixed: FP64 residual; FP64: r
-  float* e32 = nullptr;      // mixed: pair vectors (2 n floats) from here
+  double* d64 = nullptr;     // mixed: FP64 direction and A d
+  double* q64 = nullptr;
+  float* e32 = nullptr;      // mixed: FP32 inner solution, residual, direction, A p
   float* r32 = nullptr;
-  float* p32[2] = {nullptr, nullptr};
+  float* p32 = nullptr;
   float* Ap32 = nullptr;
   double* p64[2] = {nullptr, nullptr};
   double* Ap64 = nullptr;
   ReduceScratch red32, red64;
-  int corrections = 0;
+  int corrections = 0;        // mixed: flexible outer steps taken
+  int first = 1;              // mixed: the next outer step starts a direction history
+  long long inner_total = 0;  // mixed: FP32 inner iterations
   int started = 0;
   Clock::time_point t_submit, t_admit, t_done;
   sipg_request_result result{};
@@ -193,8 +158,9 @@ struct Request {
 };
 
 struct Slots {
-  CgState<double>* d32 = nullptr;  // mixed requests' inner states
-  CgState<double>* d64 = nullptr;
+  CgState<float>* d32 = nullptr;   // mixed requests' inner (FP32) states
+  CgState<double>* d64 = nullptr;  // FP64 CG states, or mixed requests' outer states
+  FcgState* fs = nullptr;          // mixed requests' flexible-step scalars
 };
 
 // One size class of requests (see the file comment).
@@ -205,7 +171,7 @@ struct Lane {
   std::vector<Request*> active;  // started requests
   std::vector<Request*> fresh;   // admitted; started at the lane's next round
   // pinned mirrors of the slot states, written by this lane's copies only
-  CgState<double>* h32 = nullptr;
+  CgState<float>* h32 = nullptr;
   CgState<double>* h64 = nullptr;
   // pinned staging and device descriptor arrays (capacity max_active; tile
   // starts max_active + 16): FP32 CG applies, FP64 CG applies, FP64 residuals
@@ -221,12 +187,12 @@ struct Lane {
   int* d_t64 = nullptr;
   int* h_tr = nullptr;
   int* d_tr = nullptr;
-  PairInst* h_v32 = nullptr;
-  PairInst* d_v32 = nullptr;
+  FcgInst* h_v32 = nullptr;  // the mixed requests of a round (inner kernels)
+  FcgInst* d_v32 = nullptr;
   VecInst<double>* h_v64 = nullptr;
   VecInst<double>* d_v64 = nullptr;
-  ServeMixed* h_m = nullptr;
-  ServeMixed* d_m = nullptr;
+  FcgInst* h_m = nullptr;    // a selection of mixed requests (start, outer step, restart)
+  FcgInst* d_m = nullptr;
   double* h_tol = nullptr;
   double* d_tol = nullptr;
   const double** h_bptr = nullptr;
@@ -261,7 +227,7 @@ size_t footprint_of(int dim, int p, int precision) {
   const size_t n = (size_t)dim * dim * (p + 1) * (p + 1);
   const size_t red = 2 * (sizeof(double) * (size_t)reduce_capacity(dim) + 256);
   if (precision == SIPG_F64) return n * (8 * 2 + 8 * 4) + red + 4096;  // x, b, r, p0, p1, Ap
-  return n * (8 * 3 + 8 * 4) + red + 4096;                             // x, b, r64 + pairs e, r, p, Ap
+  return n * (8 * 5 + 4 * 4) + red + 4096;                             // x, b, r, d, q + FP32 e, r, p, Ap
 }
 
 sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
@@ -279,11 +245,33 @@ sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
   return SIPG_OK;
 }
 
+// Gives back what admit() took before one of its steps failed: the request
+// then holds no device memory and no slot.
+sipg_status admit_rollback(Request* r, cudaStream_t s, sipg_status st) {
+  if (r->mem) cudaFreeAsync(r->mem, s);
+  if (r->x64) cudaFreeAsync(r->x64, s);
+  r->mem = nullptr;
+  r->x64 = nullptr;
+  return st;
+}
+
 // carve one pool allocation into the request's vectors
 sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
   r->x_bytes = r->n * sizeof(double);
-  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->x64, r->x_bytes, s));
-  SIPG_CUDA_TRY(cudaMallocAsync((void**)&r->mem, r->footprint - r->x_bytes, s));
+  r->x64 = nullptr;
+  r->mem = nullptr;
+  void* xa = nullptr;
+  void* ma = nullptr;
+  cudaError_t e = cudaMallocAsync(&xa, r->x_bytes, s);
+  if (e == cudaSuccess) {
+    r->x64 = (double*)xa;
+    e = cudaMallocAsync(&ma, r->footprint - r->x_bytes, s);
+    if (e == cudaSuccess) r->mem = (char*)ma;
+  }
+  if (e != cudaSuccess) {
+    set_error(std::string("sipg_server_step: admission failed: ") + cudaGetErrorString(e));
+    return admit_rollback(r, s, e == cudaErrorMemoryAllocation ? SIPG_ERR_NOMEM : SIPG_ERR_CUDA);
+  }
   char* p = r->mem;
   auto take = [&](size_t bytes) {
     char* q = p;
@@ -299,10 +287,12 @@ sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
     r->p64[1] = (double*)take(n * 8);
     r->Ap64 = (double*)take(n * 8);
   } else {
-    r->e32 = (float*)take(n * 8);
-    r->r32 = (float*)take(n * 8);
-    r->p32[0] = (float*)take(n * 8);
-    r->Ap32 = (float*)take(n * 8);
+    r->d64 = (double*)take(n * 8);
+    r->q64 = (double*)take(n * 8);
+    r->e32 = (float*)take(n * 4);
+    r->r32 = (float*)take(n * 4);
+    r->p32 = (float*)take(n * 4);
+    r->Ap32 = (float*)take(n * 4);
   }
   r->red32.partials = (double*)take(sizeof(double) * cap);
   r->red32.counter = (unsigned int*)take(256);
@@ -310,11 +300,15 @@ sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
   r->red64.partials = (double*)take(sizeof(double) * cap);
   r->red64.counter = (unsigned int*)take(256);
   r->red64.capacity = cap;
-  SIPG_CUDA_TRY(cudaMemsetAsync(r->red32.counter, 0, 4, s));
-  SIPG_CUDA_TRY(cudaMemsetAsync(r->red64.counter, 0, 4, s));
+  e = cudaMemsetAsync(r->red32.counter, 0, 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(r->red64.counter, 0, 4, s);
+  if (e != cudaSuccess) {
+    set_error(std::string("sipg_server_step: admission failed: ") + cudaGetErrorString(e));
+    return admit_rollback(r, s, SIPG_ERR_CUDA);
+  }
   const sipg_modes* modes = (r->req.sol == SIPG_SOL_MODES) ? &r->req.modes : nullptr;
   sipg_status st = rhs_f64(r->op, r->req.sol, modes, r->b64, s);
-  if (st != SIPG_OK) return st;
+  if (st != SIPG_OK) return admit_rollback(r, s, st);
   r->slot = sv->free_slots.back();
   sv->free_slots.pop_back();
   sv->used += r->footprint;
@@ -344,12 +338,11 @@ void retire(sipg_server* sv, Request* r, cudaStream_t s, sipg_status status, int
 
 ApplyArgs<float> cg_args32(const Request* r, sipg_server* sv) {
   ApplyArgs<float> a{};
-  a.in = r->p32[0];  // the direction, formed by k_cg_direction_pairs_batched
+  a.in = r->p32;  // the direction, formed by k_fcg_inner_direction_batched
   a.out = r->Ap32;
   a.dim = r->req.dim;
   a.nu = (float)r->req.pen;
-  set_penalty3(a, r->req.pen);
-  a.stp = sv->slots.d32 + r->slot;
+  a.st = sv->slots.d32 + r->slot;
   a.red = r->red32;
   return a;
 }
@@ -367,24 +360,31 @@ ApplyArgs<double> cg_args64(const Request* r, sipg_server* sv) {
   return a;
 }
 
-ServeMixed mixed_of(const Request* r, sipg_server* sv, int first) {
-  ServeMixed m;
-  m.x64 = r->x64;
-  m.b64 = r->b64;
-  m.r64 = r->r64;
-  m.e = r->e32;
-  m.r32 = r->r32;
-  m.st32 = sv->slots.d32 + r->slot;
-  m.st64 = sv->slots.d64 + r->slot;
-  m.red32 = r->red32;
-  m.red64 = r->red64;
-  m.n = r->n;
-  m.first = first;
-  m.delta = sv->opts.inner_tol;
-  m.tol = r->req.tol;
-  m.nblk = inst_blocks(r->n);
-  m.pad = 0;
-  return m;
+// inner iterations one preconditioner solve may take
+constexpr int kInnerCap = 4000;
+
+FcgInst fcg_of(const Request* r, sipg_server* sv) {
+  FcgInst v;
+  v.x = r->x64;
+  v.b = r->b64;
+  v.r64 = r->r64;
+  v.d64 = r->d64;
+  v.q64 = r->q64;
+  v.r32 = r->r32;
+  v.e32 = r->e32;
+  v.p32 = r->p32;
+  v.Ap32 = r->Ap32;
+  v.st32 = sv->slots.d32 + r->slot;
+  v.st64 = sv->slots.d64 + r->slot;
+  v.fs = sv->slots.fs + r->slot;
+  v.red32 = r->red32;
+  v.red64 = r->red64;
+  v.n = r->n;
+  v.nblk = inst_blocks(r->n);
+  v.first = r->first;
+  v.stop = (float)sv->opts.inner_tol;
+  v.max_it = kInnerCap;
+  return v;
 }
 
 // A list of requests grouped by degree, packed into one descriptor array
@@ -406,7 +406,7 @@ std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArg
     const std::vector<Request*>& g = kv.second;
     GroupLaunch gl;
     gl.p = kv.first;
-    gl.cfg = (sizeof(T) == 8) ? batched_tile(g[0]->op->cfg64) : g[0]->op->cfgdf;
+    gl.cfg = batched_tile((sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfg32);
     gl.off = off;
     gl.m = (int)g.size();
     gl.toff = toff;
@@ -441,8 +441,8 @@ sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const Ap
     cudaError_t e = (sizeof(T) == 8)
                         ? launch_apply_batched_f64(g.p, g.cfg, mode, (const ApplyArgs<double>*)(d_a + g.off),
                                                    d_t + g.toff, g.m, g.total, *g.tab, s)
-                        : launch_apply_df(g.p, g.cfg, mode, ApplyArgs<float>{}, (const ApplyArgs<float>*)(d_a + g.off),
-                                          d_t + g.toff, g.m, g.total, *g.tab, s);
+                        : launch_apply_batched_f32(g.p, g.cfg, mode, (const ApplyArgs<float>*)(d_a + g.off),
+                                                   d_t + g.toff, g.m, g.total, *g.tab, s);
     SIPG_CUDA_TRY(e);
   }
   return SIPG_OK;
@@ -451,10 +451,12 @@ sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const Ap
 sipg_status server_alloc(sipg_server* sv) {
   const int cap = sv->opts.max_active;
   SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking));
-  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<float>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d64, sizeof(CgState<double>) * cap));
-  SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMalloc(&sv->slots.fs, sizeof(FcgState) * cap));
+  SIPG_CUDA_TRY(cudaMemset(sv->slots.d32, 0, sizeof(CgState<float>) * cap));
   SIPG_CUDA_TRY(cudaMemset(sv->slots.d64, 0, sizeof(CgState<double>) * cap));
+  SIPG_CUDA_TRY(cudaMemset(sv->slots.fs, 0, sizeof(FcgState) * cap));
   int least = 0, greatest = 0;  // numerically: greatest priority is the lowest value
   SIPG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   for (int k = 0; k < kLanes; ++k) {
@@ -462,7 +464,7 @@ sipg_status server_alloc(sipg_server* sv) {
     const int prio = greatest + (least - greatest) * k / (kLanes - 1);
     SIPG_CUDA_TRY(cudaStreamCreateWithPriority(&L.s, cudaStreamNonBlocking, prio));
     SIPG_CUDA_TRY(cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming));
-    SIPG_CUDA_TRY(cudaMallocHost(&L.h32, sizeof(CgState<double>) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h32, sizeof(CgState<float>) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h64, sizeof(CgState<double>) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_a32, sizeof(ApplyArgs<float>) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&L.d_a32, sizeof(ApplyArgs<float>) * cap));
@@ -476,12 +478,12 @@ sipg_status server_alloc(sipg_server* sv) {
       SIPG_CUDA_TRY(cudaMallocHost(tiles_h[t], sizeof(int) * (cap + 16)));
       SIPG_CUDA_TRY(cudaMalloc(tiles_d[t], sizeof(int) * (cap + 16)));
     }
-    SIPG_CUDA_TRY(cudaMallocHost(&L.h_v32, sizeof(PairInst) * cap));
-    SIPG_CUDA_TRY(cudaMalloc(&L.d_v32, sizeof(PairInst) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_v32, sizeof(FcgInst) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_v32, sizeof(FcgInst) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_v64, sizeof(VecInst<double>) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&L.d_v64, sizeof(VecInst<double>) * cap));
-    SIPG_CUDA_TRY(cudaMallocHost(&L.h_m, sizeof(ServeMixed) * cap));
-    SIPG_CUDA_TRY(cudaMalloc(&L.d_m, sizeof(ServeMixed) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_m, sizeof(FcgInst) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_m, sizeof(FcgInst) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_tol, sizeof(double) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&L.d_tol, sizeof(double) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_bptr, sizeof(double*) * cap));
@@ -506,6 +508,7 @@ void server_free(sipg_server* sv) {
   if (sv->s) cudaStreamSynchronize(sv->s);
   cudaFree(sv->slots.d32);
   cudaFree(sv->slots.d64);
+  cudaFree(sv->slots.fs);
   for (Lane& L : sv->lanes) {
     cudaFreeHost(L.h32);
     cudaFreeHost(L.h64);
@@ -570,22 +573,31 @@ sipg_status lane_start(sipg_server* sv, Lane& L) {
       nmax64 = std::max(nmax64, r->n);
       ++m64;
     } else {
-      L.h_m[m32++] = mixed_of(r, sv, 1);
+      r->first = 1;
+      L.h_m[m32++] = fcg_of(r, sv);
       nmax32 = std::max(nmax32, r->n);
     }
   }
+  // the mixed requests' tolerances follow the FP64 ones in the staging
+  {
+    int j = 0;
+    for (Request* r : L.fresh)
+      if (r->req.precision != SIPG_F64) L.h_tol[m64 + j++] = r->req.tol;
+  }
+  if (m64 + m32) SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_tol, L.h_tol, sizeof(double) * (m64 + m32), cudaMemcpyHostToDevice, L.s));
   if (m64) {
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v64, L.h_v64, sizeof(VecInst<double>) * m64, cudaMemcpyHostToDevice, L.s));
-    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_tol, L.h_tol, sizeof(double) * m64, cudaMemcpyHostToDevice, L.s));
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_bptr, L.h_bptr, sizeof(double*) * m64, cudaMemcpyHostToDevice, L.s));
     k_serve_init_f64<<<dim3(vec_bpi(nmax64, m64), m64), kVecThreads, 0, L.s>>>(L.d_v64, L.d_tol, L.d_bptr);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
   }
   if (m32) {
-    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m32, cudaMemcpyHostToDevice, L.s));
-    k_serve_init_mixed<<<dim3(vec_bpi(nmax32, m32), m32), kVecThreads, 0, L.s>>>(L.d_m);
-    count_launch();
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(FcgInst) * m32, cudaMemcpyHostToDevice, L.s));
+    const dim3 g(vec_bpi(nmax32, m32), m32);
+    k_serve_init_fcg<<<g, kVecThreads, 0, L.s>>>(L.d_m, L.d_tol + m64);
+    k_fcg_restart_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
+    count_launch(2);
     SIPG_CUDA_TRY(cudaGetLastError());
   }
   SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
@@ -603,18 +615,7 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
   size_t nmax32 = 0, nmax64 = 0;
   for (int j = 0; j < (int)a32.size(); ++j) {
     Request* r = a32[j];
-    PairInst v;
-    v.x = r->e32;
-    v.pb0 = r->p32[0];
-    v.pb1 = r->p32[0];
-    v.r = r->r32;
-    v.Ap = r->Ap32;
-    v.n = r->n;
-    v.st = sv->slots.d32 + r->slot;
-    v.red = r->red32;
-    v.nblk = inst_blocks(r->n);
-    v.pad = 0;
-    L.h_v32[j] = v;
+    L.h_v32[j] = fcg_of(r, sv);
     nmax32 = std::max(nmax32, r->n);
   }
   for (int j = 0; j < (int)a64.size(); ++j) {
@@ -634,7 +635,7 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
     nmax64 = std::max(nmax64, r->n);
   }
   if (!a32.empty())
-    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v32, L.h_v32, sizeof(PairInst) * a32.size(), cudaMemcpyHostToDevice, L.s));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v32, L.h_v32, sizeof(FcgInst) * a32.size(), cudaMemcpyHostToDevice, L.s));
   if (!a64.empty())
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v64, L.h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, L.s));
   const std::vector<GroupLaunch> g32 =
@@ -649,12 +650,12 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
   for (int k = 0; k < sv->opts.iters_per_step; ++k) {
     if (!a32.empty()) {
       const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
-      k_cg_direction_pairs_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      k_fcg_inner_direction_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
       sipg_status st = launch_groups<float>(g32, APPLY_DOT, L.d_a32, L.d_t32, L.s);
       if (st != SIPG_OK) return st;
-      k_cg_update_pairs_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      k_fcg_inner_update_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
     }
@@ -668,7 +669,7 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
     }
   }
   const int cap = sv->opts.max_active;
-  SIPG_CUDA_TRY(cudaMemcpyAsync(L.h32, sv->slots.d32, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(L.h32, sv->slots.d32, sizeof(CgState<float>) * cap, cudaMemcpyDeviceToHost, L.s));
   SIPG_CUDA_TRY(cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
   SIPG_CUDA_TRY(cudaEventRecord(L.ev, L.s));
   L.busy = true;
@@ -676,8 +677,9 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
 }
 
 // After a lane's round: FP64 requests that are done retire; mixed requests
-// due a reliable update get x += e and their FP64 residual (batched FP64
-// applies, synchronously on the lane's stream), then retire or restart.
+// whose inner solve finished take their flexible-CG step in FP64 (batched,
+// synchronously on the lane's stream), then retire -- after b - A x in FP64
+// confirms the target -- or restart their inner solve.
 sipg_status lane_finish(sipg_server* sv, Lane& L) {
   std::vector<Request*> keep, fix;
   for (Request* r : L.active) {
@@ -692,64 +694,114 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
       } else {
         keep.push_back(r);
       }
-    } else {
-      if (L.h32[r->slot].done) fix.push_back(r);
-      else keep.push_back(r);
+      continue;
     }
+    const CgState<float>& h32 = L.h32[r->slot];
+    if (!h32.done) {
+      keep.push_back(r);
+      continue;
+    }
+    r->inner_total += h32.it;
+    if (h32.it == 0) {
+      // no inner step: a zero residual (b = 0 or x exact) retires, else there is no direction
+      const CgState<double>& h = L.h64[r->slot];
+      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
+      retire(sv, r, L.s, h.rr == 0.0 ? SIPG_OK : SIPG_ERR_BREAKDOWN, (int)r->inner_total, rel);
+      continue;
+    }
+    fix.push_back(r);
   }
   if (!fix.empty()) {
+    const int cap = sv->opts.max_active;
     int m = 0;
     size_t nmax = 0;
     for (Request* r : fix) {
-      L.h_m[m++] = mixed_of(r, sv, 0);
+      L.h_m[m++] = fcg_of(r, sv);
       nmax = std::max(nmax, r->n);
     }
-    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, L.s));
-    k_serve_fold<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, L.s>>>(L.d_m);
-    count_launch();
+    const dim3 g(vec_bpi(nmax, m), m);
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(FcgInst) * m, cudaMemcpyHostToDevice, L.s));
+    k_fcg_gamma_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
+    k_fcg_direction_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
+    count_launch(2);
     SIPG_CUDA_TRY(cudaGetLastError());
-    const std::vector<GroupLaunch> gr = pack_groups<double>(fix, L.h_r64, L.h_tr, [&](const Request* r) {
+    // q = A d in FP64, alpha = d.r / d.q
+    const std::vector<GroupLaunch> gq = pack_groups<double>(fix, L.h_r64, L.h_tr, [&](const Request* r) {
       ApplyArgs<double> a{};
-      a.in = r->x64;
-      a.out = r->r64;
-      a.b = r->b64;
+      a.in = r->d64;
+      a.out = r->q64;
       a.dim = r->req.dim;
       a.nu = r->req.pen;
       a.st = sv->slots.d64 + r->slot;
       a.red = r->red64;
       return a;
     });
-    sipg_status st = upload_groups<double>(gr, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
-    if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, L.d_r64, L.d_tr, L.s);
+    sipg_status st = upload_groups<double>(gq, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
+    if (st == SIPG_OK) st = launch_groups<double>(gq, APPLY_DOT, L.d_r64, L.d_tr, L.s);
     if (st != SIPG_OK) return st;
-    const int cap = sv->opts.max_active;
+    k_fcg_update_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
-    std::vector<Request*> cont;
+    std::vector<Request*> cont, chk;
     for (Request* r : fix) {
       r->corrections++;
+      r->first = 0;
       const CgState<double>& h = L.h64[r->slot];
-      const CgState<double>& h32 = L.h32[r->slot];
-      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : 0.0;
-      if (!std::isfinite(rel) || h32.status == (int)SIPG_ERR_BREAKDOWN) {
-        retire(sv, r, L.s, SIPG_ERR_BREAKDOWN, h32.it, rel);
-      } else if (rel <= r->req.tol || h.rr == 0.0) {
-        retire(sv, r, L.s, SIPG_OK, h32.it, rel);
+      const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : std::sqrt(h.rr);
+      if (!std::isfinite(rel) || h.status == (int)SIPG_ERR_BREAKDOWN) {
+        retire(sv, r, L.s, SIPG_ERR_BREAKDOWN, (int)r->inner_total, rel);
+      } else if (rel <= r->req.tol) {
+        chk.push_back(r);
       } else if (r->corrections >= 1000) {
-        retire(sv, r, L.s, SIPG_ERR_NOT_CONVERGED, h32.it, rel);
+        retire(sv, r, L.s, SIPG_ERR_NOT_CONVERGED, (int)r->inner_total, rel);
       } else {
         cont.push_back(r);
+      }
+    }
+    if (!chk.empty()) {
+      // the recursion says done: b - A x in FP64 decides
+      const std::vector<GroupLaunch> gr = pack_groups<double>(chk, L.h_r64, L.h_tr, [&](const Request* r) {
+        ApplyArgs<double> a{};
+        a.in = r->x64;
+        a.out = r->r64;
+        a.b = r->b64;
+        a.dim = r->req.dim;
+        a.nu = r->req.pen;
+        a.st = sv->slots.d64 + r->slot;
+        a.red = r->red64;
+        return a;
+      });
+      st = upload_groups<double>(gr, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
+      if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, L.d_r64, L.d_tr, L.s);
+      if (st != SIPG_OK) return st;
+      SIPG_CUDA_TRY(
+          cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));
+      SIPG_CUDA_TRY(cudaStreamSynchronize(L.s));
+      for (Request* r : chk) {
+        const CgState<double>& h = L.h64[r->slot];
+        const double rel = h.bb > 0 ? std::sqrt(h.rr / h.bb) : std::sqrt(h.rr);
+        if (rel <= r->req.tol) {
+          retire(sv, r, L.s, SIPG_OK, (int)r->inner_total, rel);
+        } else if (r->corrections >= 1000 || !std::isfinite(rel)) {
+          retire(sv, r, L.s, std::isfinite(rel) ? SIPG_ERR_NOT_CONVERGED : SIPG_ERR_BREAKDOWN, (int)r->inner_total,
+                 rel);
+        } else {
+          r->first = 1;  // a fresh direction history from the true residual
+          cont.push_back(r);
+        }
       }
     }
     if (!cont.empty()) {
       m = 0;
       nmax = 0;
       for (Request* r : cont) {
-        L.h_m[m++] = mixed_of(r, sv, 0);
+        L.h_m[m++] = fcg_of(r, sv);
         nmax = std::max(nmax, r->n);
       }
-      SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(ServeMixed) * m, cudaMemcpyHostToDevice, L.s));
-      k_serve_restart<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, L.s>>>(L.d_m);
+      SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_m, L.h_m, sizeof(FcgInst) * m, cudaMemcpyHostToDevice, L.s));
+      k_fcg_restart_batched<<<dim3(vec_bpi(nmax, m), m), kVecThreads, 0, L.s>>>(L.d_m);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
       for (Request* r : cont) keep.push_back(r);
@@ -770,7 +822,7 @@ sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** out) 
   *out = nullptr;
   sipg_server* sv = new (std::nothrow) sipg_server;
   if (!sv) return SIPG_ERR_NOMEM;
-  sipg_server_opts o = {150ull << 30, 256, 8, 0.1};
+  sipg_server_opts o = {150ull << 30, 256, 8, 1e-2};
   if (opts) o = *opts;
   if (o.max_active < 1 || o.max_active > 4096 || o.iters_per_step < 1 || !(o.inner_tol > 0 && o.inner_tol < 1)) {
     set_error("sipg_server_create: need 1 <= max_active <= 4096, iters_per_step >= 1, 0 < inner_tol < 1");
@@ -831,8 +883,19 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
     if (st != SIPG_OK) return st;
     Lane& L = sv->lanes[lane_of(r->n)];
     st = admit(sv, r, L.s);
-    if (st != SIPG_OK) return st;
     sv->queue.pop_front();
+    if (st != SIPG_OK) {
+      // the request holds nothing (admit rolled back); it retires with the
+      // error rather than being admitted again at the next step
+      r->t_admit = r->t_done = Clock::now();
+      r->result.status = st;
+      r->result.done = 1;
+      r->result.latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+      r->state = 2;
+      sv->rejected++;
+      if (st == SIPG_ERR_NOMEM) continue;  // the pool is short now; later requests may still fit
+      return st;
+    }
     L.fresh.push_back(r);
   }
   // 2. every lane whose round has ended: its results, then its next round;

@@ -16,8 +16,8 @@
 //     Q_j = w_j (kappa (d0 + dN) + nu (u0 - uN)) (consistency + penalty)
 // The 0-side element adds Q_j to its face node, the N-side element subtracts
 // it, and both lift J_j with D[.][0] / D[.][P].  This is algebraically the
-// reference's e, f, g, h and a, b, c, d of sipg_sem_2d_gpu_kernels.hpp:300-334
-// and :367-400, computed once per face instead of once per side.
+// reference's e, f, g, h and a, b, c, d of sipg_sem_2d_gpu_kernels.hpp:209-247
+// and :277-312, computed once per face instead of once per side.
 //
 // Phases of a CTA (all smem; halo elements are read from global/L2 and only
 // their one relevant face is computed):
@@ -640,6 +640,9 @@ cudaError_t launch_apply_batched_tile(int mode, const ApplyArgs<T>* insts, const
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess || mode == APPLY_PREPARE || total_tiles == 0) return err;
   const dim3 grid(total_tiles), block(TX, TY);
   switch (mode) {
@@ -651,6 +654,9 @@ cudaError_t launch_apply_batched_tile(int mode, const ApplyArgs<T>* insts, const
       break;
     case APPLY_RESID:
       k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    case APPLY_DOT:
+      k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
       break;
     default:
       return cudaErrorInvalidValue;

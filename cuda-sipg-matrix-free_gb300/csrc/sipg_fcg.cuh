@@ -1,0 +1,200 @@
+// sipg_fcg.cuh -- device steps of the flexible mixed-precision solve (no
+// counterpart in the reference): flexible CG in FP64 (Notay, SIAM J. Sci.
+// Comput. 22, 2000, truncated to one previous direction) whose
+// preconditioner is an FP32 CG run from zero on the scaled residual.
+//
+// One outer step, for each instance:
+//   restart   r32 = r64 / ||r64||, e = 0, fresh FP32 CG state        (16 B/DoF)
+//   (inner)   FP32 CG iterations on A e = r32 until its residual fell by
+//             the inner tolerance                                    (40 B/DoF each)
+//   gamma     z = ||r64|| e;  gamma = z.q_prev / d_prev.q_prev        (12 B/DoF)
+//   direction d = z - gamma d_prev (first: d = z);  d.r              (28 B/DoF)
+//   FP64 apply q = A d; alpha = d.r / d.q (APPLY_DOT)                (16 B/DoF)
+//   update    x += alpha d, r64 -= alpha q, r.r (cg_update_body)     (48 B/DoF)
+// The FP64 CgState of an instance carries r.r after the update and d.r
+// before the apply (APPLY_DOT's alpha = rr / pAp); pAp = d.q stays there for
+// the next step's gamma.  Each body works on the grid-stride slice of block
+// `bid` of `nblocks` and reduces deterministically (grid_sum_last), so the
+// single-solve kernels (bid = blockIdx.x) and the batched ones (one instance
+// per blockIdx.y, nblk blocks each) give the same iterates.
+#pragma once
+
+#include "sipg_cg.cuh"
+
+namespace sipg {
+
+// Scalars of the flexible outer loop beside its FP64 CgState.
+struct FcgState {
+  double zscale;  // ||r64|| at the inner restart: z = zscale * e
+  double gamma;   // z.q_prev / d_prev.q_prev
+};
+
+__device__ __forceinline__ void fcg_restart_body(const double* __restrict__ r64, float* __restrict__ r,
+                                                 float* __restrict__ e, size_t n, const CgState<double>* st64,
+                                                 FcgState* fs, CgState<float>* st, const ReduceScratch& red,
+                                                 float stop, int max_it, int bid, int nblocks) {
+  __shared__ float sh[32];
+  const double rr = st64->rr;
+  const double inv = rr > 0.0 ? 1.0 / sqrt(rr) : 1.0;
+  float acc = 0.f;
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float h = (float)(r64[i] * inv);
+    r[i] = h;
+    e[i] = 0.f;
+    acc = fmaf(h, h, acc);
+  }
+  const float bt = block_sum<float, kVecThreads>(acc, sh);
+  float total;
+  if (grid_sum_last<float, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
+    st->first = 1;
+    st->it = 0;
+    st->parity = 0;
+    st->beta = 0.f;
+    st->status = (int)SIPG_OK;
+    st->rr = total;
+    st->rmax = sqrtf(total);
+    st->delta = 0.f;  // no reliable updates inside a preconditioner solve
+    st->stop = stop;
+    st->max_it = max_it;
+    st->need_update = 0;
+    st->done = (total == 0.f) ? 1 : 0;
+    fs->zscale = rr > 0.0 ? sqrt(rr) : 1.0;
+  }
+}
+
+__device__ __forceinline__ void fcg_gamma_body(const float* __restrict__ e, const double* __restrict__ q, size_t n,
+                                               const CgState<double>* st64, FcgState* fs, const ReduceScratch& red,
+                                               int bid, int nblocks) {
+  __shared__ double sh[32];
+  const double zs = fs->zscale;
+  double acc = 0.0;
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride)
+    acc = fma((double)e[i] * zs, q[i], acc);
+  const double bt = block_sum<double, kVecThreads>(acc, sh);
+  double total;
+  if (grid_sum_last<double, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0)
+    fs->gamma = total / st64->pAp;
+}
+
+__device__ __forceinline__ void fcg_direction_body(const float* __restrict__ e, double* __restrict__ d,
+                                                   const double* __restrict__ r, size_t n, CgState<double>* st64,
+                                                   const FcgState* fs, const ReduceScratch& red, int first, int bid,
+                                                   int nblocks) {
+  __shared__ double sh[32];
+  const double zs = fs->zscale;
+  const double g = first ? 0.0 : fs->gamma;
+  double acc = 0.0;
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double z = (double)e[i] * zs;
+    const double di = first ? z : fma(-g, d[i], z);
+    d[i] = di;
+    acc = fma(di, r[i], acc);
+  }
+  const double bt = block_sum<double, kVecThreads>(acc, sh);
+  double total;
+  if (grid_sum_last<double, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
+    st64->rr_prev = st64->rr;  // r.r, kept for the host's progress check
+    st64->rr = total;
+    st64->parity = 0;
+    st64->done = 0;
+    if (!isfinite(total)) {
+      st64->status = (int)SIPG_ERR_BREAKDOWN;
+      st64->done = 1;
+    }
+  }
+}
+
+// ---- one solve ----
+
+static __global__ void __launch_bounds__(kVecThreads)
+    k_fcg_restart(const double* __restrict__ r64, float* __restrict__ r, float* __restrict__ e, size_t n,
+                  const CgState<double>* st64, FcgState* fs, CgState<float>* st, ReduceScratch red, float stop,
+                  int max_it) {
+  fcg_restart_body(r64, r, e, n, st64, fs, st, red, stop, max_it, blockIdx.x, gridDim.x);
+}
+
+static __global__ void __launch_bounds__(kVecThreads)
+    k_fcg_gamma(const float* __restrict__ e, const double* __restrict__ q, size_t n, const CgState<double>* st64,
+                FcgState* fs, ReduceScratch red) {
+  fcg_gamma_body(e, q, n, st64, fs, red, blockIdx.x, gridDim.x);
+}
+
+static __global__ void __launch_bounds__(kVecThreads)
+    k_fcg_direction(const float* __restrict__ e, double* __restrict__ d, const double* __restrict__ r, size_t n,
+                    CgState<double>* st64, const FcgState* fs, ReduceScratch red, int first) {
+  fcg_direction_body(e, d, r, n, st64, fs, red, first, blockIdx.x, gridDim.x);
+}
+
+// ---- many instances (instance = blockIdx.y, nblk blocks each) ----
+
+// One instance's operands of the flexible solve.
+struct FcgInst {
+  double* x;        // FP64 solution
+  const double* b;  // FP64 right-hand side
+  double* r64;      // FP64 residual
+  double* d64;      // FP64 direction
+  double* q64;      // A d
+  float* r32;       // FP32 inner residual
+  float* e32;       // FP32 inner solution
+  float* p32;       // FP32 inner direction
+  float* Ap32;      // FP32 inner A p
+  CgState<float>* st32;
+  CgState<double>* st64;
+  FcgState* fs;
+  ReduceScratch red32, red64;
+  size_t n;
+  int nblk;
+  int first;  // flexible step: the first direction of a (re)start
+  float stop;  // inner tolerance (the inner residual starts at norm 1)
+  int max_it;  // inner iterations per preconditioner solve
+};
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_restart_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  fcg_restart_body(v.r64, v.r32, v.e32, v.n, v.st64, v.fs, v.st32, v.red32, v.stop, v.max_it, blockIdx.x, v.nblk);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_gamma_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk || v.first) return;
+  fcg_gamma_body(v.e32, v.q64, v.n, v.st64, v.fs, v.red64, blockIdx.x, v.nblk);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_direction_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  fcg_direction_body(v.e32, v.d64, v.r64, v.n, v.st64, v.fs, v.red64, v.first, blockIdx.x, v.nblk);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_update_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  cg_update_body<double>(v.x, v.d64, v.d64, v.r64, v.q64, v.n, v.st64, v.red64, blockIdx.x, v.nblk);
+}
+
+// The inner FP32 CG of many instances: p = r (first) or p = r + beta p, and
+// the update e += alpha p, r -= alpha Ap with r.r and the stop test;
+// instances whose inner solve is done skip both.
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_direction_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  const CgState<float>* st = v.st32;
+  if (*(volatile const int*)&st->done) return;
+  const bool first = st->first != 0;
+  const float beta = st->beta;
+  const size_t stride = (size_t)v.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += stride)
+    v.p32[i] = first ? v.r32[i] : fmaf(beta, v.p32[i], v.r32[i]);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_update_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  cg_update_body<float>(v.e32, v.p32, v.p32, v.r32, v.Ap32, v.n, v.st32, v.red32, blockIdx.x, v.nblk);
+}
+
+}  // namespace sipg

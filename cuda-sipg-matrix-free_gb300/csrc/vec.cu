@@ -138,7 +138,9 @@ __global__ void __launch_bounds__(kVecThreads) k_dot_chunked(const double* __res
 }
 
 // Device address of the scratch array, looked up once per device with that
-// device current (the first call on each device does it).
+// device current (the first call on each device does it) and kept for the
+// life of the process: a cudaDeviceReset of the device would leave it stale,
+// which is why the entry point is documented as unusable on a reset device.
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[128] = {};
 

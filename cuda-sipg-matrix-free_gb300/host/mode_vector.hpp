@@ -4,6 +4,9 @@
 // value, no destructor, explicit free()); host_mode_vector owns a std::vector.
 // Difference: copy(host -> device) reuses the device array when the size is
 // unchanged instead of reallocating every time (mode_vector.hpp:346-357).
+// Under nvcc the handle also indexes on the device, v(i1, i2, e), as the
+// reference's does (mode_vector.hpp:108-120), so kernels written against the
+// reference's mode_vector compile against this one unchanged.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,6 +15,14 @@
 #include <vector>
 
 #include "sipg_host_common.hpp"
+
+// callable from host and device code under nvcc, as the reference's default
+// constructor, get_noe and get_nompe are (mode_vector.hpp:51,149-160)
+#ifdef __CUDACC__
+#define SIPG_HD __host__ __device__
+#else
+#define SIPG_HD
+#endif
 
 template <typename FLOAT_TYPE, typename INT_TYPE>
 class host_mode_vector;
@@ -29,7 +40,7 @@ class mode_vector {
   FLOAT_TYPE* device_array;
 
  public:
-  mode_vector() : noe(0), nompe(0), device_array(nullptr) {}
+  SIPG_HD mode_vector() : noe(0), nompe(0), device_array(nullptr) {}
   // allocates noe * nompe^2 values on the device
   mode_vector(INT_TYPE _noe, INT_TYPE _nompe) : noe(_noe), nompe(_nompe), device_array(nullptr) {
     sipg_host::check_cuda(cudaMalloc(&device_array, sizeof(FLOAT_TYPE) * (size_t)noe * nompe * nompe), "cudaMalloc");
@@ -43,9 +54,19 @@ class mode_vector {
   const FLOAT_TYPE* data() const { return device_array; }
   FLOAT_TYPE* data() { return device_array; }
   INT_TYPE size() const { return noe * nompe * nompe; }
-  INT_TYPE get_noe() const { return noe; }
-  INT_TYPE get_nompe() const { return nompe; }
+  SIPG_HD INT_TYPE get_noe() const { return noe; }
+  SIPG_HD INT_TYPE get_nompe() const { return nompe; }
   INT_TYPE HOST_DEBUG(INT_TYPE i1, INT_TYPE i2, INT_TYPE e) const { return ((i1 * nompe) + i2) * noe + e; }
+#ifdef __CUDACC__
+  // value (i1, i2) of element e, from device code (mode_vector.hpp:108-120):
+  // the handle is passed to a kernel by value and indexed there
+  __device__ inline FLOAT_TYPE& operator()(INT_TYPE i1, INT_TYPE i2, INT_TYPE e) {
+    return device_array[((i1 * nompe) + i2) * noe + e];
+  }
+  __device__ inline const FLOAT_TYPE& operator()(INT_TYPE i1, INT_TYPE i2, INT_TYPE e) const {
+    return device_array[((i1 * nompe) + i2) * noe + e];
+  }
+#endif
   void free() {
     if (device_array) sipg_host::check_cuda(cudaFree(device_array), "cudaFree");
     device_array = nullptr;

@@ -39,15 +39,17 @@ class CgResult(C.Structure):
 
 class MixedOpts(C.Structure):
     _fields_ = [("inner_tol", C.c_double), ("outer_tol", C.c_double), ("max_outer", C.c_int), ("max_inner", C.c_int),
-                ("inner", C.c_int), ("reserved", C.c_int)]
+                ("inner", C.c_int), ("outer", C.c_int)]
 
 
 INNER = {"auto": 0, "f32": 1, "pairs": 2, "f64": 3}
+OUTER = {"auto": 0, "reliable": 1, "flexible": 2}
 
 
 class MixedResult(C.Structure):
     _fields_ = [("outer_iterations", C.c_int), ("inner_iterations", C.c_int), ("rel_residual", C.c_double),
-                ("time_ms", C.c_double), ("converged", C.c_int), ("inner_kind", C.c_int)]
+                ("time_ms", C.c_double), ("converged", C.c_int), ("inner_kind", C.c_int), ("outer_kind", C.c_int),
+                ("fp64_applies", C.c_int)]
 
 
 class Problem(C.Structure):
@@ -404,17 +406,20 @@ class Operator:
         return out
 
     def solve_mixed(self, x, b, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, inner="auto",
-                    stream=None):
-        """Inner CG on the FP32 pipes (inner = "f32": FP32 vectors; "pairs":
-        double-float pairs; "auto": by the condition-number estimate) inside
-        FP64 defect correction with reliable updates: an FP64 correction
-        whenever the inner residual fell by inner_tol since the last one; stops
-        at ||b - Ax|| <= outer_tol ||b|| (FP64).  Returns (status, MixedResult)."""
+                    outer="auto", stream=None):
+        """Inner CG on the FP32 pipes inside an FP64 outer iteration; stops at
+        ||b - Ax|| <= outer_tol ||b|| (FP64).  outer = "flexible": flexible CG
+        in FP64 preconditioned by an FP32 inner CG that runs until its residual
+        fell by inner_tol; "reliable": defect correction with reliable updates
+        (an FP64 correction whenever the inner residual fell by inner_tol),
+        inner = "f32" (FP32 vectors), "pairs" (double-float pairs) or "auto"
+        (by the condition-number estimate); outer = "auto": flexible unless
+        inner names pairs or f64.  Returns (status, MixedResult)."""
         import torch
 
         self._vec(x, torch.float64)
         self._vec(b, torch.float64)
-        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER[inner], 0)
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER[inner], OUTER[outer])
         res = MixedResult()
         st = lib().sipg_solve_mixed(self._h, _ptr(x), _ptr(b), C.byref(o), C.byref(res), _stream(stream))
         if st not in (0, 3, 4):
@@ -462,13 +467,17 @@ class Batch:
     def footprint(self):
         return int(lib().sipg_batch_footprint(self._h))
 
-    def solve_mixed(self, xs, bs, inner_tol=0.1, outer_tol=1e-10, max_outer=200, max_inner=0, stream=None):
+    def solve_mixed(self, xs, bs, inner_tol=1e-2, outer_tol=1e-10, max_outer=200, max_inner=0, stream=None):
+        """Solves every problem with flexible CG in FP64 around an FP32 inner
+        CG (to relative inner_tol), all problems together; stops each at a
+        true ||b - Ax|| <= outer_tol ||b||.  Returns (status, [MixedResult])."""
         n = len(self.problems)
         assert len(xs) == n and len(bs) == n
         px = (C.c_void_p * n)(*[x.data_ptr() for x in xs])
         pb = (C.c_void_p * n)(*[b.data_ptr() for b in bs])
         res = (MixedResult * n)()
-        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER["pairs"], 0)
+        o = MixedOpts(float(inner_tol), float(outer_tol), int(max_outer), int(max_inner), INNER["auto"],
+                      OUTER["auto"])
         st = lib().sipg_batch_solve_mixed(self._h, C.cast(px, C.c_void_p), C.cast(pb, C.c_void_p), C.byref(o),
                                           C.cast(res, C.c_void_p), _stream(stream))
         if st not in (0, 3, 4):
@@ -499,7 +508,7 @@ class Server:
     """Continuous-batching solve server (sipg_server_*).  submit() queues a
     request, step() runs one scheduling step, poll() reads a result."""
 
-    def __init__(self, budget_bytes=150 << 30, max_active=256, iters_per_step=8, inner_tol=0.1):
+    def __init__(self, budget_bytes=150 << 30, max_active=256, iters_per_step=8, inner_tol=1e-2):
         o = ServerOpts(int(budget_bytes), int(max_active), int(iters_per_step), float(inner_tol))
         h = C.c_void_p()
         _check(lib().sipg_server_create(C.byref(o), C.byref(h)), "sipg_server_create")

@@ -56,7 +56,7 @@ typedef struct {
 
 /* One SIPG operator: a dim x dim uniform mesh of the unit square, degree p,
  * penalty `pen` (the reference's kernel penalty nu: interior faces get 2*nu,
- * boundary faces nu, sipg_sem_2d_gpu_kernels.hpp:300,333-334).  Opaque. */
+ * boundary faces nu, sipg_sem_2d_gpu_kernels.hpp:209,243-244).  Opaque. */
 typedef struct sipg_op sipg_op;
 
 typedef struct {
@@ -81,22 +81,42 @@ typedef enum { SIPG_INNER_AUTO = 0, SIPG_INNER_F32 = 1, SIPG_INNER_PAIRS = 2, SI
  * to the true b - A x grows with kappa: on 512 x 512, p = 6 its true relative
  * residual stalls near 1e-9 however small the tolerance. */
 
+/* Outer iteration of the mixed-precision solvers.
+ * SIPG_OUTER_RELIABLE: defect correction with reliable updates -- the inner
+ *   CG runs on, keeping its search direction, and x += e, r = b - A x happen
+ *   in FP64 whenever its residual fell by inner_tol.  Each correction is a
+ *   unit step, so the inner solution must be accurate in the residual norm:
+ *   FP32 inner vectors stall once kappa * eps_32 approaches 1.
+ * SIPG_OUTER_FLEXIBLE: flexible CG in FP64 (Notay 2000, truncated to one
+ *   previous direction) preconditioned by an FP32 inner CG that starts from
+ *   zero on the scaled residual and stops when its residual fell by
+ *   inner_tol.  The FP64 step length alpha = d.r / d.Ad (one FP64 apply per
+ *   outer step) minimises the error in the energy norm, where the rounding of
+ *   an FP32 correction costs only ~sqrt(kappa) * eps_32, so FP32 values and
+ *   accumulation serve at any condition number of the supported meshes.
+ * SIPG_OUTER_AUTO: flexible with FP32 inner vectors unless the caller names
+ *   SIPG_INNER_PAIRS or SIPG_INNER_F64 (then reliable). */
+typedef enum { SIPG_OUTER_AUTO = 0, SIPG_OUTER_RELIABLE = 1, SIPG_OUTER_FLEXIBLE = 2 } sipg_outer_kind;
+
 typedef struct {
-  double inner_tol;    /* FP64 correction once the inner residual fell by this factor since the last one (0.1) */
+  double inner_tol;    /* reliable: FP64 correction once the inner residual fell by this factor (0.1);
+                          flexible: each inner solve stops once its residual fell by this factor */
   double outer_tol;    /* stop at the FP64 relative residual ||b-Ax||/||b|| <= outer_tol (1e-10) */
-  int max_outer;       /* cap on FP64 corrections (200) */
+  int max_outer;       /* cap on FP64 corrections / flexible-CG steps (200) */
   int max_inner;       /* cap on inner iterations in total (0 = DoF) */
   int inner;           /* sipg_inner_kind (0 = auto) */
-  int reserved;
+  int outer;           /* sipg_outer_kind (0 = auto) */
 } sipg_mixed_opts;
 
 typedef struct {
-  int outer_iterations;
+  int outer_iterations; /* FP64 corrections (reliable) or flexible-CG steps */
   int inner_iterations; /* summed over all outer steps */
-  double rel_residual;  /* final ||b - A x|| / ||b|| in FP64 */
+  double rel_residual;  /* final ||b - A x|| / ||b||, recomputed in FP64 from x */
   double time_ms;
   int converged;
   int inner_kind;       /* the sipg_inner_kind used (F32, PAIRS or F64) */
+  int outer_kind;       /* the sipg_outer_kind used (RELIABLE or FLEXIBLE) */
+  int fp64_applies;     /* FP64 operator applies, residual checks included */
 } sipg_mixed_result;
 
 /* ---- tables and mesh (host side, no device needed) ---- */
@@ -138,7 +158,7 @@ size_t sipg_op_solve_footprint(int dim, int degree, sipg_precision prec);
 
 /* d_out = A d_in, one fused pass (volume + all faces).  Replaces
  * sipg_sem_2d<T>::_mvm (sipg_sem_2d.hpp:167-201: volume, flux_term6a,
- * flux_term6b) and the free function mvm (sipg_sem_2d_gpu_kernels.hpp:410-454). */
+ * flux_term6b) and the free function mvm (sipg_sem_2d_gpu_kernels.hpp:320-364). */
 sipg_status sipg_apply_f64(const sipg_op* op, const double* d_in, double* d_out, void* stream);
 sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, void* stream);
 /* Double-float pair vectors (2 ndof floats: the hi plane, then the lo plane;
@@ -255,9 +275,12 @@ sipg_status sipg_xpby_f32(size_t n, const float* d_x, float beta, float* d_y, vo
  * array in the library (held by every GPU that loads it until exit), so
  * n <= 16,777,216; larger n returns SIPG_ERR_INVALID.  The first call on each
  * device looks up the array's device address: make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
+ * stream capture.  The address is kept for the life of the process, so after
+ * a cudaDeviceReset of a device this entry point must not be called on that
+ * device again.  All calls share the array: calls that overlap on the GPU
  * (concurrent streams or threads) race and must be serialised by the caller.
- * Synchronous; deterministic. */
+ * Each call returns only once the result is in *result (it waits for the
+ * stream); deterministic. */
 sipg_status sipg_dot_f64_noalloc(size_t n, const double* d_x, const double* d_y, double* result, void* stream);
 
 /* ---- many problems at once (no reference counterpart) ---- */
@@ -280,13 +303,18 @@ sipg_status sipg_batch_destroy(sipg_batch* batch);
 sipg_status sipg_batch_op(const sipg_batch* batch, int i, sipg_op** op);
 /* Device bytes the batch holds (besides the callers' x and b). */
 size_t sipg_batch_footprint(const sipg_batch* batch);
-/* Solves A_i x_i = b_i for every problem with the mixed-precision scheme of
- * sipg_solve_mixed, all problems together: one batched FP32 apply launch per
- * degree present and one batched update per iteration, replayed as a CUDA
- * graph; problems retire as they converge.  d_x[i], d_b[i]: FP64 device
- * vectors (x holds x0).  res (array of n, may be NULL) gets each problem's
- * corrections, FP32 iterations, final FP64 relative residual; time_ms is the
- * whole batch's. */
+/* Solves A_i x_i = b_i for every problem with the flexible mixed-precision
+ * scheme of sipg_solve_mixed (flexible CG in FP64 around an FP32 inner CG to
+ * relative opts->inner_tol, default 1e-2), all problems together: the FP32
+ * inner iterations of every problem are one batched FP32 apply launch per
+ * degree present plus a batched direction and a batched update launch,
+ * replayed as a CUDA graph; the FP64 outer steps of the problems due one run
+ * as batched launches between replays; problems retire as they converge, each
+ * once b - A x recomputed in FP64 is under opts->outer_tol ||b||.  opts->inner
+ * and opts->outer must be AUTO or F32 / FLEXIBLE (else SIPG_ERR_INVALID).
+ * d_x[i], d_b[i]: FP64 device vectors (x holds x0).  res (array of n, may be
+ * NULL) gets each problem's outer steps, FP32 iterations, FP64 applies and
+ * final FP64 relative residual; time_ms is the whole batch's. */
 sipg_status sipg_batch_solve_mixed(sipg_batch* batch, double* const* d_x, const double* const* d_b,
                                    const sipg_mixed_opts* opts, sipg_mixed_result* res, void* stream);
 
@@ -296,7 +324,7 @@ typedef struct {
   size_t budget_bytes;  /* device memory the active requests may hold (150 GB) */
   int max_active;       /* requests solved concurrently, 1..4096 (256) */
   int iters_per_step;   /* CG iterations per sipg_server_step (8) */
-  double inner_tol;     /* mixed requests: reliable-update threshold (0.1) */
+  double inner_tol;     /* mixed requests: each FP32 inner solve stops once its residual fell by this (1e-2) */
 } sipg_server_opts;
 
 typedef struct {
@@ -306,14 +334,14 @@ typedef struct {
   int sol;              /* test problem (sipg_solution) whose right-hand side is built on the device */
   sipg_modes modes;     /* for SIPG_SOL_MODES */
   double tol;           /* relative FP64 residual ||b - Ax|| <= tol ||b|| */
-  int precision;        /* SIPG_F32: mixed (FP32 CG, FP64 corrections); SIPG_F64: plain FP64 CG */
+  int precision;        /* SIPG_F32: mixed (flexible CG in FP64 around an FP32 inner CG); SIPG_F64: plain FP64 CG */
 } sipg_request;
 
 typedef struct {
   int done;             /* 1 once the request retired */
   sipg_status status;   /* SIPG_OK, SIPG_ERR_NOT_CONVERGED, SIPG_ERR_BREAKDOWN, SIPG_ERR_REJECTED */
-  int iterations;       /* CG iterations (FP32 ones for mixed requests) */
-  int corrections;      /* FP64 corrections (mixed) */
+  int iterations;       /* CG iterations (FP32 inner ones for mixed requests) */
+  int corrections;      /* flexible FP64 outer steps (mixed) */
   double rel_residual;  /* final FP64 ||b - Ax|| / ||b|| */
   double queue_ms;      /* submit -> admission */
   double latency_ms;    /* submit -> retirement */

@@ -1,5 +1,5 @@
 // ref_gpu_kernels.cu -- explicit instantiations of the reference's own FP64
-// kernels (volume_gpu_kernels.hpp:9-86, sipg_sem_2d_gpu_kernels.hpp:279-406,
+// kernels (volume_gpu_kernels.hpp:9-86, sipg_sem_2d_gpu_kernels.hpp:189-316,
 // conjugate_gradient_kernels.hpp:5-38), compiled unchanged from the reference
 // headers by oracle/build_ref.py into oracle/_ref/ref_kernels.cubin for
 // oracle/ref_gpu.cpp.  TEST INFRASTRUCTURE AND BASELINE ONLY.

@@ -50,8 +50,8 @@ int sipg_oracle_laplace2d(int p, double* L);
 int sipg_oracle_mesh_coords(int dim, double* x, double* y);
 
 /* One SIPG matvec out = A in: volume (volume_gpu_kernels.hpp:9-86), then
- * flux_term6a (sipg_sem_2d_gpu_kernels.hpp:279-343), then flux_term6b
- * (:346-406).  nthreads <= 1 runs on the calling thread. */
+ * flux_term6a (sipg_sem_2d_gpu_kernels.hpp:189-253), then flux_term6b
+ * (:256-316).  nthreads <= 1 runs on the calling thread. */
 int sipg_oracle_apply(int p, int dim, double pen, const double* in, double* out, int nthreads);
 int sipg_oracle_apply_f32(int p, int dim, float pen, const float* in, float* out, int nthreads);
 /* The three pieces separately (same arithmetic as sipg_oracle_apply). */

@@ -122,3 +122,13 @@ def test_integration_binding_example_compiles(tmp_path):
                            os.path.join(ROOT, "cuda-sipg-matrix-free_gb300", "host"), "-c",
                            os.path.join(ROOT, "tests", "cpp", "integration_binding.cpp"), "-o",
                            str(tmp_path / "binding.o")])
+
+
+def test_reference_style_kernel_compiles_against_mode_vector(tmp_path):
+    # a device kernel indexing mode_vector as the reference's kernels do,
+    # v(i1, i2, e) and get_noe() on the device (compile only: no GPU here)
+    subprocess.check_call(["nvcc", "-std=c++14", "-O0", "-gencode", "arch=compute_103a,code=sm_103a", "-I",
+                           os.path.join(ROOT, "include"), "-I",
+                           os.path.join(ROOT, "cuda-sipg-matrix-free_gb300", "host"), "-c",
+                           os.path.join(ROOT, "tests", "cpp", "mode_vector_kernel.cu"), "-o",
+                           str(tmp_path / "mvk.o")])

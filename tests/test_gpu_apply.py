@@ -67,6 +67,37 @@ def test_apply_f64_vs_oracle_multi_tile(sipg, oracle, torch, p):
         assert rel_err(y, ref) <= RTOL64, (p, d, rel_err(y, ref))
 
 
+@pytest.mark.parametrize("p", range(1, 9))
+def test_apply_f32_vs_oracle_multi_tile(sipg, oracle, torch, p):
+    # the FP32 apply over several 32-element tiles in x and y, sizes that are
+    # not tile multiples: its register-resident nodal blocks (p <= 6), halo
+    # reads and face ownership across tile edges, against the FP64 oracle on
+    # the same (FP32-representable) input
+    rng = np.random.default_rng(17 + p)
+    for d in (37, 70):
+        x = rng.uniform(-1, 1, d * d * (p + 1) ** 2).astype(np.float32)
+        pen = float(p * p)
+        op = sipg.Operator(d, p, pen)
+        y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy().astype(np.float64)
+        op.close()
+        ref = oracle.apply(p, d, pen, x.astype(np.float64))
+        assert rel_err(y, ref) <= RTOL32, (p, d, rel_err(y, ref))
+
+
+@pytest.mark.parametrize("p", [4, 6])
+def test_apply_f32_full_size_vs_oracle(sipg, oracle, torch, p):
+    # full size: 1024 x 1024 (p = 4, 26.2 M DoF) and 571 x 571 (p = 6, the
+    # ~16 M DoF sweep size), input U[-1,1] seed 0 rounded to FP32
+    d = 1024 if p == 4 else 571
+    pen = float(p * p)
+    x = np.random.default_rng(0).uniform(-1.0, 1.0, d * d * (p + 1) ** 2).astype(np.float32)
+    op = sipg.Operator(d, p, pen)
+    y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy().astype(np.float64)
+    op.close()
+    ref = oracle.apply(p, d, pen, x.astype(np.float64), nthreads=8)
+    assert rel_err(y, ref) <= RTOL32, rel_err(y, ref)
+
+
 def test_apply_full_size_vs_oracle(sipg, oracle, torch):
     # the 1024 x 1024, p = 4 throughput case (26.2 M DoF), input U[-1,1] seed 0
     p, d, pen = 4, 1024, 16.0

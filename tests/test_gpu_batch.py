@@ -1,8 +1,10 @@
-"""Batched mixed-precision solves (sipg_batch_*): many right-hand sides on one
-mesh and uneven (dim, p) problems in one batch must give, problem by problem,
-what the single-problem FP64 CG gives: FP64 relative residual <= 1e-10, the
+"""Batched mixed-precision solves (sipg_batch_*: flexible CG in FP64 around an
+FP32 inner CG): many right-hand sides on one mesh and uneven (dim, p) problems
+in one batch must give, problem by problem, what the single-problem FP64 CG
+gives: FP64 relative residual <= 1e-10 (recomputed from the solution), the
 solution within 1e-7 relative of the FP64 CG solution (both stop at 1e-10),
-and the L2 error within 1.05x of the FP64 solve's."""
+and the L2 error within 1.05x of the FP64 solve's; at the 64-right-hand-side,
+256 x 256, p = 4 shape one instance is checked against the oracle's CG."""
 import numpy as np
 import pytest
 
@@ -88,4 +90,60 @@ def test_batch_retires_converged_problems(sipg, torch):
     xs2 = [torch.zeros_like(b) for b in bs]
     st, res2 = batch.solve_mixed(xs2, bs)
     assert st == 0 and all(torch.equal(a, c) for a, c in zip(xs, xs2))
+    batch.close()
+
+
+def _true_rel(op, x, b):
+    return (b - op.apply(x)).norm().item() / max(b.norm().item(), 1e-300)
+
+
+def test_batch_reports_the_flexible_fp32_scheme(sipg, torch):
+    probs = [(20, 4, 16.0), (28, 6, 36.0)]
+    batch = sipg.Batch(probs)
+    bs = [batch.op(k).rhs("sinsin") for k in range(len(probs))]
+    xs = [torch.zeros_like(b) for b in bs]
+    st, res = batch.solve_mixed(xs, bs)
+    assert st == 0
+    for k, r in enumerate(res):
+        assert r.inner_kind == 1 and r.outer_kind == 2 and r.converged == 1
+        # one FP64 apply per outer step, the initial residual and the final check(s)
+        assert r.outer_iterations + 2 <= r.fp64_applies <= r.outer_iterations + 5
+        assert _true_rel(batch.op(k), xs[k], bs[k]) <= 1.01e-10
+    with pytest.raises(sipg.SipgError):
+        # batches run the flexible scheme only
+        o = sipg.MixedOpts(0.1, 1e-10, 200, 0, sipg.INNER["pairs"], sipg.OUTER["reliable"])
+        px = (sipg.C.c_void_p * 2)(*[x.data_ptr() for x in xs])
+        pb = (sipg.C.c_void_p * 2)(*[b.data_ptr() for b in bs])
+        sipg._check(sipg.lib().sipg_batch_solve_mixed(batch._h, sipg.C.cast(px, sipg.C.c_void_p),
+                                                       sipg.C.cast(pb, sipg.C.c_void_p), sipg.C.byref(o), None,
+                                                       sipg._stream()), "batch")
+    batch.close()
+
+
+def test_batch_64_rhs_256_p4_against_the_oracle(sipg, oracle, torch):
+    # the shared-mesh batch at full shape: 64 right-hand sides of 4 sine modes
+    # (seed 1) on 256 x 256, p = 4 (104.9 M DoF in all)
+    import workloads
+
+    probs = workloads.shared_mesh_rhs(64, 256, 4, seed=1)
+    batch = sipg.Batch([(d, p, pen) for d, p, pen, _ in probs])
+    ms = [sipg.Modes.make(*m) for _, _, _, m in probs]
+    bs = [batch.op(k).rhs("modes", ms[k]) for k in range(len(probs))]
+    xs = [torch.zeros_like(b) for b in bs]
+    st, res = batch.solve_mixed(xs, bs)
+    assert st == 0
+    op = batch.op(0)
+    for k in range(len(probs)):
+        assert res[k].converged == 1
+        assert _true_rel(op, xs[k], bs[k]) <= 1.01e-10, k
+    # instance 0 against the oracle (the reference's CG restated in C) to 1e-12
+    d, p, pen, _ = probs[0]
+    it_ref, x_ref, _ = oracle.cg(p, d, pen, bs[0].cpu().numpy(), 1e-12, rel=True, nthreads=16)
+    diff = np.max(np.abs(xs[0].cpu().numpy() - x_ref)) / np.max(np.abs(x_ref))
+    assert diff <= 1e-7, diff
+    # the discretisation error of instance 0 against the analytic solution
+    x64 = torch.from_numpy(x_ref).cuda()
+    e_ref = op.err_norms("modes", x64, ms[0])
+    e_b = op.err_norms("modes", xs[0], ms[0])
+    assert e_b[0] <= 1.05 * e_ref[0], (e_b, e_ref)
     batch.close()

@@ -145,8 +145,9 @@ def test_mixed_precision_reaches_fp64_accuracy(sipg, oracle, torch):
     st, r64 = op.cg(x64, b, 1e-10, relative=True)
     assert st == 0
     xm = torch.zeros_like(b)
-    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10, inner="f32")
+    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10, inner="f32", outer="reliable")
     assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10 and rm.inner_kind == 1
+    assert rm.outer_kind == 1
     assert rm.outer_iterations >= 2 and rm.inner_iterations > 0
     # reliable updates keep the Krylov space: the FP32 iteration count stays within
     # a small factor of the FP64 one (a restarted inner solve needs orders of magnitude more)
@@ -173,9 +174,9 @@ def test_mixed_pairs_on_an_ill_conditioned_problem(sipg, torch):
     st, r64 = op.cg(x64, b, 1e-10, relative=True)
     assert st == 0
     xm = torch.zeros_like(b)
-    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10)  # auto: pairs here
+    st, rm = op.solve_mixed(xm, b, inner_tol=0.1, outer_tol=1e-10, inner="pairs")  # reliable updates
     assert st == 0 and rm.converged == 1 and rm.rel_residual <= 1e-10
-    assert rm.inner_kind == 2
+    assert rm.inner_kind == 2 and rm.outer_kind == 1
     true_rel = (b - op.apply(xm)).norm().item() / bn
     assert true_rel <= 1e-10, true_rel
     assert rm.inner_iterations <= 3 * r64.iterations, (rm.inner_iterations, r64.iterations)
@@ -193,6 +194,70 @@ def test_mixed_auto_picks_f32_for_well_conditioned(sipg, torch):
     x = torch.zeros_like(b)
     st, rm = op.solve_mixed(x, b)
     assert st == 0 and rm.inner_kind == 1 and rm.rel_residual <= 1e-10
+    op.close()
+
+
+def _true_rel(op, x, b):
+    return (b - op.apply(x)).norm().item() / b.norm().item()
+
+
+@pytest.mark.parametrize("inner_tol", [1e-1, 1e-3, 1e-5])
+def test_flexible_fp32_inner_on_an_ill_conditioned_problem(sipg, oracle, torch, inner_tol):
+    # 256 x 256, p = 6: condition number ~5e6 (kappa * eps_32 ~ 0.3), where FP32
+    # vectors stall a unit-step defect correction.  Flexible CG in FP64 with a
+    # pure FP32 inner CG (FP32 values, FP32 accumulation) reaches a TRUE FP64
+    # relative residual of 1e-10, L2 error within 1.05x of the FP64 solve's.
+    p, d, pen = 6, 256, 36.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("sinsin")
+    x64 = torch.zeros_like(b)
+    st, rr = op.solve_mixed(x64, b, inner_tol=0.1, outer_tol=1e-10, inner="f64", outer="reliable")
+    assert st == 0 and _true_rel(op, x64, b) <= 1e-10
+    xm = torch.zeros_like(b)
+    st, rm = op.solve_mixed(xm, b, inner_tol=inner_tol, outer_tol=1e-10)  # auto: flexible, FP32 inner
+    assert st == 0 and rm.converged == 1 and rm.inner_kind == 1 and rm.outer_kind == 2
+    assert rm.rel_residual <= 1e-10
+    true_rel = _true_rel(op, xm, b)
+    assert true_rel <= 1.01e-10, true_rel
+    # one FP64 apply per outer step, plus the residual checks
+    assert rm.outer_iterations + 1 <= rm.fp64_applies <= rm.outer_iterations + 4
+    e64 = op.err_norms("sinsin", x64)
+    em = op.err_norms("sinsin", xm)
+    assert em[0] <= 1.05 * e64[0], (em, e64)
+    assert (xm - x64).abs().max().item() <= 1e-7 * x64.abs().max().item()
+    op.close()
+
+
+def test_flexible_matches_the_oracle_solution(sipg, oracle, torch):
+    # a small mesh where the oracle's CG to 1e-13 is the answer: the flexible
+    # mixed solve to 1e-11 lands within the residual bound of it
+    p, d, pen = 4, 24, 16.0
+    op = sipg.Operator(d, p, pen)
+    b = op.rhs("sinsin")
+    it_ref, x_ref, _ = oracle.cg(p, d, pen, b.cpu().numpy(), 1e-13, rel=True, nthreads=4)
+    x = torch.zeros_like(b)
+    st, rm = op.solve_mixed(x, b, inner_tol=1e-2, outer_tol=1e-11, outer="flexible")
+    assert st == 0 and rm.outer_kind == 2 and rm.rel_residual <= 1e-11
+    diff = np.max(np.abs(x.cpu().numpy() - x_ref)) / np.max(np.abs(x_ref))
+    assert diff <= 1e-8, diff
+    op.close()
+
+
+def test_flexible_rejects_a_pairs_inner(sipg, torch):
+    op = sipg.Operator(8, 3, 9.0)
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    with pytest.raises(sipg.SipgError):
+        op.solve_mixed(x, b, inner="pairs", outer="flexible")
+    op.close()
+
+
+def test_flexible_reports_not_converged_at_max_outer(sipg, torch):
+    op = sipg.Operator(64, 4, 16.0)
+    b = op.rhs("sinsin")
+    x = torch.zeros_like(b)
+    st, rm = op.solve_mixed(x, b, inner_tol=0.5, outer_tol=1e-12, max_outer=2, outer="flexible")
+    assert st == 3 and rm.converged == 0 and rm.outer_iterations == 2
     op.close()
 
 

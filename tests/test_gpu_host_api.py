@@ -78,3 +78,21 @@ def test_device_problem_and_fp32_and_generic_cg(driver_output):
     gen = next(r for r in driver_output if r["case"] == "generic")
     assert abs(gen["it_generic"] - gen["it_fused"]) <= 1
     assert gen["rel_diff"] <= 1e-9
+
+
+def test_reference_style_kernel_on_mode_vector(sipg, tmp_path):
+    """A kernel written against the reference's mode_vector (passed by value,
+    indexed v(i1, i2, e) on the device, get_noe() in device code) compiles
+    with nvcc against the host API's mode_vector and indexes the same values
+    as HOST_DEBUG on the host."""
+    sipg.lib()  # built
+    exe = str(tmp_path / "mode_vector_kernel")
+    subprocess.check_call(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-I",
+                           os.path.join(ROOT, "include"), "-I", os.path.join(PKG, "host"),
+                           os.path.join(ROOT, "tests", "cpp", "mode_vector_kernel.cu"), "-L",
+                           os.path.join(PKG, "lib"), "-lsipg_gb300", "-Xlinker", "-rpath=" + os.path.join(PKG, "lib"),
+                           "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, (out.stdout, out.stderr)
+    row = json.loads(out.stdout.strip().splitlines()[-1])
+    assert row["case"] == "mode_vector_kernel" and row["max_abs_err"] == 0.0

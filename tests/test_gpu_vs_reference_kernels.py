@@ -55,6 +55,25 @@ def test_apply_full_size_matches_reference_kernels(sipg, torch):
     op.close()
 
 
+@pytest.mark.parametrize("p", range(1, 9))
+def test_apply_sweep_sizes_match_reference_kernels(sipg, torch, p):
+    # the constant ~16 M DoF sweep: dim = round(4000 / (p + 1)) (2000^2 at p = 1
+    # ... 444^2 at p = 8), input U[-1,1] from seed 0 as the throughput bench
+    # uses, each degree's default tile shape (and the p = 8 shared-memory
+    # coefficient path) against the reference's kernels on the same vector
+    d = round(4000 / (p + 1))
+    pen = float(p * p)
+    ref = oracle_lib.ref_gpu()
+    op = sipg.Operator(d, p, pen)
+    x = torch.from_numpy(np.random.default_rng(0).uniform(-1.0, 1.0, op.ndof)).cuda()
+    y_ref = torch.empty_like(x)
+    ref.apply(p, d, pen, x.data_ptr(), y_ref.data_ptr())
+    torch.cuda.synchronize()
+    y = op.apply(x)
+    assert rel(y, y_ref) <= 1e-12, (p, d, rel(y, y_ref))
+    op.close()
+
+
 @pytest.mark.parametrize("p,d,pen,sol", [(4, 16, 16.0, "sinsin"), (2, 64, 4.0, "E"), (6, 32, 3600.0, "E")])
 def test_cg_iterations_match_reference_cg(sipg, torch, p, d, pen, sol):
     ref = oracle_lib.ref_gpu()
