@@ -18,7 +18,7 @@
 // captured K at a time in a CUDA graph with every scalar on the device:
 //   k_sipg_apply<APPLY_DOT>: Ap, p.Ap, alpha = (r.z) / p.Ap
 //   k_pcg_update:            x += alpha p, r -= alpha Ap, r.r (the stop test)
-//   k_pcg_precond:           z = M r, r.z, beta = (r.z)_new / (r.z)_old
+//   k_cross_apply<P, 1>:     z = M r, r.z, beta = (r.z)_new / (r.z)_old
 //   k_cg_direction:          p = z + beta p
 #include <cmath>
 #include <new>
@@ -121,83 +121,107 @@ int build_prec_rows(const HostTables& t, double pen_in, std::vector<double>& row
 }
 }  // namespace
 
-// z = M r at one DoF i = k * noe + e (node k = i1 * n + i2 of element e), in
-// the reference kernel's order: the diagonal, the row, the column
-__device__ __forceinline__ double prec_value(const double* __restrict__ rows, const double* __restrict__ r,
-                                             size_t i, size_t noe, int p) {
-  const int n = p + 1, R = 2 * p + 1;
-  const int k = (int)(i / noe);
-  const size_t e = i - (size_t)k * noe;
-  const int i1 = k / n, i2 = k - i1 * n;
-  const double* row = rows + (size_t)k * R;
-  int q = 0;
-  double v = 0.0;
-  v += __ldg(row + q) * r[i];
-  for (int j = 0; j < n; ++j)
-    if (j != i2) v += __ldg(row + (++q)) * r[(size_t)(i1 * n + j) * noe + e];
-  for (int j = 0; j < n; ++j)
-    if (j != i1) v += __ldg(row + (++q)) * r[(size_t)(j * n + i2) * noe + e];
-  return v;
-}
+// The cross-pattern operators -- the stored volume operator of
+// volume_mvm<T, same> (mode_matrix_kernels.hpp:7-65) and the block-Jacobi
+// preconditioner applied the same way (sipg_sem_2d.hpp:205-224) -- with value
+// r of row (i1,i2) of element e's operator at
+// mat[((i1*n + i2)*(2p+1) + r)*mat_noe + (mat_noe == 1 ? 0 : e)] (the
+// reference's mode_matrix layout; one operator for every element, mat_noe =
+// 1, or one per element, mat_noe = noe) and out(i1,i2,e) = diagonal, then the
+// row (i1, j != i2), then the column (j != i1, i2), in the reference kernel's
+// order.
+//
+// One thread per element, kCrossThreads consecutive elements per block: each
+// thread first copies its element's n^2 input values into its own column of
+// shared memory (plane by plane, so every load is a coalesced run of
+// consecutive elements), then forms the n^2 outputs from there.  Every input
+// value is read from HBM once (16 B/DoF with the write; per-element operators
+// add their (2p+1) values per DoF) -- where a thread per DoF reads each value
+// 2p+1 times, from planes far apart in the vector.  A thread reads only the
+// column it wrote, so no barrier is needed.  MODE 1 (the PCG step) also forms
+// r.z, its deterministic grid reduction and the step's beta.
+constexpr int kCrossThreads = 64;
 
-// The stored-operator apply of volume_mvm<T, same> (mode_matrix_kernels.hpp:
-// 7-65): value r of row (i1,i2) of element e's operator at
-// mat[((i1*n + i2)*(2p+1) + r)*mat_noe + (mat_noe == 1 ? 0 : e)] -- the
-// reference's mode_matrix layout -- one operator for every element
-// (mat_noe = 1) or one per element (mat_noe = noe).
-__global__ void __launch_bounds__(kVecThreads) k_stored_apply(const double* __restrict__ mat, size_t mat_noe,
-                                                              const double* __restrict__ in, double* __restrict__ out,
-                                                              size_t n, size_t noe, int p) {
-  const int nn1 = p + 1, R = 2 * p + 1;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int k = (int)(i / noe);
-    const size_t e = i - (size_t)k * noe;
-    const int i1 = k / nn1, i2 = k - i1 * nn1;
-    const double* row = mat + (size_t)k * R * mat_noe + (mat_noe == 1 ? 0 : e);
-    int q = 0;
-    double v = 0.0;
-    v += __ldg(row) * in[i];
-    for (int j = 0; j < nn1; ++j)
-      if (j != i2) v += __ldg(row + (size_t)(++q) * mat_noe) * in[(size_t)(i1 * nn1 + j) * noe + e];
-    for (int j = 0; j < nn1; ++j)
-      if (j != i1) v += __ldg(row + (size_t)(++q) * mat_noe) * in[(size_t)(j * nn1 + i2) * noe + e];
-    out[i] = v;
-  }
-}
-
-__global__ void __launch_bounds__(kVecThreads) k_prec_apply(const double* __restrict__ rows,
-                                                            const double* __restrict__ in, double* __restrict__ out,
-                                                            size_t n, size_t noe, int p) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    out[i] = prec_value(rows, in, i, noe, p);
-}
-
-// z = M r and r.z; the first call of a solve sets (r.z)_old, later ones beta
-__global__ void __launch_bounds__(kVecThreads) k_pcg_precond(const double* __restrict__ rows,
-                                                             const double* __restrict__ r, double* __restrict__ z,
-                                                             size_t n, size_t noe, int p, CgState<double>* st,
-                                                             ReduceScratch red) {
+template <int P, int MODE>
+__global__ void __launch_bounds__(kCrossThreads)
+    k_cross_apply(const double* __restrict__ mat, size_t mat_noe, const double* __restrict__ in,
+                  double* __restrict__ out, size_t noe, CgState<double>* st, ReduceScratch red) {
+  constexpr int N1 = P + 1, NN = N1 * N1, R = 2 * P + 1;
+  __shared__ double col[NN][kCrossThreads];
   __shared__ double sh[32];
-  if (*(volatile int*)&st->done) return;
+  if (MODE == 1 && *(volatile int*)&st->done) return;
+  const int t = threadIdx.x;
+  const size_t tiles = (noe + kCrossThreads - 1) / kCrossThreads;
   double acc = 0.0;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const double zi = prec_value(rows, r, i, noe, p);
-    z[i] = zi;
-    acc = fma(zi, r[i], acc);
-  }
-  const double bt = block_sum<double, kVecThreads>(acc, sh);
-  double total;
-  if (grid_sum_last<double, kVecThreads>(bt, red, gridDim.x, sh, &total) && threadIdx.x == 0) {
-    if (!st->first) st->beta = total / st->rr;
-    st->rr = total;
-    if (!isfinite(total)) {
-      st->status = (int)SIPG_ERR_BREAKDOWN;
-      st->done = 1;
+  for (size_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const size_t e = tile * kCrossThreads + t;
+    if (e < noe) {
+#pragma unroll
+      for (int k = 0; k < NN; ++k) col[k][t] = __ldg(in + (size_t)k * noe + e);
+      const size_t me = (mat_noe == 1) ? 0 : e;
+#pragma unroll 1
+      for (int k = 0; k < NN; ++k) {
+        const int i1 = k / N1, i2 = k - i1 * N1;
+        const double* row = mat + (size_t)k * R * mat_noe + me;
+        int q = 0;
+        double v = 0.0;
+        v += __ldg(row) * col[k][t];
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+          if (j != i2) v += __ldg(row + (size_t)(++q) * mat_noe) * col[i1 * N1 + j][t];
+#pragma unroll
+        for (int j = 0; j < N1; ++j)
+          if (j != i1) v += __ldg(row + (size_t)(++q) * mat_noe) * col[j * N1 + i2][t];
+        out[(size_t)k * noe + e] = v;
+        if (MODE == 1) acc = fma(v, col[k][t], acc);
+      }
     }
   }
+  if (MODE == 1) {
+    const double bt = block_sum<double, kCrossThreads>(acc, sh);
+    double total;
+    if (grid_sum_last<double, kCrossThreads>(bt, red, gridDim.x, sh, &total) && t == 0) {
+      if (!st->first) st->beta = total / st->rr;
+      st->rr = total;
+      if (!isfinite(total)) {
+        st->status = (int)SIPG_ERR_BREAKDOWN;
+        st->done = 1;
+      }
+    }
+  }
+}
+
+// Launches the cross-pattern operator of degree p; mode 0: out = M in, mode
+// 1: z = M r with r.z and beta into st (its reduction over at most
+// red.capacity blocks).
+cudaError_t launch_cross(int p, int mode, const double* mat, size_t mat_noe, const double* in, double* out,
+                         size_t noe, CgState<double>* st, const ReduceScratch& red, cudaStream_t s) {
+  const size_t tiles = (noe + kCrossThreads - 1) / kCrossThreads;
+  size_t cap = 152 * 32;
+  if (mode == 1 && (size_t)red.capacity < cap) cap = (size_t)red.capacity;
+  const int grid = (int)std::max<size_t>(1, std::min(tiles, cap));
+#define SIPG_CROSS_CASE(PP)                                                                     \
+  case PP:                                                                                      \
+    if (mode == 1)                                                                              \
+      k_cross_apply<PP, 1><<<grid, kCrossThreads, 0, s>>>(mat, mat_noe, in, out, noe, st, red); \
+    else                                                                                        \
+      k_cross_apply<PP, 0><<<grid, kCrossThreads, 0, s>>>(mat, mat_noe, in, out, noe, st, red); \
+    break;
+  switch (p) {
+    SIPG_CROSS_CASE(1)
+    SIPG_CROSS_CASE(2)
+    SIPG_CROSS_CASE(3)
+    SIPG_CROSS_CASE(4)
+    SIPG_CROSS_CASE(5)
+    SIPG_CROSS_CASE(6)
+    SIPG_CROSS_CASE(7)
+    SIPG_CROSS_CASE(8)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef SIPG_CROSS_CASE
+  count_launch();
+  return cudaGetLastError();
 }
 
 // After r = b - A x: the reference's loop test starts from rr = 1 rather than
@@ -336,9 +360,9 @@ sipg_status enqueue_iteration(sipg_op* op, PcgCache& c, double* x, cudaStream_t 
   a.red = c.red;
   SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_DOT, a, op->tab, s));
   k_pcg_update<<<vb, kVecThreads, 0, s>>>(x, c.p, c.r, c.Ap, c.n, c.st, c.red);
-  k_pcg_precond<<<vb, kVecThreads, 0, s>>>(c.rows, c.r, c.z, c.n, (size_t)op->noe, op->p, c.st, c.red);
+  SIPG_CUDA_TRY(launch_cross(op->p, 1, c.rows, 1, c.r, c.z, (size_t)op->noe, c.st, c.red, s));
   k_cg_direction<double><<<vb, kVecThreads, 0, s>>>(c.p, c.z, c.n, c.st);
-  count_launch(3);
+  count_launch(2);
   SIPG_CUDA_TRY(cudaGetLastError());
   return SIPG_OK;
 }
@@ -384,10 +408,9 @@ sipg_status sipg_apply_prec_f64(sipg_op* op, const double* d_in, double* d_out, 
   sipg_status st = cache_get(op, false, &c);
   if (st != SIPG_OK) return st;
   const size_t n = (size_t)op->ndof;
-  k_prec_apply<<<vec_grid(n), kVecThreads, 0, (cudaStream_t)stream>>>(c->rows, d_in, d_out, n, (size_t)op->noe,
-                                                                       op->p);
-  count_launch();
-  SIPG_CUDA_TRY(cudaGetLastError());
+  (void)n;
+  SIPG_CUDA_TRY(launch_cross(op->p, 0, c->rows, 1, d_in, d_out, (size_t)op->noe, nullptr, ReduceScratch{},
+                             (cudaStream_t)stream));
   return SIPG_OK;
 }
 
@@ -399,10 +422,9 @@ sipg_status sipg_volume_mvm_f64(int dim, int degree, const double* d_mat, int ma
     return SIPG_ERR_INVALID;
   }
   const size_t noe = (size_t)dim * dim, n = noe * (size_t)(degree + 1) * (degree + 1);
-  k_stored_apply<<<vec_grid(n), kVecThreads, 0, (cudaStream_t)stream>>>(d_mat, (size_t)mat_noe, d_in, d_out, n,
-                                                                         noe, degree);
-  count_launch();
-  SIPG_CUDA_TRY(cudaGetLastError());
+  (void)n;
+  SIPG_CUDA_TRY(launch_cross(degree, 0, d_mat, (size_t)mat_noe, d_in, d_out, noe, nullptr, ReduceScratch{},
+                             (cudaStream_t)stream));
   return SIPG_OK;
 }
 
@@ -437,9 +459,9 @@ sipg_status sipg_pcg_f64(sipg_op* op, double* d_x, const double* d_b, double tol
   a.red = c.red;
   SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_RESID, a, op->tab, s));
   k_pcg_force_start<<<1, 1, 0, s>>>(c.st, max_i);
-  k_pcg_precond<<<vb, kVecThreads, 0, s>>>(c.rows, c.r, c.z, c.n, (size_t)op->noe, op->p, c.st, c.red);
+  SIPG_CUDA_TRY(launch_cross(op->p, 1, c.rows, 1, c.r, c.z, (size_t)op->noe, c.st, c.red, s));
   k_cg_direction<double><<<vb, kVecThreads, 0, s>>>(c.p, c.z, c.n, c.st);
-  count_launch(5);
+  count_launch(4);
   SIPG_CUDA_TRY(cudaGetLastError());
   CgState<double>* hs = c.st_host;
   long long launched = 0;

@@ -201,6 +201,16 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
                                            int nblocks) {
   constexpr int N = P, N1 = P + 1, NN = N1 * N1, TE = TX * TY;
   constexpr bool kCols = ApplyColumnForm<T, P>::value;
+  // FP32: every sum whose coefficients add up to zero (a derivative row D, a
+  // stiffness row K = D^T W D) is taken over differences from one value of
+  // the line, v_i - v_0, which leaves it unchanged in exact arithmetic and
+  // drops the part common to the line exactly.  Rounding then scales with
+  // the variation of u across an element (h |grad u|), not with u itself: on
+  // a smooth vector the FP32 operator's relative error falls from
+  // ~kappa eps_32 (~1 at 512 x 512, p = 6) to ~dim eps_32, which is what an
+  // FP32 inner solve needs to see the smooth modes.  (FP64 keeps the plain
+  // sums: its results stay bit-identical to the unpivoted kernel's.)
+  constexpr bool kPivot = sizeof(T) == 4;
   using S = ApplySmem<T, P, TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T red_sh[32];
@@ -272,16 +282,18 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll
     for (int j = 0; j < N1; ++j) {  // LEFT face of this element (x face slot tx)
       T d = T(0);
+      const T pv = kPivot ? U(0, j) : T(0);
 #pragma unroll
-      for (int i = 0; i < N1; ++i) d = fma(tb.D0[i], U(i, j), d);
+      for (int i = 0; i < N1; ++i) d = fma(tb.D0[i], kPivot ? U(i, j) - pv : U(i, j), d);
       XFr(ty, 0, j, tx) = U(0, j);
       XFr(ty, 1, j, tx) = d;
     }
 #pragma unroll
     for (int j = 0; j < N1; ++j) {  // DOWN face (y face slot ty+1)
       T d = T(0);
+      const T pv = kPivot ? U(j, 0) : T(0);
 #pragma unroll
-      for (int i = 0; i < N1; ++i) d = fma(tb.D0[i], U(j, i), d);
+      for (int i = 0; i < N1; ++i) d = fma(tb.D0[i], kPivot ? U(j, i) - pv : U(j, i), d);
       YFr(ty + 1, 0, j, tx) = U(j, 0);
       YFr(ty + 1, 1, j, tx) = d;
     }
@@ -297,7 +309,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         for (int i = 0; i < N1; ++i) {
           const T v = ld(j * N1 + i, he);
           if (i == 0) u0 = v;
-          d = fma(tb.D0[i], v, d);
+          d = fma(tb.D0[i], kPivot ? v - u0 : v, d);
         }
         YFr(0, 0, j, t) = u0;
         YFr(0, 1, j, t) = d;
@@ -314,7 +326,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         for (int i = 0; i < N1; ++i) {
           const T v = ld(i * N1 + j, he);
           if (i == 0) u0 = v;
-          d = fma(tb.D0[i], v, d);
+          d = fma(tb.D0[i], kPivot ? v - u0 : v, d);
         }
         XFr(r, 0, j, TX) = u0;
         XFr(r, 1, j, TX) = d;
@@ -329,8 +341,9 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
       T dN = T(0);
+      const T pv = kPivot ? U(0, j) : T(0);
 #pragma unroll
-      for (int i = 0; i < N1; ++i) dN = fma(tb.DN[i], U(i, j), dN);
+      for (int i = 0; i < N1; ++i) dN = fma(tb.DN[i], kPivot ? U(i, j) - pv : U(i, j), dN);
       const T u0 = rint ? XFr(ty, 0, j, tx + 1) : T(0);
       const T d0 = rint ? XFr(ty, 1, j, tx + 1) : T(0);
       T J, Q;
@@ -342,8 +355,9 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll
     for (int j = 0; j < N1; ++j) {
       T dN = T(0);
+      const T pv = kPivot ? U(j, 0) : T(0);
 #pragma unroll
-      for (int i = 0; i < N1; ++i) dN = fma(tb.DN[i], U(j, i), dN);
+      for (int i = 0; i < N1; ++i) dN = fma(tb.DN[i], kPivot ? U(j, i) - pv : U(j, i), dN);
       const T u0 = uint_ ? YFr(ty, 0, j, tx) : T(0);
       const T d0 = uint_ ? YFr(ty, 1, j, tx) : T(0);
       T J, Q;
@@ -376,12 +390,13 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
       const size_t he = (size_t)hy * dim + hx;
 #pragma unroll(ApplyColumnForm<T, P>::halo_unroll)
       for (int j = 0; j < N1; ++j) {
-        T dN = T(0), uN = T(0);
+        T dN = T(0), uN = T(0), v0 = T(0);
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
           const T v = ld(j * N1 + i, he);
+          if (i == 0) v0 = v;
           if (i == N) uN = v;
-          dN = fma(tb.DN[i], v, dN);
+          dN = fma(tb.DN[i], kPivot ? v - v0 : v, dN);
         }
         T J, Q;
         combine(j, true, YFr(TY, 0, j, t), YFr(TY, 1, j, t), uN, dN, J, Q);
@@ -395,12 +410,13 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
       const size_t he = (size_t)hy * dim + (x0 - 1);
 #pragma unroll(ApplyColumnForm<T, P>::halo_unroll)
       for (int j = 0; j < N1; ++j) {
-        T dN = T(0), uN = T(0);
+        T dN = T(0), uN = T(0), v0 = T(0);
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
           const T v = ld(i * N1 + j, he);
+          if (i == 0) v0 = v;
           if (i == N) uN = v;
-          dN = fma(tb.DN[i], v, dN);
+          dN = fma(tb.DN[i], kPivot ? v - v0 : v, dN);
         }
         T J, Q;
         combine(j, true, XFr(r, 0, j, 0), XFr(r, 1, j, 0), uN, dN, J, Q);
@@ -442,19 +458,26 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
                                          (j == 0) ? YFr(ty + 1, 1, i1, tx) : T(0), (j == N) ? YFr(ty, 1, i1, tx) : T(0));
           o[j] = fma(tb.D0[i1], eJ[j], fma(tb.DN[i1], fJ[j], seed));
         }
+        T p0[N1];  // the x-sums' pivots u(0, j) (FP32)
+#pragma unroll
+        for (int j = 0; j < N1; ++j) p0[j] = kPivot ? Uv(0, j) : T(0);
 #pragma unroll
         for (int i = 0; i < N1; ++i) {
 #pragma unroll
-          for (int j = 0; j < N1; ++j) o[j] = fma(KWv((i1 * N1 + i) * N1 + j), Uv(i, j), o[j]);
+          for (int j = 0; j < N1; ++j)
+            o[j] = fma(KWv((i1 * N1 + i) * N1 + j), kPivot ? Uv(i, j) - p0[j] : Uv(i, j), o[j]);
         }
+        T cp[N1];  // the row (i1, .), less its first value (FP32)
 #pragma unroll
         for (int i = 0; i < N1; ++i) c[i] = U(i1, i);
+#pragma unroll
+        for (int i = 0; i < N1; ++i) cp[i] = kPivot ? c[i] - c[0] : c[i];
         const T gj = YFr(ty + 1, 0, i1, tx), hj = YFr(ty, 0, i1, tx);
 #pragma unroll
         for (int j = 0; j < N1; ++j) {
           T v = o[j];
 #pragma unroll
-          for (int i = 0; i < N1; ++i) v = fma(KWv((j * N1 + i) * N1 + i1), c[i], v);
+          for (int i = 0; i < N1; ++i) v = fma(KWv((j * N1 + i) * N1 + i1), cp[i], v);
           v = fma(tb.D0[j], gj, v);
           o[j] = fma(tb.DN[j], hj, v);
         }
@@ -481,6 +504,11 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         T r[N1];
 #pragma unroll
         for (int i = 0; i < N1; ++i) r[i] = U(i, j);
+        if (kPivot) {
+          const T r0 = r[0];
+#pragma unroll
+          for (int i = 0; i < N1; ++i) r[i] = r[i] - r0;
+        }
 #pragma unroll
         for (int i1 = 0; i1 < N1; ++i1) {
           T s = T(0);
@@ -495,6 +523,11 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         T c[N1];
 #pragma unroll
         for (int i = 0; i < N1; ++i) c[i] = U(j, i);
+        if (kPivot) {
+          const T c0 = c[0];
+#pragma unroll
+          for (int i = 0; i < N1; ++i) c[i] = c[i] - c0;
+        }
 #pragma unroll
         for (int i2 = 0; i2 < N1; ++i2) {
           T s = T(0);

@@ -132,3 +132,41 @@ def test_server_small_request_not_held_behind_a_large_one(sipg, torch):
     ref = _reference(sipg, torch, 16, 3, 9.0, modes)
     assert np.max(np.abs(x - ref)) <= 1e-6 * np.max(np.abs(ref))
     sv.close()  # the large request is dropped unfinished
+
+
+def test_server_interleaved_precisions_against_the_oracle(sipg, oracle, torch):
+    """Mixed-precision (flexible CG in FP64 around an FP32 inner CG) and plain
+    FP64 requests on 64^2..128^2 meshes, interleaved in one server: every
+    result reaches a true relative residual under its tolerance (recomputed
+    here in FP64) and agrees with the oracle's CG (the reference's algorithm
+    restated in C) to 1e-12 within the bound the two residuals allow."""
+    cases = [(64, 4, 1e-10, sipg.F32), (96, 3, 1e-10, sipg.F64), (128, 2, 1e-8, sipg.F32),
+             (80, 6, 1e-10, sipg.F32), (64, 5, 1e-8, sipg.F64), (112, 4, 1e-10, sipg.F32)]
+    modes = sipg.Modes.make([1.0, -0.7, 0.3, 1.5], [1, 4, 7, 2], [2, 3, 1, 8])
+    sv = sipg.Server(max_active=8, iters_per_step=8)
+    ids = []
+    for d, p, tol, prec in cases:
+        ids.append(sv.submit(d, p, float(p * p), tol, modes=modes, precision=prec)[0])
+        sv.step()
+    for _ in range(1000000):
+        active, _ = sv.step()
+        if active == 0 and sv.stats().queued == 0:
+            break
+    for rid, (d, p, tol, prec) in zip(ids, cases):
+        res = sv.poll(rid)
+        assert res.done == 1 and res.status == 0, (d, p, prec, res.status)
+        n = d * d * (p + 1) ** 2
+        x = sv.solution(rid, n)
+        op = sipg.Operator(d, p, float(p * p))
+        b = op.rhs("modes", modes)
+        xt = torch.from_numpy(x).cuda()
+        true_rel = ((b - op.apply(xt)).norm() / b.norm()).item()
+        assert true_rel <= 1.01 * tol, (d, p, prec, true_rel)
+        it_ref, x_ref, _ = oracle.cg(p, d, float(p * p), b.cpu().numpy(), 1e-12, rel=True, nthreads=8)
+        bound = 1e-4 if tol == 1e-8 else 1e-6
+        assert np.max(np.abs(x - x_ref)) <= bound * np.max(np.abs(x_ref)), (d, p, prec)
+        if prec == sipg.F32:
+            assert res.corrections >= 1 and res.iterations > 0
+        op.close()
+        sv.release(rid)
+    sv.close()
