@@ -711,8 +711,11 @@ def run_mixed(args):
     return 0
 
 
-def _batch_case(torch, sipg, workloads, probs):
-    """Batched mixed solve of `probs` [(dim, p, pen, modes)] vs one-at-a-time FP64."""
+def _batch_case(torch, sipg, workloads, probs, cpu=True):
+    """Batched mixed solve of `probs` [(dim, p, pen, modes)] (flexible CG in
+    FP64 around an FP32 inner CG, every problem to a true relative residual of
+    1e-10) vs the same solves one at a time with the plain FP64 CG (relative
+    1e-10 on its recursive residual; its true residuals are reported)."""
     batch = sipg.Batch([(d, p, pen) for d, p, pen, _ in probs])
     bs = [batch.op(k).rhs("modes", sipg.Modes.make(*m)) for k, (_, _, _, m) in enumerate(probs)]
     xs = [torch.zeros_like(b) for b in bs]
@@ -729,10 +732,13 @@ def _batch_case(torch, sipg, workloads, probs):
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     ok = sum(1 for r in res if r.converged)
+    true_b = max(_true_rel(batch.op(k), xs[k], bs[k]) for k in range(len(probs)))
     # one at a time, plain FP64 CG (operators reused across equal problems)
     ops = {}
     t_seq = 0.0
     worst = 0.0
+    true_64 = 0.0
+    its64 = []
     for k, (d, p, pen, _) in enumerate(probs):
         key = (d, p, pen)
         if key not in ops:
@@ -740,17 +746,47 @@ def _batch_case(torch, sipg, workloads, probs):
         x = torch.zeros_like(bs[k])
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ops[key].cg(x, bs[k], 1e-10, relative=True)
+        _, r64 = ops[key].cg(x, bs[k], 1e-10, relative=True)
         torch.cuda.synchronize()
         t_seq += time.perf_counter() - t0
+        its64.append(r64.iterations)
+        true_64 = max(true_64, _true_rel(ops[key], x, bs[k]))
         worst = max(worst, float(((xs[k] - x).norm() / max(x.norm().item(), 1e-300)).item()))
     for op in ops.values():
         op.close()
     n = len(probs)
+    dofs = [workloads.ndof(d, p) for d, p, _, _ in probs]
+    bytes_b = sum(nk * (8 + FP32_INNER_BYTES_PER_IT * r.inner_iterations + FLEX_OUTER_BYTES * r.outer_iterations +
+                        RESID_BYTES * (r.fp64_applies - r.outer_iterations)) for nk, r in zip(dofs, res))
+    bytes_64 = sum(nk * (8 + RESID_BYTES + CG64_BYTES_PER_IT * it) for nk, it in zip(dofs, its64))
+    peak, src = measured_peaks()
     out = {"problems": n, "status": st, "converged": ok, "batch_solves_per_s": n / t_batch,
            "fp64_one_at_a_time_solves_per_s": n / t_seq, "speedup": t_seq / t_batch,
-           "max_rel_diff_vs_fp64": worst, "total_dof": sum(workloads.ndof(d, p) for d, p, _, _ in probs),
-           "inner_iterations_max": max(r.inner_iterations for r in res)}
+           "max_true_rel_residual_batch": true_b, "max_true_rel_residual_fp64_cg": true_64,
+           "max_rel_diff_vs_fp64": worst, "total_dof": sum(dofs),
+           "inner_iterations_max": max(r.inner_iterations for r in res),
+           "outer_steps_max": max(r.outer_iterations for r in res),
+           "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak,
+                        "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src,
+                        "batch_achieved": bytes_b / t_batch / 1e9, "batch_frac": bytes_b / t_batch / 1e9 / peak,
+                        "fp64_achieved": bytes_64 / t_seq / 1e9, "fp64_frac": bytes_64 / t_seq / 1e9 / peak},
+           "timing": "wall clock around each whole batch / solve, synchronised"}
+    if cpu:
+        import oracle_lib
+
+        orc = oracle_lib.load()
+        nthreads = os.cpu_count() or 1
+        kbig = max(range(n), key=lambda k: dofs[k])
+        d, p, pen, _ = probs[kbig]
+        bn = bs[kbig].cpu().numpy()
+        t0 = time.perf_counter()
+        orc.cg(p, d, pen, bn, 0.0, max_it=4, nthreads=nthreads)
+        per_dof_it = (time.perf_counter() - t0) / 4 / dofs[kbig]
+        est = sum(nk * it for nk, it in zip(dofs, its64)) * per_dof_it
+        out["cpu_baseline"] = {"value": n / est, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                               "sample": "4 oracle CG iterations on the largest problem (%dx%d, p=%d), %.3g s per "
+                                         "DoF-iteration, scaled to every problem's FP64 iteration count" %
+                                         (d, d, p, per_dof_it)}
     batch.close()
     return out
 
@@ -764,12 +800,13 @@ def run_batch(args):
     sampler = ClockSampler(0)
     sampler.start()
     n0 = sipg.launch_count()
-    a = _batch_case(torch, sipg, workloads, workloads.shared_mesh_rhs(64, 256, 4, seed=1))
-    b = _batch_case(torch, sipg, workloads, workloads.uneven_problems(args.uneven, seed=2))
+    cpu = not args.no_cpu_baseline
+    a = _batch_case(torch, sipg, workloads, workloads.shared_mesh_rhs(64, 256, 4, seed=1), cpu)
+    b = _batch_case(torch, sipg, workloads, workloads.uneven_problems(args.uneven, seed=2), cpu)
     launches = sipg.launch_count() - n0
     clocks = sampler.stop()
     line = _base_line(args, "solves/s, batched mixed-precision solves to 1e-10 (64 RHS on 256x256 p=4)",
-                      a["batch_solves_per_s"], "solves/s", True, "f32 pairs (inner) + f64 (outer)",
+                      a["batch_solves_per_s"], "solves/s", True, "f32 (inner) + f64 (outer)",
                       {"workload": "(a) 64 RHS, 256x256 quads p=4, 4 sine modes each (seed 1); "
                                    "(b) %d problems, N log-uniform [16,256], p in 2..8 (seed 2)" % args.uneven},
                       shared_mesh=a, uneven=b, clocks=clocks, gpu_launches=launches)

@@ -557,6 +557,7 @@ sipg_status sipg_op_destroy(sipg_op* op) {
   ws_free(op->ws32);
   if (op->mixed_free) op->mixed_free(op->mixed);
   if (op->pcg_free) op->pcg_free(op->pcg);
+  if (op->tl_free) op->tl_free(op->tl);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
   for (cudaStream_t h : op->hs)

@@ -144,9 +144,11 @@ struct MixedCache {
   CgState<double>* stp_host = nullptr;
   ReduceScratch red64{}, red32{};
   cudaStream_t cap = nullptr;
-  cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
-  int exec_k[4] = {0, 0, 0, 0};
-  int exec_gen[4] = {-1, -1, -1, -1};
+  cudaGraphExec_t exec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int exec_k[5] = {0, 0, 0, 0, 0};
+  int exec_gen[5] = {-1, -1, -1, -1, -1};
+  unsigned long long exec_launches[5] = {0, 0, 0, 0, 0};  // kernel launches one replay makes
+  void* tl = nullptr;  // the op's two-level preconditioner (owned by the op)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // flexible outer kind (allocated on its first use): the FP64 direction d and
   // q = A d, and its scalars
@@ -256,7 +258,18 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
   a.nu = (float)op->pen;
   a.st = m.st32;
   a.red = m.red32;
-  if (kind == SIPG_INNER_F64) {
+  if (kind == SIPG_INNER_F32_TWOLEVEL) {
+    // z = M r (two-level; r.z and beta), p = z + beta p, Ap and alpha, then
+    // e += alpha p, r -= alpha Ap and the stop test on r.r
+    float* z = m.p[1];
+    const sipg_status pst = twolevel_enqueue(op, m.tl, m.r, z, m.st32, m.red32, s);
+    if (pst != SIPG_OK) return pst;
+    k_cg_direction<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], z, m.n, m.st32);
+    count_launch();
+    a.in = m.p[0];
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_DOT, a, op->tab, s));
+    k_pcg_update_f32<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.r, m.Ap, m.n, m.st32, m.red32);
+  } else if (kind == SIPG_INNER_F64) {
     k_cg_direction<double><<<vec_grid(m.n), kVecThreads, 0, s>>>((double*)m.p[0], (const double*)m.r, m.n, m.stp);
     count_launch();
     ApplyArgs<double> d{};
@@ -304,13 +317,19 @@ sipg_status capture(sipg_op* op, MixedCache& m, int kind, int K) {
     ApplyArgs<double> prep{};
     prep.dim = op->dim;
     SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_PREPARE, prep, op->tab, m.cap));
-  } else if (kind == SIPG_INNER_PAIRS)
+  } else if (kind == SIPG_INNER_PAIRS) {
     SIPG_CUDA_TRY(launch_apply_df(op->p, op->cfgdf, APPLY_PREPARE, none, nullptr, nullptr, 0, 0, op->tab, m.cap));
+  }
   else
     SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_PREPARE, none, op->tab, m.cap));
   SIPG_CUDA_TRY(cudaStreamBeginCapture(m.cap, cudaStreamCaptureModeThreadLocal));
   sipg_status st = SIPG_OK;
+  // the launches counted while capturing are the graph's, not executed ones
+  const unsigned long long c0 = g_launches.load();
   for (int k = 0; k < K && st == SIPG_OK; ++k) st = enqueue_iteration(op, m, kind, m.cap);
+  const unsigned long long c1 = g_launches.load();
+  g_launches.fetch_sub(c1 - c0);
+  m.exec_launches[kind] = c1 - c0;
   cudaGraph_t g = nullptr;
   const cudaError_t end = cudaStreamEndCapture(m.cap, &g);
   if (st != SIPG_OK) {
@@ -370,7 +389,7 @@ template <typename StT>
 sipg_status run_inner(Solve& v, int kind, StT* st_dev, StT* st_host) {
   for (;;) {
     SIPG_CUDA_TRY(cudaGraphLaunch(v.m->exec[kind], v.s));
-    count_launch(3ULL * v.K);
+    count_launch(v.m->exec_launches[kind]);
     SIPG_CUDA_TRY(cudaMemcpyAsync(st_host, st_dev, sizeof(StT), cudaMemcpyDeviceToHost, v.s));
     SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
     if (st_host->done) return SIPG_OK;
@@ -439,7 +458,7 @@ constexpr int kFlexibleInnerCap = 4000;
 
 // Flexible CG in FP64 with the FP32 inner CG as its preconditioner (see the
 // top of this file).
-sipg_status solve_flexible(Solve& v, const sipg_mixed_opts& o, long long max_inner) {
+sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long long max_inner) {
   MixedCache& m = *v.m;
   const size_t n = v.n;
   const int vb = v.vb;
@@ -463,7 +482,7 @@ sipg_status solve_flexible(Solve& v, const sipg_mixed_opts& o, long long max_inn
                                              kFlexibleInnerCap);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
-    st = run_inner(v, SIPG_INNER_F32, m.st32, m.st32_host);
+    st = run_inner(v, kind, m.st32, m.st32_host);
     if (st != SIPG_OK) return st;
     v.inner_total += m.st32_host->it;
     if (m.st32_host->it == 0) {
@@ -523,18 +542,25 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   sipg_mixed_opts o = {0.1, 1e-10, 200, 0, SIPG_INNER_AUTO, SIPG_OUTER_AUTO};
   if (opts) o = *opts;
   if (!(o.inner_tol > 0) || !(o.inner_tol < 1) || !(o.outer_tol > 0) || o.max_outer < 1 || o.inner < 0 ||
-      o.inner > 3 || o.outer < 0 || o.outer > 2) {
-    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1, inner in 0..3, outer in 0..2");
+      o.inner > 4 || o.outer < 0 || o.outer > 2) {
+    set_error("sipg_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1, inner in 0..4, outer in 0..2");
     return SIPG_ERR_INVALID;
   }
   int outer = o.outer;
   if (outer == SIPG_OUTER_AUTO)
     outer = (o.inner == SIPG_INNER_PAIRS || o.inner == SIPG_INNER_F64) ? SIPG_OUTER_RELIABLE : SIPG_OUTER_FLEXIBLE;
-  if (outer == SIPG_OUTER_FLEXIBLE && o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32) {
-    set_error("sipg_solve_mixed: the flexible outer kind runs an FP32 inner CG (inner = AUTO or F32)");
+  if (outer == SIPG_OUTER_FLEXIBLE && o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32 &&
+      o.inner != SIPG_INNER_F32_TWOLEVEL) {
+    set_error("sipg_solve_mixed: the flexible outer kind runs an FP32 inner CG (inner = AUTO, F32 or F32_TWOLEVEL)");
     return SIPG_ERR_INVALID;
   }
-  const int kind = outer == SIPG_OUTER_FLEXIBLE ? (int)SIPG_INNER_F32 : choose_inner(o.inner, op->p, op->dim, op->pen);
+  if (outer == SIPG_OUTER_RELIABLE && o.inner == SIPG_INNER_F32_TWOLEVEL) {
+    set_error("sipg_solve_mixed: the two-level-preconditioned inner CG runs under the flexible outer kind");
+    return SIPG_ERR_INVALID;
+  }
+  const int kind = outer == SIPG_OUTER_FLEXIBLE
+                       ? (o.inner == SIPG_INNER_F32 ? (int)SIPG_INNER_F32 : (int)SIPG_INNER_F32_TWOLEVEL)
+                       : choose_inner(o.inner, op->p, op->dim, op->pen);
   cudaStream_t s = (cudaStream_t)stream;
   SIPG_CUDA_TRY(cudaSetDevice(op->device));
   const size_t n = (size_t)op->ndof;
@@ -542,6 +568,10 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   sipg_status st = cache_get(op, &mp);
   if (st != SIPG_OK) return st;
   MixedCache& m = *mp;
+  if (kind == SIPG_INNER_F32_TWOLEVEL && !m.tl) {
+    st = twolevel_get(op, &m.tl);
+    if (st != SIPG_OK) return st;
+  }
   const int K = n <= (1u << 20) ? 32 : 8;  // inner iterations per graph launch
   st = capture(op, m, kind, K);
   if (st != SIPG_OK) return st;
@@ -555,7 +585,7 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
   v.bnorm = std::sqrt(m.st64_host->bb);
-  const sipg_status status = outer == SIPG_OUTER_FLEXIBLE ? solve_flexible(v, o, max_inner)
+  const sipg_status status = outer == SIPG_OUTER_FLEXIBLE ? solve_flexible(v, kind, o, max_inner)
                                                           : solve_reliable(v, kind, o, max_inner);
   if (status == SIPG_ERR_CUDA || status == SIPG_ERR_NOMEM) return status;
   SIPG_CUDA_TRY(cudaEventRecord(m.ev1, s));

@@ -53,6 +53,7 @@ __device__ __forceinline__ void fcg_restart_body(const double* __restrict__ r64,
     st->beta = 0.f;
     st->status = (int)SIPG_OK;
     st->rr = total;
+    st->rres = total;  // the preconditioned inner solve's stop test reads r.r here
     st->rmax = sqrtf(total);
     st->delta = 0.f;  // no reliable updates inside a preconditioner solve
     st->stop = stop;
@@ -107,6 +108,38 @@ __device__ __forceinline__ void fcg_direction_body(const float* __restrict__ e, 
   }
 }
 
+// The update of a preconditioned inner CG (rr holds r.z, set by the
+// preconditioner's last kernel): x += alpha p, r -= alpha Ap, rres = r.r,
+// it++, and the stop test on sqrt(rres).
+template <typename T>
+__device__ __forceinline__ void pcg_update_body(T* __restrict__ x, const T* __restrict__ p, T* __restrict__ r,
+                                                const T* __restrict__ Ap, size_t n, CgState<T>* st,
+                                                const ReduceScratch& red, int bid, int nblocks) {
+  __shared__ T sh[32];
+  if (*(volatile int*)&st->done) return;
+  const T alpha = st->alpha;
+  T acc = T(0);
+  const size_t stride = (size_t)nblocks * blockDim.x;
+  for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const T ri = fma(-alpha, Ap[i], r[i]);
+    r[i] = ri;
+    acc = fma(ri, ri, acc);
+  }
+  const T bt = block_sum<T, kVecThreads>(acc, sh);
+  T total;
+  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
+    st->rres = total;
+    st->it += 1;
+    st->first = 0;
+    st->done = !(sqrt(total) > st->stop && st->it < st->max_it);
+    if (!isfinite(total)) {
+      st->status = (int)SIPG_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+  }
+}
+
 // ---- one solve ----
 
 static __global__ void __launch_bounds__(kVecThreads)
@@ -114,6 +147,12 @@ static __global__ void __launch_bounds__(kVecThreads)
                   const CgState<double>* st64, FcgState* fs, CgState<float>* st, ReduceScratch red, float stop,
                   int max_it) {
   fcg_restart_body(r64, r, e, n, st64, fs, st, red, stop, max_it, blockIdx.x, gridDim.x);
+}
+
+static __global__ void __launch_bounds__(kVecThreads)
+    k_pcg_update_f32(float* __restrict__ x, const float* __restrict__ p, float* __restrict__ r,
+                     const float* __restrict__ Ap, size_t n, CgState<float>* st, ReduceScratch red) {
+  pcg_update_body<float>(x, p, r, Ap, n, st, red, blockIdx.x, gridDim.x);
 }
 
 static __global__ void __launch_bounds__(kVecThreads)

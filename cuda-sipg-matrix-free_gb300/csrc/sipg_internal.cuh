@@ -272,4 +272,18 @@ struct sipg_op {
   void (*mixed_free)(void*) = nullptr;
   void* pcg = nullptr;  // the block-Jacobi preconditioner and PCG workspace
   void (*pcg_free)(void*) = nullptr;
+  void* tl = nullptr;  // the two-level preconditioner of the mixed solve (twolevel.cu)
+  void (*tl_free)(void*) = nullptr;
 };
+
+namespace sipg {
+// The operator's two-level preconditioner (block-Jacobi + vertex-grid
+// multigrid, twolevel.cu), built on first use: synchronous, not during stream
+// capture.
+sipg_status twolevel_get(sipg_op* op, void** handle);
+// Enqueues z = M r on s in FP32; with st (an inner PCG state) every kernel is
+// skipped once st->done and the last one sets st->rr = r.z and beta.
+sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float* r, float* z, CgState<float>* st,
+                             const ReduceScratch& red, cudaStream_t s);
+int twolevel_levels(const void* handle);
+}  // namespace sipg

@@ -1,0 +1,756 @@
+// twolevel.cu -- the two-level preconditioner of the mixed-precision inner
+// solve (no counterpart in the reference):
+//
+//   z = B^-1 r + P V(P^T r)
+//
+// B^-1: exact element block-Jacobi.  The diagonal block of an element
+//   depends only on which of its four faces lie on the domain boundary, so a
+//   mesh has at most nine distinct blocks (one for dim = 1, four for dim = 2);
+//   they are probed from the FP64 operator on a mesh of min(dim, 3) elements
+//   per side (checkerboard colouring: face neighbours never share a probe) and
+//   inverted on the host.
+// P: the continuous bilinear (Q1) functions on the (dim + 1)^2 element
+//   vertices, sampled at each element's LGL nodes; P^T r sums each vertex's
+//   hat function against r over the (up to four) elements around it.
+// V: one symmetric multigrid V-cycle on the Q1 vertex grid for the coarse
+//   operator A_0 = P^T A P (probed from the FP64 operator with nine colours
+//   of vertices -- its stencil is 9-point), Galerkin levels A_{l+1} =
+//   P_l^T A_l P_l down to at most kTlCoarsestCells cells per side (built on
+//   the host; a level of m cells goes to ceil(m/2), odd m with one coarse
+//   cell of a single fine cell at its end), two damped-Jacobi sweeps before
+//   and after each coarse correction, the coarsest level by its dense
+//   inverse.
+//
+// The block part removes the degree's share of the condition number, the
+// coarse part the mesh size's: CG iterations stay flat in dim (measured with
+// a CPU restatement, FP64, pen p^2, 16^2..64^2: p = 2: 24, 4: 41-44, 6:
+// 59-62, 8: 76-79, against 119-376 for plain CG at p = 4, 6).  That is what
+// lets the inner solve run in FP32: unpreconditioned, kappa ~ 2e7 at 512^2,
+// p = 6 and FP32 CG (kappa eps_32 ~ 1) needs ~2,000 iterations to reduce its
+// residual 100-fold.
+//
+// The kernels are templates on the value type: the inner solve runs the
+// float ones; the set-up probes with the double ones.
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "sipg_cg.cuh"
+
+using namespace sipg;
+
+namespace sipg {
+
+constexpr int kTlElemThreads = 64;  // element kernels: one thread per element
+constexpr int kTlVecThreads = 256;  // vertex kernels: one thread per vertex
+constexpr int kTlCoarsestCells = 8; // coarsen while a level has more cells per side
+constexpr int kTlTypes = 16;        // element types: bit 0 LEFT, 1 RIGHT, 2 DOWN, 3 UP face on the boundary
+
+// Element type of element (row, col): which faces are on the domain boundary
+// (row 0 is the top row, so its UP face is).
+__host__ __device__ inline int tl_elem_type(int row, int col, int dim) {
+  return (col == 0 ? 1 : 0) | (col == dim - 1 ? 2 : 0) | (row == dim - 1 ? 4 : 0) | (row == 0 ? 8 : 0);
+}
+
+// 1-D interpolation weight of fine vertex i (of a level with m cells) from
+// coarse vertex J: the coarse vertices sit at the even fine vertices and at
+// m; an odd fine vertex other than m is the midpoint of its two neighbours.
+template <typename T>
+__host__ __device__ inline T tl_w(int i, int J, int m) {
+  if (i % 2 == 0 || i == m) return ((i + 1) / 2 == J) ? T(1) : T(0);
+  return (J == (i - 1) / 2 || J == (i + 1) / 2) ? T(0.5) : T(0);
+}
+
+// One level of the vertex grid (device pointers).
+template <typename T>
+struct TlLev {
+  int m;        // cells per side; (m + 1)^2 vertices, v = vy * (m + 1) + vx, vy bottom-up
+  const T* S;   // stencil planes [9][nv], entry k = (dy + 1) * 3 + (dx + 1)
+  const T* wd;  // omega / diagonal
+  T* b;         // right-hand side
+  T* x;         // V-cycle iterate (the result)
+  T* y;         // second buffer of the smoothing sweeps
+};
+
+// The element's bilinear hat functions at its LGL nodes: l[a][i] = (1 -+ x_i) / 2.
+template <typename T, int P>
+struct TlHat {
+  T l[2][P + 1];
+};
+
+__device__ __forceinline__ bool tl_done(const int* done) { return done && *(volatile const int*)done; }
+
+template <typename T>
+__device__ __forceinline__ T tl_stencil(const TlLev<T>& L, const T* __restrict__ x, int vx, int vy) {
+  const int n1 = L.m + 1, nv = n1 * n1, v = vy * n1 + vx;
+  T s = T(0);
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int ux = vx + dx, uy = vy + dy;
+      if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
+      s = fma(L.S[((dy + 1) * 3 + (dx + 1)) * nv + v], x[uy * n1 + ux], s);
+    }
+  return s;
+}
+
+// ---- the DG <-> Q1 transfers (one thread per element, 64 per block) ----
+
+// corner sums cp[(a * 2 + b) * noe + e] = sum_{i1,i2} l_a(x_i1) l_b(x_i2) r(i1,i2,e)
+template <typename T, int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_restrict_elem(const T* __restrict__ r, T* __restrict__ cp, size_t noe, const __grid_constant__ TlHat<T, P> h,
+                       const int* done) {
+  constexpr int N1 = P + 1;
+  if (tl_done(done)) return;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < noe; e += (size_t)gridDim.x * blockDim.x) {
+    T c00 = T(0), c01 = T(0), c10 = T(0), c11 = T(0);
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      T s0 = T(0), s1 = T(0);
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2) {
+        const T v = __ldg(r + (size_t)(i1 * N1 + i2) * noe + e);
+        s0 = fma(h.l[0][i2], v, s0);
+        s1 = fma(h.l[1][i2], v, s1);
+      }
+      c00 = fma(h.l[0][i1], s0, c00);
+      c01 = fma(h.l[0][i1], s1, c01);
+      c10 = fma(h.l[1][i1], s0, c10);
+      c11 = fma(h.l[1][i1], s1, c11);
+    }
+    cp[0 * noe + e] = c00;
+    cp[1 * noe + e] = c01;
+    cp[2 * noe + e] = c10;
+    cp[3 * noe + e] = c11;
+  }
+}
+
+// b0 at vertex (vx, vy): the corner sums of the elements around it, in a fixed order
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads)
+    k_tl_restrict_vert(const T* __restrict__ cp, T* __restrict__ b0, int dim, const int* done) {
+  if (tl_done(done)) return;
+  const int n1 = dim + 1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n1 * n1) return;
+  const int vx = v % n1, vy = v / n1;
+  const size_t noe = (size_t)dim * dim;
+  T acc = T(0);
+  for (int R = vy - 1; R <= vy; ++R) {  // element rows counted bottom-up
+    if (R < 0 || R >= dim) continue;
+    for (int col = vx - 1; col <= vx; ++col) {
+      if (col < 0 || col >= dim) continue;
+      const size_t e = (size_t)(dim - 1 - R) * dim + col;
+      const int a = vx - col, b = vy - R;
+      acc += cp[(size_t)(a * 2 + b) * noe + e];
+    }
+  }
+  b0[v] = acc;
+}
+
+// out = P xv: the Q1 function of vertex values xv at every element's nodes
+template <typename T, int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_prolong(const T* __restrict__ xv, T* __restrict__ out, int dim, const __grid_constant__ TlHat<T, P> h) {
+  constexpr int N1 = P + 1;
+  const size_t noe = (size_t)dim * dim;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < noe; e += (size_t)gridDim.x * blockDim.x) {
+    const int row = (int)(e / dim), col = (int)(e % dim), R = dim - 1 - row;
+    const T x00 = xv[R * (dim + 1) + col], x10 = xv[R * (dim + 1) + col + 1];
+    const T x01 = xv[(R + 1) * (dim + 1) + col], x11 = xv[(R + 1) * (dim + 1) + col + 1];
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1)
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2)
+        out[(size_t)(i1 * N1 + i2) * noe + e] =
+            h.l[0][i1] * (h.l[0][i2] * x00 + h.l[1][i2] * x01) + h.l[1][i1] * (h.l[0][i2] * x10 + h.l[1][i2] * x11);
+  }
+}
+
+// ---- the V-cycle on the vertex grid ----
+
+// two damped-Jacobi sweeps from zero: x1 = wd b, x = x1 + wd (b - A x1)
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_presmooth(TlLev<T> L, const int* done) {
+  if (tl_done(done)) return;
+  const int n1 = L.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int vx = v % n1, vy = v / n1;
+  T s = T(0);
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int ux = vx + dx, uy = vy + dy;
+      if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
+      const int u = uy * n1 + ux;
+      s = fma(L.S[((dy + 1) * 3 + (dx + 1)) * nv + v], L.wd[u] * L.b[u], s);
+    }
+  const T x1 = L.wd[v] * L.b[v];
+  L.x[v] = fma(L.wd[v], L.b[v] - s, x1);
+}
+
+// coarse right-hand side: C.b = P^T (F.b - A F.x)
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_restrict_resid(TlLev<T> F, TlLev<T> C, const int* done) {
+  if (tl_done(done)) return;
+  const int cn1 = C.m + 1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= cn1 * cn1) return;
+  const int J = v % cn1, I = v / cn1, fn1 = F.m + 1;
+  T acc = T(0);
+  for (int iy = 2 * I - 1; iy <= 2 * I + 1; ++iy) {
+    if (iy < 0 || iy > F.m) continue;
+    const T wy = tl_w<T>(iy, I, F.m);
+    if (wy == T(0)) continue;
+    for (int ix = 2 * J - 1; ix <= 2 * J + 1; ++ix) {
+      if (ix < 0 || ix > F.m) continue;
+      const T wx = tl_w<T>(ix, J, F.m);
+      if (wx == T(0)) continue;
+      const T res = F.b[iy * fn1 + ix] - tl_stencil(F, F.x, ix, iy);
+      acc = fma(wx * wy, res, acc);
+    }
+  }
+  C.b[v] = acc;
+}
+
+// the fine iterate plus the prolonged coarse correction, at vertex (ux, uy)
+template <typename T>
+__device__ __forceinline__ T tl_corrected(const TlLev<T>& F, const TlLev<T>& C, int ux, int uy) {
+  const int cn1 = C.m + 1;
+  T c = T(0);
+  const bool px = (ux % 2 == 0) || (ux == F.m), py = (uy % 2 == 0) || (uy == F.m);
+  const int jx0 = px ? (ux + 1) / 2 : (ux - 1) / 2, jx1 = px ? jx0 : (ux + 1) / 2;
+  const int jy0 = py ? (uy + 1) / 2 : (uy - 1) / 2, jy1 = py ? jy0 : (uy + 1) / 2;
+  const T wx = px ? T(1) : T(0.5), wy = py ? T(1) : T(0.5);
+  if (px && py) {
+    c = C.x[jy0 * cn1 + jx0];
+  } else if (px) {
+    c = wy * (C.x[jy0 * cn1 + jx0] + C.x[jy1 * cn1 + jx0]);
+  } else if (py) {
+    c = wx * (C.x[jy0 * cn1 + jx0] + C.x[jy0 * cn1 + jx1]);
+  } else {
+    c = T(0.25) * ((C.x[jy0 * cn1 + jx0] + C.x[jy0 * cn1 + jx1]) + (C.x[jy1 * cn1 + jx0] + C.x[jy1 * cn1 + jx1]));
+  }
+  return F.x[uy * (F.m + 1) + ux] + c;
+}
+
+// first post-sweep on x + P C.x: y = xc + wd (b - A xc)
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_post1(TlLev<T> F, TlLev<T> C, const int* done) {
+  if (tl_done(done)) return;
+  const int n1 = F.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int vx = v % n1, vy = v / n1;
+  T s = T(0);
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int ux = vx + dx, uy = vy + dy;
+      if (ux < 0 || uy < 0 || ux > F.m || uy > F.m) continue;
+      s = fma(F.S[((dy + 1) * 3 + (dx + 1)) * nv + v], tl_corrected(F, C, ux, uy), s);
+    }
+  F.y[v] = fma(F.wd[v], F.b[v] - s, tl_corrected(F, C, vx, vy));
+}
+
+// second post-sweep: x = y + wd (b - A y)
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_post2(TlLev<T> L, const int* done) {
+  if (tl_done(done)) return;
+  const int n1 = L.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  L.x[v] = fma(L.wd[v], L.b[v] - tl_stencil(L, L.y, v % n1, v / n1), L.y[v]);
+}
+
+// coarsest level: x = A^-1 b (dense, one block)
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const int* done) {
+  if (tl_done(done)) return;
+  const int nv = (L.m + 1) * (L.m + 1);
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    T s = T(0);
+    for (int u = 0; u < nv; ++u) s = fma(ainv[v * nv + u], L.b[u], s);
+    L.x[v] = s;
+  }
+}
+
+// z = B^-1 r + P x0 (x0: the level-0 V-cycle result).  MODE 1: also r.z and
+// the PCG bookkeeping of the inner state (first: rr = r.z; else beta =
+// r.z / rr, rr = r.z).
+template <typename T, int P, int MODE>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ binv,
+                int dim, const __grid_constant__ TlHat<T, P> h, CgState<T>* st, ReduceScratch red) {
+  constexpr int N1 = P + 1, NN = N1 * N1;
+  __shared__ T col[NN][kTlElemThreads];
+  __shared__ T sh[32];
+  if (MODE == 1 && *(volatile int*)&st->done) return;
+  const int t = threadIdx.x;
+  const size_t noe = (size_t)dim * dim;
+  T acc = T(0);
+  const size_t tiles = (noe + kTlElemThreads - 1) / kTlElemThreads;
+  for (size_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const size_t e = tile * kTlElemThreads + t;
+    if (e >= noe) continue;
+#pragma unroll
+    for (int k = 0; k < NN; ++k) col[k][t] = __ldg(r + (size_t)k * noe + e);
+    const int row = (int)(e / dim), cl = (int)(e % dim), R = dim - 1 - row;
+    const T* __restrict__ B = binv + (size_t)tl_elem_type(row, cl, dim) * NN * NN;
+    const T x00 = x0[R * (dim + 1) + cl], x10 = x0[R * (dim + 1) + cl + 1];
+    const T x01 = x0[(R + 1) * (dim + 1) + cl], x11 = x0[(R + 1) * (dim + 1) + cl + 1];
+#pragma unroll 1
+    for (int k = 0; k < NN; ++k) {
+      const int i1 = k / N1, i2 = k - i1 * N1;
+      T v = h.l[0][i1] * (h.l[0][i2] * x00 + h.l[1][i2] * x01) + h.l[1][i1] * (h.l[0][i2] * x10 + h.l[1][i2] * x11);
+#pragma unroll
+      for (int j = 0; j < NN; ++j) v = fma(__ldg(B + k * NN + j), col[j][t], v);
+      z[(size_t)k * noe + e] = v;
+      if (MODE == 1) acc = fma(v, col[k][t], acc);
+    }
+  }
+  if (MODE == 1) {
+    const T bt = block_sum<T, kTlElemThreads>(acc, sh);
+    T total;
+    if (grid_sum_last<T, kTlElemThreads>(bt, red, gridDim.x, sh, &total) && t == 0) {
+      if (!st->first) st->beta = total / st->rr;
+      st->rr = total;
+      if (!(total > T(0)) || !isfinite(total)) {
+        st->status = (int)SIPG_ERR_BREAKDOWN;
+        st->done = 1;
+      }
+    }
+  }
+}
+
+// ---- host side ----
+
+int tl_grid(size_t n, int threads, int cap) {
+  return (int)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)cap));
+}
+
+template <typename T, int P>
+TlHat<T, P> tl_hat(const HostTables& h) {
+  TlHat<T, P> t;
+  for (int i = 0; i <= P; ++i) {
+    t.l[0][i] = (T)(0.5 * (1.0 - h.nodes[i]));
+    t.l[1][i] = (T)(0.5 * (1.0 + h.nodes[i]));
+  }
+  return t;
+}
+
+#define SIPG_TL_DISPATCH(FN, T, p, ...)  \
+  switch (p) {                             \
+    case 1: FN<T, 1>(__VA_ARGS__); break;  \
+    case 2: FN<T, 2>(__VA_ARGS__); break;  \
+    case 3: FN<T, 3>(__VA_ARGS__); break;  \
+    case 4: FN<T, 4>(__VA_ARGS__); break;  \
+    case 5: FN<T, 5>(__VA_ARGS__); break;  \
+    case 6: FN<T, 6>(__VA_ARGS__); break;  \
+    case 7: FN<T, 7>(__VA_ARGS__); break;  \
+    case 8: FN<T, 8>(__VA_ARGS__); break;  \
+  }
+
+template <typename T, int P>
+void tl_launch_restrict_elem(const HostTables& h, const T* r, T* cp, size_t noe, const int* done, cudaStream_t s) {
+  k_tl_restrict_elem<T, P><<<tl_grid(noe, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(r, cp, noe,
+                                                                                             tl_hat<T, P>(h), done);
+}
+template <typename T, int P>
+void tl_launch_prolong(const HostTables& h, const T* xv, T* out, int dim, cudaStream_t s) {
+  k_tl_prolong<T, P><<<tl_grid((size_t)dim * dim, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(
+      xv, out, dim, tl_hat<T, P>(h));
+}
+template <typename T, int P>
+void tl_launch_finish(const HostTables& h, int mode, const T* r, T* z, const T* x0, const T* binv, int dim,
+                      CgState<T>* st, ReduceScratch red, cudaStream_t s) {
+  const size_t noe = (size_t)dim * dim;
+  if (mode == 1)
+    k_tl_finish<T, P, 1><<<tl_grid(noe, kTlElemThreads, red.capacity), kTlElemThreads, 0, s>>>(
+        r, z, x0, binv, dim, tl_hat<T, P>(h), st, red);
+  else
+    k_tl_finish<T, P, 0><<<tl_grid(noe, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(r, z, x0, binv, dim,
+                                                                                           tl_hat<T, P>(h), st, red);
+}
+
+// Gauss-Jordan inverse with partial pivoting (n <= 81); false if singular.
+bool tl_invert(std::vector<double>& a, int n) {
+  std::vector<double> inv((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(a[(size_t)r * n + c]) > std::fabs(a[(size_t)piv * n + c])) piv = r;
+    if (!(std::fabs(a[(size_t)piv * n + c]) > 0.0)) return false;
+    if (piv != c)
+      for (int k = 0; k < n; ++k) {
+        std::swap(a[(size_t)piv * n + k], a[(size_t)c * n + k]);
+        std::swap(inv[(size_t)piv * n + k], inv[(size_t)c * n + k]);
+      }
+    const double d = 1.0 / a[(size_t)c * n + c];
+    for (int k = 0; k < n; ++k) {
+      a[(size_t)c * n + k] *= d;
+      inv[(size_t)c * n + k] *= d;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[(size_t)r * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) {
+        a[(size_t)r * n + k] -= f * a[(size_t)c * n + k];
+        inv[(size_t)r * n + k] -= f * inv[(size_t)c * n + k];
+      }
+    }
+  }
+  a.swap(inv);
+  return true;
+}
+
+// Host 9-point stencil of one level: S[k * nv + v].
+struct HostLevel {
+  int m = 0;
+  std::vector<double> S;
+  double omega = 0;
+};
+
+void host_stencil_apply(const HostLevel& L, const std::vector<double>& x, std::vector<double>& y) {
+  const int n1 = L.m + 1, nv = n1 * n1;
+  y.assign(nv, 0.0);
+  for (int vy = 0; vy <= L.m; ++vy)
+    for (int vx = 0; vx <= L.m; ++vx) {
+      const int v = vy * n1 + vx;
+      double s = 0.0;
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int ux = vx + dx, uy = vy + dy;
+          if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
+          s += L.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + v] * x[uy * n1 + ux];
+        }
+      y[v] = s;
+    }
+}
+
+// the next level's stencil: P^T A P by probing with nine colours
+HostLevel host_galerkin(const HostLevel& F) {
+  HostLevel C;
+  C.m = (F.m + 1) / 2;
+  const int cn1 = C.m + 1, cnv = cn1 * cn1, fn1 = F.m + 1, fnv = fn1 * fn1;
+  C.S.assign((size_t)9 * cnv, 0.0);
+  std::vector<double> xc(cnv), xf(fnv), yf, yc(cnv);
+  for (int cy = 0; cy < 3; ++cy)
+    for (int cx = 0; cx < 3; ++cx) {
+      for (int v = 0; v < cnv; ++v) xc[v] = ((v % cn1) % 3 == cx && (v / cn1) % 3 == cy) ? 1.0 : 0.0;
+      for (int iy = 0; iy <= F.m; ++iy)  // P
+        for (int ix = 0; ix <= F.m; ++ix) {
+          double s = 0.0;
+          for (int I = std::max(0, (iy - 1) / 2); I <= std::min(C.m, (iy + 1) / 2 + 1); ++I)
+            for (int J = std::max(0, (ix - 1) / 2); J <= std::min(C.m, (ix + 1) / 2 + 1); ++J)
+              s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * xc[I * cn1 + J];
+          xf[iy * fn1 + ix] = s;
+        }
+      host_stencil_apply(F, xf, yf);
+      for (int I = 0; I <= C.m; ++I)  // P^T
+        for (int J = 0; J <= C.m; ++J) {
+          double s = 0.0;
+          for (int iy = std::max(0, 2 * I - 1); iy <= std::min(F.m, 2 * I + 1); ++iy)
+            for (int ix = std::max(0, 2 * J - 1); ix <= std::min(F.m, 2 * J + 1); ++ix)
+              s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * yf[iy * fn1 + ix];
+          yc[I * cn1 + J] = s;
+        }
+      for (int I = 0; I <= C.m; ++I)
+        for (int J = 0; J <= C.m; ++J)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int ux = J + dx, uy = I + dy;
+              if (ux < 0 || uy < 0 || ux > C.m || uy > C.m || ux % 3 != cx || uy % 3 != cy) continue;
+              C.S[(size_t)((dy + 1) * 3 + (dx + 1)) * cnv + I * cn1 + J] = yc[I * cn1 + J];
+            }
+    }
+  return C;
+}
+
+// omega = 1.52 / lambda_max(D^-1 A) (power iteration from a fixed vector)
+double host_omega(const HostLevel& L) {
+  const int n1 = L.m + 1, nv = n1 * n1;
+  std::vector<double> x(nv), y;
+  for (int v = 0; v < nv; ++v) x[v] = std::sin(0.7 * v + 0.3) + 0.5;
+  double lam = 1.0;
+  for (int it = 0; it < 40; ++it) {
+    host_stencil_apply(L, x, y);
+    double nrm = 0.0, nx = 0.0;
+    for (int v = 0; v < nv; ++v) {
+      y[v] /= L.S[(size_t)4 * nv + v];
+      nrm += y[v] * y[v];
+      nx += x[v] * x[v];
+    }
+    lam = std::sqrt(nrm / nx);
+    const double s = 1.0 / std::sqrt(nrm);
+    for (int v = 0; v < nv; ++v) x[v] = y[v] * s;
+  }
+  return 1.6 / (1.05 * lam);
+}
+
+}  // namespace sipg
+
+namespace {
+
+// Everything the preconditioner keeps on the device for one operator.
+struct TwoLevel {
+  int dim = 0, p = 0;
+  float* binv = nullptr;  // [16][nn][nn] block inverses
+  float* cp = nullptr;    // [4][noe] corner sums
+  float* ainv = nullptr;  // coarsest level's dense inverse
+  std::vector<TlLev<float>> lev;
+  std::vector<void*> allocs;
+  ~TwoLevel() {
+    for (void* a : allocs) cudaFree(a);
+  }
+};
+
+void twolevel_free(void* p) { delete static_cast<TwoLevel*>(p); }
+
+template <typename T>
+sipg_status dalloc(TwoLevel& tl, T** out, size_t count) {
+  void* p = nullptr;
+  SIPG_CUDA_TRY(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)));
+  tl.allocs.push_back(p);
+  *out = static_cast<T*>(p);
+  return SIPG_OK;
+}
+
+// Element block inverses: probe the diagonal blocks with the FP64 operator on
+// a mesh of min(dim, 3) elements per side, one checkerboard colour and node
+// at a time.
+sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
+  const int p = op->p, n1 = p + 1, nn = n1 * n1, dm = std::min(op->dim, 3), noe = dm * dm;
+  sipg_op* small = nullptr;
+  sipg_status st = sipg_op_create(dm, p, op->pen, &small);
+  if (st != SIPG_OK) return st;
+  const size_t n = (size_t)nn * noe;
+  double *dx = nullptr, *dy = nullptr;
+  std::vector<double> hx(n), hy(n);
+  std::vector<std::vector<double>> blk(kTlTypes);
+  cudaError_t e = cudaMalloc(&dx, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dy, n * sizeof(double));
+  for (int color = 0; color < 2 && e == cudaSuccess && st == SIPG_OK; ++color)
+    for (int k = 0; k < nn && e == cudaSuccess && st == SIPG_OK; ++k) {
+      std::fill(hx.begin(), hx.end(), 0.0);
+      for (int el = 0; el < noe; ++el)
+        if (((el / dm) + (el % dm)) % 2 == color) hx[(size_t)k * noe + el] = 1.0;
+      e = cudaMemcpy(dx, hx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) break;
+      st = sipg_apply_f64(small, dx, dy, nullptr);
+      if (st != SIPG_OK) break;
+      e = cudaMemcpy(hy.data(), dy, n * sizeof(double), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) break;
+      for (int el = 0; el < noe; ++el) {
+        if (((el / dm) + (el % dm)) % 2 != color) continue;
+        std::vector<double>& B = blk[tl_elem_type(el / dm, el % dm, dm)];
+        if (B.empty()) B.assign((size_t)nn * nn, 0.0);
+        for (int j = 0; j < nn; ++j) B[(size_t)j * nn + k] = hy[(size_t)j * noe + el];
+      }
+    }
+  cudaFree(dx);
+  cudaFree(dy);
+  sipg_op_destroy(small);
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(e);
+  table.assign((size_t)kTlTypes * nn * nn, 0.0f);
+  for (int t = 0; t < kTlTypes; ++t) {
+    if (blk[t].empty()) continue;
+    if (!tl_invert(blk[t], nn)) {
+      set_error("two-level preconditioner: singular element block");
+      return SIPG_ERR_INVALID;
+    }
+    for (size_t i = 0; i < (size_t)nn * nn; ++i) table[(size_t)t * nn * nn + i] = (float)blk[t][i];
+  }
+  return SIPG_OK;
+}
+
+// The level-0 vertex operator P^T A P, probed with the FP64 operator and nine
+// colours of vertices.
+sipg_status build_level0(sipg_op* op, HostLevel& L0) {
+  const int dim = op->dim, p = op->p, n1 = dim + 1, nv = n1 * n1;
+  const size_t noe = (size_t)dim * dim, n = (size_t)op->ndof;
+  L0.m = dim;
+  L0.S.assign((size_t)9 * nv, 0.0);
+  double *xv = nullptr, *xd = nullptr, *yd = nullptr, *cp = nullptr, *yv = nullptr;
+  cudaError_t e = cudaMalloc(&xv, nv * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&yv, nv * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&xd, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&yd, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&cp, 4 * noe * sizeof(double));
+  std::vector<double> hx(nv), hy(nv);
+  sipg_status st = SIPG_OK;
+  for (int c = 0; c < 9 && e == cudaSuccess && st == SIPG_OK; ++c) {
+    const int cx = c % 3, cy = c / 3;
+    for (int v = 0; v < nv; ++v) hx[v] = ((v % n1) % 3 == cx && (v / n1) % 3 == cy) ? 1.0 : 0.0;
+    e = cudaMemcpy(xv, hx.data(), nv * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) break;
+    SIPG_TL_DISPATCH(tl_launch_prolong, double, p, op->tab, xv, xd, dim, (cudaStream_t)0)
+    count_launch();
+    st = sipg_apply_f64(op, xd, yd, nullptr);
+    if (st != SIPG_OK) break;
+    SIPG_TL_DISPATCH(tl_launch_restrict_elem, double, p, op->tab, yd, cp, noe, (const int*)nullptr, (cudaStream_t)0)
+    k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads>>>(cp, yv, dim, nullptr);
+    count_launch(2);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(hy.data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) break;
+    for (int vy = 0; vy <= dim; ++vy)
+      for (int vx = 0; vx <= dim; ++vx)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int ux = vx + dx, uy = vy + dy;
+            if (ux < 0 || uy < 0 || ux > dim || uy > dim || ux % 3 != cx || uy % 3 != cy) continue;
+            L0.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + vy * n1 + vx] = hy[vy * n1 + vx];
+          }
+  }
+  cudaFree(xv);
+  cudaFree(yv);
+  cudaFree(xd);
+  cudaFree(yd);
+  cudaFree(cp);
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(e);
+  return SIPG_OK;
+}
+
+sipg_status build(sipg_op* op, TwoLevel& tl) {
+  tl.dim = op->dim;
+  tl.p = op->p;
+  const int nn = (op->p + 1) * (op->p + 1);
+  std::vector<float> table;
+  sipg_status st = build_blocks(op, table);
+  if (st != SIPG_OK) return st;
+  st = dalloc(tl, &tl.binv, table.size());
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(cudaMemcpy(tl.binv, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
+  (void)nn;
+  st = dalloc(tl, &tl.cp, 4 * (size_t)op->noe);
+  if (st != SIPG_OK) return st;
+  // the vertex-grid hierarchy
+  std::vector<HostLevel> H(1);
+  st = build_level0(op, H[0]);
+  if (st != SIPG_OK) return st;
+  while (H.back().m > kTlCoarsestCells) {
+    H.back().omega = host_omega(H.back());
+    H.push_back(host_galerkin(H.back()));
+  }
+  for (const HostLevel& L : H) {
+    const int nv = (L.m + 1) * (L.m + 1);
+    TlLev<float> d{};
+    d.m = L.m;
+    float *S = nullptr, *wd = nullptr;
+    st = dalloc(tl, &S, (size_t)9 * nv);
+    if (st == SIPG_OK) st = dalloc(tl, &wd, nv);
+    if (st == SIPG_OK) st = dalloc(tl, &d.b, nv);
+    if (st == SIPG_OK) st = dalloc(tl, &d.x, nv);
+    if (st == SIPG_OK) st = dalloc(tl, &d.y, nv);
+    if (st != SIPG_OK) return st;
+    std::vector<float> hs((size_t)9 * nv), hw(nv);
+    for (size_t i = 0; i < hs.size(); ++i) hs[i] = (float)L.S[i];
+    for (int v = 0; v < nv; ++v) hw[v] = (float)(L.omega / L.S[(size_t)4 * nv + v]);
+    SIPG_CUDA_TRY(cudaMemcpy(S, hs.data(), hs.size() * sizeof(float), cudaMemcpyHostToDevice));
+    SIPG_CUDA_TRY(cudaMemcpy(wd, hw.data(), hw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    d.S = S;
+    d.wd = wd;
+    tl.lev.push_back(d);
+  }
+  // the coarsest level's dense inverse
+  const HostLevel& Lc = H.back();
+  const int cn1 = Lc.m + 1, cnv = cn1 * cn1;
+  std::vector<double> A((size_t)cnv * cnv, 0.0);
+  for (int v = 0; v < cnv; ++v)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int ux = v % cn1 + dx, uy = v / cn1 + dy;
+        if (ux < 0 || uy < 0 || ux > Lc.m || uy > Lc.m) continue;
+        A[(size_t)v * cnv + uy * cn1 + ux] = Lc.S[(size_t)((dy + 1) * 3 + (dx + 1)) * cnv + v];
+      }
+  if (!tl_invert(A, cnv)) {
+    set_error("two-level preconditioner: singular coarsest operator");
+    return SIPG_ERR_INVALID;
+  }
+  std::vector<float> af(A.begin(), A.end());
+  st = dalloc(tl, &tl.ainv, af.size());
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(cudaMemcpy(tl.ainv, af.data(), af.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return SIPG_OK;
+}
+
+}  // namespace
+
+namespace sipg {
+
+// The operator's two-level preconditioner, built on first use (synchronous;
+// not during stream capture).
+sipg_status twolevel_get(sipg_op* op, void** out) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (!op->tl) {
+    SIPG_CUDA_TRY(cudaSetDevice(op->device));
+    TwoLevel* tl = new (std::nothrow) TwoLevel;
+    if (!tl) return SIPG_ERR_NOMEM;
+    const sipg_status st = build(op, *tl);
+    if (st != SIPG_OK) {
+      delete tl;
+      return st;
+    }
+    op->tl = tl;
+    op->tl_free = twolevel_free;
+  }
+  *out = op->tl;
+  return SIPG_OK;
+}
+
+// Enqueues z = M r on s (FP32).  With st (the inner PCG state): every kernel
+// is skipped once st->done, and the last one sets r.z and beta in st.
+sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float* r, float* z, CgState<float>* st,
+                             const ReduceScratch& red, cudaStream_t s) {
+  const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
+  const int* done = st ? &st->done : nullptr;
+  const int dim = tl.dim, nl = (int)tl.lev.size();
+  const size_t noe = (size_t)dim * dim;
+  SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, done, s)
+  const int nv0 = (dim + 1) * (dim + 1);
+  k_tl_restrict_vert<float><<<tl_grid(nv0, kTlVecThreads, 1 << 30), kTlVecThreads, 0, s>>>(tl.cp, tl.lev[0].b, dim,
+                                                                                          done);
+  count_launch(2);
+  auto grid = [&](const TlLev<float>& L) { return tl_grid((size_t)(L.m + 1) * (L.m + 1), kTlVecThreads, 1 << 30); };
+  for (int l = 0; l + 1 < nl; ++l) {
+    k_tl_presmooth<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], done);
+    k_tl_restrict_resid<float><<<grid(tl.lev[l + 1]), kTlVecThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
+    count_launch(2);
+  }
+  k_tl_dense<float><<<1, kTlVecThreads, 0, s>>>(tl.lev[nl - 1], tl.ainv, done);
+  count_launch();
+  for (int l = nl - 2; l >= 0; --l) {
+    k_tl_post1<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
+    k_tl_post2<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], done);
+    count_launch(2);
+  }
+  SIPG_TL_DISPATCH(tl_launch_finish, float, tl.p, op->tab, st ? 1 : 0, r, z, tl.lev[0].x, tl.binv, dim, st, red, s)
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+// Levels of the vertex hierarchy (for reports), 0 if not built.
+int twolevel_levels(const void* handle) {
+  return handle ? (int)static_cast<const TwoLevel*>(handle)->lev.size() : 0;
+}
+
+}  // namespace sipg
+
+extern "C" sipg_status sipg_apply_twolevel_f32(sipg_op* op, const float* d_r, float* d_z, void* stream) {
+  if (!op || !d_r || !d_z || d_r == d_z) {
+    set_error("sipg_apply_twolevel_f32: null or aliased vectors");
+    return SIPG_ERR_INVALID;
+  }
+  SIPG_CUDA_TRY(cudaSetDevice(op->device));
+  void* tl = nullptr;
+  sipg_status st = twolevel_get(op, &tl);
+  if (st != SIPG_OK) return st;
+  return twolevel_enqueue(op, tl, d_r, d_z, nullptr, ReduceScratch{}, (cudaStream_t)stream);
+}

@@ -42,7 +42,7 @@ class MixedOpts(C.Structure):
                 ("inner", C.c_int), ("outer", C.c_int)]
 
 
-INNER = {"auto": 0, "f32": 1, "pairs": 2, "f64": 3}
+INNER = {"auto": 0, "f32": 1, "pairs": 2, "f64": 3, "twolevel": 4}
 OUTER = {"auto": 0, "reliable": 1, "flexible": 2}
 
 
@@ -115,6 +115,7 @@ _SIGS = {
     "sipg_apply_prec_f64": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_volume_mvm_f64": (C.c_int, [C.c_int, C.c_int, _VP, C.c_int, _VP, _VP, _VP]),
     "sipg_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), C.POINTER(MixedResult), _VP]),
+    "sipg_apply_twolevel_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
     "sipg_rhs_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP]),
     "sipg_err_norms_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP, _VP]),
     "sipg_last_error": (C.c_char_p, []),
@@ -410,11 +411,13 @@ class Operator:
         """Inner CG on the FP32 pipes inside an FP64 outer iteration; stops at
         ||b - Ax|| <= outer_tol ||b|| (FP64).  outer = "flexible": flexible CG
         in FP64 preconditioned by an FP32 inner CG that runs until its residual
-        fell by inner_tol; "reliable": defect correction with reliable updates
-        (an FP64 correction whenever the inner residual fell by inner_tol),
-        inner = "f32" (FP32 vectors), "pairs" (double-float pairs) or "auto"
-        (by the condition-number estimate); outer = "auto": flexible unless
-        inner names pairs or f64.  Returns (status, MixedResult)."""
+        fell by inner_tol -- inner = "twolevel" (the default: the inner CG
+        preconditioned by the two-level preconditioner) or "f32" (plain);
+        "reliable": defect correction with reliable updates (an FP64 correction
+        whenever the inner residual fell by inner_tol), inner = "f32" (FP32
+        vectors), "pairs" (double-float pairs), "f64" or "auto" (by the
+        condition-number estimate); outer = "auto": flexible unless inner names
+        pairs or f64.  Returns (status, MixedResult)."""
         import torch
 
         self._vec(x, torch.float64)
@@ -425,6 +428,17 @@ class Operator:
         if st not in (0, 3, 4):
             _check(st, "solve_mixed")
         return st, res
+
+    def apply_twolevel(self, r, out=None, stream=None):
+        """out = M r, the two-level preconditioner of the flexible mixed solve
+        (float32 CUDA tensors)."""
+        import torch
+
+        self._vec(r, torch.float32)
+        if out is None:
+            out = torch.empty_like(r)
+        _check(lib().sipg_apply_twolevel_f32(self._h, _ptr(r), _ptr(out), _stream(stream)), "apply_twolevel")
+        return out
 
     def rhs(self, sol, modes=None, out=None, stream=None):
         """Right-hand side of a test problem (SOL name or id) as a float64 CUDA vector."""

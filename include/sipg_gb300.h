@@ -74,7 +74,21 @@ typedef struct {
  * p = 1..8 at penalty p^2).  SIPG_INNER_PAIRS: double-float vectors (two FP32
  * planes) and the compensated apply, ~48-bit values on the FP32 pipes -- any
  * condition number.  SIPG_INNER_AUTO picks F32 when kappa * 2^-24 < 0.01. */
-typedef enum { SIPG_INNER_AUTO = 0, SIPG_INNER_F32 = 1, SIPG_INNER_PAIRS = 2, SIPG_INNER_F64 = 3 } sipg_inner_kind;
+typedef enum {
+  SIPG_INNER_AUTO = 0,
+  SIPG_INNER_F32 = 1,
+  SIPG_INNER_PAIRS = 2,
+  SIPG_INNER_F64 = 3,
+  SIPG_INNER_F32_TWOLEVEL = 4
+} sipg_inner_kind;
+/* SIPG_INNER_F32_TWOLEVEL (flexible outer kind only; its default): the FP32
+ * inner CG preconditioned by the operator's two-level preconditioner -- exact
+ * element block-Jacobi plus a coarse correction on the continuous bilinear
+ * functions of the element vertices, solved by one multigrid V-cycle (see
+ * sipg_apply_twolevel_f32).  Its iteration count no longer grows with the
+ * mesh, so the FP32 inner CG works at every condition number of the supported
+ * meshes; unpreconditioned (SIPG_INNER_F32) FP32 CG slows down sharply once
+ * kappa * eps_32 approaches 1. */
 /* SIPG_INNER_F64 is the same reliable-update loop with FP64 vectors and the
  * FP64 apply: the all-FP64 yardstick.  The plain CG (sipg_cg_f64, the
  * reference's algorithm) stops on its recursively updated residual, whose gap
@@ -94,7 +108,8 @@ typedef enum { SIPG_INNER_AUTO = 0, SIPG_INNER_F32 = 1, SIPG_INNER_PAIRS = 2, SI
  *   outer step) minimises the error in the energy norm, where the rounding of
  *   an FP32 correction costs only ~sqrt(kappa) * eps_32, so FP32 values and
  *   accumulation serve at any condition number of the supported meshes.
- * SIPG_OUTER_AUTO: flexible with FP32 inner vectors unless the caller names
+ * SIPG_OUTER_AUTO: flexible (with the two-level-preconditioned FP32 inner CG
+ *   unless the caller names SIPG_INNER_F32) unless the caller names
  *   SIPG_INNER_PAIRS or SIPG_INNER_F64 (then reliable). */
 typedef enum { SIPG_OUTER_AUTO = 0, SIPG_OUTER_RELIABLE = 1, SIPG_OUTER_FLEXIBLE = 2 } sipg_outer_kind;
 
@@ -252,6 +267,17 @@ sipg_status sipg_pcg_f64(sipg_op* op, double* d_x, const double* d_b, double tol
  * counterpart. */
 sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* d_b, const sipg_mixed_opts* opts,
                              sipg_mixed_result* res, void* stream);
+
+/* d_z = M d_r, the two-level preconditioner of the flexible mixed solve, on
+ * FP32 vectors: M = B^-1 + P V P^T, B^-1 the exact inverse of every element's
+ * diagonal block of A, P the continuous bilinear functions of the element
+ * vertices sampled at the LGL nodes, V one symmetric multigrid V-cycle (two
+ * damped-Jacobi sweeps before and after each coarse correction, Galerkin
+ * levels, the coarsest by its dense inverse) for P^T A P.  Built on the first
+ * call on an op (synchronous: a few FP64 applies to probe A, then host work;
+ * not during stream capture) and kept with the op.  No reference
+ * counterpart. */
+sipg_status sipg_apply_twolevel_f32(sipg_op* op, const float* d_r, float* d_z, void* stream);
 
 /* The vector steps of the reference's CG, for callers that iterate around
  * their own operator (an abs_mvm implementation).  sipg_dot_* is

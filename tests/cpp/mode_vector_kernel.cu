@@ -5,7 +5,8 @@
 // It applies the nodal mass matrix of the SIPG-SEM basis, out(i1,i2,e) =
 // (h/2)^2 w_i1 w_i2 in(i1,i2,e), with the LGL weights from the C ABI.  Prints
 // one JSON line with the largest difference from the same product formed on
-// the host through HOST_DEBUG indexing (exit 0 only when it is zero).
+// the host through HOST_DEBUG indexing, relative to the largest value (exit 0
+// when it is at rounding level).
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -40,16 +41,19 @@ int main() {
   mass_kernel<double><<<dim3((noe + 127) / 128, n, n), 128>>>(d_in, d_out, d_w, scale);
   if (cudaDeviceSynchronize() != cudaSuccess) return 3;
   host_mode_vector<double, int> h_out(d_out);
-  double maxerr = 0.0;
+  double maxerr = 0.0, maxref = 0.0;
   for (int i1 = 0; i1 < n; ++i1)
     for (int i2 = 0; i2 < n; ++i2)
       for (int e = 0; e < noe; ++e) {
         const double ref = scale * w[i1] * w[i2] * h_in.data()[d_in.HOST_DEBUG(i1, i2, e)];
         maxerr = std::fmax(maxerr, std::fabs(h_out.data()[d_out.HOST_DEBUG(i1, i2, e)] - ref));
+        maxref = std::fmax(maxref, std::fabs(ref));
       }
-  std::printf("{\"case\": \"mode_vector_kernel\", \"dim\": %d, \"p\": %d, \"max_abs_err\": %.3e}\n", dim, p, maxerr);
+  const double rel = maxref > 0 ? maxerr / maxref : maxerr;
+  std::printf("{\"case\": \"mode_vector_kernel\", \"dim\": %d, \"p\": %d, \"max_rel_err\": %.3e}\n", dim, p, rel);
   cudaFree(d_w);
   d_in.free();
   d_out.free();
-  return maxerr == 0.0 ? 0 : 1;
+  // a wrong index gives an O(1) error; the device's products may round differently in the last bit
+  return rel <= 1e-14 ? 0 : 1;
 }

@@ -188,12 +188,16 @@ def test_mixed_pairs_on_an_ill_conditioned_problem(sipg, torch):
     op.close()
 
 
-def test_mixed_auto_picks_f32_for_well_conditioned(sipg, torch):
+def test_mixed_auto_picks_flexible_twolevel(sipg, torch):
     op = sipg.Operator(16, 2, 4.0)
     b = op.rhs("sinsin")
     x = torch.zeros_like(b)
     st, rm = op.solve_mixed(x, b)
-    assert st == 0 and rm.inner_kind == 1 and rm.rel_residual <= 1e-10
+    assert st == 0 and rm.inner_kind == 4 and rm.outer_kind == 2 and rm.rel_residual <= 1e-10
+    # the reliable-update loop with auto inner still picks FP32 vectors on a well-conditioned problem
+    x.zero_()
+    st, rm = op.solve_mixed(x, b, outer="reliable")
+    assert st == 0 and rm.inner_kind == 1 and rm.outer_kind == 1 and rm.rel_residual <= 1e-10
     op.close()
 
 
@@ -201,8 +205,9 @@ def _true_rel(op, x, b):
     return (b - op.apply(x)).norm().item() / b.norm().item()
 
 
-@pytest.mark.parametrize("inner_tol", [1e-1, 1e-3, 1e-5])
-def test_flexible_fp32_inner_on_an_ill_conditioned_problem(sipg, oracle, torch, inner_tol):
+@pytest.mark.parametrize("inner,inner_tol", [("twolevel", 1e-1), ("twolevel", 1e-3), ("twolevel", 1e-5),
+                                             ("f32", 1e-1)])
+def test_flexible_fp32_inner_on_an_ill_conditioned_problem(sipg, oracle, torch, inner, inner_tol):
     # 256 x 256, p = 6: condition number ~5e6 (kappa * eps_32 ~ 0.3), where FP32
     # vectors stall a unit-step defect correction.  Flexible CG in FP64 with a
     # pure FP32 inner CG (FP32 values, FP32 accumulation) reaches a TRUE FP64
@@ -214,8 +219,8 @@ def test_flexible_fp32_inner_on_an_ill_conditioned_problem(sipg, oracle, torch, 
     st, rr = op.solve_mixed(x64, b, inner_tol=0.1, outer_tol=1e-10, inner="f64", outer="reliable")
     assert st == 0 and _true_rel(op, x64, b) <= 1e-10
     xm = torch.zeros_like(b)
-    st, rm = op.solve_mixed(xm, b, inner_tol=inner_tol, outer_tol=1e-10)  # auto: flexible, FP32 inner
-    assert st == 0 and rm.converged == 1 and rm.inner_kind == 1 and rm.outer_kind == 2
+    st, rm = op.solve_mixed(xm, b, inner_tol=inner_tol, outer_tol=1e-10, inner=inner, outer="flexible")
+    assert st == 0 and rm.converged == 1 and rm.inner_kind == sipg.INNER[inner] and rm.outer_kind == 2
     assert rm.rel_residual <= 1e-10
     true_rel = _true_rel(op, xm, b)
     assert true_rel <= 1.01e-10, true_rel
