@@ -48,7 +48,7 @@ FP32_INNER_BYTES_PER_IT = 40  # the same iteration on FP32 vectors
 FLEX_OUTER_BYTES = 120       # flexible outer step: inner restart 16 + gamma 12 + direction 28 + FP64 apply 16 + update 48
 RESID_BYTES = 24             # r = b - A x in FP64: read x, b; write r
 RELIABLE_UPDATE_BYTES = 64   # reliable update: x += e 24, r = b - A x 24, inner restart 16
-MIXED_INNER_TOL = 1e-2       # the flexible solve's inner tolerance (measured fastest at 512^2, p = 6)
+MIXED_INNER_TOL = 3e-2       # the flexible solve's inner tolerance (measured fastest at 512^2, p = 6: 54 ms, 1e-2: 56)
 
 
 def fp64_flops_per_dof(p):
@@ -465,7 +465,15 @@ def _roofline_solve(bytes_total, ms, fp64_applies, ndof, p, fp64_peak):
 
 
 def _true_rel(op, x, b):
-    """||b - A x|| / ||b||, recomputed in FP64 from the returned solution."""
+    """||b - A x|| / ||b||, recomputed in FP64 from the returned solution
+    (sipg_residual_f64: the operator's zero-sum contractions over differences,
+    whose rounding stays far below the plain sums' on a smooth solution)."""
+    return float(op.true_residual(x, b))
+
+
+def _plain_rel(op, x, b):
+    """The same with the plain FP64 apply (sipg_apply_f64), whose rounding puts
+    a floor near 1e-10 under it on the larger smooth problems."""
     return float((b - op.apply(x)).norm().item() / b.norm().item())
 
 
@@ -503,6 +511,7 @@ def mixed_metrics(torch, sipg, reps=3, cpu=True, fp64_peak=None, dim=512, p=6, i
     def record(name, ms, iters, fp64_applies, bytes_total, extra):
         l2, h1, mx = op.err_norms("sinsin", x)
         arms[name] = dict({"ms": ms, "solves_per_s": 1e3 / ms, "true_rel_residual": _true_rel(op, x, b),
+                           "true_rel_residual_plain_sums": _plain_rel(op, x, b),
                            "L2": l2, "H1": h1, "max_err": mx,
                            "roofline": _roofline_solve(bytes_total, ms, fp64_applies, n, p, fp64_peak)}, **extra)
         if iters is not None:

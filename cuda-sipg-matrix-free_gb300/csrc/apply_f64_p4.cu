@@ -6,7 +6,7 @@
 namespace sipg {
 cudaError_t launch_apply_f64_p4(const TileCfg& cfg, int mode, const ApplyArgs<double>& a, const HostTables& h,
                                   cudaStream_t s) {
-  if (is_pernode(cfg, 4)) return launch_apply_pernode<double, 4>(cfg, mode, a, h, s);
+  if (is_pernode(cfg, 4)) return launch_apply_pernode<double, 4>(cfg, apply_base_mode(mode), a, h, s);
   return launch_apply_p<double, 4>(cfg, mode, a, h, s);
 }
 cudaError_t launch_apply_batched_f64_p4(const TileCfg& cfg, int mode, const ApplyArgs<double>* insts,

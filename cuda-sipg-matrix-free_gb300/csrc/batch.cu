@@ -6,13 +6,16 @@
 // vectors, device states and reduction scratch, resident on the device for
 // the life of the batch.  The scheme is the flexible one of mixed.cu, per
 // instance (sipg_fcg.cuh): flexible CG in FP64 around an FP32 inner CG (FP32
-// values and accumulation) that restarts from zero on the scaled residual.
+// values and accumulation) preconditioned by the two-level preconditioner
+// (twolevel.cu; tables shared by the instances of one operator, scratch per
+// instance), restarting from zero on the scaled residual.
 //
-// One inner iteration of the whole batch is one batched FP32 apply launch
-// per degree present (k_sipg_apply_batched in APPLY_DOT mode: the instances'
-// tiles concatenated into one grid), with a batched direction launch before
-// it and a batched update launch after it; K iterations are captured once as
-// a CUDA graph and replayed.  An instance whose inner solve has finished
+// One inner iteration of the whole batch is the batched preconditioner
+// (element kernels one launch per degree present, vertex-grid kernels one
+// launch per level for all instances), a batched direction launch, one
+// batched FP32 apply launch per degree (k_sipg_apply_batched in APPLY_DOT
+// mode: the instances' tiles concatenated into one grid) and a batched update
+// launch; K iterations are captured once as a CUDA graph and replayed.  An instance whose inner solve has finished
 // skips the replays (its blocks return at once) until the host, between
 // replays, runs its FP64 outer step together with every other instance due
 // one (batched gamma / direction / FP64 apply / update launches over that
@@ -27,6 +30,7 @@
 #include <vector>
 
 #include "sipg_fcg.cuh"
+#include "sipg_twolevel.cuh"
 
 using namespace sipg;
 
@@ -64,6 +68,9 @@ struct BInst {
   float* e32 = nullptr;
   float* p32 = nullptr;
   float* Ap32 = nullptr;
+  float* z32 = nullptr;   // preconditioned residual
+  float* tls = nullptr;   // the preconditioner's scratch
+  void* tl = nullptr;     // the operator's two-level preconditioner (owned by the op)
   CgState<float>* st32 = nullptr;   // (in the batch's contiguous state arrays)
   CgState<double>* st64 = nullptr;
   FcgState* fs = nullptr;
@@ -95,6 +102,8 @@ struct sipg_batch {
   CgState<double>* st64 = nullptr;  // n outer states
   FcgState* fs = nullptr;           // n flexible-step scalars
   FcgInst* d_vec = nullptr;         // every instance (the inner graph)
+  TlInst* d_tl = nullptr;           // every instance's preconditioner operands, grouped by degree
+  TlPlan tlplan;
   FcgInst* d_sel = nullptr;         // a selection (capacity n)
   FcgInst* h_sel = nullptr;         // pinned
   ApplyArgs<double>* h_sub = nullptr;  // pinned staging for FP64 apply args
@@ -104,6 +113,7 @@ struct sipg_batch {
   cudaStream_t cap = nullptr;
   cudaGraphExec_t exec = nullptr;
   int K = 8;
+  unsigned long long graph_launches = 0;  // kernel launches one replay makes
   int bpi = 1;  // blocks per instance for the vector kernels
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -119,6 +129,8 @@ static void batch_free(sipg_batch* b) {
     cudaFree(i.e32);
     cudaFree(i.p32);
     cudaFree(i.Ap32);
+    cudaFree(i.z32);
+    cudaFree(i.tls);
     cudaFree(i.red32.partials);
     cudaFree(i.red32.counter);
     cudaFree(i.red64.partials);
@@ -134,6 +146,7 @@ static void batch_free(sipg_batch* b) {
   cudaFree(b->st64);
   cudaFree(b->fs);
   cudaFree(b->d_vec);
+  cudaFree(b->d_tl);
   cudaFree(b->d_sel);
   cudaFreeHost(b->h_sel);
   cudaFreeHost(b->h_sub);
@@ -160,6 +173,7 @@ static FcgInst inst_of(const sipg_batch* b, int k, double* x, const double* rhs,
   v.e32 = i.e32;
   v.p32 = i.p32;
   v.Ap32 = i.Ap32;
+  v.z32 = i.z32;
   v.st32 = i.st32;
   v.st64 = i.st64;
   v.fs = i.fs;
@@ -193,6 +207,10 @@ static sipg_status batch_alloc(sipg_batch* b) {
     SIPG_CUDA_TRY(cudaMalloc(&i.e32, i.n * sizeof(float)));
     SIPG_CUDA_TRY(cudaMalloc(&i.p32, i.n * sizeof(float)));
     SIPG_CUDA_TRY(cudaMalloc(&i.Ap32, i.n * sizeof(float)));
+    SIPG_CUDA_TRY(cudaMalloc(&i.z32, i.n * sizeof(float)));
+    sipg_status tst = twolevel_get(i.op, &i.tl);
+    if (tst != SIPG_OK) return tst;
+    SIPG_CUDA_TRY(cudaMalloc(&i.tls, twolevel_scratch_floats(i.tl) * sizeof(float)));
     i.st32 = b->st32 + k;
     i.st64 = b->st64 + k;
     i.fs = b->fs + k;
@@ -244,6 +262,18 @@ static sipg_status batch_alloc(sipg_batch* b) {
     SIPG_CUDA_TRY(cudaMemcpy(g.d_cg, args.data(), sizeof(ApplyArgs<float>) * m, cudaMemcpyHostToDevice));
     SIPG_CUDA_TRY(cudaMemcpy(g.d_tiles32, ts.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
   }
+  // the preconditioner operands in degree-group order, and their launch plan
+  std::vector<TlInst> htl;
+  std::vector<const HostTables*> tabs;
+  for (const BGroup& g : b->groups)
+    for (int k : g.members) {
+      BInst& i = b->inst[k];
+      htl.push_back(twolevel_inst(i.tl, i.tls, i.r32, i.z32, i.st32, i.red32));
+      tabs.push_back(&i.op->tab);
+    }
+  b->tlplan = twolevel_plan(htl.data(), tabs.data(), n);
+  SIPG_CUDA_TRY(cudaMalloc(&b->d_tl, sizeof(TlInst) * n));
+  SIPG_CUDA_TRY(cudaMemcpy(b->d_tl, htl.data(), sizeof(TlInst) * n, cudaMemcpyHostToDevice));
   std::vector<FcgInst> vec(n);
   for (int k = 0; k < n; ++k) vec[k] = inst_of(b, k, nullptr, nullptr, 1, 0.f);
   SIPG_CUDA_TRY(cudaMalloc(&b->d_vec, sizeof(FcgInst) * n));
@@ -274,8 +304,14 @@ static sipg_status batch_capture(sipg_batch* b) {
   SIPG_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   const dim3 vg(b->bpi, b->n);
+  // the launches counted while capturing are the graph's, not executed ones
+  const unsigned long long c0 = g_launches.load();
   for (int k = 0; k < b->K && err == cudaSuccess; ++k) {
-    k_fcg_inner_direction_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
+    // z = M r (two-level), p = z + beta p, Ap and alpha, then the update
+    if (twolevel_enqueue_batched(b->d_tl, b->tlplan, b->cap) != SIPG_OK) err = cudaErrorUnknown;
+    if (err != cudaSuccess) break;
+    k_fcg_inner_pdirection_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
+    count_launch();
     err = cudaGetLastError();
     for (BGroup& g : b->groups) {
       if (err != cudaSuccess) break;
@@ -283,9 +319,13 @@ static sipg_status batch_capture(sipg_batch* b) {
                                      b->inst[g.members[0]].op->tab, b->cap);
     }
     if (err != cudaSuccess) break;
-    k_fcg_inner_update_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
+    k_fcg_inner_pupdate_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
+    count_launch();
     err = cudaGetLastError();
   }
+  const unsigned long long c1 = g_launches.load();
+  g_launches.fetch_sub(c1 - c0);
+  b->graph_launches = c1 - c0;
   cudaError_t e2 = cudaStreamEndCapture(b->cap, &graph);
   if (err != cudaSuccess || e2 != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
@@ -313,7 +353,7 @@ static sipg_status batch_apply64(sipg_batch* b, const std::vector<int>& sel, int
       BInst& i = b->inst[k];
       if (i.p != g.p) continue;
       ApplyArgs<double> a{};
-      if (mode == APPLY_RESID) {
+      if (apply_base_mode(mode) == APPLY_RESID) {
         a.in = d_x[k];
         a.out = i.r64;
         a.b = d_b[k];
@@ -420,8 +460,9 @@ size_t sipg_batch_footprint(const sipg_batch* b) {
   if (!b) return 0;
   size_t bytes = 0;
   for (const BInst& i : b->inst)
-    bytes += i.n * (3 * 8 + 4 * 4) + 2 * sizeof(double) * reduce_capacity(i.dim) + sizeof(CgState<double>) +
-             sizeof(CgState<float>) + sizeof(FcgState);
+    bytes += i.n * (3 * 8 + 5 * 4) + twolevel_scratch_floats(i.tl) * sizeof(float) +
+             2 * sizeof(double) * reduce_capacity(i.dim) + sizeof(CgState<double>) + sizeof(CgState<float>) +
+             sizeof(FcgState) + sizeof(TlInst);
   return bytes;
 }
 
@@ -442,9 +483,9 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     set_error("sipg_batch_solve_mixed: need 0 < inner_tol < 1, outer_tol > 0, max_outer >= 1");
     return SIPG_ERR_INVALID;
   }
-  if ((o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32) ||
+  if ((o.inner != SIPG_INNER_AUTO && o.inner != SIPG_INNER_F32_TWOLEVEL) ||
       (o.outer != SIPG_OUTER_AUTO && o.outer != SIPG_OUTER_FLEXIBLE)) {
-    set_error("sipg_batch_solve_mixed: batches run the flexible outer kind with an FP32 inner CG");
+    set_error("sipg_batch_solve_mixed: batches run the flexible outer kind with the two-level FP32 inner CG");
     return SIPG_ERR_INVALID;
   }
   cudaStream_t s = (cudaStream_t)stream;
@@ -472,7 +513,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
   k_batch_park<<<(n + 127) / 128, 128, 0, s>>>(b->d_sel, n);
   count_launch(2);
   SIPG_CUDA_TRY(cudaGetLastError());
-  st = batch_apply64(b, all, APPLY_RESID, d_x, d_b, s);
+  st = batch_apply64(b, all, APPLY_RESID_PIVOT, d_x, d_b, s);
   if (st != SIPG_OK) return st;
   st = read_states(b, s, false, true);
   if (st != SIPG_OK) return st;
@@ -501,7 +542,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     if (!active) break;
     // FP32 inner iterations of every instance still in an inner solve
     SIPG_CUDA_TRY(cudaGraphLaunch(b->exec, s));
-    count_launch((unsigned long long)(b->groups.size() + 2) * b->K);
+    count_launch(b->graph_launches);
     st = read_states(b, s, true, false);
     if (st != SIPG_OK) return st;
     std::vector<int> sel;
@@ -521,7 +562,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     k_fcg_direction_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
     count_launch(2);
     SIPG_CUDA_TRY(cudaGetLastError());
-    st = batch_apply64(b, sel, APPLY_DOT, d_x, d_b, s);
+    st = batch_apply64(b, sel, APPLY_DOT_PIVOT, d_x, d_b, s);
     if (st != SIPG_OK) return st;
     k_fcg_update_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
     count_launch();
@@ -549,7 +590,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     }
     if (!chk.empty()) {
       // the recursion says done: b - A x in FP64 decides
-      st = batch_apply64(b, chk, APPLY_RESID, d_x, d_b, s);
+      st = batch_apply64(b, chk, APPLY_RESID_PIVOT, d_x, d_b, s);
       if (st != SIPG_OK) return st;
       st = read_states(b, s, false, true);
       if (st != SIPG_OK) return st;
@@ -579,7 +620,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
       res[k].rel_residual = rel[k];
       res[k].time_ms = ms;
       res[k].converged = conv[k];
-      res[k].inner_kind = SIPG_INNER_F32;
+      res[k].inner_kind = SIPG_INNER_F32_TWOLEVEL;
       res[k].outer_kind = SIPG_OUTER_FLEXIBLE;
       res[k].fp64_applies = fp64[k];
     }

@@ -365,8 +365,11 @@ struct Solve {
   double rel = INFINITY;
 };
 
-// r64 = b - A x in FP64 (APPLY_RESID: r.r into st64, it = 0), read back.
-sipg_status true_residual(Solve& v, double* rr_out) {
+// r64 = b - A x in FP64 (r.r into st64, it = 0), read back: with the
+// pivoted sums (APPLY_RESID_PIVOT), or the plain ones for the all-FP64
+// reliable-update yardstick, whose inner iterations run the plain FP64 apply
+// (checking them against the other rounding floor would only slow it down).
+sipg_status true_residual(Solve& v, double* rr_out, bool plain = false) {
   MixedCache& m = *v.m;
   ApplyArgs<double> a{};
   a.in = v.x;
@@ -376,7 +379,7 @@ sipg_status true_residual(Solve& v, double* rr_out) {
   a.nu = v.op->pen;
   a.st = m.st64;
   a.red = m.red64;
-  SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_RESID, a, v.op->tab, v.s));
+  SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, plain ? APPLY_RESID : APPLY_RESID_PIVOT, a, v.op->tab, v.s));
   ++v.fp64_applies;
   SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, v.s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
@@ -410,7 +413,7 @@ sipg_status solve_reliable(Solve& v, int kind, const sipg_mixed_opts& o, long lo
   auto inner_status = [&]() { return st_double ? m.stp_host->status : m.st32_host->status; };
   for (;;) {
     double rr = 0;
-    sipg_status st = true_residual(v, &rr);
+    sipg_status st = true_residual(v, &rr, kind == SIPG_INNER_F64);
     if (st != SIPG_OK) return st;
     v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
     if (!std::isfinite(v.rel)) {
@@ -506,7 +509,7 @@ sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long lo
     a.nu = v.op->pen;
     a.st = m.st64;
     a.red = m.red64;
-    SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_DOT, a, v.op->tab, s));
+    SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_DOT_PIVOT, a, v.op->tab, s));
     ++v.fp64_applies;
     k_cg_update<double><<<vb, kVecThreads, 0, s>>>(v.x, m.d64, m.d64, m.r64, m.q64, n, m.st64, m.red64);
     count_launch();
@@ -603,4 +606,36 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     res->fp64_applies = v.fp64_applies;
   }
   return status;
+}
+
+extern "C" sipg_status sipg_residual_f64(sipg_op* op, const double* d_x, const double* d_b, double* d_r, double* rel,
+                                         void* stream) {
+  if (!op || !d_x || !d_b || !rel) {
+    set_error("sipg_residual_f64: null argument");
+    return SIPG_ERR_INVALID;
+  }
+  SIPG_CUDA_TRY(cudaSetDevice(op->device));
+  MixedCache* mp = nullptr;
+  sipg_status st = cache_get(op, &mp);
+  if (st != SIPG_OK) return st;
+  MixedCache& m = *mp;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t n = (size_t)op->ndof;
+  k_cg_init<double><<<vec_grid(n), kVecThreads, 0, s>>>(d_b, n, m.st64, 0.0, 0, 1, m.red64);
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  ApplyArgs<double> a{};
+  a.in = d_x;
+  a.out = d_r ? d_r : m.r64;
+  a.b = d_b;
+  a.dim = op->dim;
+  a.nu = op->pen;
+  a.st = m.st64;
+  a.red = m.red64;
+  SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_RESID_PIVOT, a, op->tab, s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
+  const double bb = m.st64_host->bb, rr = m.st64_host->rr;
+  *rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+  return SIPG_OK;
 }

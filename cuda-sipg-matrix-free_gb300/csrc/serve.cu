@@ -8,11 +8,14 @@
 //      rejected); an admitted request gets its vectors from the stream-ordered
 //      pool allocator, its right-hand side built on the device, x = 0, and a
 //      slot in the device state arrays;
-//   2. runs K CG iterations of every active request together: per degree one
-//      batched apply launch for the mixed requests (the FP32 inner CG of the
-//      flexible mixed-precision solve, sipg_fcg.cuh: FP32 vectors and the
-//      FP32 apply, the requests' tiles concatenated) and one for the FP64
-//      ones (k_sipg_apply_batched), then one batched update per precision --
+//   2. runs K CG iterations of every active request together: for the mixed
+//      requests the FP32 inner CG of the flexible mixed-precision solve
+//      (sipg_fcg.cuh), preconditioned by each operator's two-level
+//      preconditioner (twolevel.cu; batched over the requests, scratch per
+//      request), with per degree one batched FP32 apply launch (the
+//      requests' tiles concatenated); for the FP64 ones per degree one
+//      batched apply (k_sipg_apply_batched); then one batched update per
+//      precision --
 //      requests admitted while others are mid-solve simply join the next
 //      launches;
 //   3. reads all active states with one copy; mixed requests whose inner
@@ -44,6 +47,7 @@
 #include <vector>
 
 #include "sipg_fcg.cuh"
+#include "sipg_twolevel.cuh"
 
 using namespace sipg;
 
@@ -145,6 +149,9 @@ struct Request {
   float* r32 = nullptr;
   float* p32 = nullptr;
   float* Ap32 = nullptr;
+  float* z32 = nullptr;      // mixed: preconditioned residual
+  float* tls = nullptr;      // mixed: the preconditioner's scratch
+  void* tl = nullptr;        // mixed: the operator's two-level preconditioner (owned by the op)
   double* p64[2] = {nullptr, nullptr};
   double* Ap64 = nullptr;
   ReduceScratch red32, red64;
@@ -193,6 +200,8 @@ struct Lane {
   VecInst<double>* d_v64 = nullptr;
   FcgInst* h_m = nullptr;    // a selection of mixed requests (start, outer step, restart)
   FcgInst* d_m = nullptr;
+  TlInst* h_tl = nullptr;    // the round's mixed requests' preconditioner operands, by degree
+  TlInst* d_tl = nullptr;
   double* h_tol = nullptr;
   double* d_tol = nullptr;
   const double** h_bptr = nullptr;
@@ -227,7 +236,7 @@ size_t footprint_of(int dim, int p, int precision) {
   const size_t n = (size_t)dim * dim * (p + 1) * (p + 1);
   const size_t red = 2 * (sizeof(double) * (size_t)reduce_capacity(dim) + 256);
   if (precision == SIPG_F64) return n * (8 * 2 + 8 * 4) + red + 4096;  // x, b, r, p0, p1, Ap
-  return n * (8 * 5 + 4 * 4) + red + 4096;                             // x, b, r, d, q + FP32 e, r, p, Ap
+  return n * (8 * 5 + 4 * 5) + twolevel_scratch_floats_for(dim) * 4 + red + 4096;  // x, b, r, d, q + FP32 e, r, p, Ap, z
 }
 
 sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
@@ -293,6 +302,8 @@ sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
     r->r32 = (float*)take(n * 4);
     r->p32 = (float*)take(n * 4);
     r->Ap32 = (float*)take(n * 4);
+    r->z32 = (float*)take(n * 4);
+    r->tls = (float*)take(twolevel_scratch_floats_for(r->req.dim) * 4);
   }
   r->red32.partials = (double*)take(sizeof(double) * cap);
   r->red32.counter = (unsigned int*)take(256);
@@ -309,6 +320,11 @@ sipg_status admit(sipg_server* sv, Request* r, cudaStream_t s) {
   const sipg_modes* modes = (r->req.sol == SIPG_SOL_MODES) ? &r->req.modes : nullptr;
   sipg_status st = rhs_f64(r->op, r->req.sol, modes, r->b64, s);
   if (st != SIPG_OK) return admit_rollback(r, s, st);
+  if (r->req.precision != SIPG_F64) {
+    // the operator's preconditioner, built on its first mixed request (synchronous)
+    st = twolevel_get(r->op, &r->tl);
+    if (st != SIPG_OK) return admit_rollback(r, s, st);
+  }
   r->slot = sv->free_slots.back();
   sv->free_slots.pop_back();
   sv->used += r->footprint;
@@ -374,6 +390,7 @@ FcgInst fcg_of(const Request* r, sipg_server* sv) {
   v.e32 = r->e32;
   v.p32 = r->p32;
   v.Ap32 = r->Ap32;
+  v.z32 = r->z32;
   v.st32 = sv->slots.d32 + r->slot;
   v.st64 = sv->slots.d64 + r->slot;
   v.fs = sv->slots.fs + r->slot;
@@ -484,6 +501,8 @@ sipg_status server_alloc(sipg_server* sv) {
     SIPG_CUDA_TRY(cudaMalloc(&L.d_v64, sizeof(VecInst<double>) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_m, sizeof(FcgInst) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&L.d_m, sizeof(FcgInst) * cap));
+    SIPG_CUDA_TRY(cudaMallocHost(&L.h_tl, sizeof(TlInst) * cap));
+    SIPG_CUDA_TRY(cudaMalloc(&L.d_tl, sizeof(TlInst) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_tol, sizeof(double) * cap));
     SIPG_CUDA_TRY(cudaMalloc(&L.d_tol, sizeof(double) * cap));
     SIPG_CUDA_TRY(cudaMallocHost(&L.h_bptr, sizeof(double*) * cap));
@@ -530,6 +549,8 @@ void server_free(sipg_server* sv) {
     cudaFree(L.d_v64);
     cudaFreeHost(L.h_m);
     cudaFree(L.d_m);
+    cudaFreeHost(L.h_tl);
+    cudaFree(L.d_tl);
     cudaFreeHost(L.h_tol);
     cudaFree(L.d_tol);
     cudaFreeHost(L.h_bptr);
@@ -634,8 +655,22 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
     L.h_v64[j] = v;
     nmax64 = std::max(nmax64, r->n);
   }
-  if (!a32.empty())
+  TlPlan tlplan;
+  if (!a32.empty()) {
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v32, L.h_v32, sizeof(FcgInst) * a32.size(), cudaMemcpyHostToDevice, L.s));
+    // the preconditioner operands, grouped by degree
+    std::vector<Request*> byp(a32);
+    std::stable_sort(byp.begin(), byp.end(),
+                     [](const Request* x, const Request* y) { return x->req.degree < y->req.degree; });
+    std::vector<const HostTables*> tabs;
+    for (size_t j = 0; j < byp.size(); ++j) {
+      Request* r = byp[j];
+      L.h_tl[j] = twolevel_inst(r->tl, r->tls, r->r32, r->z32, sv->slots.d32 + r->slot, r->red32);
+      tabs.push_back(&r->op->tab);
+    }
+    tlplan = twolevel_plan(L.h_tl, tabs.data(), (int)byp.size());
+    SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_tl, L.h_tl, sizeof(TlInst) * byp.size(), cudaMemcpyHostToDevice, L.s));
+  }
   if (!a64.empty())
     SIPG_CUDA_TRY(cudaMemcpyAsync(L.d_v64, L.h_v64, sizeof(VecInst<double>) * a64.size(), cudaMemcpyHostToDevice, L.s));
   const std::vector<GroupLaunch> g32 =
@@ -650,12 +685,14 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
   for (int k = 0; k < sv->opts.iters_per_step; ++k) {
     if (!a32.empty()) {
       const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
-      k_fcg_inner_direction_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      sipg_status st = twolevel_enqueue_batched(L.d_tl, tlplan, L.s);
+      if (st != SIPG_OK) return st;
+      k_fcg_inner_pdirection_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
-      sipg_status st = launch_groups<float>(g32, APPLY_DOT, L.d_a32, L.d_t32, L.s);
+      st = launch_groups<float>(g32, APPLY_DOT, L.d_a32, L.d_t32, L.s);
       if (st != SIPG_OK) return st;
-      k_fcg_inner_update_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      k_fcg_inner_pupdate_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
     }
@@ -737,7 +774,7 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
       return a;
     });
     sipg_status st = upload_groups<double>(gq, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
-    if (st == SIPG_OK) st = launch_groups<double>(gq, APPLY_DOT, L.d_r64, L.d_tr, L.s);
+    if (st == SIPG_OK) st = launch_groups<double>(gq, APPLY_DOT_PIVOT, L.d_r64, L.d_tr, L.s);
     if (st != SIPG_OK) return st;
     k_fcg_update_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
     count_launch();
@@ -774,7 +811,7 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
         return a;
       });
       st = upload_groups<double>(gr, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
-      if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID, L.d_r64, L.d_tr, L.s);
+      if (st == SIPG_OK) st = launch_groups<double>(gr, APPLY_RESID_PIVOT, L.d_r64, L.d_tr, L.s);
       if (st != SIPG_OK) return st;
       SIPG_CUDA_TRY(
           cudaMemcpyAsync(L.h64, sv->slots.d64, sizeof(CgState<double>) * cap, cudaMemcpyDeviceToHost, L.s));

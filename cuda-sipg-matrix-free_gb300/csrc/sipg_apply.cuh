@@ -201,16 +201,18 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
                                            int nblocks) {
   constexpr int N = P, N1 = P + 1, NN = N1 * N1, TE = TX * TY;
   constexpr bool kCols = ApplyColumnForm<T, P>::value;
-  // FP32: every sum whose coefficients add up to zero (a derivative row D, a
+  constexpr int BASE = apply_base_mode(MODE);
+  // FP32 (and the FP64 *_PIVOT modes): every sum whose coefficients add up to zero (a derivative row D, a
   // stiffness row K = D^T W D) is taken over differences from one value of
   // the line, v_i - v_0, which leaves it unchanged in exact arithmetic and
   // drops the part common to the line exactly.  Rounding then scales with
   // the variation of u across an element (h |grad u|), not with u itself: on
   // a smooth vector the FP32 operator's relative error falls from
   // ~kappa eps_32 (~1 at 512 x 512, p = 6) to ~dim eps_32, which is what an
-  // FP32 inner solve needs to see the smooth modes.  (FP64 keeps the plain
-  // sums: its results stay bit-identical to the unpivoted kernel's.)
-  constexpr bool kPivot = sizeof(T) == 4;
+  // FP32 inner solve needs to see the smooth modes.  (The other FP64 modes
+  // keep the plain sums: their results stay bit-identical to the unpivoted
+  // kernel's.)
+  constexpr bool kPivot = sizeof(T) == 4 || MODE != BASE;
   using S = ApplySmem<T, P, TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T red_sh[32];
@@ -221,7 +223,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   constexpr bool kKwSmem = KwInSmem<T, P>::value;
   auto KWv = [&](int k) -> T { return kKwSmem ? kws[k] : tb.KW[k]; };
 
-  constexpr bool kDot = (MODE == APPLY_CG || MODE == APPLY_DOT);  // p.Ap -> alpha
+  constexpr bool kDot = (BASE == APPLY_CG || BASE == APPLY_DOT);  // p.Ap -> alpha
   if (kDot) {
     if (*(volatile int*)&a.st->done) return;  // converged: the launch is a no-op
   }
@@ -237,7 +239,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   bool first = true;
   T beta = T(0);
   int par = 0;
-  if (MODE == APPLY_CG) {
+  if (BASE == APPLY_CG) {
     first = a.st->first != 0;
     beta = a.st->beta;
     par = a.st->parity;
@@ -247,7 +249,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
   // value k of element ee as the operator sees it (CG: p = r + beta p_old)
   auto ld = [&](int k, size_t ee) -> T {
     const T r = __ldg(a.in + (size_t)k * noe + ee);
-    if (MODE == APPLY_CG) return first ? r : fma(beta, __ldg(pold + (size_t)k * noe + ee), r);
+    if (BASE == APPLY_CG) return first ? r : fma(beta, __ldg(pold + (size_t)k * noe + ee), r);
     return r;
   };
   constexpr bool kRegs = NodalInRegs<T, P>::value;
@@ -485,13 +487,13 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
         for (int j = 0; j < N1; ++j) {
           const int k = i1 * N1 + j;
           const size_t gk = (size_t)k * noe + e;
-          if (MODE == APPLY_RESID) {
+          if (BASE == APPLY_RESID) {
             const T rv = __ldg(a.b + gk) - o[j];
             a.out[gk] = rv;
             acc = fma(rv, rv, acc);
           } else {
             a.out[gk] = o[j];
-            if (MODE == APPLY_CG) pnew[gk] = c[j];
+            if (BASE == APPLY_CG) pnew[gk] = c[j];
             if (kDot) acc = fma(c[j], o[j], acc);
           }
         }
@@ -548,7 +550,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
 #pragma unroll
       for (int k = 0; k < NN; ++k) {
         const size_t gk = (size_t)k * noe + e;
-        if (MODE == APPLY_RESID) {
+        if (BASE == APPLY_RESID) {
           const T rv = __ldg(a.b + gk) - o[k];
           a.out[gk] = rv;
           acc = fma(rv, rv, acc);
@@ -556,7 +558,7 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
           a.out[gk] = o[k];
           if (kDot) {
             const T pk = kRegs ? ureg[kRegs ? k : 0] : us[k * TE + t];
-            if (MODE == APPLY_CG) pnew[gk] = pk;
+            if (BASE == APPLY_CG) pnew[gk] = pk;
             acc = fma(pk, o[k], acc);
           }
         }
@@ -564,11 +566,11 @@ __device__ __forceinline__ void apply_tile(const ApplyArgs<T>& a, const Tab<T, P
     }
   }
 
-  if (MODE != APPLY_PLAIN) {
+  if (BASE != APPLY_PLAIN) {
     const T bt = block_sum<T, TE>(acc, red_sh);
     T total;
     if (grid_sum_last<T, TE>(bt, a.red, bid, nblocks, red_sh, &total) && t == 0)
-      apply_finish<T, MODE>(a.st, total, par);
+      apply_finish<T, BASE>(a.st, total, par);
   }
 }
 
@@ -618,6 +620,16 @@ cudaError_t launch_apply_tile(int mode, const ApplyArgs<T>& a, const Tab<T, P>& 
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem);
+  if constexpr (sizeof(T) == 8) {
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_RESID_PIVOT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_sipg_apply<T, P, TX, TY, APPLY_DOT_PIVOT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  } else {
+    mode = apply_base_mode(mode);  // the FP32 sums are always pivoted
+  }
   if (err != cudaSuccess) return err;
   switch (mode) {
     case APPLY_PREPARE:
@@ -633,6 +645,12 @@ cudaError_t launch_apply_tile(int mode, const ApplyArgs<T>& a, const Tab<T, P>& 
       break;
     case APPLY_DOT:
       k_sipg_apply<T, P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(a, tb);
+      break;
+    case APPLY_RESID_PIVOT:
+      if constexpr (sizeof(T) == 8) k_sipg_apply<T, P, TX, TY, APPLY_RESID_PIVOT><<<grid, block, smem, s>>>(a, tb);
+      break;
+    case APPLY_DOT_PIVOT:
+      if constexpr (sizeof(T) == 8) k_sipg_apply<T, P, TX, TY, APPLY_DOT_PIVOT><<<grid, block, smem, s>>>(a, tb);
       break;
     default:
       return cudaErrorInvalidValue;
@@ -676,6 +694,16 @@ cudaError_t launch_apply_batched_tile(int mode, const ApplyArgs<T>* insts, const
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if constexpr (sizeof(T) == 8) {
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID_PIVOT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT_PIVOT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  } else {
+    mode = apply_base_mode(mode);
+  }
   if (err != cudaSuccess || mode == APPLY_PREPARE || total_tiles == 0) return err;
   const dim3 grid(total_tiles), block(TX, TY);
   switch (mode) {
@@ -690,6 +718,14 @@ cudaError_t launch_apply_batched_tile(int mode, const ApplyArgs<T>* insts, const
       break;
     case APPLY_DOT:
       k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    case APPLY_RESID_PIVOT:
+      if constexpr (sizeof(T) == 8)
+        k_sipg_apply_batched<T, P, TX, TY, APPLY_RESID_PIVOT><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
+      break;
+    case APPLY_DOT_PIVOT:
+      if constexpr (sizeof(T) == 8)
+        k_sipg_apply_batched<T, P, TX, TY, APPLY_DOT_PIVOT><<<grid, block, smem, s>>>(insts, tile_start, ninst, tb);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -180,6 +180,7 @@ struct FcgInst {
   float* e32;       // FP32 inner solution
   float* p32;       // FP32 inner direction
   float* Ap32;      // FP32 inner A p
+  float* z32;       // FP32 preconditioned residual (two-level inner kind)
   CgState<float>* st32;
   CgState<double>* st64;
   FcgState* fs;
@@ -234,6 +235,28 @@ static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_update_batched
   const FcgInst v = insts[blockIdx.y];
   if ((int)blockIdx.x >= v.nblk) return;
   cg_update_body<float>(v.e32, v.p32, v.p32, v.r32, v.Ap32, v.n, v.st32, v.red32, blockIdx.x, v.nblk);
+}
+
+// The same for the two-level-preconditioned inner CG: p = z + beta p (first:
+// p = z; z, r.z and beta come from the preconditioner), and the update with
+// the stop test on r.r (pcg_update_body).
+static __global__ void __launch_bounds__(kVecThreads)
+    k_fcg_inner_pdirection_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  const CgState<float>* st = v.st32;
+  if (*(volatile const int*)&st->done) return;
+  const bool first = st->first != 0;
+  const float beta = st->beta;
+  const size_t stride = (size_t)v.nblk * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += stride)
+    v.p32[i] = first ? v.z32[i] : fmaf(beta, v.p32[i], v.z32[i]);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_pupdate_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  pcg_update_body<float>(v.e32, v.p32, v.r32, v.Ap32, v.n, v.st32, v.red32, blockIdx.x, v.nblk);
 }
 
 }  // namespace sipg

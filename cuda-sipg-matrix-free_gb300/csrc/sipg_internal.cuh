@@ -108,8 +108,21 @@ enum ApplyMode : int {
   APPLY_CG = 1,     // u = r + beta p_old (u = r on the first iteration); p_new = u; y = A u; pAp -> alpha;
                     // the parity of the direction buffers flips
   APPLY_RESID = 2,  // y = b - A u; r.r -> rr, stop/done set
-  APPLY_DOT = 3     // y = A p for a direction p formed beforehand (k_cg_direction*); p.Ap -> alpha
+  APPLY_DOT = 3,    // y = A p for a direction p formed beforehand (k_cg_direction*); p.Ap -> alpha
+  // FP64: APPLY_RESID / APPLY_DOT with every zero-sum contraction taken over
+  // differences from one value of its element line (the FP32 apply always
+  // does this): the residual checks and outer steps of the mixed solvers,
+  // where a smooth iterate's rounding in the plain sums would put a floor
+  // near 1e-10 under the true relative residual at 1024^2, p = 4.  The FP64
+  // CG and the plain apply keep the plain sums.  (The per-node FP64 tile of
+  // small meshes runs the plain modes for these.)
+  APPLY_RESID_PIVOT = 4,
+  APPLY_DOT_PIVOT = 5
 };
+// The plain mode a pivoted one computes.
+__host__ __device__ constexpr int apply_base_mode(int mode) {
+  return mode == APPLY_RESID_PIVOT ? APPLY_RESID : (mode == APPLY_DOT_PIVOT ? APPLY_DOT : mode);
+}
 
 template <typename T>
 struct ApplyArgs {

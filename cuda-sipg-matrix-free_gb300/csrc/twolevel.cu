@@ -34,9 +34,11 @@
 #include <algorithm>
 #include <cmath>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "sipg_cg.cuh"
+#include "sipg_twolevel.cuh"
 
 using namespace sipg;
 
@@ -61,17 +63,6 @@ __host__ __device__ inline T tl_w(int i, int J, int m) {
   if (i % 2 == 0 || i == m) return ((i + 1) / 2 == J) ? T(1) : T(0);
   return (J == (i - 1) / 2 || J == (i + 1) / 2) ? T(0.5) : T(0);
 }
-
-// One level of the vertex grid (device pointers).
-template <typename T>
-struct TlLev {
-  int m;        // cells per side; (m + 1)^2 vertices, v = vy * (m + 1) + vx, vy bottom-up
-  const T* S;   // stencil planes [9][nv], entry k = (dy + 1) * 3 + (dx + 1)
-  const T* wd;  // omega / diagonal
-  T* b;         // right-hand side
-  T* x;         // V-cycle iterate (the result)
-  T* y;         // second buffer of the smoothing sweeps
-};
 
 // The element's bilinear hat functions at its LGL nodes: l[a][i] = (1 -+ x_i) / 2.
 template <typename T, int P>
@@ -100,12 +91,10 @@ __device__ __forceinline__ T tl_stencil(const TlLev<T>& L, const T* __restrict__
 
 // corner sums cp[(a * 2 + b) * noe + e] = sum_{i1,i2} l_a(x_i1) l_b(x_i2) r(i1,i2,e)
 template <typename T, int P>
-__global__ void __launch_bounds__(kTlElemThreads)
-    k_tl_restrict_elem(const T* __restrict__ r, T* __restrict__ cp, size_t noe, const __grid_constant__ TlHat<T, P> h,
-                       const int* done) {
+__device__ __forceinline__ void tl_restrict_elem_body(const T* __restrict__ r, T* __restrict__ cp, size_t noe,
+                                                      const TlHat<T, P>& h, int bid, int nb) {
   constexpr int N1 = P + 1;
-  if (tl_done(done)) return;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < noe; e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = (size_t)bid * blockDim.x + threadIdx.x; e < noe; e += (size_t)nb * blockDim.x) {
     T c00 = T(0), c01 = T(0), c10 = T(0), c11 = T(0);
 #pragma unroll
     for (int i1 = 0; i1 < N1; ++i1) {
@@ -128,12 +117,18 @@ __global__ void __launch_bounds__(kTlElemThreads)
   }
 }
 
-// b0 at vertex (vx, vy): the corner sums of the elements around it, in a fixed order
-template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads)
-    k_tl_restrict_vert(const T* __restrict__ cp, T* __restrict__ b0, int dim, const int* done) {
+template <typename T, int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_restrict_elem(const T* __restrict__ r, T* __restrict__ cp, size_t noe, const __grid_constant__ TlHat<T, P> h,
+                       const int* done) {
   if (tl_done(done)) return;
-  const int n1 = dim + 1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  tl_restrict_elem_body<T, P>(r, cp, noe, h, blockIdx.x, gridDim.x);
+}
+
+// b0 at vertex v = (vx, vy): the corner sums of the elements around it, in a fixed order
+template <typename T>
+__device__ __forceinline__ void tl_restrict_vert_body(const T* __restrict__ cp, T* __restrict__ b0, int dim, int v) {
+  const int n1 = dim + 1;
   if (v >= n1 * n1) return;
   const int vx = v % n1, vy = v / n1;
   const size_t noe = (size_t)dim * dim;
@@ -148,6 +143,13 @@ __global__ void __launch_bounds__(kTlVecThreads)
     }
   }
   b0[v] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads)
+    k_tl_restrict_vert(const T* __restrict__ cp, T* __restrict__ b0, int dim, const int* done) {
+  if (tl_done(done)) return;
+  tl_restrict_vert_body<T>(cp, b0, dim, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // out = P xv: the Q1 function of vertex values xv at every element's nodes
@@ -173,9 +175,8 @@ __global__ void __launch_bounds__(kTlElemThreads)
 
 // two damped-Jacobi sweeps from zero: x1 = wd b, x = x1 + wd (b - A x1)
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_presmooth(TlLev<T> L, const int* done) {
-  if (tl_done(done)) return;
-  const int n1 = L.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tl_presmooth_body(const TlLev<T>& L, int v) {
+  const int n1 = L.m + 1, nv = n1 * n1;
   if (v >= nv) return;
   const int vx = v % n1, vy = v / n1;
   T s = T(0);
@@ -192,11 +193,10 @@ __global__ void __launch_bounds__(kTlVecThreads) k_tl_presmooth(TlLev<T> L, cons
   L.x[v] = fma(L.wd[v], L.b[v] - s, x1);
 }
 
-// coarse right-hand side: C.b = P^T (F.b - A F.x)
+// coarse right-hand side at coarse vertex v: C.b = P^T (F.b - A F.x)
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_restrict_resid(TlLev<T> F, TlLev<T> C, const int* done) {
-  if (tl_done(done)) return;
-  const int cn1 = C.m + 1, v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tl_restrict_resid_body(const TlLev<T>& F, const TlLev<T>& C, int v) {
+  const int cn1 = C.m + 1;
   if (v >= cn1 * cn1) return;
   const int J = v % cn1, I = v / cn1, fn1 = F.m + 1;
   T acc = T(0);
@@ -238,9 +238,8 @@ __device__ __forceinline__ T tl_corrected(const TlLev<T>& F, const TlLev<T>& C, 
 
 // first post-sweep on x + P C.x: y = xc + wd (b - A xc)
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_post1(TlLev<T> F, TlLev<T> C, const int* done) {
-  if (tl_done(done)) return;
-  const int n1 = F.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tl_post1_body(const TlLev<T>& F, const TlLev<T>& C, int v) {
+  const int n1 = F.m + 1, nv = n1 * n1;
   if (v >= nv) return;
   const int vx = v % n1, vy = v / n1;
   T s = T(0);
@@ -257,17 +256,15 @@ __global__ void __launch_bounds__(kTlVecThreads) k_tl_post1(TlLev<T> F, TlLev<T>
 
 // second post-sweep: x = y + wd (b - A y)
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_post2(TlLev<T> L, const int* done) {
-  if (tl_done(done)) return;
-  const int n1 = L.m + 1, nv = n1 * n1, v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tl_post2_body(const TlLev<T>& L, int v) {
+  const int n1 = L.m + 1, nv = n1 * n1;
   if (v >= nv) return;
   L.x[v] = fma(L.wd[v], L.b[v] - tl_stencil(L, L.y, v % n1, v / n1), L.y[v]);
 }
 
 // coarsest level: x = A^-1 b (dense, one block)
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const int* done) {
-  if (tl_done(done)) return;
+__device__ __forceinline__ void tl_dense_body(const TlLev<T>& L, const T* __restrict__ ainv) {
   const int nv = (L.m + 1) * (L.m + 1);
   for (int v = threadIdx.x; v < nv; v += blockDim.x) {
     T s = T(0);
@@ -276,22 +273,47 @@ __global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T*
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_presmooth(TlLev<T> L, const int* done) {
+  if (tl_done(done)) return;
+  tl_presmooth_body<T>(L, blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_restrict_resid(TlLev<T> F, TlLev<T> C, const int* done) {
+  if (tl_done(done)) return;
+  tl_restrict_resid_body<T>(F, C, blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_post1(TlLev<T> F, TlLev<T> C, const int* done) {
+  if (tl_done(done)) return;
+  tl_post1_body<T>(F, C, blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_post2(TlLev<T> L, const int* done) {
+  if (tl_done(done)) return;
+  tl_post2_body<T>(L, blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const int* done) {
+  if (tl_done(done)) return;
+  tl_dense_body<T>(L, ainv);
+}
+
 // z = B^-1 r + P x0 (x0: the level-0 V-cycle result).  MODE 1: also r.z and
 // the PCG bookkeeping of the inner state (first: rr = r.z; else beta =
-// r.z / rr, rr = r.z).
+// r.z / rr, rr = r.z), reduced over the nb blocks of this instance.
 template <typename T, int P, int MODE>
-__global__ void __launch_bounds__(kTlElemThreads)
-    k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ binv,
-                int dim, const __grid_constant__ TlHat<T, P> h, CgState<T>* st, ReduceScratch red) {
+__device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0,
+                                               const T* __restrict__ binv, int dim, const TlHat<T, P>& h,
+                                               CgState<T>* st, const ReduceScratch& red, int bid, int nb) {
   constexpr int N1 = P + 1, NN = N1 * N1;
   __shared__ T col[NN][kTlElemThreads];
   __shared__ T sh[32];
-  if (MODE == 1 && *(volatile int*)&st->done) return;
   const int t = threadIdx.x;
   const size_t noe = (size_t)dim * dim;
   T acc = T(0);
   const size_t tiles = (noe + kTlElemThreads - 1) / kTlElemThreads;
-  for (size_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+  for (size_t tile = bid; tile < tiles; tile += nb) {
     const size_t e = tile * kTlElemThreads + t;
     if (e >= noe) continue;
 #pragma unroll
@@ -313,7 +335,7 @@ __global__ void __launch_bounds__(kTlElemThreads)
   if (MODE == 1) {
     const T bt = block_sum<T, kTlElemThreads>(acc, sh);
     T total;
-    if (grid_sum_last<T, kTlElemThreads>(bt, red, gridDim.x, sh, &total) && t == 0) {
+    if (grid_sum_last<T, kTlElemThreads>(bt, red, bid, nb, sh, &total) && t == 0) {
       if (!st->first) st->beta = total / st->rr;
       st->rr = total;
       if (!(total > T(0)) || !isfinite(total)) {
@@ -322,6 +344,63 @@ __global__ void __launch_bounds__(kTlElemThreads)
       }
     }
   }
+}
+
+template <typename T, int P, int MODE>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ binv,
+                int dim, const __grid_constant__ TlHat<T, P> h, CgState<T>* st, ReduceScratch red) {
+  if (MODE == 1 && *(volatile int*)&st->done) return;
+  tl_finish_body<T, P, MODE>(r, z, x0, binv, dim, h, st, red, blockIdx.x, gridDim.x);
+}
+
+// ---- many instances (instance = blockIdx.y; element kernels per degree group) ----
+
+__device__ __forceinline__ bool tlb_skip(const TlInst& v) { return *(volatile const int*)&v.st->done != 0; }
+
+template <int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tlb_restrict_elem(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
+  const TlInst& v = insts[first + blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk || tlb_skip(v)) return;
+  tl_restrict_elem_body<float, P>(v.r, v.cp, (size_t)v.dim * v.dim, h, blockIdx.x, v.nblk);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_restrict_vert(const TlInst* __restrict__ insts) {
+  const TlInst& v = insts[blockIdx.y];
+  if (tlb_skip(v)) return;
+  tl_restrict_vert_body<float>(v.cp, v.lev[0].b, v.dim, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_presmooth(const TlInst* __restrict__ insts, int l) {
+  const TlInst& v = insts[blockIdx.y];
+  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  tl_presmooth_body<float>(v.lev[l], blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_restrict_resid(const TlInst* __restrict__ insts, int l) {
+  const TlInst& v = insts[blockIdx.y];
+  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  tl_restrict_resid_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_dense(const TlInst* __restrict__ insts) {
+  const TlInst& v = insts[blockIdx.y];
+  if (tlb_skip(v)) return;
+  tl_dense_body<float>(v.lev[v.nl - 1], v.ainv);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_post1(const TlInst* __restrict__ insts, int l) {
+  const TlInst& v = insts[blockIdx.y];
+  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  tl_post1_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(kTlVecThreads) k_tlb_post2(const TlInst* __restrict__ insts, int l) {
+  const TlInst& v = insts[blockIdx.y];
+  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  tl_post2_body<float>(v.lev[l], blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tlb_finish(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
+  const TlInst& v = insts[first + blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk || tlb_skip(v)) return;
+  tl_finish_body<float, P, 1>(v.r, v.z, v.lev[0].x, v.binv, v.dim, h, v.st, v.red, blockIdx.x, v.nblk);
 }
 
 // ---- host side ----
@@ -407,6 +486,26 @@ bool tl_invert(std::vector<double>& a, int n) {
   return true;
 }
 
+// Runs f(lo, hi) over [0, n) split across host threads when n is large (the
+// set-up of a large mesh's hierarchy is host work proportional to its
+// vertices); each row range is written by one thread, so results do not
+// depend on the split.
+template <typename F>
+void host_rows(int n, F f) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int nt = (n >= 256 && hw > 1) ? (int)std::min<unsigned>(hw, (unsigned)(n / 64)) : 1;
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t) {
+    const int lo = (int)((long long)n * t / nt), hi = (int)((long long)n * (t + 1) / nt);
+    th.emplace_back([=] { f(lo, hi); });
+  }
+  for (std::thread& t : th) t.join();
+}
+
 // Host 9-point stencil of one level: S[k * nv + v].
 struct HostLevel {
   int m = 0;
@@ -417,18 +516,20 @@ struct HostLevel {
 void host_stencil_apply(const HostLevel& L, const std::vector<double>& x, std::vector<double>& y) {
   const int n1 = L.m + 1, nv = n1 * n1;
   y.assign(nv, 0.0);
-  for (int vy = 0; vy <= L.m; ++vy)
-    for (int vx = 0; vx <= L.m; ++vx) {
-      const int v = vy * n1 + vx;
-      double s = 0.0;
-      for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int ux = vx + dx, uy = vy + dy;
-          if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
-          s += L.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + v] * x[uy * n1 + ux];
-        }
-      y[v] = s;
-    }
+  host_rows(n1, [&](int lo, int hi) {
+    for (int vy = lo; vy < hi; ++vy)
+      for (int vx = 0; vx <= L.m; ++vx) {
+        const int v = vy * n1 + vx;
+        double s = 0.0;
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int ux = vx + dx, uy = vy + dy;
+            if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
+            s += L.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + v] * x[uy * n1 + ux];
+          }
+        y[v] = s;
+      }
+  });
 }
 
 // the next level's stencil: P^T A P by probing with nine colours
@@ -437,36 +538,44 @@ HostLevel host_galerkin(const HostLevel& F) {
   C.m = (F.m + 1) / 2;
   const int cn1 = C.m + 1, cnv = cn1 * cn1, fn1 = F.m + 1, fnv = fn1 * fn1;
   C.S.assign((size_t)9 * cnv, 0.0);
-  std::vector<double> xc(cnv), xf(fnv), yf, yc(cnv);
+  std::vector<double> xc(cnv), xf(fnv), yf;
+  std::vector<std::vector<double>> ycs(9, std::vector<double>(cnv));
   for (int cy = 0; cy < 3; ++cy)
     for (int cx = 0; cx < 3; ++cx) {
+      std::vector<double>& yc = ycs[cy * 3 + cx];
       for (int v = 0; v < cnv; ++v) xc[v] = ((v % cn1) % 3 == cx && (v / cn1) % 3 == cy) ? 1.0 : 0.0;
-      for (int iy = 0; iy <= F.m; ++iy)  // P
-        for (int ix = 0; ix <= F.m; ++ix) {
-          double s = 0.0;
-          for (int I = std::max(0, (iy - 1) / 2); I <= std::min(C.m, (iy + 1) / 2 + 1); ++I)
-            for (int J = std::max(0, (ix - 1) / 2); J <= std::min(C.m, (ix + 1) / 2 + 1); ++J)
-              s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * xc[I * cn1 + J];
-          xf[iy * fn1 + ix] = s;
-        }
+      host_rows(fn1, [&](int lo, int hi) {  // P
+        for (int iy = lo; iy < hi; ++iy)
+          for (int ix = 0; ix <= F.m; ++ix) {
+            double s = 0.0;
+            for (int I = std::max(0, (iy - 1) / 2); I <= std::min(C.m, (iy + 1) / 2 + 1); ++I)
+              for (int J = std::max(0, (ix - 1) / 2); J <= std::min(C.m, (ix + 1) / 2 + 1); ++J)
+                s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * xc[I * cn1 + J];
+            xf[iy * fn1 + ix] = s;
+          }
+      });
       host_stencil_apply(F, xf, yf);
-      for (int I = 0; I <= C.m; ++I)  // P^T
-        for (int J = 0; J <= C.m; ++J) {
-          double s = 0.0;
-          for (int iy = std::max(0, 2 * I - 1); iy <= std::min(F.m, 2 * I + 1); ++iy)
-            for (int ix = std::max(0, 2 * J - 1); ix <= std::min(F.m, 2 * J + 1); ++ix)
-              s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * yf[iy * fn1 + ix];
-          yc[I * cn1 + J] = s;
-        }
-      for (int I = 0; I <= C.m; ++I)
-        for (int J = 0; J <= C.m; ++J)
-          for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-              const int ux = J + dx, uy = I + dy;
-              if (ux < 0 || uy < 0 || ux > C.m || uy > C.m || ux % 3 != cx || uy % 3 != cy) continue;
-              C.S[(size_t)((dy + 1) * 3 + (dx + 1)) * cnv + I * cn1 + J] = yc[I * cn1 + J];
-            }
+      host_rows(cn1, [&](int lo, int hi) {  // P^T
+        for (int I = lo; I < hi; ++I)
+          for (int J = 0; J <= C.m; ++J) {
+            double s = 0.0;
+            for (int iy = std::max(0, 2 * I - 1); iy <= std::min(F.m, 2 * I + 1); ++iy)
+              for (int ix = std::max(0, 2 * J - 1); ix <= std::min(F.m, 2 * J + 1); ++ix)
+                s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * yf[iy * fn1 + ix];
+            yc[I * cn1 + J] = s;
+          }
+      });
     }
+  host_rows(cn1, [&](int lo, int hi) {  // entry (v, u) is probe colour(u)'s result at v
+    for (int I = lo; I < hi; ++I)
+      for (int J = 0; J <= C.m; ++J)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int ux = J + dx, uy = I + dy;
+            if (ux < 0 || uy < 0 || ux > C.m || uy > C.m) continue;
+            C.S[(size_t)((dy + 1) * 3 + (dx + 1)) * cnv + I * cn1 + J] = ycs[(uy % 3) * 3 + ux % 3][I * cn1 + J];
+          }
+  });
   return C;
 }
 
@@ -581,7 +690,8 @@ sipg_status build_level0(sipg_op* op, HostLevel& L0) {
   if (e == cudaSuccess) e = cudaMalloc(&xd, n * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&yd, n * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&cp, 4 * noe * sizeof(double));
-  std::vector<double> hx(nv), hy(nv);
+  std::vector<double> hx(nv);
+  std::vector<std::vector<double>> hys(9, std::vector<double>(nv));
   sipg_status st = SIPG_OK;
   for (int c = 0; c < 9 && e == cudaSuccess && st == SIPG_OK; ++c) {
     const int cx = c % 3, cy = c / 3;
@@ -596,17 +706,21 @@ sipg_status build_level0(sipg_op* op, HostLevel& L0) {
     k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads>>>(cp, yv, dim, nullptr);
     count_launch(2);
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(hy.data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hys[c].data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) break;
-    for (int vy = 0; vy <= dim; ++vy)
-      for (int vx = 0; vx <= dim; ++vx)
-        for (int dy = -1; dy <= 1; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int ux = vx + dx, uy = vy + dy;
-            if (ux < 0 || uy < 0 || ux > dim || uy > dim || ux % 3 != cx || uy % 3 != cy) continue;
-            L0.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + vy * n1 + vx] = hy[vy * n1 + vx];
-          }
   }
+  if (e == cudaSuccess && st == SIPG_OK)  // entry (v, u) is probe colour(u)'s result at v
+    host_rows(n1, [&](int lo, int hi) {
+      for (int vy = lo; vy < hi; ++vy)
+        for (int vx = 0; vx <= dim; ++vx)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int ux = vx + dx, uy = vy + dy;
+              if (ux < 0 || uy < 0 || ux > dim || uy > dim) continue;
+              L0.S[(size_t)((dy + 1) * 3 + (dx + 1)) * nv + vy * n1 + vx] =
+                  hys[(uy % 3) * 3 + ux % 3][vy * n1 + vx];
+            }
+    });
   cudaFree(xv);
   cudaFree(yv);
   cudaFree(xd);
@@ -635,6 +749,10 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
   st = build_level0(op, H[0]);
   if (st != SIPG_OK) return st;
   while (H.back().m > kTlCoarsestCells) {
+    if ((int)H.size() >= kTlMaxLevels) {
+      set_error("two-level preconditioner: mesh too large for the vertex-grid hierarchy");
+      return SIPG_ERR_UNSUPPORTED;
+    }
     H.back().omega = host_omega(H.back());
     H.push_back(host_galerkin(H.back()));
   }
@@ -739,6 +857,129 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
 // Levels of the vertex hierarchy (for reports), 0 if not built.
 int twolevel_levels(const void* handle) {
   return handle ? (int)static_cast<const TwoLevel*>(handle)->lev.size() : 0;
+}
+
+// ---- many instances ----
+
+namespace {
+size_t round16(size_t n) { return (n + 3) & ~size_t(3); }  // floats, to a 16-byte multiple
+}  // namespace
+
+size_t twolevel_scratch_floats_for(int dim) {
+  size_t n = round16(4 * (size_t)dim * dim);
+  for (int m = dim;; m = (m + 1) / 2) {
+    n += 3 * round16((size_t)(m + 1) * (m + 1));
+    if (m <= kTlCoarsestCells) break;
+  }
+  return n;
+}
+
+size_t twolevel_scratch_floats(const void* handle) {
+  const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
+  size_t n = round16(4 * (size_t)tl.dim * tl.dim);
+  for (const TlLev<float>& L : tl.lev) n += 3 * round16((size_t)(L.m + 1) * (L.m + 1));
+  return n;
+}
+
+TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* z, CgState<float>* st,
+                     const ReduceScratch& red) {
+  const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
+  TlInst v{};
+  v.r = r;
+  v.z = z;
+  v.binv = tl.binv;
+  v.ainv = tl.ainv;
+  v.st = st;
+  v.red = red;
+  v.dim = tl.dim;
+  v.p = tl.p;
+  v.nl = (int)tl.lev.size();
+  v.nblk = tl_grid((size_t)tl.dim * tl.dim, kTlElemThreads, red.capacity);
+  float* q = scratch;
+  v.cp = q;
+  q += round16(4 * (size_t)tl.dim * tl.dim);
+  for (int l = 0; l < v.nl; ++l) {
+    const size_t nv = round16((size_t)(tl.lev[l].m + 1) * (tl.lev[l].m + 1));
+    v.lev[l] = tl.lev[l];  // m, S, wd shared with the op
+    v.lev[l].b = q;
+    v.lev[l].x = q + nv;
+    v.lev[l].y = q + 2 * nv;
+    q += 3 * nv;
+  }
+  return v;
+}
+
+TlPlan twolevel_plan(const TlInst* h, const HostTables* const* tabs, int n) {
+  TlPlan plan;
+  plan.n = n;
+  for (int i = 0; i < n; ++i) {
+    plan.maxl = std::max(plan.maxl, h[i].nl);
+    plan.nblk_max = std::max(plan.nblk_max, h[i].nblk);
+    if ((int)plan.nv_max.size() < h[i].nl) plan.nv_max.resize(h[i].nl, 0);
+    for (int l = 0; l < h[i].nl; ++l)
+      plan.nv_max[l] = std::max(plan.nv_max[l], (h[i].lev[l].m + 1) * (h[i].lev[l].m + 1));
+    if (plan.groups.empty() || plan.groups.back().p != h[i].p) plan.groups.push_back({h[i].p, i, 0, 0, tabs[i]});
+    TlPlan::Group& g = plan.groups.back();
+    g.count += 1;
+    g.nblk_max = std::max(g.nblk_max, h[i].nblk);
+  }
+  return plan;
+}
+
+template <int P>
+void tlb_elem_launch(int which, const TlInst* d, const TlPlan::Group& g, cudaStream_t s) {
+  const dim3 grid(g.nblk_max, g.count);
+  if (which == 0)
+    k_tlb_restrict_elem<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
+  else
+    k_tlb_finish<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
+}
+
+sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
+  if (plan.n == 0) return SIPG_OK;
+  const int n = plan.n;
+  for (const TlPlan::Group& g : plan.groups) {
+    switch (g.p) {
+      case 1: tlb_elem_launch<1>(0, d, g, s); break;
+      case 2: tlb_elem_launch<2>(0, d, g, s); break;
+      case 3: tlb_elem_launch<3>(0, d, g, s); break;
+      case 4: tlb_elem_launch<4>(0, d, g, s); break;
+      case 5: tlb_elem_launch<5>(0, d, g, s); break;
+      case 6: tlb_elem_launch<6>(0, d, g, s); break;
+      case 7: tlb_elem_launch<7>(0, d, g, s); break;
+      case 8: tlb_elem_launch<8>(0, d, g, s); break;
+    }
+  }
+  auto vgrid = [&](int l) { return dim3(tl_grid((size_t)plan.nv_max[l], kTlVecThreads, 1 << 30), n); };
+  k_tlb_restrict_vert<<<vgrid(0), kTlVecThreads, 0, s>>>(d);
+  count_launch(plan.groups.size() + 1);
+  for (int l = 0; l + 1 < plan.maxl; ++l) {
+    k_tlb_presmooth<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
+    k_tlb_restrict_resid<<<vgrid(l + 1), kTlVecThreads, 0, s>>>(d, l);
+    count_launch(2);
+  }
+  k_tlb_dense<<<dim3(1, n), kTlVecThreads, 0, s>>>(d);
+  count_launch();
+  for (int l = plan.maxl - 2; l >= 0; --l) {
+    k_tlb_post1<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
+    k_tlb_post2<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
+    count_launch(2);
+  }
+  for (const TlPlan::Group& g : plan.groups) {
+    switch (g.p) {
+      case 1: tlb_elem_launch<1>(1, d, g, s); break;
+      case 2: tlb_elem_launch<2>(1, d, g, s); break;
+      case 3: tlb_elem_launch<3>(1, d, g, s); break;
+      case 4: tlb_elem_launch<4>(1, d, g, s); break;
+      case 5: tlb_elem_launch<5>(1, d, g, s); break;
+      case 6: tlb_elem_launch<6>(1, d, g, s); break;
+      case 7: tlb_elem_launch<7>(1, d, g, s); break;
+      case 8: tlb_elem_launch<8>(1, d, g, s); break;
+    }
+  }
+  count_launch(plan.groups.size());
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
 }
 
 }  // namespace sipg

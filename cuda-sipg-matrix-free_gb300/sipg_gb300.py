@@ -116,6 +116,7 @@ _SIGS = {
     "sipg_volume_mvm_f64": (C.c_int, [C.c_int, C.c_int, _VP, C.c_int, _VP, _VP, _VP]),
     "sipg_solve_mixed": (C.c_int, [_VP, _VP, _VP, C.POINTER(MixedOpts), C.POINTER(MixedResult), _VP]),
     "sipg_apply_twolevel_f32": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "sipg_residual_f64": (C.c_int, [_VP, _VP, _VP, _VP, C.POINTER(C.c_double), _VP]),
     "sipg_rhs_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP]),
     "sipg_err_norms_f64": (C.c_int, [_VP, C.c_int, C.POINTER(Modes), _VP, _VP, _VP]),
     "sipg_last_error": (C.c_char_p, []),
@@ -428,6 +429,18 @@ class Operator:
         if st not in (0, 3, 4):
             _check(st, "solve_mixed")
         return st, res
+
+    def true_residual(self, x, b, stream=None):
+        """||b - A x|| / ||b|| evaluated in FP64 with the operator's zero-sum
+        contractions over differences (sipg_residual_f64)."""
+        import torch
+
+        self._vec(x, torch.float64)
+        self._vec(b, torch.float64)
+        rel = C.c_double()
+        _check(lib().sipg_residual_f64(self._h, _ptr(x), _ptr(b), None, C.byref(rel), _stream(stream)),
+               "true_residual")
+        return rel.value
 
     def apply_twolevel(self, r, out=None, stream=None):
         """out = M r, the two-level preconditioner of the flexible mixed solve
