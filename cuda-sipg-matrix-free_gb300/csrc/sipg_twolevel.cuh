@@ -19,8 +19,8 @@ struct TlLev {
   const T* S;   // stencil planes [9][nv], entry k = (dy + 1) * 3 + (dx + 1)
   const T* wd;  // omega / diagonal
   T* b;         // right-hand side
-  T* x;         // V-cycle iterate (the result)
-  T* y;         // second buffer of the smoothing sweeps
+  T* x;         // pre-smoothed iterate
+  T* y;         // V-cycle result
 };
 
 // One problem's preconditioner operands: z = M r with its own scratch (the
@@ -29,7 +29,7 @@ struct TlInst {
   const float* r;
   float* z;
   float* cp;           // [4][noe] corner sums
-  const float* binv;   // [16][nn][nn] element block inverses
+  const float* fdm;    // [16][3][nn] element block factors (fast diagonalisation)
   const float* ainv;   // the coarsest level's dense inverse
   CgState<float>* st;  // the inner PCG state (r.z and beta are set here)
   ReduceScratch red;
@@ -44,7 +44,7 @@ struct TlPlan {
   int n = 0;
   int maxl = 0;
   int nblk_max = 0;
-  std::vector<int> nv_max;  // per level: the largest vertex count
+  std::vector<int> side_max;  // per level: the largest vertices per side
   struct Group {
     int p, first, count, nblk_max;
     const HostTables* tab;

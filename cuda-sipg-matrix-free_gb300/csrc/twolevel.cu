@@ -125,31 +125,31 @@ __global__ void __launch_bounds__(kTlElemThreads)
   tl_restrict_elem_body<T, P>(r, cp, noe, h, blockIdx.x, gridDim.x);
 }
 
-// b0 at vertex v = (vx, vy): the corner sums of the elements around it, in a fixed order
+// b0 at vertex (vx, vy): the corner sums of the elements around it, in a fixed order
 template <typename T>
-__device__ __forceinline__ void tl_restrict_vert_body(const T* __restrict__ cp, T* __restrict__ b0, int dim, int v) {
-  const int n1 = dim + 1;
-  if (v >= n1 * n1) return;
-  const int vx = v % n1, vy = v / n1;
+__device__ __forceinline__ T tl_corner_sum(const T* __restrict__ cp, int dim, int vx, int vy) {
   const size_t noe = (size_t)dim * dim;
   T acc = T(0);
+#pragma unroll
   for (int R = vy - 1; R <= vy; ++R) {  // element rows counted bottom-up
     if (R < 0 || R >= dim) continue;
+#pragma unroll
     for (int col = vx - 1; col <= vx; ++col) {
       if (col < 0 || col >= dim) continue;
       const size_t e = (size_t)(dim - 1 - R) * dim + col;
       const int a = vx - col, b = vy - R;
-      acc += cp[(size_t)(a * 2 + b) * noe + e];
+      acc += __ldg(cp + (size_t)(a * 2 + b) * noe + e);
     }
   }
-  b0[v] = acc;
+  return acc;
 }
 
+// b0 = the vertex sums of the corner sums (used by the set-up's probing)
 template <typename T>
 __global__ void __launch_bounds__(kTlVecThreads)
-    k_tl_restrict_vert(const T* __restrict__ cp, T* __restrict__ b0, int dim, const int* done) {
-  if (tl_done(done)) return;
-  tl_restrict_vert_body<T>(cp, b0, dim, blockIdx.x * blockDim.x + threadIdx.x);
+    k_tl_restrict_vert(const T* __restrict__ cp, T* __restrict__ b0, int dim) {
+  const int n1 = dim + 1, v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n1 * n1) b0[v] = tl_corner_sum(cp, dim, v % n1, v / n1);
 }
 
 // out = P xv: the Q1 function of vertex values xv at every element's nodes
@@ -172,50 +172,103 @@ __global__ void __launch_bounds__(kTlElemThreads)
 }
 
 // ---- the V-cycle on the vertex grid ----
+//
+// Per level: b the right-hand side, x the pre-smoothed iterate, y the
+// V-cycle result.  The vertex kernels are latency bound (a level-0 grid of
+// (dim + 1)^2 vertices is a few MB), so each level takes one fused kernel on
+// the way down and one on the way up, each block working on a square tile of
+// vertices through shared-memory windows that hold zero outside the level.
 
-// two damped-Jacobi sweeps from zero: x1 = wd b, x = x1 + wd (b - A x1)
-template <typename T>
-__device__ __forceinline__ void tl_presmooth_body(const TlLev<T>& L, int v) {
-  const int n1 = L.m + 1, nv = n1 * n1;
-  if (v >= nv) return;
-  const int vx = v % n1, vy = v / n1;
+constexpr int kTlDown = 16;          // coarse vertices per side of a down tile
+constexpr int kTlUp = 32;            // fine vertices per side of an up tile
+constexpr int kTlTileThreads = 256;  // threads of the tile kernels
+
+// The level's 9-point stencil at vertex (ix, iy) applied to a window w
+// (row stride W) whose entry [ly][lx] holds vertex (ix - 1 + lx, iy - 1 + ly)
+// of the 3 x 3 patch around it: the caller passes w = &win[cy - 1][cx - 1].
+template <typename T, int W>
+__device__ __forceinline__ T tl_stencil_win(const TlLev<T>& L, const T (*w)[W], int v, int nv) {
   T s = T(0);
 #pragma unroll
-  for (int dy = -1; dy <= 1; ++dy)
+  for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx) s = fma(__ldg(L.S + (size_t)(dy * 3 + dx) * nv + v), w[dy][dx], s);
+  return s;
+}
+
+// One down step for the 16 x 16 tile (tx, ty) of coarse vertices: on the
+// fine level F (with cp: b from the element corner sums, level 0)
+//   x1 = wd b,   x = x1 + wd (b - A x1)   (two damped-Jacobi sweeps from zero),
+// then C.b = P^T (b - A x).  The tile's fine footprint is [2 cx0 - 1,
+// 2 cx0 + 31]^2; x is needed one vertex beyond it, b and x1 two.  The block
+// writes x (and, from cp, b) at the fine vertices [2 cx0, 2 cx0 + 32)^2 it
+// owns; every fine vertex has exactly one owner.
+template <typename T>
+__device__ __forceinline__ void tl_down_body(const TlLev<T>& F, const TlLev<T>& C, const T* __restrict__ cp, int dim,
+                                             int tx, int ty) {
+  constexpr int W3 = 2 * kTlDown + 5, W2 = W3 - 2, W1 = W3 - 4;  // 37, 35, 33
+  __shared__ T sb[W3][W3], sx1[W3][W3], sx[W2][W2], sr[W1][W1];
+  const int m = F.m, n1 = m + 1, nv = n1 * n1;
+  const int cx0 = tx * kTlDown, cy0 = ty * kTlDown;
+  const int ox = 2 * cx0 - 3, oy = 2 * cy0 - 3;  // fine vertex of window entry [0][0] of sb
+  auto owned = [&](int ix, int iy) { return ix >= 2 * cx0 && ix < 2 * cx0 + 2 * kTlDown && iy >= 2 * cy0 && iy < 2 * cy0 + 2 * kTlDown; };
+  auto inside = [&](int ix, int iy) { return ix >= 0 && iy >= 0 && ix <= m && iy <= m; };
+  for (int i = threadIdx.x; i < W3 * W3; i += kTlTileThreads) {
+    const int ly = i / W3, lx = i - ly * W3, ix = ox + lx, iy = oy + ly;
+    T b = T(0), x1 = T(0);
+    if (inside(ix, iy)) {
+      const int v = iy * n1 + ix;
+      if (cp) {
+        b = tl_corner_sum(cp, dim, ix, iy);
+        if (owned(ix, iy)) F.b[v] = b;
+      } else {
+        b = F.b[v];
+      }
+      x1 = F.wd[v] * b;
+    }
+    sb[ly][lx] = b;
+    sx1[ly][lx] = x1;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W2 * W2; i += kTlTileThreads) {
+    const int ly = i / W2, lx = i - ly * W2, ix = ox + 1 + lx, iy = oy + 1 + ly;
+    T x = T(0);
+    if (inside(ix, iy)) {
+      const int v = iy * n1 + ix;
+      x = fma(F.wd[v], sb[ly + 1][lx + 1] - tl_stencil_win<T, W3>(F, (const T(*)[W3]) & sx1[ly][lx], v, nv),
+              sx1[ly + 1][lx + 1]);
+      if (owned(ix, iy)) F.x[v] = x;
+    }
+    sx[ly][lx] = x;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W1 * W1; i += kTlTileThreads) {
+    const int ly = i / W1, lx = i - ly * W1, ix = ox + 2 + lx, iy = oy + 2 + ly;
+    T res = T(0);
+    if (inside(ix, iy))
+      res = sb[ly + 2][lx + 2] - tl_stencil_win<T, W2>(F, (const T(*)[W2]) & sx[ly][lx], iy * n1 + ix, nv);
+    sr[ly][lx] = res;
+  }
+  __syncthreads();
+  const int J = cx0 + (int)threadIdx.x % kTlDown, I = cy0 + (int)threadIdx.x / kTlDown;
+  if (J > C.m || I > C.m) return;
+  T acc = T(0);
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy) {
+    const int iy = 2 * I + dy;
+    if (iy < 0 || iy > m) continue;
+    const T wy = tl_w<T>(iy, I, m);
 #pragma unroll
     for (int dx = -1; dx <= 1; ++dx) {
-      const int ux = vx + dx, uy = vy + dy;
-      if (ux < 0 || uy < 0 || ux > L.m || uy > L.m) continue;
-      const int u = uy * n1 + ux;
-      s = fma(L.S[((dy + 1) * 3 + (dx + 1)) * nv + v], L.wd[u] * L.b[u], s);
-    }
-  const T x1 = L.wd[v] * L.b[v];
-  L.x[v] = fma(L.wd[v], L.b[v] - s, x1);
-}
-
-// coarse right-hand side at coarse vertex v: C.b = P^T (F.b - A F.x)
-template <typename T>
-__device__ __forceinline__ void tl_restrict_resid_body(const TlLev<T>& F, const TlLev<T>& C, int v) {
-  const int cn1 = C.m + 1;
-  if (v >= cn1 * cn1) return;
-  const int J = v % cn1, I = v / cn1, fn1 = F.m + 1;
-  T acc = T(0);
-  for (int iy = 2 * I - 1; iy <= 2 * I + 1; ++iy) {
-    if (iy < 0 || iy > F.m) continue;
-    const T wy = tl_w<T>(iy, I, F.m);
-    if (wy == T(0)) continue;
-    for (int ix = 2 * J - 1; ix <= 2 * J + 1; ++ix) {
-      if (ix < 0 || ix > F.m) continue;
-      const T wx = tl_w<T>(ix, J, F.m);
-      if (wx == T(0)) continue;
-      const T res = F.b[iy * fn1 + ix] - tl_stencil(F, F.x, ix, iy);
-      acc = fma(wx * wy, res, acc);
+      const int ix = 2 * J + dx;
+      if (ix < 0 || ix > m) continue;
+      acc = fma(wy * tl_w<T>(ix, J, m), sr[iy - oy - 2][ix - ox - 2], acc);
     }
   }
-  C.b[v] = acc;
+  C.b[I * (C.m + 1) + J] = acc;
 }
 
-// the fine iterate plus the prolonged coarse correction, at vertex (ux, uy)
+// The pre-smoothed iterate plus the prolonged coarse result at fine vertex (ux, uy).
 template <typename T>
 __device__ __forceinline__ T tl_corrected(const TlLev<T>& F, const TlLev<T>& C, int ux, int uy) {
   const int cn1 = C.m + 1;
@@ -225,73 +278,76 @@ __device__ __forceinline__ T tl_corrected(const TlLev<T>& F, const TlLev<T>& C, 
   const int jy0 = py ? (uy + 1) / 2 : (uy - 1) / 2, jy1 = py ? jy0 : (uy + 1) / 2;
   const T wx = px ? T(1) : T(0.5), wy = py ? T(1) : T(0.5);
   if (px && py) {
-    c = C.x[jy0 * cn1 + jx0];
+    c = C.y[jy0 * cn1 + jx0];
   } else if (px) {
-    c = wy * (C.x[jy0 * cn1 + jx0] + C.x[jy1 * cn1 + jx0]);
+    c = wy * (C.y[jy0 * cn1 + jx0] + C.y[jy1 * cn1 + jx0]);
   } else if (py) {
-    c = wx * (C.x[jy0 * cn1 + jx0] + C.x[jy0 * cn1 + jx1]);
+    c = wx * (C.y[jy0 * cn1 + jx0] + C.y[jy0 * cn1 + jx1]);
   } else {
-    c = T(0.25) * ((C.x[jy0 * cn1 + jx0] + C.x[jy0 * cn1 + jx1]) + (C.x[jy1 * cn1 + jx0] + C.x[jy1 * cn1 + jx1]));
+    c = T(0.25) * ((C.y[jy0 * cn1 + jx0] + C.y[jy0 * cn1 + jx1]) + (C.y[jy1 * cn1 + jx0] + C.y[jy1 * cn1 + jx1]));
   }
   return F.x[uy * (F.m + 1) + ux] + c;
 }
 
-// first post-sweep on x + P C.x: y = xc + wd (b - A xc)
+// One up step for the 32 x 32 tile (tx, ty) of fine vertices: with
+// xc = x + P C.y, two damped-Jacobi sweeps
+//   y1 = xc + wd (b - A xc),   F.y = y1 + wd (b - A y1).
 template <typename T>
-__device__ __forceinline__ void tl_post1_body(const TlLev<T>& F, const TlLev<T>& C, int v) {
-  const int n1 = F.m + 1, nv = n1 * n1;
-  if (v >= nv) return;
-  const int vx = v % n1, vy = v / n1;
-  T s = T(0);
-#pragma unroll
-  for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-    for (int dx = -1; dx <= 1; ++dx) {
-      const int ux = vx + dx, uy = vy + dy;
-      if (ux < 0 || uy < 0 || ux > F.m || uy > F.m) continue;
-      s = fma(F.S[((dy + 1) * 3 + (dx + 1)) * nv + v], tl_corrected(F, C, ux, uy), s);
+__device__ __forceinline__ void tl_up_body(const TlLev<T>& F, const TlLev<T>& C, int tx, int ty) {
+  constexpr int W2 = kTlUp + 4, W1 = kTlUp + 2;  // 36, 34
+  __shared__ T sxc[W2][W2], sy[W1][W1];
+  const int m = F.m, n1 = m + 1, nv = n1 * n1;
+  const int fx0 = tx * kTlUp, fy0 = ty * kTlUp;
+  const int ox = fx0 - 2, oy = fy0 - 2;  // fine vertex of window entry [0][0] of sxc
+  auto inside = [&](int ix, int iy) { return ix >= 0 && iy >= 0 && ix <= m && iy <= m; };
+  for (int i = threadIdx.x; i < W2 * W2; i += kTlTileThreads) {
+    const int ly = i / W2, lx = i - ly * W2, ix = ox + lx, iy = oy + ly;
+    sxc[ly][lx] = inside(ix, iy) ? tl_corrected(F, C, ix, iy) : T(0);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W1 * W1; i += kTlTileThreads) {
+    const int ly = i / W1, lx = i - ly * W1, ix = ox + 1 + lx, iy = oy + 1 + ly;
+    T y = T(0);
+    if (inside(ix, iy)) {
+      const int v = iy * n1 + ix;
+      y = fma(F.wd[v], F.b[v] - tl_stencil_win<T, W2>(F, (const T(*)[W2]) & sxc[ly][lx], v, nv), sxc[ly + 1][lx + 1]);
     }
-  F.y[v] = fma(F.wd[v], F.b[v] - s, tl_corrected(F, C, vx, vy));
+    sy[ly][lx] = y;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kTlUp * kTlUp; i += kTlTileThreads) {
+    const int ly = i / kTlUp, lx = i - ly * kTlUp, ix = fx0 + lx, iy = fy0 + ly;
+    if (!inside(ix, iy)) continue;
+    const int v = iy * n1 + ix;
+    F.y[v] = fma(F.wd[v], F.b[v] - tl_stencil_win<T, W1>(F, (const T(*)[W1]) & sy[ly][lx], v, nv), sy[ly + 1][lx + 1]);
+  }
 }
 
-// second post-sweep: x = y + wd (b - A y)
-template <typename T>
-__device__ __forceinline__ void tl_post2_body(const TlLev<T>& L, int v) {
-  const int n1 = L.m + 1, nv = n1 * n1;
-  if (v >= nv) return;
-  L.x[v] = fma(L.wd[v], L.b[v] - tl_stencil(L, L.y, v % n1, v / n1), L.y[v]);
-}
-
-// coarsest level: x = A^-1 b (dense, one block)
+// coarsest level: y = A^-1 b (dense, one block)
 template <typename T>
 __device__ __forceinline__ void tl_dense_body(const TlLev<T>& L, const T* __restrict__ ainv) {
   const int nv = (L.m + 1) * (L.m + 1);
   for (int v = threadIdx.x; v < nv; v += blockDim.x) {
     T s = T(0);
     for (int u = 0; u < nv; ++u) s = fma(ainv[v * nv + u], L.b[u], s);
-    L.x[v] = s;
+    L.y[v] = s;
   }
 }
 
+__host__ __device__ inline int tl_tiles(int verts, int tile) { return (verts + tile - 1) / tile; }
+
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_presmooth(TlLev<T> L, const int* done) {
+__global__ void __launch_bounds__(kTlTileThreads)
+    k_tl_down(TlLev<T> F, TlLev<T> C, const T* __restrict__ cp, int dim, const int* done) {
   if (tl_done(done)) return;
-  tl_presmooth_body<T>(L, blockIdx.x * blockDim.x + threadIdx.x);
+  const int t = tl_tiles(C.m + 1, kTlDown);
+  tl_down_body<T>(F, C, cp, dim, blockIdx.x % t, blockIdx.x / t);
 }
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_restrict_resid(TlLev<T> F, TlLev<T> C, const int* done) {
+__global__ void __launch_bounds__(kTlTileThreads) k_tl_up(TlLev<T> F, TlLev<T> C, const int* done) {
   if (tl_done(done)) return;
-  tl_restrict_resid_body<T>(F, C, blockIdx.x * blockDim.x + threadIdx.x);
-}
-template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_post1(TlLev<T> F, TlLev<T> C, const int* done) {
-  if (tl_done(done)) return;
-  tl_post1_body<T>(F, C, blockIdx.x * blockDim.x + threadIdx.x);
-}
-template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_post2(TlLev<T> L, const int* done) {
-  if (tl_done(done)) return;
-  tl_post2_body<T>(L, blockIdx.x * blockDim.x + threadIdx.x);
+  const int t = tl_tiles(F.m + 1, kTlUp);
+  tl_up_body<T>(F, C, blockIdx.x % t, blockIdx.x / t);
 }
 template <typename T>
 __global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const int* done) {
@@ -299,12 +355,24 @@ __global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T*
   tl_dense_body<T>(L, ainv);
 }
 
-// z = B^-1 r + P x0 (x0: the level-0 V-cycle result).  MODE 1: also r.z and
-// the PCG bookkeeping of the inner state (first: rr = r.z; else beta =
-// r.z / rr, rr = r.z), reduced over the nb blocks of this instance.
+// The Q1 function of the element's corner values at node (i1, i2).
+template <typename T, int P>
+__device__ __forceinline__ T tl_q1(const TlHat<T, P>& h, int i1, int i2, T x00, T x01, T x10, T x11) {
+  return h.l[0][i1] * (h.l[0][i2] * x00 + h.l[1][i2] * x01) + h.l[1][i1] * (h.l[0][i2] * x10 + h.l[1][i2] * x11);
+}
+
+// z = B^-1 r + P x0 (x0: the level-0 V-cycle result), B^-1 by fast
+// diagonalisation.  With R[i1][i2] the element's residual (node i1 N1 + i2)
+// and its type's factors V_x, V_y, D^-1 (fdm: [V_x | V_y | D^-1] per type),
+//   B^-1 r = V_x (D^-1 o U) V_y^T,   U = V_x^T R V_y,
+// four 1-D transforms of N1^3 multiply-adds each, done in place on the
+// element's column of shared memory with the 1-D factor in registers.
+// MODE 1: also r.z = sum D^-1 o U o U + r.(P x0) and the PCG bookkeeping of
+// the inner state (first: rr = r.z; else beta = r.z / rr, rr = r.z), reduced
+// over the nb blocks of this instance.
 template <typename T, int P, int MODE>
 __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0,
-                                               const T* __restrict__ binv, int dim, const TlHat<T, P>& h,
+                                               const T* __restrict__ fdm, int dim, const TlHat<T, P>& h,
                                                CgState<T>* st, const ReduceScratch& red, int bid, int nb) {
   constexpr int N1 = P + 1, NN = N1 * N1;
   __shared__ T col[NN][kTlElemThreads];
@@ -316,20 +384,73 @@ __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __res
   for (size_t tile = bid; tile < tiles; tile += nb) {
     const size_t e = tile * kTlElemThreads + t;
     if (e >= noe) continue;
-#pragma unroll
-    for (int k = 0; k < NN; ++k) col[k][t] = __ldg(r + (size_t)k * noe + e);
     const int row = (int)(e / dim), cl = (int)(e % dim), R = dim - 1 - row;
-    const T* __restrict__ B = binv + (size_t)tl_elem_type(row, cl, dim) * NN * NN;
     const T x00 = x0[R * (dim + 1) + cl], x10 = x0[R * (dim + 1) + cl + 1];
     const T x01 = x0[(R + 1) * (dim + 1) + cl], x11 = x0[(R + 1) * (dim + 1) + cl + 1];
-#pragma unroll 1
-    for (int k = 0; k < NN; ++k) {
-      const int i1 = k / N1, i2 = k - i1 * N1;
-      T v = h.l[0][i1] * (h.l[0][i2] * x00 + h.l[1][i2] * x01) + h.l[1][i1] * (h.l[0][i2] * x10 + h.l[1][i2] * x11);
+    const T* __restrict__ F = fdm + (size_t)tl_elem_type(row, cl, dim) * 3 * NN;
+    T f[NN], c[N1];
 #pragma unroll
-      for (int j = 0; j < NN; ++j) v = fma(__ldg(B + k * NN + j), col[j][t], v);
-      z[(size_t)k * noe + e] = v;
-      if (MODE == 1) acc = fma(v, col[k][t], acc);
+    for (int k = 0; k < NN; ++k) col[k][t] = __ldg(r + (size_t)k * noe + e);
+    if (MODE == 1) {
+#pragma unroll 1
+      for (int i1 = 0; i1 < N1; ++i1)
+#pragma unroll
+        for (int i2 = 0; i2 < N1; ++i2) acc = fma(col[i1 * N1 + i2][t], tl_q1<T, P>(h, i1, i2, x00, x01, x10, x11), acc);
+    }
+#pragma unroll
+    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + k);  // V_x
+    // U1 = V_x^T R (along i1)
+#pragma unroll 1
+    for (int i2 = 0; i2 < N1; ++i2) {
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) c[i1] = col[i1 * N1 + i2][t];
+#pragma unroll
+      for (int a = 0; a < N1; ++a) {
+        T s = T(0);
+#pragma unroll
+        for (int i1 = 0; i1 < N1; ++i1) s = fma(f[i1 * N1 + a], c[i1], s);
+        col[a * N1 + i2][t] = s;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + NN + k);  // V_y
+    // D^-1 o (U1 V_y), then its product with V_y^T (along i2)
+#pragma unroll 1
+    for (int a = 0; a < N1; ++a) {
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2) c[i2] = col[a * N1 + i2][t];
+      T u[N1];
+#pragma unroll
+      for (int b = 0; b < N1; ++b) {
+        T s = T(0);
+#pragma unroll
+        for (int i2 = 0; i2 < N1; ++i2) s = fma(f[i2 * N1 + b], c[i2], s);
+        const T d = __ldg(F + 2 * NN + a * N1 + b);
+        if (MODE == 1) acc = fma(s * s, d, acc);
+        u[b] = s * d;
+      }
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2) {
+        T s = T(0);
+#pragma unroll
+        for (int b = 0; b < N1; ++b) s = fma(f[i2 * N1 + b], u[b], s);
+        col[a * N1 + i2][t] = s;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + k);  // V_x
+    // z = V_x (...) + P x0 (along i1)
+#pragma unroll 1
+    for (int i2 = 0; i2 < N1; ++i2) {
+#pragma unroll
+      for (int a = 0; a < N1; ++a) c[a] = col[a * N1 + i2][t];
+#pragma unroll
+      for (int i1 = 0; i1 < N1; ++i1) {
+        T s = tl_q1<T, P>(h, i1, i2, x00, x01, x10, x11);
+#pragma unroll
+        for (int a = 0; a < N1; ++a) s = fma(f[i1 * N1 + a], c[a], s);
+        z[(size_t)(i1 * N1 + i2) * noe + e] = s;
+      }
     }
   }
   if (MODE == 1) {
@@ -348,10 +469,10 @@ __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __res
 
 template <typename T, int P, int MODE>
 __global__ void __launch_bounds__(kTlElemThreads)
-    k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ binv,
+    k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ fdm,
                 int dim, const __grid_constant__ TlHat<T, P> h, CgState<T>* st, ReduceScratch red) {
   if (MODE == 1 && *(volatile int*)&st->done) return;
-  tl_finish_body<T, P, MODE>(r, z, x0, binv, dim, h, st, red, blockIdx.x, gridDim.x);
+  tl_finish_body<T, P, MODE>(r, z, x0, fdm, dim, h, st, red, blockIdx.x, gridDim.x);
 }
 
 // ---- many instances (instance = blockIdx.y; element kernels per degree group) ----
@@ -365,42 +486,32 @@ __global__ void __launch_bounds__(kTlElemThreads)
   if ((int)blockIdx.x >= v.nblk || tlb_skip(v)) return;
   tl_restrict_elem_body<float, P>(v.r, v.cp, (size_t)v.dim * v.dim, h, blockIdx.x, v.nblk);
 }
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_restrict_vert(const TlInst* __restrict__ insts) {
-  const TlInst& v = insts[blockIdx.y];
-  if (tlb_skip(v)) return;
-  tl_restrict_vert_body<float>(v.cp, v.lev[0].b, v.dim, blockIdx.x * blockDim.x + threadIdx.x);
-}
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_presmooth(const TlInst* __restrict__ insts, int l) {
+// level l -> l + 1 of every instance that has level l + 1 (grid.x: the largest tile count)
+__global__ void __launch_bounds__(kTlTileThreads) k_tlb_down(const TlInst* __restrict__ insts, int l) {
   const TlInst& v = insts[blockIdx.y];
   if (l + 1 >= v.nl || tlb_skip(v)) return;
-  tl_presmooth_body<float>(v.lev[l], blockIdx.x * blockDim.x + threadIdx.x);
-}
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_restrict_resid(const TlInst* __restrict__ insts, int l) {
-  const TlInst& v = insts[blockIdx.y];
-  if (l + 1 >= v.nl || tlb_skip(v)) return;
-  tl_restrict_resid_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x * blockDim.x + threadIdx.x);
+  const int t = tl_tiles(v.lev[l + 1].m + 1, kTlDown);
+  if ((int)blockIdx.x >= t * t) return;
+  tl_down_body<float>(v.lev[l], v.lev[l + 1], l == 0 ? v.cp : nullptr, v.dim, blockIdx.x % t, blockIdx.x / t);
 }
 __global__ void __launch_bounds__(kTlVecThreads) k_tlb_dense(const TlInst* __restrict__ insts) {
   const TlInst& v = insts[blockIdx.y];
   if (tlb_skip(v)) return;
   tl_dense_body<float>(v.lev[v.nl - 1], v.ainv);
 }
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_post1(const TlInst* __restrict__ insts, int l) {
+__global__ void __launch_bounds__(kTlTileThreads) k_tlb_up(const TlInst* __restrict__ insts, int l) {
   const TlInst& v = insts[blockIdx.y];
   if (l + 1 >= v.nl || tlb_skip(v)) return;
-  tl_post1_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x * blockDim.x + threadIdx.x);
-}
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_post2(const TlInst* __restrict__ insts, int l) {
-  const TlInst& v = insts[blockIdx.y];
-  if (l + 1 >= v.nl || tlb_skip(v)) return;
-  tl_post2_body<float>(v.lev[l], blockIdx.x * blockDim.x + threadIdx.x);
+  const int t = tl_tiles(v.lev[l].m + 1, kTlUp);
+  if ((int)blockIdx.x >= t * t) return;
+  tl_up_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x % t, blockIdx.x / t);
 }
 template <int P>
 __global__ void __launch_bounds__(kTlElemThreads)
     k_tlb_finish(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
   const TlInst& v = insts[first + blockIdx.y];
   if ((int)blockIdx.x >= v.nblk || tlb_skip(v)) return;
-  tl_finish_body<float, P, 1>(v.r, v.z, v.lev[0].x, v.binv, v.dim, h, v.st, v.red, blockIdx.x, v.nblk);
+  tl_finish_body<float, P, 1>(v.r, v.z, v.lev[0].y, v.fdm, v.dim, h, v.st, v.red, blockIdx.x, v.nblk);
 }
 
 // ---- host side ----
@@ -442,14 +553,14 @@ void tl_launch_prolong(const HostTables& h, const T* xv, T* out, int dim, cudaSt
       xv, out, dim, tl_hat<T, P>(h));
 }
 template <typename T, int P>
-void tl_launch_finish(const HostTables& h, int mode, const T* r, T* z, const T* x0, const T* binv, int dim,
+void tl_launch_finish(const HostTables& h, int mode, const T* r, T* z, const T* x0, const T* fdm, int dim,
                       CgState<T>* st, ReduceScratch red, cudaStream_t s) {
   const size_t noe = (size_t)dim * dim;
   if (mode == 1)
     k_tl_finish<T, P, 1><<<tl_grid(noe, kTlElemThreads, red.capacity), kTlElemThreads, 0, s>>>(
-        r, z, x0, binv, dim, tl_hat<T, P>(h), st, red);
+        r, z, x0, fdm, dim, tl_hat<T, P>(h), st, red);
   else
-    k_tl_finish<T, P, 0><<<tl_grid(noe, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(r, z, x0, binv, dim,
+    k_tl_finish<T, P, 0><<<tl_grid(noe, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(r, z, x0, fdm, dim,
                                                                                            tl_hat<T, P>(h), st, red);
 }
 
@@ -483,6 +594,108 @@ bool tl_invert(std::vector<double>& a, int n) {
     }
   }
   a.swap(inv);
+  return true;
+}
+
+// Symmetric eigen-decomposition a = Q diag(lam) Q^T by cyclic Jacobi
+// rotations (n <= 9; a is overwritten).
+void tl_jacobi_eig(std::vector<double>& a, int n, std::vector<double>& lam, std::vector<double>& Q) {
+  Q.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        tot += a[(size_t)i * n + j] * a[(size_t)i * n + j];
+        if (i != j) off += a[(size_t)i * n + j] * a[(size_t)i * n + j];
+      }
+    if (off <= 1e-30 * tot) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        // the rotation in the (p, q) plane that zeroes a_pq: cot 2 theta = (a_qq - a_pp) / (2 a_pq)
+        const double th = (a[(size_t)q * n + q] - a[(size_t)p * n + p]) / (2.0 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
+          a[(size_t)k * n + p] = c * akp - sn * akq;
+          a[(size_t)k * n + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
+          a[(size_t)p * n + k] = c * apk - sn * aqk;
+          a[(size_t)q * n + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double qkp = Q[(size_t)k * n + p], qkq = Q[(size_t)k * n + q];
+          Q[(size_t)k * n + p] = c * qkp - sn * qkq;
+          Q[(size_t)k * n + q] = sn * qkp + c * qkq;
+        }
+      }
+  }
+  lam.resize(n);
+  for (int i = 0; i < n; ++i) lam[i] = a[(size_t)i * n + i];
+}
+
+// Fast diagonalisation of one element block B (nn x nn, node k = i1 n1 +
+// i2, i1 along x): the SIPG element block is separable,
+//   B = L_x (x) W + W (x) L_y,   W = diag(w),
+// L_x the 1-D operator along x with its own face terms (which of the LEFT /
+// RIGHT faces are on the boundary), L_y along y.  With L V = W V Lambda and
+// V^T W V = I in each direction, B^-1 = (V_x (x) V_y) D^-1 (V_x (x) V_y)^T,
+// D = Lambda_x (x) I + I (x) Lambda_y.  out = [V_x | V_y | D^-1] (3 n1^2
+// floats; V[i][a] at i n1 + a, D^-1[a][b] at a n1 + b).  False if B is not
+// of this form (to 1e-9) or D is not positive.
+bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
+  const int nn = n1 * n1;
+  auto b = [&](int i1, int i2, int j1, int j2) { return B[(size_t)(i1 * n1 + i2) * nn + (j1 * n1 + j2)]; };
+  std::vector<double> Lx((size_t)n1 * n1), Ly((size_t)n1 * n1);
+  // off-diagonals from the first row / column of nodes; the split of the
+  // diagonal is free up to L_x + c W, L_y - c W: take L_y[0][0] = 0
+  for (int i = 0; i < n1; ++i)
+    for (int j = 0; j < n1; ++j) {
+      if (i != j) {
+        Lx[(size_t)i * n1 + j] = b(i, 0, j, 0) / w[0];
+        Ly[(size_t)i * n1 + j] = b(0, i, 0, j) / w[0];
+      }
+    }
+  for (int i = 0; i < n1; ++i) Lx[(size_t)i * n1 + i] = b(i, 0, i, 0) / w[0];
+  for (int j = 0; j < n1; ++j) Ly[(size_t)j * n1 + j] = (b(0, j, 0, j) - Lx[0] * w[j]) / w[0];
+  double err = 0.0, mx = 0.0;
+  for (int i1 = 0; i1 < n1; ++i1)
+    for (int i2 = 0; i2 < n1; ++i2)
+      for (int j1 = 0; j1 < n1; ++j1)
+        for (int j2 = 0; j2 < n1; ++j2) {
+          const double m = (i2 == j2 ? Lx[(size_t)i1 * n1 + j1] * w[i2] : 0.0) +
+                           (i1 == j1 ? w[i1] * Ly[(size_t)i2 * n1 + j2] : 0.0);
+          err = std::max(err, std::fabs(m - b(i1, i2, j1, j2)));
+          mx = std::max(mx, std::fabs(b(i1, i2, j1, j2)));
+        }
+  if (!(err <= 1e-9 * mx)) return false;
+  std::vector<double> V[2], lam[2];
+  for (int d = 0; d < 2; ++d) {
+    const std::vector<double>& L = d ? Ly : Lx;
+    std::vector<double> C((size_t)n1 * n1), Q;
+    for (int i = 0; i < n1; ++i)
+      for (int j = 0; j < n1; ++j)
+        C[(size_t)i * n1 + j] = 0.5 * (L[(size_t)i * n1 + j] + L[(size_t)j * n1 + i]) / std::sqrt(w[i] * w[j]);
+    tl_jacobi_eig(C, n1, lam[d], Q);
+    V[d].resize((size_t)n1 * n1);
+    for (int i = 0; i < n1; ++i)
+      for (int a = 0; a < n1; ++a) V[d][(size_t)i * n1 + a] = Q[(size_t)i * n1 + a] / std::sqrt(w[i]);
+  }
+  for (int i = 0; i < nn; ++i) {
+    out[i] = (float)V[0][i];
+    out[nn + i] = (float)V[1][i];
+  }
+  for (int a = 0; a < n1; ++a)
+    for (int c = 0; c < n1; ++c) {
+      const double dsum = lam[0][a] + lam[1][c];
+      if (!(dsum > 0.0)) return false;
+      out[2 * nn + a * n1 + c] = (float)(1.0 / dsum);
+    }
   return true;
 }
 
@@ -607,7 +820,7 @@ namespace {
 // Everything the preconditioner keeps on the device for one operator.
 struct TwoLevel {
   int dim = 0, p = 0;
-  float* binv = nullptr;  // [16][nn][nn] block inverses
+  float* fdm = nullptr;   // [16][3][nn] element block factors [V_x | V_y | D^-1]
   float* cp = nullptr;    // [4][noe] corner sums
   float* ainv = nullptr;  // coarsest level's dense inverse
   std::vector<TlLev<float>> lev;
@@ -628,9 +841,9 @@ sipg_status dalloc(TwoLevel& tl, T** out, size_t count) {
   return SIPG_OK;
 }
 
-// Element block inverses: probe the diagonal blocks with the FP64 operator on
-// a mesh of min(dim, 3) elements per side, one checkerboard colour and node
-// at a time.
+// Element block inverses by fast diagonalisation: probe the diagonal blocks
+// with the FP64 operator on a mesh of min(dim, 3) elements per side, one
+// checkerboard colour and node at a time, and factor each (tl_fdm).
 sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
   const int p = op->p, n1 = p + 1, nn = n1 * n1, dm = std::min(op->dim, 3), noe = dm * dm;
   sipg_op* small = nullptr;
@@ -665,14 +878,13 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
   sipg_op_destroy(small);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(e);
-  table.assign((size_t)kTlTypes * nn * nn, 0.0f);
+  table.assign((size_t)kTlTypes * 3 * nn, 0.0f);
   for (int t = 0; t < kTlTypes; ++t) {
     if (blk[t].empty()) continue;
-    if (!tl_invert(blk[t], nn)) {
-      set_error("two-level preconditioner: singular element block");
+    if (!tl_fdm(blk[t], op->tab.w, n1, table.data() + (size_t)t * 3 * nn)) {
+      set_error("two-level preconditioner: an element block is not of the form W (x) L_x + L_y (x) W, or not SPD");
       return SIPG_ERR_INVALID;
     }
-    for (size_t i = 0; i < (size_t)nn * nn; ++i) table[(size_t)t * nn * nn + i] = (float)blk[t][i];
   }
   return SIPG_OK;
 }
@@ -703,7 +915,7 @@ sipg_status build_level0(sipg_op* op, HostLevel& L0) {
     st = sipg_apply_f64(op, xd, yd, nullptr);
     if (st != SIPG_OK) break;
     SIPG_TL_DISPATCH(tl_launch_restrict_elem, double, p, op->tab, yd, cp, noe, (const int*)nullptr, (cudaStream_t)0)
-    k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads>>>(cp, yv, dim, nullptr);
+    k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads>>>(cp, yv, dim);
     count_launch(2);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(hys[c].data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost);
@@ -738,9 +950,9 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
   std::vector<float> table;
   sipg_status st = build_blocks(op, table);
   if (st != SIPG_OK) return st;
-  st = dalloc(tl, &tl.binv, table.size());
+  st = dalloc(tl, &tl.fdm, table.size());
   if (st != SIPG_OK) return st;
-  SIPG_CUDA_TRY(cudaMemcpy(tl.binv, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
+  SIPG_CUDA_TRY(cudaMemcpy(tl.fdm, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
   (void)nn;
   st = dalloc(tl, &tl.cp, 4 * (size_t)op->noe);
   if (st != SIPG_OK) return st;
@@ -831,24 +1043,20 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
   const int dim = tl.dim, nl = (int)tl.lev.size();
   const size_t noe = (size_t)dim * dim;
   SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, done, s)
-  const int nv0 = (dim + 1) * (dim + 1);
-  k_tl_restrict_vert<float><<<tl_grid(nv0, kTlVecThreads, 1 << 30), kTlVecThreads, 0, s>>>(tl.cp, tl.lev[0].b, dim,
-                                                                                          done);
-  count_launch(2);
-  auto grid = [&](const TlLev<float>& L) { return tl_grid((size_t)(L.m + 1) * (L.m + 1), kTlVecThreads, 1 << 30); };
+  count_launch();
   for (int l = 0; l + 1 < nl; ++l) {
-    k_tl_presmooth<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], done);
-    k_tl_restrict_resid<float><<<grid(tl.lev[l + 1]), kTlVecThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
-    count_launch(2);
+    const int t = tl_tiles(tl.lev[l + 1].m + 1, kTlDown);
+    k_tl_down<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], l == 0 ? tl.cp : nullptr, dim, done);
+    count_launch();
   }
   k_tl_dense<float><<<1, kTlVecThreads, 0, s>>>(tl.lev[nl - 1], tl.ainv, done);
   count_launch();
   for (int l = nl - 2; l >= 0; --l) {
-    k_tl_post1<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
-    k_tl_post2<float><<<grid(tl.lev[l]), kTlVecThreads, 0, s>>>(tl.lev[l], done);
-    count_launch(2);
+    const int t = tl_tiles(tl.lev[l].m + 1, kTlUp);
+    k_tl_up<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
+    count_launch();
   }
-  SIPG_TL_DISPATCH(tl_launch_finish, float, tl.p, op->tab, st ? 1 : 0, r, z, tl.lev[0].x, tl.binv, dim, st, red, s)
+  SIPG_TL_DISPATCH(tl_launch_finish, float, tl.p, op->tab, st ? 1 : 0, r, z, tl.lev[0].y, tl.fdm, dim, st, red, s)
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
   return SIPG_OK;
@@ -887,7 +1095,7 @@ TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* 
   TlInst v{};
   v.r = r;
   v.z = z;
-  v.binv = tl.binv;
+  v.fdm = tl.fdm;
   v.ainv = tl.ainv;
   v.st = st;
   v.red = red;
@@ -915,9 +1123,8 @@ TlPlan twolevel_plan(const TlInst* h, const HostTables* const* tabs, int n) {
   for (int i = 0; i < n; ++i) {
     plan.maxl = std::max(plan.maxl, h[i].nl);
     plan.nblk_max = std::max(plan.nblk_max, h[i].nblk);
-    if ((int)plan.nv_max.size() < h[i].nl) plan.nv_max.resize(h[i].nl, 0);
-    for (int l = 0; l < h[i].nl; ++l)
-      plan.nv_max[l] = std::max(plan.nv_max[l], (h[i].lev[l].m + 1) * (h[i].lev[l].m + 1));
+    if ((int)plan.side_max.size() < h[i].nl) plan.side_max.resize(h[i].nl, 0);
+    for (int l = 0; l < h[i].nl; ++l) plan.side_max[l] = std::max(plan.side_max[l], h[i].lev[l].m + 1);
     if (plan.groups.empty() || plan.groups.back().p != h[i].p) plan.groups.push_back({h[i].p, i, 0, 0, tabs[i]});
     TlPlan::Group& g = plan.groups.back();
     g.count += 1;
@@ -950,20 +1157,20 @@ sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaSt
       case 8: tlb_elem_launch<8>(0, d, g, s); break;
     }
   }
-  auto vgrid = [&](int l) { return dim3(tl_grid((size_t)plan.nv_max[l], kTlVecThreads, 1 << 30), n); };
-  k_tlb_restrict_vert<<<vgrid(0), kTlVecThreads, 0, s>>>(d);
-  count_launch(plan.groups.size() + 1);
+  count_launch(plan.groups.size());
+  auto tiles = [&](int l, int tile) {
+    const int t = tl_tiles(plan.side_max[l], tile);
+    return dim3(t * t, n);
+  };
   for (int l = 0; l + 1 < plan.maxl; ++l) {
-    k_tlb_presmooth<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
-    k_tlb_restrict_resid<<<vgrid(l + 1), kTlVecThreads, 0, s>>>(d, l);
-    count_launch(2);
+    k_tlb_down<<<tiles(l + 1, kTlDown), kTlTileThreads, 0, s>>>(d, l);
+    count_launch();
   }
   k_tlb_dense<<<dim3(1, n), kTlVecThreads, 0, s>>>(d);
   count_launch();
   for (int l = plan.maxl - 2; l >= 0; --l) {
-    k_tlb_post1<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
-    k_tlb_post2<<<vgrid(l), kTlVecThreads, 0, s>>>(d, l);
-    count_launch(2);
+    k_tlb_up<<<tiles(l, kTlUp), kTlTileThreads, 0, s>>>(d, l);
+    count_launch();
   }
   for (const TlPlan::Group& g : plan.groups) {
     switch (g.p) {
