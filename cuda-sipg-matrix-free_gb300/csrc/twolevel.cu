@@ -323,10 +323,17 @@ __device__ __forceinline__ void tl_up_body(const TlLev<T>& F, const TlLev<T>& C,
   }
 }
 
-// coarsest level: y = A^-1 b (dense, one block)
+// coarsest level: y = A^-1 b (dense, one block).  With cp (a mesh of at most
+// 8 x 8 elements, whose level 0 is the coarsest) b is first formed from the
+// element corner sums.
 template <typename T>
-__device__ __forceinline__ void tl_dense_body(const TlLev<T>& L, const T* __restrict__ ainv) {
+__device__ __forceinline__ void tl_dense_body(const TlLev<T>& L, const T* __restrict__ ainv, const T* __restrict__ cp,
+                                              int dim) {
   const int nv = (L.m + 1) * (L.m + 1);
+  if (cp) {
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) L.b[v] = tl_corner_sum(cp, dim, v % (L.m + 1), v / (L.m + 1));
+    __syncthreads();
+  }
   for (int v = threadIdx.x; v < nv; v += blockDim.x) {
     T s = T(0);
     for (int u = 0; u < nv; ++u) s = fma(ainv[v * nv + u], L.b[u], s);
@@ -350,9 +357,10 @@ __global__ void __launch_bounds__(kTlTileThreads) k_tl_up(TlLev<T> F, TlLev<T> C
   tl_up_body<T>(F, C, blockIdx.x % t, blockIdx.x / t);
 }
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads) k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const int* done) {
+__global__ void __launch_bounds__(kTlVecThreads)
+    k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const T* __restrict__ cp, int dim, const int* done) {
   if (tl_done(done)) return;
-  tl_dense_body<T>(L, ainv);
+  tl_dense_body<T>(L, ainv, cp, dim);
 }
 
 // The Q1 function of the element's corner values at node (i1, i2).
@@ -497,7 +505,7 @@ __global__ void __launch_bounds__(kTlTileThreads) k_tlb_down(const TlInst* __res
 __global__ void __launch_bounds__(kTlVecThreads) k_tlb_dense(const TlInst* __restrict__ insts) {
   const TlInst& v = insts[blockIdx.y];
   if (tlb_skip(v)) return;
-  tl_dense_body<float>(v.lev[v.nl - 1], v.ainv);
+  tl_dense_body<float>(v.lev[v.nl - 1], v.ainv, v.nl == 1 ? v.cp : nullptr, v.dim);
 }
 __global__ void __launch_bounds__(kTlTileThreads) k_tlb_up(const TlInst* __restrict__ insts, int l) {
   const TlInst& v = insts[blockIdx.y];
@@ -1049,7 +1057,7 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
     k_tl_down<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], l == 0 ? tl.cp : nullptr, dim, done);
     count_launch();
   }
-  k_tl_dense<float><<<1, kTlVecThreads, 0, s>>>(tl.lev[nl - 1], tl.ainv, done);
+  k_tl_dense<float><<<1, kTlVecThreads, 0, s>>>(tl.lev[nl - 1], tl.ainv, nl == 1 ? tl.cp : nullptr, dim, done);
   count_launch();
   for (int l = nl - 2; l >= 0; --l) {
     const int t = tl_tiles(tl.lev[l].m + 1, kTlUp);

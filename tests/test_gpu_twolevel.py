@@ -22,7 +22,7 @@ def torch():
     return t
 
 
-@pytest.mark.parametrize("p,dim", [(1, 1), (2, 2), (3, 5), (4, 9), (6, 12), (8, 17), (2, 33), (5, 20)])
+@pytest.mark.parametrize("p,dim", [(1, 1), (2, 2), (3, 5), (4, 8), (4, 9), (6, 12), (8, 17), (2, 33), (5, 20), (3, 65), (2, 70)])
 def test_twolevel_matches_cpu_restatement(sipg, oracle, torch, p, dim):
     pen = float(p * p)
     op = sipg.Operator(dim, p, pen)
