@@ -647,6 +647,11 @@ void tl_jacobi_eig(std::vector<double>& a, int n, std::vector<double>& lam, std:
   for (int i = 0; i < n; ++i) lam[i] = a[(size_t)i * n + i];
 }
 
+// Generalised eigenvalues of an element block at most this fraction of the
+// largest in magnitude count as zero (a singular block, as the single element
+// of a 1 x 1 mesh at p = 1 and penalty 1 is): their modes are left out.
+constexpr double kTlNullRel = 1e-12;
+
 // Fast diagonalisation of one element block B (nn x nn, node k = i1 n1 +
 // i2, i1 along x): the SIPG element block is separable,
 //   B = L_x (x) W + W (x) L_y,   W = diag(w),
@@ -654,8 +659,8 @@ void tl_jacobi_eig(std::vector<double>& a, int n, std::vector<double>& lam, std:
 // RIGHT faces are on the boundary), L_y along y.  With L V = W V Lambda and
 // V^T W V = I in each direction, B^-1 = (V_x (x) V_y) D^-1 (V_x (x) V_y)^T,
 // D = Lambda_x (x) I + I (x) Lambda_y.  out = [V_x | V_y | D^-1] (3 n1^2
-// floats; V[i][a] at i n1 + a, D^-1[a][b] at a n1 + b).  False if B is not
-// of this form (to 1e-9) or D is not positive.
+// floats; V[i][a] at i n1 + a, D^-1[a][b] at a n1 + b; zero for a null
+// mode).  False if B is not of this form (to 1e-9) or is zero.
 bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
   const int nn = n1 * n1;
   auto b = [&](int i1, int i2, int j1, int j2) { return B[(size_t)(i1 * n1 + i2) * nn + (j1 * n1 + j2)]; };
@@ -698,13 +703,15 @@ bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
     out[i] = (float)V[0][i];
     out[nn + i] = (float)V[1][i];
   }
+  double dmax = 0.0;
+  for (int a = 0; a < n1; ++a)
+    for (int c = 0; c < n1; ++c) dmax = std::max(dmax, std::fabs(lam[0][a] + lam[1][c]));
   for (int a = 0; a < n1; ++a)
     for (int c = 0; c < n1; ++c) {
       const double dsum = lam[0][a] + lam[1][c];
-      if (!(dsum > 0.0)) return false;
-      out[2 * nn + a * n1 + c] = (float)(1.0 / dsum);
+      out[2 * nn + a * n1 + c] = std::fabs(dsum) <= kTlNullRel * dmax ? 0.0f : (float)(1.0 / dsum);
     }
-  return true;
+  return dmax > 0.0;
 }
 
 // Runs f(lo, hi) over [0, n) split across host threads when n is large (the
@@ -890,7 +897,7 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
   for (int t = 0; t < kTlTypes; ++t) {
     if (blk[t].empty()) continue;
     if (!tl_fdm(blk[t], op->tab.w, n1, table.data() + (size_t)t * 3 * nn)) {
-      set_error("two-level preconditioner: an element block is not of the form W (x) L_x + L_y (x) W, or not SPD");
+      set_error("two-level preconditioner: an element block is not of the form W (x) L_x + L_y (x) W");
       return SIPG_ERR_INVALID;
     }
   }

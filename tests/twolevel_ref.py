@@ -7,6 +7,8 @@ M r = B^-1 r + P V(P^T r):
   operator (the oracle's matvec) on a mesh of min(dim, 3) elements per side
   with a checkerboard colouring; blocks are keyed by which faces lie on the
   domain boundary (bit 0 LEFT, 1 RIGHT, 2 DOWN, 3 UP; row 0 is the top row).
+  It is formed from the block's generalised eigenvectors (B V = W V mu, W the
+  nodal quadrature weights), leaving out null modes, |mu| <= 1e-12 max |mu|.
 - P: bilinear hat functions of the (dim + 1)^2 vertices (bottom-up vertex rows)
   at each element's LGL nodes (node (i1, i2): i1 along x, i2 along y).
 - V: one V-cycle for A_0 = P^T A P (probed with nine vertex colours),
@@ -17,9 +19,11 @@ M r = B^-1 r + P V(P^T r):
   sin(0.7 v + 0.3) + 0.5, the coarsest level by its dense inverse.
 """
 import numpy as np
+import scipy.linalg
 import scipy.sparse as sp
 
 COARSEST = 8
+NULL_REL = 1e-12
 
 
 def elem_type(row, col, dim):
@@ -44,7 +48,19 @@ def blocks(orc, p, pen, dim):
                     continue
                 t = elem_type(e // dm, e % dm, dm)
                 out.setdefault(t, np.zeros((nn, nn)))[:, k] = y[:, e]
-    return {t: np.linalg.inv(b) for t, b in out.items()}
+    xi, w = orc.lgl(n1)
+    W = np.kron(np.diag(w), np.diag(w))
+    return {t: block_inverse(b, W) for t, b in out.items()}
+
+
+def block_inverse(B, W):
+    """V diag(1/mu) V^T from B V = W V diag(mu), V^T W V = I: the inverse of
+    B, with the modes of |mu| <= 1e-12 max |mu| left out (a singular block)."""
+    mu, V = scipy.linalg.eigh(B, W)
+    keep = np.abs(mu) > NULL_REL * np.abs(mu).max()
+    inv = np.zeros_like(mu)
+    inv[keep] = 1.0 / mu[keep]
+    return (V * inv) @ V.T
 
 
 def prolongation(orc, p, dim):
