@@ -34,6 +34,7 @@ struct TlInst {
   CgState<float>* st;  // the inner PCG state (r.z and beta are set here)
   ReduceScratch red;
   int dim, p, nl;      // mesh, degree, levels
+  int tail0;           // first level of the one-block tail (levels of at most 32 cells per side)
   int nblk;            // blocks of the element kernels (and of its r.z reduction)
   TlLev<float> lev[kTlMaxLevels];
 };
@@ -44,6 +45,7 @@ struct TlPlan {
   int n = 0;
   int maxl = 0;
   int nblk_max = 0;
+  int max_tail0 = 0;
   std::vector<int> side_max;  // per level: the largest vertices per side
   struct Group {
     int p, first, count, nblk_max;

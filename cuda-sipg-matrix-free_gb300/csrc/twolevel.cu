@@ -182,17 +182,43 @@ __global__ void __launch_bounds__(kTlElemThreads)
 constexpr int kTlDown = 16;          // coarse vertices per side of a down tile
 constexpr int kTlUp = 32;            // fine vertices per side of an up tile
 constexpr int kTlTileThreads = 256;  // threads of the tile kernels
+constexpr int kTlTailCells = 32;     // levels of at most this many cells per side run in one block
+constexpr int kTlTailThreads = 1024;
 
-// The level's 9-point stencil at vertex (ix, iy) applied to a window w
-// (row stride W) whose entry [ly][lx] holds vertex (ix - 1 + lx, iy - 1 + ly)
-// of the 3 x 3 patch around it: the caller passes w = &win[cy - 1][cx - 1].
+// The vertex kernels wait on memory, not arithmetic: each pass of a tile
+// kernel first loads what every one of its thread's steps needs (stencil
+// rows, weights, right-hand sides) and only then computes, so that all of a
+// thread's loads are in flight together.
+template <int N>
+__host__ __device__ constexpr int tl_steps() {
+  return (N + kTlTileThreads - 1) / kTlTileThreads;
+}
+
+// A vertex's stencil row (S[k] = entry k of its 9-point row), damping and
+// right-hand side.
+template <typename T>
+struct TlRow {
+  T S[9];
+  T wd, b;
+};
+
+template <typename T>
+__device__ __forceinline__ void tl_load_row(const TlLev<T>& L, int v, int nv, bool ok, bool with_b, TlRow<T>& r) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) r.S[k] = ok ? __ldg(L.S + (size_t)k * nv + v) : T(0);
+  r.wd = ok ? __ldg(L.wd + v) : T(0);
+  r.b = (ok && with_b) ? __ldg(L.b + v) : T(0);
+}
+
+// The row applied to the 3 x 3 patch of window w around the vertex (w points
+// at the patch's corner [0][0], row stride W).
 template <typename T, int W>
-__device__ __forceinline__ T tl_stencil_win(const TlLev<T>& L, const T (*w)[W], int v, int nv) {
+__device__ __forceinline__ T tl_row_apply(const TlRow<T>& r, const T* w) {
   T s = T(0);
 #pragma unroll
   for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-    for (int dx = 0; dx < 3; ++dx) s = fma(__ldg(L.S + (size_t)(dy * 3 + dx) * nv + v), w[dy][dx], s);
+    for (int dx = 0; dx < 3; ++dx) s = fma(r.S[dy * 3 + dx], w[dy * W + dx], s);
   return s;
 }
 
@@ -208,49 +234,72 @@ __device__ __forceinline__ void tl_down_body(const TlLev<T>& F, const TlLev<T>& 
                                              int tx, int ty) {
   constexpr int W3 = 2 * kTlDown + 5, W2 = W3 - 2, W1 = W3 - 4;  // 37, 35, 33
   __shared__ T sb[W3][W3], sx1[W3][W3], sx[W2][W2], sr[W1][W1];
-  const int m = F.m, n1 = m + 1, nv = n1 * n1;
+  const int m = F.m, n1 = m + 1, nv = n1 * n1, t = threadIdx.x;
   const int cx0 = tx * kTlDown, cy0 = ty * kTlDown;
   const int ox = 2 * cx0 - 3, oy = 2 * cy0 - 3;  // fine vertex of window entry [0][0] of sb
-  auto owned = [&](int ix, int iy) { return ix >= 2 * cx0 && ix < 2 * cx0 + 2 * kTlDown && iy >= 2 * cy0 && iy < 2 * cy0 + 2 * kTlDown; };
+  auto owned = [&](int ix, int iy) {
+    return ix >= 2 * cx0 && ix < 2 * cx0 + 2 * kTlDown && iy >= 2 * cy0 && iy < 2 * cy0 + 2 * kTlDown;
+  };
   auto inside = [&](int ix, int iy) { return ix >= 0 && iy >= 0 && ix <= m && iy <= m; };
-  for (int i = threadIdx.x; i < W3 * W3; i += kTlTileThreads) {
-    const int ly = i / W3, lx = i - ly * W3, ix = ox + lx, iy = oy + ly;
-    T b = T(0), x1 = T(0);
-    if (inside(ix, iy)) {
-      const int v = iy * n1 + ix;
-      if (cp) {
-        b = tl_corner_sum(cp, dim, ix, iy);
-        if (owned(ix, iy)) F.b[v] = b;
-      } else {
-        b = F.b[v];
-      }
-      x1 = F.wd[v] * b;
+  {  // b and x1 on the W3 window
+    constexpr int NS = tl_steps<W3 * W3>();
+    T b[NS], w[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W3, lx = i - ly * W3, ix = ox + lx, iy = oy + ly;
+      const bool ok = i < W3 * W3 && inside(ix, iy);
+      const int v = ok ? iy * n1 + ix : 0;
+      b[k] = ok ? (cp ? tl_corner_sum(cp, dim, ix, iy) : __ldg(F.b + v)) : T(0);
+      w[k] = ok ? __ldg(F.wd + v) : T(0);
     }
-    sb[ly][lx] = b;
-    sx1[ly][lx] = x1;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < W2 * W2; i += kTlTileThreads) {
-    const int ly = i / W2, lx = i - ly * W2, ix = ox + 1 + lx, iy = oy + 1 + ly;
-    T x = T(0);
-    if (inside(ix, iy)) {
-      const int v = iy * n1 + ix;
-      x = fma(F.wd[v], sb[ly + 1][lx + 1] - tl_stencil_win<T, W3>(F, (const T(*)[W3]) & sx1[ly][lx], v, nv),
-              sx1[ly + 1][lx + 1]);
-      if (owned(ix, iy)) F.x[v] = x;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W3, lx = i - ly * W3;
+      if (i >= W3 * W3) break;
+      sb[ly][lx] = b[k];
+      sx1[ly][lx] = w[k] * b[k];
+      if (cp && inside(ox + lx, oy + ly) && owned(ox + lx, oy + ly)) F.b[(oy + ly) * n1 + ox + lx] = b[k];
     }
-    sx[ly][lx] = x;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < W1 * W1; i += kTlTileThreads) {
-    const int ly = i / W1, lx = i - ly * W1, ix = ox + 2 + lx, iy = oy + 2 + ly;
-    T res = T(0);
-    if (inside(ix, iy))
-      res = sb[ly + 2][lx + 2] - tl_stencil_win<T, W2>(F, (const T(*)[W2]) & sx[ly][lx], iy * n1 + ix, nv);
-    sr[ly][lx] = res;
+  {  // x on the W2 window
+    constexpr int NS = tl_steps<W2 * W2>();
+    TlRow<T> r[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W2, lx = i - ly * W2, ix = ox + 1 + lx, iy = oy + 1 + ly;
+      const bool ok = i < W2 * W2 && inside(ix, iy);
+      tl_load_row(F, ok ? iy * n1 + ix : 0, nv, ok, false, r[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W2, lx = i - ly * W2, ix = ox + 1 + lx, iy = oy + 1 + ly;
+      if (i >= W2 * W2) break;
+      // outside the level the row is zero and so is x
+      const T x = fma(r[k].wd, sb[ly + 1][lx + 1] - tl_row_apply<T, W3>(r[k], &sx1[ly][lx]), sx1[ly + 1][lx + 1]);
+      sx[ly][lx] = x;
+      if (inside(ix, iy) && owned(ix, iy)) F.x[iy * n1 + ix] = x;
+    }
   }
   __syncthreads();
-  const int J = cx0 + (int)threadIdx.x % kTlDown, I = cy0 + (int)threadIdx.x / kTlDown;
+  {  // the residual on the footprint (W1 window)
+    constexpr int NS = tl_steps<W1 * W1>();
+    TlRow<T> r[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W1, lx = i - ly * W1, ix = ox + 2 + lx, iy = oy + 2 + ly;
+      const bool ok = i < W1 * W1 && inside(ix, iy);
+      tl_load_row(F, ok ? iy * n1 + ix : 0, nv, ok, false, r[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W1, lx = i - ly * W1, ix = ox + 2 + lx, iy = oy + 2 + ly;
+      if (i >= W1 * W1) break;
+      sr[ly][lx] = inside(ix, iy) ? sb[ly + 2][lx + 2] - tl_row_apply<T, W2>(r[k], &sx[ly][lx]) : T(0);
+    }
+  }
+  __syncthreads();
+  const int J = cx0 + t % kTlDown, I = cy0 + t / kTlDown;
   if (J > C.m || I > C.m) return;
   T acc = T(0);
 #pragma unroll
@@ -268,25 +317,38 @@ __device__ __forceinline__ void tl_down_body(const TlLev<T>& F, const TlLev<T>& 
   C.b[I * (C.m + 1) + J] = acc;
 }
 
+// The prolongation of the coarse result at fine vertex (ux, uy): the coarse
+// vertices it lies between, (jx0, jx1) x (jy0, jy1), and its weights.
+struct TlProlong {
+  int jx0, jx1, jy0, jy1;
+  bool px, py;  // on a coarse vertex line in x, in y
+};
+__device__ __forceinline__ TlProlong tl_prolong_at(int ux, int uy, int m) {
+  TlProlong q;
+  q.px = (ux % 2 == 0) || (ux == m);
+  q.py = (uy % 2 == 0) || (uy == m);
+  q.jx0 = q.px ? (ux + 1) / 2 : (ux - 1) / 2;
+  q.jx1 = q.px ? q.jx0 : (ux + 1) / 2;
+  q.jy0 = q.py ? (uy + 1) / 2 : (uy - 1) / 2;
+  q.jy1 = q.py ? q.jy0 : (uy + 1) / 2;
+  return q;
+}
+// c = [c00 c01; c10 c11] (c_ab at (jy_a, jx_b)) combined with the weights
+template <typename T>
+__device__ __forceinline__ T tl_prolong_value(const TlProlong& q, T c00, T c01, T c10, T c11) {
+  if (q.px && q.py) return c00;
+  if (q.px) return T(0.5) * (c00 + c10);
+  if (q.py) return T(0.5) * (c00 + c01);
+  return T(0.25) * ((c00 + c01) + (c10 + c11));
+}
+
 // The pre-smoothed iterate plus the prolonged coarse result at fine vertex (ux, uy).
 template <typename T>
 __device__ __forceinline__ T tl_corrected(const TlLev<T>& F, const TlLev<T>& C, int ux, int uy) {
   const int cn1 = C.m + 1;
-  T c = T(0);
-  const bool px = (ux % 2 == 0) || (ux == F.m), py = (uy % 2 == 0) || (uy == F.m);
-  const int jx0 = px ? (ux + 1) / 2 : (ux - 1) / 2, jx1 = px ? jx0 : (ux + 1) / 2;
-  const int jy0 = py ? (uy + 1) / 2 : (uy - 1) / 2, jy1 = py ? jy0 : (uy + 1) / 2;
-  const T wx = px ? T(1) : T(0.5), wy = py ? T(1) : T(0.5);
-  if (px && py) {
-    c = C.y[jy0 * cn1 + jx0];
-  } else if (px) {
-    c = wy * (C.y[jy0 * cn1 + jx0] + C.y[jy1 * cn1 + jx0]);
-  } else if (py) {
-    c = wx * (C.y[jy0 * cn1 + jx0] + C.y[jy0 * cn1 + jx1]);
-  } else {
-    c = T(0.25) * ((C.y[jy0 * cn1 + jx0] + C.y[jy0 * cn1 + jx1]) + (C.y[jy1 * cn1 + jx0] + C.y[jy1 * cn1 + jx1]));
-  }
-  return F.x[uy * (F.m + 1) + ux] + c;
+  const TlProlong q = tl_prolong_at(ux, uy, F.m);
+  return F.x[uy * (F.m + 1) + ux] + tl_prolong_value(q, C.y[q.jy0 * cn1 + q.jx0], C.y[q.jy0 * cn1 + q.jx1],
+                                                      C.y[q.jy1 * cn1 + q.jx0], C.y[q.jy1 * cn1 + q.jx1]);
 }
 
 // One up step for the 32 x 32 tile (tx, ty) of fine vertices: with
@@ -296,49 +358,138 @@ template <typename T>
 __device__ __forceinline__ void tl_up_body(const TlLev<T>& F, const TlLev<T>& C, int tx, int ty) {
   constexpr int W2 = kTlUp + 4, W1 = kTlUp + 2;  // 36, 34
   __shared__ T sxc[W2][W2], sy[W1][W1];
-  const int m = F.m, n1 = m + 1, nv = n1 * n1;
+  const int m = F.m, n1 = m + 1, nv = n1 * n1, cn1 = C.m + 1, t = threadIdx.x;
   const int fx0 = tx * kTlUp, fy0 = ty * kTlUp;
   const int ox = fx0 - 2, oy = fy0 - 2;  // fine vertex of window entry [0][0] of sxc
   auto inside = [&](int ix, int iy) { return ix >= 0 && iy >= 0 && ix <= m && iy <= m; };
-  for (int i = threadIdx.x; i < W2 * W2; i += kTlTileThreads) {
-    const int ly = i / W2, lx = i - ly * W2, ix = ox + lx, iy = oy + ly;
-    sxc[ly][lx] = inside(ix, iy) ? tl_corrected(F, C, ix, iy) : T(0);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < W1 * W1; i += kTlTileThreads) {
-    const int ly = i / W1, lx = i - ly * W1, ix = ox + 1 + lx, iy = oy + 1 + ly;
-    T y = T(0);
-    if (inside(ix, iy)) {
-      const int v = iy * n1 + ix;
-      y = fma(F.wd[v], F.b[v] - tl_stencil_win<T, W2>(F, (const T(*)[W2]) & sxc[ly][lx], v, nv), sxc[ly + 1][lx + 1]);
+  {  // xc on the W2 window
+    constexpr int NS = tl_steps<W2 * W2>();
+    T xv[NS], c[NS][4];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W2, lx = i - ly * W2, ix = ox + lx, iy = oy + ly;
+      const bool ok = i < W2 * W2 && inside(ix, iy);
+      const TlProlong q = tl_prolong_at(ok ? ix : 0, ok ? iy : 0, m);
+      xv[k] = ok ? __ldg(F.x + iy * n1 + ix) : T(0);
+      c[k][0] = ok ? __ldg(C.y + q.jy0 * cn1 + q.jx0) : T(0);
+      c[k][1] = ok ? __ldg(C.y + q.jy0 * cn1 + q.jx1) : T(0);
+      c[k][2] = ok ? __ldg(C.y + q.jy1 * cn1 + q.jx0) : T(0);
+      c[k][3] = ok ? __ldg(C.y + q.jy1 * cn1 + q.jx1) : T(0);
     }
-    sy[ly][lx] = y;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W2, lx = i - ly * W2, ix = ox + lx, iy = oy + ly;
+      if (i >= W2 * W2) break;
+      const bool ok = inside(ix, iy);
+      const TlProlong q = tl_prolong_at(ok ? ix : 0, ok ? iy : 0, m);
+      sxc[ly][lx] = ok ? xv[k] + tl_prolong_value(q, c[k][0], c[k][1], c[k][2], c[k][3]) : T(0);
+    }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kTlUp * kTlUp; i += kTlTileThreads) {
-    const int ly = i / kTlUp, lx = i - ly * kTlUp, ix = fx0 + lx, iy = fy0 + ly;
-    if (!inside(ix, iy)) continue;
-    const int v = iy * n1 + ix;
-    F.y[v] = fma(F.wd[v], F.b[v] - tl_stencil_win<T, W1>(F, (const T(*)[W1]) & sy[ly][lx], v, nv), sy[ly + 1][lx + 1]);
+  {  // y1 on the W1 window
+    constexpr int NS = tl_steps<W1 * W1>();
+    TlRow<T> r[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W1, lx = i - ly * W1, ix = ox + 1 + lx, iy = oy + 1 + ly;
+      const bool ok = i < W1 * W1 && inside(ix, iy);
+      tl_load_row(F, ok ? iy * n1 + ix : 0, nv, ok, true, r[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / W1, lx = i - ly * W1;
+      if (i >= W1 * W1) break;
+      // outside the level the row, b and xc are zero and so is y1
+      sy[ly][lx] = fma(r[k].wd, r[k].b - tl_row_apply<T, W2>(r[k], &sxc[ly][lx]), sxc[ly + 1][lx + 1]);
+    }
+  }
+  __syncthreads();
+  {  // y on the tile
+    constexpr int NS = tl_steps<kTlUp * kTlUp>();
+    TlRow<T> r[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / kTlUp, lx = i - ly * kTlUp, ix = fx0 + lx, iy = fy0 + ly;
+      const bool ok = i < kTlUp * kTlUp && inside(ix, iy);
+      tl_load_row(F, ok ? iy * n1 + ix : 0, nv, ok, true, r[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const int i = k * kTlTileThreads + t, ly = i / kTlUp, lx = i - ly * kTlUp, ix = fx0 + lx, iy = fy0 + ly;
+      if (i >= kTlUp * kTlUp || !inside(ix, iy)) continue;
+      F.y[iy * n1 + ix] = fma(r[k].wd, r[k].b - tl_row_apply<T, W1>(r[k], &sy[ly][lx]), sy[ly + 1][lx + 1]);
+    }
   }
 }
 
-// coarsest level: y = A^-1 b (dense, one block).  With cp (a mesh of at most
-// 8 x 8 elements, whose level 0 is the coarsest) b is first formed from the
-// element corner sums.
-template <typename T>
-__device__ __forceinline__ void tl_dense_body(const TlLev<T>& L, const T* __restrict__ ainv, const T* __restrict__ cp,
-                                              int dim) {
-  const int nv = (L.m + 1) * (L.m + 1);
-  if (cp) {
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) L.b[v] = tl_corner_sum(cp, dim, v % (L.m + 1), v / (L.m + 1));
+// The coarse end of the V-cycle in one block: from level l0 (at most
+// kTlTailCells cells per side; its b given, or from the corner sums cp when
+// l0 = 0) down to the coarsest level, its dense solve, and back up to l0's
+// result y.  Every phase is one pass over a level's vertices followed by a
+// block barrier; x1 and the residual live in y on the way down, the
+// corrected iterate and the first post-sweep in y and x on the way up.
+template <typename T, typename LevAt>
+__device__ __forceinline__ void tl_tail_body(LevAt lev, int l0, int nl, const T* __restrict__ ainv,
+                                             const T* __restrict__ cp, int dim) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (l0 == 0 && cp) {
+    const TlLev<T> F = lev(0);
+    const int n1 = F.m + 1;
+    for (int v = tid; v < n1 * n1; v += nt) F.b[v] = tl_corner_sum(cp, dim, v % n1, v / n1);
     __syncthreads();
   }
-  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
-    T s = T(0);
-    for (int u = 0; u < nv; ++u) s = fma(ainv[v * nv + u], L.b[u], s);
-    L.y[v] = s;
+  for (int l = l0; l + 1 < nl; ++l) {
+    const TlLev<T> F = lev(l), C = lev(l + 1);
+    const int m = F.m, n1 = m + 1, nv = n1 * n1;
+    for (int v = tid; v < nv; v += nt) F.y[v] = F.wd[v] * F.b[v];  // x1
+    __syncthreads();
+    for (int v = tid; v < nv; v += nt) F.x[v] = fma(F.wd[v], F.b[v] - tl_stencil(F, F.y, v % n1, v / n1), F.y[v]);
+    __syncthreads();
+    for (int v = tid; v < nv; v += nt) F.y[v] = F.b[v] - tl_stencil(F, F.x, v % n1, v / n1);  // residual
+    __syncthreads();
+    const int cn1 = C.m + 1;
+    for (int v = tid; v < cn1 * cn1; v += nt) {
+      const int J = v % cn1, I = v / cn1;
+      T acc = T(0);
+      for (int iy = 2 * I - 1; iy <= 2 * I + 1; ++iy) {
+        if (iy < 0 || iy > m) continue;
+        const T wy = tl_w<T>(iy, I, m);
+        for (int ix = 2 * J - 1; ix <= 2 * J + 1; ++ix) {
+          if (ix < 0 || ix > m) continue;
+          acc = fma(wy * tl_w<T>(ix, J, m), F.y[iy * n1 + ix], acc);
+        }
+      }
+      C.b[v] = acc;
+    }
+    __syncthreads();
   }
+  {
+    const TlLev<T> L = lev(nl - 1);
+    const int nv = (L.m + 1) * (L.m + 1);
+    for (int v = tid; v < nv; v += nt) {
+      T acc = T(0);
+      for (int u = 0; u < nv; ++u) acc = fma(ainv[v * nv + u], L.b[u], acc);
+      L.y[v] = acc;
+    }
+    __syncthreads();
+  }
+  for (int l = nl - 2; l >= l0; --l) {
+    const TlLev<T> F = lev(l), C = lev(l + 1);
+    const int n1 = F.m + 1, nv = n1 * n1;
+    for (int v = tid; v < nv; v += nt) F.y[v] = tl_corrected(F, C, v % n1, v / n1);  // xc
+    __syncthreads();
+    for (int v = tid; v < nv; v += nt) F.x[v] = fma(F.wd[v], F.b[v] - tl_stencil(F, F.y, v % n1, v / n1), F.y[v]);
+    __syncthreads();
+    for (int v = tid; v < nv; v += nt) F.y[v] = fma(F.wd[v], F.b[v] - tl_stencil(F, F.x, v % n1, v / n1), F.x[v]);
+    __syncthreads();
+  }
+}
+
+// The first level of the one-block tail.
+__host__ __device__ inline int tl_tail_level(const int* m, int nl) {
+  int l = 0;
+  while (l + 1 < nl && m[l] > kTlTailCells) ++l;
+  return l;
 }
 
 __host__ __device__ inline int tl_tiles(int verts, int tile) { return (verts + tile - 1) / tile; }
@@ -356,11 +507,18 @@ __global__ void __launch_bounds__(kTlTileThreads) k_tl_up(TlLev<T> F, TlLev<T> C
   const int t = tl_tiles(F.m + 1, kTlUp);
   tl_up_body<T>(F, C, blockIdx.x % t, blockIdx.x / t);
 }
+// The levels of one preconditioner (kernel parameter).
 template <typename T>
-__global__ void __launch_bounds__(kTlVecThreads)
-    k_tl_dense(TlLev<T> L, const T* __restrict__ ainv, const T* __restrict__ cp, int dim, const int* done) {
+struct TlLevels {
+  TlLev<T> lev[kTlMaxLevels];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kTlTailThreads)
+    k_tl_tail(const __grid_constant__ TlLevels<T> L, int l0, int nl, const T* __restrict__ ainv,
+              const T* __restrict__ cp, int dim, const int* done) {
   if (tl_done(done)) return;
-  tl_dense_body<T>(L, ainv, cp, dim);
+  tl_tail_body<T>([&](int l) { return L.lev[l]; }, l0, nl, ainv, cp, dim);
 }
 
 // The Q1 function of the element's corner values at node (i1, i2).
@@ -497,19 +655,19 @@ __global__ void __launch_bounds__(kTlElemThreads)
 // level l -> l + 1 of every instance that has level l + 1 (grid.x: the largest tile count)
 __global__ void __launch_bounds__(kTlTileThreads) k_tlb_down(const TlInst* __restrict__ insts, int l) {
   const TlInst& v = insts[blockIdx.y];
-  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  if (l >= v.tail0 || tlb_skip(v)) return;
   const int t = tl_tiles(v.lev[l + 1].m + 1, kTlDown);
   if ((int)blockIdx.x >= t * t) return;
   tl_down_body<float>(v.lev[l], v.lev[l + 1], l == 0 ? v.cp : nullptr, v.dim, blockIdx.x % t, blockIdx.x / t);
 }
-__global__ void __launch_bounds__(kTlVecThreads) k_tlb_dense(const TlInst* __restrict__ insts) {
+__global__ void __launch_bounds__(kTlTailThreads) k_tlb_tail(const TlInst* __restrict__ insts) {
   const TlInst& v = insts[blockIdx.y];
   if (tlb_skip(v)) return;
-  tl_dense_body<float>(v.lev[v.nl - 1], v.ainv, v.nl == 1 ? v.cp : nullptr, v.dim);
+  tl_tail_body<float>([&](int l) { return v.lev[l]; }, v.tail0, v.nl, v.ainv, v.cp, v.dim);
 }
 __global__ void __launch_bounds__(kTlTileThreads) k_tlb_up(const TlInst* __restrict__ insts, int l) {
   const TlInst& v = insts[blockIdx.y];
-  if (l + 1 >= v.nl || tlb_skip(v)) return;
+  if (l >= v.tail0 || tlb_skip(v)) return;
   const int t = tl_tiles(v.lev[l].m + 1, kTlUp);
   if ((int)blockIdx.x >= t * t) return;
   tl_up_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x % t, blockIdx.x / t);
@@ -839,6 +997,7 @@ struct TwoLevel {
   float* cp = nullptr;    // [4][noe] corner sums
   float* ainv = nullptr;  // coarsest level's dense inverse
   std::vector<TlLev<float>> lev;
+  int tail0 = 0;          // first level of the one-block tail
   std::vector<void*> allocs;
   ~TwoLevel() {
     for (void* a : allocs) cudaFree(a);
@@ -1003,6 +1162,9 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
     d.wd = wd;
     tl.lev.push_back(d);
   }
+  std::vector<int> ms;
+  for (const TlLev<float>& L : tl.lev) ms.push_back(L.m);
+  tl.tail0 = tl_tail_level(ms.data(), (int)ms.size());
   // the coarsest level's dense inverse
   const HostLevel& Lc = H.back();
   const int cn1 = Lc.m + 1, cnv = cn1 * cn1;
@@ -1059,14 +1221,17 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
   const size_t noe = (size_t)dim * dim;
   SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, done, s)
   count_launch();
-  for (int l = 0; l + 1 < nl; ++l) {
+  const int l0 = tl.tail0;
+  for (int l = 0; l < l0; ++l) {
     const int t = tl_tiles(tl.lev[l + 1].m + 1, kTlDown);
     k_tl_down<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], l == 0 ? tl.cp : nullptr, dim, done);
     count_launch();
   }
-  k_tl_dense<float><<<1, kTlVecThreads, 0, s>>>(tl.lev[nl - 1], tl.ainv, nl == 1 ? tl.cp : nullptr, dim, done);
+  TlLevels<float> levels{};
+  for (int l = 0; l < nl; ++l) levels.lev[l] = tl.lev[l];
+  k_tl_tail<float><<<1, kTlTailThreads, 0, s>>>(levels, l0, nl, tl.ainv, tl.cp, dim, done);
   count_launch();
-  for (int l = nl - 2; l >= 0; --l) {
+  for (int l = l0 - 1; l >= 0; --l) {
     const int t = tl_tiles(tl.lev[l].m + 1, kTlUp);
     k_tl_up<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
     count_launch();
@@ -1117,6 +1282,7 @@ TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* 
   v.dim = tl.dim;
   v.p = tl.p;
   v.nl = (int)tl.lev.size();
+  v.tail0 = tl.tail0;
   v.nblk = tl_grid((size_t)tl.dim * tl.dim, kTlElemThreads, red.capacity);
   float* q = scratch;
   v.cp = q;
@@ -1138,6 +1304,7 @@ TlPlan twolevel_plan(const TlInst* h, const HostTables* const* tabs, int n) {
   for (int i = 0; i < n; ++i) {
     plan.maxl = std::max(plan.maxl, h[i].nl);
     plan.nblk_max = std::max(plan.nblk_max, h[i].nblk);
+    plan.max_tail0 = std::max(plan.max_tail0, h[i].tail0);
     if ((int)plan.side_max.size() < h[i].nl) plan.side_max.resize(h[i].nl, 0);
     for (int l = 0; l < h[i].nl; ++l) plan.side_max[l] = std::max(plan.side_max[l], h[i].lev[l].m + 1);
     if (plan.groups.empty() || plan.groups.back().p != h[i].p) plan.groups.push_back({h[i].p, i, 0, 0, tabs[i]});
@@ -1177,13 +1344,13 @@ sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaSt
     const int t = tl_tiles(plan.side_max[l], tile);
     return dim3(t * t, n);
   };
-  for (int l = 0; l + 1 < plan.maxl; ++l) {
+  for (int l = 0; l < plan.max_tail0; ++l) {
     k_tlb_down<<<tiles(l + 1, kTlDown), kTlTileThreads, 0, s>>>(d, l);
     count_launch();
   }
-  k_tlb_dense<<<dim3(1, n), kTlVecThreads, 0, s>>>(d);
+  k_tlb_tail<<<dim3(1, n), kTlTailThreads, 0, s>>>(d);
   count_launch();
-  for (int l = plan.maxl - 2; l >= 0; --l) {
+  for (int l = plan.max_tail0 - 1; l >= 0; --l) {
     k_tlb_up<<<tiles(l, kTlUp), kTlTileThreads, 0, s>>>(d, l);
     count_launch();
   }
