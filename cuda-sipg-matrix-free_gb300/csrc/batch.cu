@@ -562,8 +562,13 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
     k_fcg_direction_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
     count_launch(2);
     SIPG_CUDA_TRY(cudaGetLastError());
-    st = batch_apply64(b, sel, APPLY_DOT_PIVOT, d_x, d_b, s);
-    if (st != SIPG_OK) return st;
+    {
+      std::vector<int> piv, plain;
+      for (int k : sel) (rel[k] > kFcgPivotRel ? piv : plain).push_back(k);
+      if (!piv.empty()) st = batch_apply64(b, piv, APPLY_DOT_PIVOT, d_x, d_b, s);
+      if (st == SIPG_OK && !plain.empty()) st = batch_apply64(b, plain, APPLY_DOT, d_x, d_b, s);
+      if (st != SIPG_OK) return st;
+    }
     k_fcg_update_batched<<<sg, kVecThreads, 0, s>>>(b->d_sel);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
@@ -585,6 +590,7 @@ sipg_status sipg_batch_solve_mixed(sipg_batch* b, double* const* d_x, const doub
         rel[k] = r;
         retire(k, SIPG_ERR_NOT_CONVERGED);
       } else {
+        rel[k] = r;
         cont.push_back(k);
       }
     }

@@ -509,7 +509,8 @@ sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long lo
     a.nu = v.op->pen;
     a.st = m.st64;
     a.red = m.red64;
-    SIPG_CUDA_TRY(launch_apply_f64(v.op->p, v.op->cfg64, APPLY_DOT_PIVOT, a, v.op->tab, s));
+    SIPG_CUDA_TRY(
+        launch_apply_f64(v.op->p, v.op->cfg64, v.rel > kFcgPivotRel ? APPLY_DOT_PIVOT : APPLY_DOT, a, v.op->tab, s));
     ++v.fp64_applies;
     k_cg_update<double><<<vb, kVecThreads, 0, s>>>(v.x, m.d64, m.d64, m.r64, m.q64, n, m.st64, m.red64);
     count_launch();

@@ -156,6 +156,7 @@ struct Request {
   double* Ap64 = nullptr;
   ReduceScratch red32, red64;
   int corrections = 0;        // mixed: flexible outer steps taken
+  double rel = 1.0;           // mixed: the relative residual the last outer step or check left
   int first = 1;              // mixed: the next outer step starts a direction history
   long long inner_total = 0;  // mixed: FP32 inner iterations
   int started = 0;
@@ -408,21 +409,26 @@ FcgInst fcg_of(const Request* r, sipg_server* sv) {
 // (group g's arguments from `off`, its tile starts from `toff`).
 struct GroupLaunch {
   int p;
+  int key;  // the caller's split of a degree's requests (0 unless it asks for one)
   TileCfg cfg;
   int off, m, toff, total;
   const HostTables* tab;
 };
 
-template <typename T, typename Build>
-std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArgs<T>* h_a, int* h_t, Build build) {
-  std::map<int, std::vector<Request*>> by_p;
-  for (Request* r : list) by_p[r->req.degree].push_back(r);
+// The requests of `list` grouped by (degree, key(request)), their apply
+// arguments in h_a and tile offsets in h_t.
+template <typename T, typename Build, typename Key>
+std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArgs<T>* h_a, int* h_t, Build build,
+                                     Key key) {
+  std::map<std::pair<int, int>, std::vector<Request*>> by_p;
+  for (Request* r : list) by_p[{r->req.degree, key(r)}].push_back(r);
   std::vector<GroupLaunch> out;
   int off = 0, toff = 0;
   for (auto& kv : by_p) {
     const std::vector<Request*>& g = kv.second;
     GroupLaunch gl;
-    gl.p = kv.first;
+    gl.p = kv.first.first;
+    gl.key = kv.first.second;
     gl.cfg = batched_tile((sizeof(T) == 8) ? g[0]->op->cfg64 : g[0]->op->cfg32);
     gl.off = off;
     gl.m = (int)g.size();
@@ -440,6 +446,10 @@ std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArg
   }
   return out;
 }
+template <typename T, typename Build>
+std::vector<GroupLaunch> pack_groups(const std::vector<Request*>& list, ApplyArgs<T>* h_a, int* h_t, Build build) {
+  return pack_groups<T>(list, h_a, h_t, build, [](const Request*) { return 0; });
+}
 
 template <typename T>
 sipg_status upload_groups(const std::vector<GroupLaunch>& gs, const ApplyArgs<T>* h_a, ApplyArgs<T>* d_a, const int* h_t,
@@ -451,14 +461,16 @@ sipg_status upload_groups(const std::vector<GroupLaunch>& gs, const ApplyArgs<T>
   return SIPG_OK;
 }
 
+// Launches every group in `mode` (groups of key 1: in mode_key1 when that is given).
 template <typename T>
 sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const ApplyArgs<T>* d_a, const int* d_t,
-                          cudaStream_t s) {
+                          cudaStream_t s, int mode_key1 = -1) {
   for (const GroupLaunch& g : gs) {
+    const int mode_g = (g.key == 1 && mode_key1 >= 0) ? mode_key1 : mode;
     cudaError_t e = (sizeof(T) == 8)
-                        ? launch_apply_batched_f64(g.p, g.cfg, mode, (const ApplyArgs<double>*)(d_a + g.off),
+                        ? launch_apply_batched_f64(g.p, g.cfg, mode_g, (const ApplyArgs<double>*)(d_a + g.off),
                                                    d_t + g.toff, g.m, g.total, *g.tab, s)
-                        : launch_apply_batched_f32(g.p, g.cfg, mode, (const ApplyArgs<float>*)(d_a + g.off),
+                        : launch_apply_batched_f32(g.p, g.cfg, mode_g, (const ApplyArgs<float>*)(d_a + g.off),
                                                    d_t + g.toff, g.m, g.total, *g.tab, s);
     SIPG_CUDA_TRY(e);
   }
@@ -772,9 +784,9 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
       a.st = sv->slots.d64 + r->slot;
       a.red = r->red64;
       return a;
-    });
+    }, [](const Request* r) { return r->rel > kFcgPivotRel ? 1 : 0; });
     sipg_status st = upload_groups<double>(gq, L.h_r64, L.d_r64, L.h_tr, L.d_tr, L.s);
-    if (st == SIPG_OK) st = launch_groups<double>(gq, APPLY_DOT_PIVOT, L.d_r64, L.d_tr, L.s);
+    if (st == SIPG_OK) st = launch_groups<double>(gq, APPLY_DOT, L.d_r64, L.d_tr, L.s, APPLY_DOT_PIVOT);
     if (st != SIPG_OK) return st;
     k_fcg_update_batched<<<g, kVecThreads, 0, L.s>>>(L.d_m);
     count_launch();
@@ -794,6 +806,7 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
       } else if (r->corrections >= 1000) {
         retire(sv, r, L.s, SIPG_ERR_NOT_CONVERGED, (int)r->inner_total, rel);
       } else {
+        r->rel = rel;
         cont.push_back(r);
       }
     }
@@ -826,6 +839,7 @@ sipg_status lane_finish(sipg_server* sv, Lane& L) {
                  rel);
         } else {
           r->first = 1;  // a fresh direction history from the true residual
+          r->rel = rel;
           cont.push_back(r);
         }
       }

@@ -168,6 +168,16 @@ __device__ __forceinline__ void pcg_update_body(T* __restrict__ x, const T* __re
   }
 }
 
+// The FP64 product q = A d of a flexible step is taken with pivoted sums
+// (APPLY_DOT_PIVOT) while the step starts from a relative residual above
+// this, plain sums (APPLY_DOT) below it.  Plain sums round at the scale of
+// |d|, pivoted ones at the scale of its differences: at the first steps d is
+// as large as the solution and plain rounding would leave a floor near 1e-10
+// in the recursively updated residual; once the residual is below 1e-2, |d|
+// is about that fraction of the solution and the plain rounding is that much
+// smaller.  The closing check b - A x always uses pivoted sums.
+constexpr double kFcgPivotRel = 1e-2;
+
 // ---- one solve ----
 
 static __global__ void __launch_bounds__(kVecThreads)
