@@ -44,7 +44,9 @@ THESIS_K20X_GDOFS = 1.031  # Thesis_TEXT.pdf p.54 T4.15: 1024^2, p=4, volume+flu
 # Algorithmic HBM bytes per DoF of the solver steps (each vector a kernel must
 # read or write, once):
 CG64_BYTES_PER_IT = 80       # FP64 CG iteration: apply (read r, p; write p, Ap) + update (read x, p, r, Ap; write x, r)
-FP32_INNER_BYTES_PER_IT = 40  # the same iteration on FP32 vectors
+FP32_INNER_BYTES_PER_IT = 48  # FP32 inner iteration with the two-level preconditioner: z = M r (read r, write z),
+                              # the CG-mode apply (read z, p; write p, Ap), the update (read x, p, r, Ap; write x, r);
+                              # the preconditioner's vertex levels (~1 B/DoF) are left out
 FLEX_OUTER_BYTES = 120       # flexible outer step: inner restart 16 + gamma 12 + direction 28 + FP64 apply 16 + update 48
 RESID_BYTES = 24             # r = b - A x in FP64: read x, b; write r
 RELIABLE_UPDATE_BYTES = 64   # reliable update: x += e 24, r = b - A x 24, inner restart 16

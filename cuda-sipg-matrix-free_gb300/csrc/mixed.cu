@@ -136,6 +136,9 @@ struct MixedCache {
   float* e = nullptr;
   float* p[2] = {nullptr, nullptr};
   float* Ap = nullptr;
+  float* z = nullptr;  // two-level inner kind: z = M r
+  int* nz = nullptr;       // set-up: 1 if the start vector has a non-zero entry
+  int* nz_host = nullptr;
   CgState<double>* st64 = nullptr;
   CgState<float>* st32 = nullptr;   // inner state, FP32 kind
   CgState<double>* stp = nullptr;   // inner state, pairs kind
@@ -168,6 +171,9 @@ struct MixedCache {
     cudaFree(p[0]);
     cudaFree(p[1]);
     cudaFree(Ap);
+    cudaFree(z);
+    cudaFree(nz);
+    cudaFreeHost(nz_host);
     cudaFree(st64);
     cudaFree(st32);
     cudaFree(stp);
@@ -213,6 +219,8 @@ sipg_status cache_alloc(MixedCache& m, size_t n, int cap) {
   SIPG_CUDA_TRY(cudaMallocHost(&m.st64_host, sizeof(CgState<double>)));
   SIPG_CUDA_TRY(cudaMallocHost(&m.st32_host, sizeof(CgState<float>)));
   SIPG_CUDA_TRY(cudaMallocHost(&m.stp_host, sizeof(CgState<double>)));
+  SIPG_CUDA_TRY(cudaMalloc(&m.nz, sizeof(int)));
+  SIPG_CUDA_TRY(cudaMallocHost(&m.nz_host, sizeof(int)));
   ReduceScratch* reds[2] = {&m.red64, &m.red32};
   for (ReduceScratch* r : reds) {
     SIPG_CUDA_TRY(cudaMalloc(&r->partials, sizeof(double) * cap));
@@ -259,16 +267,17 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
   a.st = m.st32;
   a.red = m.red32;
   if (kind == SIPG_INNER_F32_TWOLEVEL) {
-    // z = M r (two-level; r.z and beta), p = z + beta p, Ap and alpha, then
-    // e += alpha p, r -= alpha Ap and the stop test on r.r
-    float* z = m.p[1];
-    const sipg_status pst = twolevel_enqueue(op, m.tl, m.r, z, m.st32, m.red32, s);
+    // z = M r (two-level, from the corner sums of r that the restart or the
+    // previous update left; r.z and beta); the apply in CG mode forms
+    // p = z + beta p_old on the fly, Ap and alpha; then e += alpha p,
+    // r -= alpha Ap, the stop test on r.r and the corner sums of the new r
+    sipg_status pst = twolevel_enqueue(op, m.tl, m.r, m.z, m.st32, m.red32, s, true);
     if (pst != SIPG_OK) return pst;
-    k_cg_direction<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], z, m.n, m.st32);
-    count_launch();
-    a.in = m.p[0];
-    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_DOT, a, op->tab, s));
-    k_pcg_update_f32<<<vec_grid(m.n), kVecThreads, 0, s>>>(m.e, m.p[0], m.r, m.Ap, m.n, m.st32, m.red32);
+    a.in = m.z;
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_CG, a, op->tab, s));
+    pst = twolevel_enqueue_update(op, m.tl, m.e, m.p[0], m.p[1], m.r, m.Ap, m.st32, m.red32, s);
+    if (pst != SIPG_OK) return pst;
+    return SIPG_OK;
   } else if (kind == SIPG_INNER_F64) {
     k_cg_direction<double><<<vec_grid(m.n), kVecThreads, 0, s>>>((double*)m.p[0], (const double*)m.r, m.n, m.stp);
     count_launch();
@@ -363,7 +372,19 @@ struct Solve {
   long long inner_total = 0;
   int fp64_applies = 0;
   double rel = INFINITY;
+  bool x_zero = false;  // the start vector is zero (its residual needs no apply)
 };
+
+// The state after r = b - A x with x = 0: r.r = b.b (k_cg_init left it in bb).
+__global__ void k_resid_of_zero(CgState<double>* st) { apply_finish<double, APPLY_RESID>(st, st->bb, 0); }
+
+// flag = 1 if any x_i != 0 (every writer stores the same value)
+__global__ void __launch_bounds__(kVecThreads) k_any_nonzero(const double* __restrict__ x, size_t n, int* flag) {
+  bool nz = false;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    nz = nz || x[i] != 0.0;
+  if (__syncthreads_or(nz) && threadIdx.x == 0) *flag = 1;
+}
 
 // r64 = b - A x in FP64 (r.r into st64, it = 0), read back: with the
 // pivoted sums (APPLY_RESID_PIVOT), or the plain ones for the all-FP64
@@ -371,6 +392,18 @@ struct Solve {
 // (checking them against the other rounding floor would only slow it down).
 sipg_status true_residual(Solve& v, double* rr_out, bool plain = false) {
   MixedCache& m = *v.m;
+  if (v.x_zero) {
+    // x = 0: r = b exactly, r.r = b.b (from the set-up), no apply
+    v.x_zero = false;
+    SIPG_CUDA_TRY(cudaMemcpyAsync(m.r64, v.b, v.n * sizeof(double), cudaMemcpyDeviceToDevice, v.s));
+    k_resid_of_zero<<<1, 1, 0, v.s>>>(m.st64);
+    count_launch();
+    SIPG_CUDA_TRY(cudaGetLastError());
+    SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, v.s));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
+    *rr_out = m.st64_host->rr;
+    return SIPG_OK;
+  }
   ApplyArgs<double> a{};
   a.in = v.x;
   a.out = m.r64;
@@ -485,6 +518,10 @@ sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long lo
                                              kFlexibleInnerCap);
     count_launch();
     SIPG_CUDA_TRY(cudaGetLastError());
+    if (kind == SIPG_INNER_F32_TWOLEVEL) {
+      st = twolevel_enqueue_restrict(v.op, m.tl, m.r, s);
+      if (st != SIPG_OK) return st;
+    }
     st = run_inner(v, kind, m.st32, m.st32_host);
     if (st != SIPG_OK) return st;
     v.inner_total += m.st32_host->it;
@@ -576,6 +613,7 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
     st = twolevel_get(op, &m.tl);
     if (st != SIPG_OK) return st;
   }
+  if (kind == SIPG_INNER_F32_TWOLEVEL && !m.z) SIPG_CUDA_TRY(cudaMalloc(&m.z, n * sizeof(float)));
   const int K = n <= (1u << 20) ? 32 : 8;  // inner iterations per graph launch
   st = capture(op, m, kind, K);
   if (st != SIPG_OK) return st;
@@ -584,11 +622,15 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   SIPG_CUDA_TRY(cudaEventRecord(m.ev0, s));
   // ||b|| in FP64; the FP64 state's stop threshold outer_tol ||b||
   k_cg_init<double><<<v.vb, kVecThreads, 0, s>>>(d_b, n, m.st64, o.outer_tol, 1, 1 << 30, m.red64);
-  count_launch();
+  SIPG_CUDA_TRY(cudaMemsetAsync(m.nz, 0, sizeof(int), s));
+  k_any_nonzero<<<v.vb, kVecThreads, 0, s>>>(d_x, n, m.nz);
+  count_launch(2);
   SIPG_CUDA_TRY(cudaGetLastError());
   SIPG_CUDA_TRY(cudaMemcpyAsync(m.st64_host, m.st64, sizeof(CgState<double>), cudaMemcpyDeviceToHost, s));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(m.nz_host, m.nz, sizeof(int), cudaMemcpyDeviceToHost, s));
   SIPG_CUDA_TRY(cudaStreamSynchronize(s));
   v.bnorm = std::sqrt(m.st64_host->bb);
+  v.x_zero = *m.nz_host == 0;
   const sipg_status status = outer == SIPG_OUTER_FLEXIBLE ? solve_flexible(v, kind, o, max_inner)
                                                           : solve_reliable(v, kind, o, max_inner);
   if (status == SIPG_ERR_CUDA || status == SIPG_ERR_NOMEM) return status;

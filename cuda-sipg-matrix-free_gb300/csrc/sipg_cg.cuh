@@ -50,6 +50,20 @@ __device__ __forceinline__ void cg_bookkeep(CgState<T>* st, T total) {
   }
 }
 
+// The preconditioned inner CG's bookkeeping once r.r of the updated residual
+// is known (one thread): it, the stop test on sqrt(r.r).
+template <typename T>
+__device__ __forceinline__ void pcg_update_bookkeep(CgState<T>* st, T total) {
+  st->rres = total;
+  st->it += 1;
+  st->first = 0;
+  st->done = !(sqrt(total) > st->stop && st->it < st->max_it);
+  if (!isfinite(total)) {
+    st->status = (int)SIPG_ERR_BREAKDOWN;
+    st->done = 1;
+  }
+}
+
 // x += alpha p, r -= alpha Ap, r.r reduced; then the bookkeeping.  Block
 // `bid` of `nblocks` works on a grid-stride slice of the vectors.
 template <typename T>

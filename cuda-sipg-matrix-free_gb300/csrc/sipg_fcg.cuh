@@ -156,16 +156,8 @@ __device__ __forceinline__ void pcg_update_body(T* __restrict__ x, const T* __re
   }
   const T bt = block_sum<T, kVecThreads>(acc, sh);
   T total;
-  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0) {
-    st->rres = total;
-    st->it += 1;
-    st->first = 0;
-    st->done = !(sqrt(total) > st->stop && st->it < st->max_it);
-    if (!isfinite(total)) {
-      st->status = (int)SIPG_ERR_BREAKDOWN;
-      st->done = 1;
-    }
-  }
+  if (grid_sum_last<T, kVecThreads>(bt, red, bid, nblocks, sh, &total) && threadIdx.x == 0)
+    pcg_update_bookkeep<T>(st, total);
 }
 
 // The FP64 product q = A d of a flexible step is taken with pivoted sums
@@ -190,6 +182,16 @@ static __global__ void __launch_bounds__(kVecThreads)
 static __global__ void __launch_bounds__(kVecThreads)
     k_pcg_update_f32(float* __restrict__ x, const float* __restrict__ p, float* __restrict__ r,
                      const float* __restrict__ Ap, size_t n, CgState<float>* st, ReduceScratch red) {
+  pcg_update_body<float>(x, p, r, Ap, n, st, red, blockIdx.x, gridDim.x);
+}
+
+// The same after an apply in CG mode: p is the direction that apply just
+// wrote (pb1 if the state's parity is 1, else pb0).
+static __global__ void __launch_bounds__(kVecThreads)
+    k_pcg_update_f32_par(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
+                         float* __restrict__ r, const float* __restrict__ Ap, size_t n, CgState<float>* st,
+                         ReduceScratch red) {
+  const float* __restrict__ p = st->parity ? pb1 : pb0;
   pcg_update_body<float>(x, p, r, Ap, n, st, red, blockIdx.x, gridDim.x);
 }
 

@@ -295,8 +295,17 @@ namespace sipg {
 // capture.
 sipg_status twolevel_get(sipg_op* op, void** handle);
 // Enqueues z = M r on s in FP32; with st (an inner PCG state) every kernel is
-// skipped once st->done and the last one sets st->rr = r.z and beta.
+// skipped once st->done and the last one sets st->rr = r.z and beta.  With
+// cp_ready the restriction of r is already in place (twolevel_enqueue_restrict,
+// or the update below) and is not enqueued again.
 sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float* r, float* z, CgState<float>* st,
-                             const ReduceScratch& red, cudaStream_t s);
+                             const ReduceScratch& red, cudaStream_t s, bool cp_ready);
+sipg_status twolevel_enqueue_restrict(const sipg_op* op, const void* handle, const float* r, cudaStream_t s);
+// The inner PCG update x += alpha p, r -= alpha Ap after a CG-mode apply (p
+// by the state's parity from pb0 / pb1), r.r and the stop test, fused with
+// the restriction of the new r.
+sipg_status twolevel_enqueue_update(const sipg_op* op, const void* handle, float* x, const float* pb0,
+                                    const float* pb1, float* r, const float* Ap, CgState<float>* st,
+                                    const ReduceScratch& red, cudaStream_t s);
 int twolevel_levels(const void* handle);
 }  // namespace sipg

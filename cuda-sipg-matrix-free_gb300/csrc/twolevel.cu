@@ -125,6 +125,52 @@ __global__ void __launch_bounds__(kTlElemThreads)
   tl_restrict_elem_body<T, P>(r, cp, noe, h, blockIdx.x, gridDim.x);
 }
 
+// The inner PCG update fused with the restriction of the new residual, one
+// thread per element: x += alpha p, r -= alpha Ap (p: the direction the
+// CG-mode apply just wrote, pb1 if the state's parity is 1), r.r and the stop
+// test, and the corner sums cp of the new r that the next z = M r starts from.
+template <int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_update_restrict(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
+                         float* __restrict__ r, const float* __restrict__ Ap, float* __restrict__ cp, size_t noe,
+                         CgState<float>* st, ReduceScratch red, const __grid_constant__ TlHat<float, P> h) {
+  constexpr int N1 = P + 1;
+  __shared__ float sh[32];
+  if (*(volatile int*)&st->done) return;
+  const float alpha = st->alpha;
+  const float* __restrict__ p = st->parity ? pb1 : pb0;
+  float acc = 0.f;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < noe; e += (size_t)gridDim.x * blockDim.x) {
+    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+#pragma unroll
+    for (int i1 = 0; i1 < N1; ++i1) {
+      float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2) {
+        const size_t g = (size_t)(i1 * N1 + i2) * noe + e;
+        x[g] = fmaf(alpha, p[g], x[g]);
+        const float ri = fmaf(-alpha, Ap[g], r[g]);
+        r[g] = ri;
+        acc = fmaf(ri, ri, acc);
+        s0 = fmaf(h.l[0][i2], ri, s0);
+        s1 = fmaf(h.l[1][i2], ri, s1);
+      }
+      c00 = fmaf(h.l[0][i1], s0, c00);
+      c01 = fmaf(h.l[0][i1], s1, c01);
+      c10 = fmaf(h.l[1][i1], s0, c10);
+      c11 = fmaf(h.l[1][i1], s1, c11);
+    }
+    cp[0 * noe + e] = c00;
+    cp[1 * noe + e] = c01;
+    cp[2 * noe + e] = c10;
+    cp[3 * noe + e] = c11;
+  }
+  const float bt = block_sum<float, kTlElemThreads>(acc, sh);
+  float total;
+  if (grid_sum_last<float, kTlElemThreads>(bt, red, blockIdx.x, gridDim.x, sh, &total) && threadIdx.x == 0)
+    pcg_update_bookkeep<float>(st, total);
+}
+
 // b0 at vertex (vx, vy): the corner sums of the elements around it, in a fixed order
 template <typename T>
 __device__ __forceinline__ T tl_corner_sum(const T* __restrict__ cp, int dim, int vx, int vy) {
@@ -527,12 +573,19 @@ __device__ __forceinline__ T tl_q1(const TlHat<T, P>& h, int i1, int i2, T x00, 
   return h.l[0][i1] * (h.l[0][i2] * x00 + h.l[1][i2] * x01) + h.l[1][i1] * (h.l[0][i2] * x10 + h.l[1][i2] * x11);
 }
 
+// Floats of one factor of an element type's table (V_x, V_y or D^-1, n1^2
+// values), padded to a 16-byte multiple so that each is read as float4s.
+__host__ __device__ constexpr int tl_fdm_stride(int n1) { return (n1 * n1 + 3) & ~3; }
+
 // z = B^-1 r + P x0 (x0: the level-0 V-cycle result), B^-1 by fast
 // diagonalisation.  With R[i1][i2] the element's residual (node i1 N1 + i2)
 // and its type's factors V_x, V_y, D^-1 (fdm: [V_x | V_y | D^-1] per type),
 //   B^-1 r = V_x (D^-1 o U) V_y^T,   U = V_x^T R V_y,
-// four 1-D transforms of N1^3 multiply-adds each, done in place on the
-// element's column of shared memory with the 1-D factor in registers.
+// four 1-D transforms of N1^3 multiply-adds each, with the transform's 1-D
+// factor in registers (read as float4s) and the element's nodal block in a
+// column of shared memory between transforms: the first transform reads r
+// straight from global memory and the last writes z there, so each of the
+// two middle passes costs one shared-memory read and write per node.
 // MODE 1: also r.z = sum D^-1 o U o U + r.(P x0) and the PCG bookkeeping of
 // the inner state (first: rr = r.z; else beta = r.z / rr, rr = r.z), reduced
 // over the nb blocks of this instance.
@@ -540,36 +593,44 @@ template <typename T, int P, int MODE>
 __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0,
                                                const T* __restrict__ fdm, int dim, const TlHat<T, P>& h,
                                                CgState<T>* st, const ReduceScratch& red, int bid, int nb) {
-  constexpr int N1 = P + 1, NN = N1 * N1;
+  static_assert(sizeof(T) == 4, "the element-block factors are FP32");
+  constexpr int N1 = P + 1, NN = N1 * N1, FS = tl_fdm_stride(N1);
   __shared__ T col[NN][kTlElemThreads];
   __shared__ T sh[32];
   const int t = threadIdx.x;
   const size_t noe = (size_t)dim * dim;
   T acc = T(0);
+  T f[FS];
+  auto load_factor = [&](const T* __restrict__ src) {
+    const float4* __restrict__ s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+    for (int q = 0; q < FS / 4; ++q) {
+      const float4 v = __ldg(s4 + q);
+      f[4 * q] = v.x;
+      f[4 * q + 1] = v.y;
+      f[4 * q + 2] = v.z;
+      f[4 * q + 3] = v.w;
+    }
+  };
   const size_t tiles = (noe + kTlElemThreads - 1) / kTlElemThreads;
   for (size_t tile = bid; tile < tiles; tile += nb) {
     const size_t e = tile * kTlElemThreads + t;
     if (e >= noe) continue;
     const int row = (int)(e / dim), cl = (int)(e % dim), R = dim - 1 - row;
+    const T* __restrict__ F = fdm + (size_t)tl_elem_type(row, cl, dim) * 3 * FS;
     const T x00 = x0[R * (dim + 1) + cl], x10 = x0[R * (dim + 1) + cl + 1];
     const T x01 = x0[(R + 1) * (dim + 1) + cl], x11 = x0[(R + 1) * (dim + 1) + cl + 1];
-    const T* __restrict__ F = fdm + (size_t)tl_elem_type(row, cl, dim) * 3 * NN;
-    T f[NN], c[N1];
+    load_factor(F);  // V_x
+    // U1 = V_x^T R (along i1), R read column by column from global memory
 #pragma unroll
-    for (int k = 0; k < NN; ++k) col[k][t] = __ldg(r + (size_t)k * noe + e);
-    if (MODE == 1) {
-#pragma unroll 1
-      for (int i1 = 0; i1 < N1; ++i1)
-#pragma unroll
-        for (int i2 = 0; i2 < N1; ++i2) acc = fma(col[i1 * N1 + i2][t], tl_q1<T, P>(h, i1, i2, x00, x01, x10, x11), acc);
-    }
-#pragma unroll
-    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + k);  // V_x
-    // U1 = V_x^T R (along i1)
-#pragma unroll 1
     for (int i2 = 0; i2 < N1; ++i2) {
+      T c[N1];
 #pragma unroll
-      for (int i1 = 0; i1 < N1; ++i1) c[i1] = col[i1 * N1 + i2][t];
+      for (int i1 = 0; i1 < N1; ++i1) c[i1] = __ldg(r + (size_t)(i1 * N1 + i2) * noe + e);
+      if (MODE == 1) {
+#pragma unroll
+        for (int i1 = 0; i1 < N1; ++i1) acc = fma(c[i1], tl_q1<T, P>(h, i1, i2, x00, x01, x10, x11), acc);
+      }
 #pragma unroll
       for (int a = 0; a < N1; ++a) {
         T s = T(0);
@@ -578,22 +639,21 @@ __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __res
         col[a * N1 + i2][t] = s;
       }
     }
-#pragma unroll
-    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + NN + k);  // V_y
+    load_factor(F + FS);  // V_y
     // D^-1 o (U1 V_y), then its product with V_y^T (along i2)
 #pragma unroll 1
     for (int a = 0; a < N1; ++a) {
+      T c[N1], u[N1];
 #pragma unroll
       for (int i2 = 0; i2 < N1; ++i2) c[i2] = col[a * N1 + i2][t];
-      T u[N1];
 #pragma unroll
       for (int b = 0; b < N1; ++b) {
         T s = T(0);
 #pragma unroll
         for (int i2 = 0; i2 < N1; ++i2) s = fma(f[i2 * N1 + b], c[i2], s);
-        const T d = __ldg(F + 2 * NN + a * N1 + b);
-        if (MODE == 1) acc = fma(s * s, d, acc);
-        u[b] = s * d;
+        const T dv = __ldg(F + 2 * FS + a * N1 + b);
+        if (MODE == 1) acc = fma(s * s, dv, acc);
+        u[b] = s * dv;
       }
 #pragma unroll
       for (int i2 = 0; i2 < N1; ++i2) {
@@ -603,11 +663,11 @@ __device__ __forceinline__ void tl_finish_body(const T* __restrict__ r, T* __res
         col[a * N1 + i2][t] = s;
       }
     }
-#pragma unroll
-    for (int k = 0; k < NN; ++k) f[k] = __ldg(F + k);  // V_x
+    load_factor(F);  // V_x
     // z = V_x (...) + P x0 (along i1)
 #pragma unroll 1
     for (int i2 = 0; i2 < N1; ++i2) {
+      T c[N1];
 #pragma unroll
       for (int a = 0; a < N1; ++a) c[a] = col[a * N1 + i2][t];
 #pragma unroll
@@ -714,6 +774,13 @@ void tl_launch_restrict_elem(const HostTables& h, const T* r, T* cp, size_t noe,
                                                                                              tl_hat<T, P>(h), done);
 }
 template <typename T, int P>
+void tl_launch_update_restrict(const HostTables& h, float* x, const float* pb0, const float* pb1, float* r,
+                               const float* Ap, float* cp, size_t noe, CgState<float>* st, ReduceScratch red,
+                               cudaStream_t s) {
+  k_tl_update_restrict<P><<<tl_grid(noe, kTlElemThreads, red.capacity), kTlElemThreads, 0, s>>>(
+      x, pb0, pb1, r, Ap, cp, noe, st, red, tl_hat<float, P>(h));
+}
+template <typename T, int P>
 void tl_launch_prolong(const HostTables& h, const T* xv, T* out, int dim, cudaStream_t s) {
   k_tl_prolong<T, P><<<tl_grid((size_t)dim * dim, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(
       xv, out, dim, tl_hat<T, P>(h));
@@ -816,9 +883,9 @@ constexpr double kTlNullRel = 1e-12;
 // L_x the 1-D operator along x with its own face terms (which of the LEFT /
 // RIGHT faces are on the boundary), L_y along y.  With L V = W V Lambda and
 // V^T W V = I in each direction, B^-1 = (V_x (x) V_y) D^-1 (V_x (x) V_y)^T,
-// D = Lambda_x (x) I + I (x) Lambda_y.  out = [V_x | V_y | D^-1] (3 n1^2
-// floats; V[i][a] at i n1 + a, D^-1[a][b] at a n1 + b; zero for a null
-// mode).  False if B is not of this form (to 1e-9) or is zero.
+// D = Lambda_x (x) I + I (x) Lambda_y.  out = [V_x | V_y | D^-1], each
+// tl_fdm_stride(n1) floats (V[i][a] at i n1 + a, D^-1[a][b] at a n1 + b;
+// zero for a null mode).  False if B is not of this form (to 1e-9) or is zero.
 bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
   const int nn = n1 * n1;
   auto b = [&](int i1, int i2, int j1, int j2) { return B[(size_t)(i1 * n1 + i2) * nn + (j1 * n1 + j2)]; };
@@ -857,9 +924,10 @@ bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
     for (int i = 0; i < n1; ++i)
       for (int a = 0; a < n1; ++a) V[d][(size_t)i * n1 + a] = Q[(size_t)i * n1 + a] / std::sqrt(w[i]);
   }
+  const int fs = tl_fdm_stride(n1);
   for (int i = 0; i < nn; ++i) {
     out[i] = (float)V[0][i];
-    out[nn + i] = (float)V[1][i];
+    out[fs + i] = (float)V[1][i];
   }
   double dmax = 0.0;
   for (int a = 0; a < n1; ++a)
@@ -867,7 +935,7 @@ bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
   for (int a = 0; a < n1; ++a)
     for (int c = 0; c < n1; ++c) {
       const double dsum = lam[0][a] + lam[1][c];
-      out[2 * nn + a * n1 + c] = std::fabs(dsum) <= kTlNullRel * dmax ? 0.0f : (float)(1.0 / dsum);
+      out[2 * fs + a * n1 + c] = std::fabs(dsum) <= kTlNullRel * dmax ? 0.0f : (float)(1.0 / dsum);
     }
   return dmax > 0.0;
 }
@@ -993,7 +1061,7 @@ namespace {
 // Everything the preconditioner keeps on the device for one operator.
 struct TwoLevel {
   int dim = 0, p = 0;
-  float* fdm = nullptr;   // [16][3][nn] element block factors [V_x | V_y | D^-1]
+  float* fdm = nullptr;   // [16][3][tl_fdm_stride] element block factors [V_x | V_y | D^-1]
   float* cp = nullptr;    // [4][noe] corner sums
   float* ainv = nullptr;  // coarsest level's dense inverse
   std::vector<TlLev<float>> lev;
@@ -1052,10 +1120,11 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
   sipg_op_destroy(small);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(e);
-  table.assign((size_t)kTlTypes * 3 * nn, 0.0f);
+  const int fs = tl_fdm_stride(n1);
+  table.assign((size_t)kTlTypes * 3 * fs, 0.0f);
   for (int t = 0; t < kTlTypes; ++t) {
     if (blk[t].empty()) continue;
-    if (!tl_fdm(blk[t], op->tab.w, n1, table.data() + (size_t)t * 3 * nn)) {
+    if (!tl_fdm(blk[t], op->tab.w, n1, table.data() + (size_t)t * 3 * fs)) {
       set_error("two-level preconditioner: an element block is not of the form W (x) L_x + L_y (x) W");
       return SIPG_ERR_INVALID;
     }
@@ -1214,13 +1283,15 @@ sipg_status twolevel_get(sipg_op* op, void** out) {
 // Enqueues z = M r on s (FP32).  With st (the inner PCG state): every kernel
 // is skipped once st->done, and the last one sets r.z and beta in st.
 sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float* r, float* z, CgState<float>* st,
-                             const ReduceScratch& red, cudaStream_t s) {
+                             const ReduceScratch& red, cudaStream_t s, bool cp_ready) {
   const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
   const int* done = st ? &st->done : nullptr;
   const int dim = tl.dim, nl = (int)tl.lev.size();
   const size_t noe = (size_t)dim * dim;
-  SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, done, s)
-  count_launch();
+  if (!cp_ready) {
+    SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, done, s)
+    count_launch();
+  }
   const int l0 = tl.tail0;
   for (int l = 0; l < l0; ++l) {
     const int t = tl_tiles(tl.lev[l + 1].m + 1, kTlDown);
@@ -1237,6 +1308,31 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
     count_launch();
   }
   SIPG_TL_DISPATCH(tl_launch_finish, float, tl.p, op->tab, st ? 1 : 0, r, z, tl.lev[0].y, tl.fdm, dim, st, red, s)
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+// Enqueues the restriction of r into the preconditioner's corner sums (what a
+// twolevel_enqueue with cp_ready expects).
+sipg_status twolevel_enqueue_restrict(const sipg_op* op, const void* handle, const float* r, cudaStream_t s) {
+  const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
+  const size_t noe = (size_t)tl.dim * tl.dim;
+  SIPG_TL_DISPATCH(tl_launch_restrict_elem, float, tl.p, op->tab, r, tl.cp, noe, nullptr, s)
+  count_launch();
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+// Enqueues the inner PCG update x += alpha p, r -= alpha Ap with r.r, the stop
+// test and the restriction of the new r (the next z = M r then runs with
+// cp_ready).
+sipg_status twolevel_enqueue_update(const sipg_op* op, const void* handle, float* x, const float* pb0,
+                                    const float* pb1, float* r, const float* Ap, CgState<float>* st,
+                                    const ReduceScratch& red, cudaStream_t s) {
+  const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
+  const size_t noe = (size_t)tl.dim * tl.dim;
+  SIPG_TL_DISPATCH(tl_launch_update_restrict, float, tl.p, op->tab, x, pb0, pb1, r, Ap, tl.cp, noe, st, red, s)
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
   return SIPG_OK;
@@ -1382,5 +1478,5 @@ extern "C" sipg_status sipg_apply_twolevel_f32(sipg_op* op, const float* d_r, fl
   void* tl = nullptr;
   sipg_status st = twolevel_get(op, &tl);
   if (st != SIPG_OK) return st;
-  return twolevel_enqueue(op, tl, d_r, d_z, nullptr, ReduceScratch{}, (cudaStream_t)stream);
+  return twolevel_enqueue(op, tl, d_r, d_z, nullptr, ReduceScratch{}, (cudaStream_t)stream, false);
 }
