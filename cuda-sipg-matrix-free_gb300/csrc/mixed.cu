@@ -268,14 +268,18 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
   a.red = m.red32;
   if (kind == SIPG_INNER_F32_TWOLEVEL) {
     // z = M r (two-level, from the corner sums of r that the restart or the
-    // previous update left; r.z and beta); the apply in CG mode forms
-    // p = z + beta p_old on the fly, Ap and alpha; then e += alpha p,
-    // r -= alpha Ap, the stop test on r.r and the corner sums of the new r
+    // previous update left; r.z and beta), p = z + beta p, Ap and alpha;
+    // then e += alpha p, r -= alpha Ap, the stop test on r.r and the corner
+    // sums of the new r.  (Forming p inside the apply, its CG mode, was
+    // slower: the FP32 apply is issue-bound and the second input vector
+    // costs it more than the separate pass over p and z.)
     sipg_status pst = twolevel_enqueue(op, m.tl, m.r, m.z, m.st32, m.red32, s, true);
     if (pst != SIPG_OK) return pst;
-    a.in = m.z;
-    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_CG, a, op->tab, s));
-    pst = twolevel_enqueue_update(op, m.tl, m.e, m.p[0], m.p[1], m.r, m.Ap, m.st32, m.red32, s);
+    k_cg_direction<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], m.z, m.n, m.st32);
+    count_launch();
+    a.in = m.p[0];
+    SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_DOT, a, op->tab, s));
+    pst = twolevel_enqueue_update(op, m.tl, m.e, m.p[0], m.p[0], m.r, m.Ap, m.st32, m.red32, s);
     if (pst != SIPG_OK) return pst;
     return SIPG_OK;
   } else if (kind == SIPG_INNER_F64) {

@@ -185,16 +185,6 @@ static __global__ void __launch_bounds__(kVecThreads)
   pcg_update_body<float>(x, p, r, Ap, n, st, red, blockIdx.x, gridDim.x);
 }
 
-// The same after an apply in CG mode: p is the direction that apply just
-// wrote (pb1 if the state's parity is 1, else pb0).
-static __global__ void __launch_bounds__(kVecThreads)
-    k_pcg_update_f32_par(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
-                         float* __restrict__ r, const float* __restrict__ Ap, size_t n, CgState<float>* st,
-                         ReduceScratch red) {
-  const float* __restrict__ p = st->parity ? pb1 : pb0;
-  pcg_update_body<float>(x, p, r, Ap, n, st, red, blockIdx.x, gridDim.x);
-}
-
 static __global__ void __launch_bounds__(kVecThreads)
     k_fcg_gamma(const float* __restrict__ e, const double* __restrict__ q, size_t n, const CgState<double>* st64,
                 FcgState* fs, ReduceScratch red) {

@@ -301,9 +301,9 @@ sipg_status twolevel_get(sipg_op* op, void** handle);
 sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float* r, float* z, CgState<float>* st,
                              const ReduceScratch& red, cudaStream_t s, bool cp_ready);
 sipg_status twolevel_enqueue_restrict(const sipg_op* op, const void* handle, const float* r, cudaStream_t s);
-// The inner PCG update x += alpha p, r -= alpha Ap after a CG-mode apply (p
-// by the state's parity from pb0 / pb1), r.r and the stop test, fused with
-// the restriction of the new r.
+// The inner PCG update x += alpha p, r -= alpha Ap (p by the state's parity
+// from pb0 / pb1; the same pointer twice for a direction kept in place), r.r
+// and the stop test, fused with the restriction of the new r.
 sipg_status twolevel_enqueue_update(const sipg_op* op, const void* handle, float* x, const float* pb0,
                                     const float* pb1, float* r, const float* Ap, CgState<float>* st,
                                     const ReduceScratch& red, cudaStream_t s);

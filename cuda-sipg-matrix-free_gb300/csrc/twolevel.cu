@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(kTlElemThreads)
 }
 
 // The inner PCG update fused with the restriction of the new residual, one
-// thread per element: x += alpha p, r -= alpha Ap (p: the direction the
-// CG-mode apply just wrote, pb1 if the state's parity is 1), r.r and the stop
-// test, and the corner sums cp of the new r that the next z = M r starts from.
+// thread per element: x += alpha p, r -= alpha Ap (p: pb1 if the state's
+// parity is 1, else pb0), r.r and the stop test, and the corner sums cp of
+// the new r that the next z = M r starts from.
 template <int P>
 __global__ void __launch_bounds__(kTlElemThreads)
     k_tl_update_restrict(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
