@@ -101,19 +101,16 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_update(T* __restrict__ x, co
 // whose occupancy shared memory caps at a few CTAs per SM -- read one vector
 // instead of two, which hides most of its load latency.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_cg_direction(T* __restrict__ p, const T* __restrict__ r, size_t n,
-                                                              const CgState<T>* st) {
-  if (*(volatile const int*)&st->done) return;
-  const bool first = st->first != 0;
-  const T beta = st->beta;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
+__device__ __forceinline__ void cg_direction_body(T* __restrict__ p, const T* __restrict__ r, size_t n, bool first,
+                                                  T beta, int bid, int nblocks) {
+  const size_t stride = (size_t)nblocks * blockDim.x;
   size_t head = 0;  // FP32 with 16-byte aligned vectors: four per thread and step
   if constexpr (sizeof(T) == 4) {
     if (aligned16(p, r)) {
       head = n & ~size_t(3);
       float4* __restrict__ p4 = reinterpret_cast<float4*>(p);
       const float4* __restrict__ r4 = reinterpret_cast<const float4*>(r);
-      for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < head / 4; i += stride) {
+      for (size_t i = (size_t)bid * blockDim.x + threadIdx.x; i < head / 4; i += stride) {
         const float4 rv = r4[i];
         if (first) {
           p4[i] = rv;
@@ -128,8 +125,15 @@ __global__ void __launch_bounds__(kVecThreads) k_cg_direction(T* __restrict__ p,
       }
     }
   }
-  for (size_t i = head + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+  for (size_t i = head + (size_t)bid * blockDim.x + threadIdx.x; i < n; i += stride)
     p[i] = first ? r[i] : fma(beta, p[i], r[i]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_cg_direction(T* __restrict__ p, const T* __restrict__ r, size_t n,
+                                                              const CgState<T>* st) {
+  if (*(volatile const int*)&st->done) return;
+  cg_direction_body<T>(p, r, n, st->first != 0, st->beta, blockIdx.x, gridDim.x);
 }
 
 // Per-instance vector operands of a batch (instance = blockIdx.y).  Each

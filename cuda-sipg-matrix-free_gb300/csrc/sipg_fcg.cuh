@@ -276,11 +276,7 @@ static __global__ void __launch_bounds__(kVecThreads)
   if ((int)blockIdx.x >= v.nblk) return;
   const CgState<float>* st = v.st32;
   if (*(volatile const int*)&st->done) return;
-  const bool first = st->first != 0;
-  const float beta = st->beta;
-  const size_t stride = (size_t)v.nblk * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += stride)
-    v.p32[i] = first ? v.z32[i] : fmaf(beta, v.p32[i], v.z32[i]);
+  cg_direction_body<float>(v.p32, v.z32, v.n, st->first != 0, st->beta, blockIdx.x, v.nblk);
 }
 
 static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_pupdate_batched(const FcgInst* __restrict__ insts) {
