@@ -33,8 +33,11 @@
 // float ones; the set-up probes with the double ones.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <new>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "sipg_cg.cuh"
@@ -1086,7 +1089,33 @@ sipg_status dalloc(TwoLevel& tl, T** out, size_t count) {
 // Element block inverses by fast diagonalisation: probe the diagonal blocks
 // with the FP64 operator on a mesh of min(dim, 3) elements per side, one
 // checkerboard colour and node at a time, and factor each (tl_fdm).
+// The element-block factors depend on the degree, the penalty and (below 3
+// elements per side) the mesh, not on the mesh size: each set is probed once
+// per process and kept.
+std::mutex g_fdm_mutex;
+std::map<std::tuple<int, double, int>, std::vector<float>> g_fdm_cache;
+
+sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table);
+
 sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
+  const auto key = std::make_tuple(op->p, op->pen, std::min(op->dim, 3));
+  {
+    std::lock_guard<std::mutex> lock(g_fdm_mutex);
+    auto it = g_fdm_cache.find(key);
+    if (it != g_fdm_cache.end()) {
+      table = it->second;
+      return SIPG_OK;
+    }
+  }
+  const sipg_status st = build_blocks_probe(op, table);
+  if (st == SIPG_OK) {
+    std::lock_guard<std::mutex> lock(g_fdm_mutex);
+    g_fdm_cache[key] = table;
+  }
+  return st;
+}
+
+sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table) {
   const int p = op->p, n1 = p + 1, nn = n1 * n1, dm = std::min(op->dim, 3), noe = dm * dm;
   sipg_op* small = nullptr;
   sipg_status st = sipg_op_create(dm, p, op->pen, &small);
@@ -1134,7 +1163,7 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
 
 // The level-0 vertex operator P^T A P, probed with the FP64 operator and nine
 // colours of vertices.
-sipg_status build_level0(sipg_op* op, HostLevel& L0) {
+sipg_status build_level0_probe(sipg_op* op, HostLevel& L0) {
   const int dim = op->dim, p = op->p, n1 = dim + 1, nv = n1 * n1;
   const size_t noe = (size_t)dim * dim, n = (size_t)op->ndof;
   L0.m = dim;
@@ -1183,6 +1212,52 @@ sipg_status build_level0(sipg_op* op, HostLevel& L0) {
   cudaFree(cp);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(e);
+  return SIPG_OK;
+}
+
+// Meshes larger than this get their level-0 operator stamped from one of
+// this many elements per side.
+constexpr int kTlStampMesh = 6;
+
+// Vertex v (0..m) of a large level as the vertex of the kTlStampMesh level
+// whose row has the same entries: the two vertices at each end as they are,
+// every other one as the middle vertex.
+int tl_stamp_class(int v, int m) {
+  if (v <= 2) return v;
+  if (v >= m - 2) return kTlStampMesh - (m - v);
+  return kTlStampMesh / 2;
+}
+
+// The level-0 vertex operator of op.  Its rows are a(phi_v, phi_u) for the
+// bilinear vertex functions, which are continuous, so every jump term of the
+// SIPG form vanishes between them and only the vertices on the boundary see
+// the Nitsche terms; in 2-D the element and face terms do not depend on the
+// element size.  So every row of a mesh with more than kTlStampMesh elements
+// per side equals a row of the kTlStampMesh mesh (its two end vertices per
+// axis, or its middle one) and is copied from it: nine probes of a 6 x 6 mesh
+// instead of nine applies on the full mesh.
+sipg_status build_level0(sipg_op* op, HostLevel& L0) {
+  const int dim = op->dim;
+  if (dim <= kTlStampMesh) return build_level0_probe(op, L0);
+  sipg_op* small = nullptr;
+  sipg_status st = sipg_op_create(kTlStampMesh, op->p, op->pen, &small);
+  if (st != SIPG_OK) return st;
+  HostLevel Ls;
+  st = build_level0_probe(small, Ls);
+  sipg_op_destroy(small);
+  if (st != SIPG_OK) return st;
+  const int n1 = dim + 1, nv = n1 * n1, ns = kTlStampMesh + 1, nvs = ns * ns;
+  L0.m = dim;
+  L0.S.assign((size_t)9 * nv, 0.0);
+  host_rows(n1, [&](int lo, int hi) {
+    for (int vy = lo; vy < hi; ++vy) {
+      const int cy = tl_stamp_class(vy, dim);
+      for (int vx = 0; vx <= dim; ++vx) {
+        const int c = cy * ns + tl_stamp_class(vx, dim);
+        for (int k = 0; k < 9; ++k) L0.S[(size_t)k * nv + vy * n1 + vx] = Ls.S[(size_t)k * nvs + c];
+      }
+    }
+  });
   return SIPG_OK;
 }
 
