@@ -361,7 +361,7 @@ def run_ours(args):
         cpu = not args.no_cpu_baseline
         for key, fn in (("mixed", lambda: mixed_metrics(torch, sipg, reps=3, cpu=cpu, fp64_peak=fp64_peak)),
                         ("solve16", lambda: solve16_metrics(torch, sipg, steps=20, warmup=3, cpu=cpu)),
-                        ("serve", lambda: serve_metrics(sipg, workloads, 50.0, args.serve_requests))):
+                        ("serve", lambda: serve_metrics(sipg, workloads, 50.0, args.serve_requests, cpu=cpu))):
             smp = ClockSampler(local)
             smp.start()
             n1 = sipg.launch_count()
@@ -834,6 +834,8 @@ def _serve_stream(sipg, reqs, precision, max_active=256, budget=150 << 30):
     pending = list(reqs)
     inflight = {}
     lat, failed = [], 0
+    algo_bytes = 0.0  # algorithmic HBM bytes of the completed solves
+    dof_its = 0.0     # sum of DoF x iterations (FP64: CG iterations)
     peak_bytes = 0
     t0 = time.perf_counter()
     i = 0
@@ -857,6 +859,14 @@ def _serve_stream(sipg, reqs, precision, max_active=256, budget=150 << 30):
             if r.done:
                 if r.status == 0:
                     lat.append(r.latency_ms)
+                    _, d, p, _, _, _ = pending[inflight[rid]]
+                    nk = d * d * (p + 1) * (p + 1)
+                    if precision == sipg.F64:
+                        algo_bytes += nk * (8 + RESID_BYTES + CG64_BYTES_PER_IT * r.iterations)
+                    else:
+                        algo_bytes += nk * (8 + RESID_BYTES + FP32_INNER_BYTES_PER_IT * r.iterations +
+                                            FLEX_OUTER_BYTES * r.corrections)
+                    dof_its += nk * r.iterations
                 else:
                     failed += 1
                 srv.release(rid)
@@ -865,20 +875,48 @@ def _serve_stream(sipg, reqs, precision, max_active=256, budget=150 << 30):
     srv.close()
     lat.sort()
     q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
+    peak, src = measured_peaks()
     return {"requests": len(reqs), "completed": len(lat), "failed": failed, "wall_s": wall,
             "solves_per_s": len(lat) / wall, "p50_ms": q(0.5), "p99_ms": q(0.99), "max_ms": lat[-1] if lat else None,
             "peak_bytes_in_use": peak_bytes, "budget_bytes": budget,
-            "arrival_span_s": reqs[-1][0] if reqs else 0.0}
+            "arrival_span_s": reqs[-1][0] if reqs else 0.0,
+            "dof_iterations": dof_its,
+            "roofline": {"bound": "hbm", "achieved": algo_bytes / wall / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo_bytes / wall / 1e9 / peak, "algorithmic_bytes": algo_bytes,
+                         "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src,
+                         "note": "over the stream's wall time, arrival gaps included: the server's use of HBM, "
+                                 "not one kernel's efficiency"}}
 
 
-def serve_metrics(sipg, workloads, rate, count):
+def serve_metrics(sipg, workloads, rate, count, cpu=True):
     """The first `count` requests of the seed-3 stream at `rate` requests/s,
-    served once with every request mixed precision and once plain FP64."""
+    served once with every request mixed precision and once plain FP64; the
+    CPU baseline is the oracle's CG on all host cores, its cost per DoF and
+    iteration measured on one 256 x 256, p = 4 problem and scaled to the
+    FP64 arm's iteration counts."""
     reqs = workloads.request_stream(count=count, rate=rate, seed=3)
-    return {"rate_per_s": rate, "requests": count,
-            "stream": "the first %d of the 10,000-request stream (seed 3): Poisson arrivals at %g/s, N log-uniform "
-                      "[8,512], p in 2..8, tol in {1e-8, 1e-10}, 150 GB budget" % (count, rate),
-            "mixed": _serve_stream(sipg, reqs, sipg.F32), "fp64": _serve_stream(sipg, reqs, sipg.F64)}
+    out = {"rate_per_s": rate, "requests": count,
+           "stream": "the first %d of the 10,000-request stream (seed 3): Poisson arrivals at %g/s, N log-uniform "
+                     "[8,512], p in 2..8, tol in {1e-8, 1e-10}, 150 GB budget" % (count, rate),
+           "mixed": _serve_stream(sipg, reqs, sipg.F32), "fp64": _serve_stream(sipg, reqs, sipg.F64)}
+    if cpu and out["fp64"]["completed"]:
+        import numpy as np
+
+        import oracle_lib
+
+        orc = oracle_lib.load()
+        nthreads = os.cpu_count() or 1
+        d, p = 256, 4
+        b = np.random.default_rng(0).uniform(-1.0, 1.0, d * d * (p + 1) ** 2)
+        t0 = time.perf_counter()
+        orc.cg(p, d, float(p * p), b, 0.0, max_it=4, nthreads=nthreads)
+        per_dof_it = (time.perf_counter() - t0) / 4 / b.size
+        est = out["fp64"]["dof_iterations"] * per_dof_it
+        out["cpu_baseline"] = {"value": out["fp64"]["completed"] / est, "unit": "solves/s", "cores": nthreads,
+                               "kind": "port",
+                               "sample": "4 oracle CG iterations on 256x256, p=4 (%.3g s per DoF-iteration), "
+                                         "scaled to the FP64 arm's iterations of every request" % per_dof_it}
+    return out
 
 
 def run_serve(args):
@@ -891,7 +929,8 @@ def run_serve(args):
     sampler = ClockSampler(0)
     sampler.start()
     n0 = sipg.launch_count()
-    sweep = [serve_metrics(sipg, workloads, rate, args.requests) for rate in rates]
+    sweep = [serve_metrics(sipg, workloads, rate, args.requests, cpu=(k == 0 and not args.no_cpu_baseline))
+             for k, rate in enumerate(rates)]
     launches = sipg.launch_count() - n0
     clocks = sampler.stop()
     head = sweep[0]
