@@ -226,6 +226,7 @@ struct sipg_server {
   size_t used = 0;
   Lane lanes[kLanes];
   unsigned long long completed = 0, rejected = 0;
+  double setup_ms = 0;  // admission: operator and preconditioner set-up
 };
 
 namespace {
@@ -930,10 +931,12 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   while (!sv->queue.empty() && !sv->free_slots.empty()) {
     Request* r = sv->queue.front();
     if (sv->used + r->footprint > sv->opts.budget_bytes) break;  // FIFO: wait for memory
+    const auto t_setup = Clock::now();
     sipg_status st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &r->op);
     if (st != SIPG_OK) return st;
     Lane& L = sv->lanes[lane_of(r->n)];
     st = admit(sv, r, L.s);
+    sv->setup_ms += std::chrono::duration<double, std::milli>(Clock::now() - t_setup).count();
     sv->queue.pop_front();
     if (st != SIPG_OK) {
       // the request holds nothing (admit rolled back); it retires with the
@@ -1036,6 +1039,7 @@ sipg_status sipg_server_stats(const sipg_server* sv, sipg_server_stats_t* out) {
   out->completed = sv->completed;
   out->rejected = sv->rejected;
   out->bytes_in_use = sv->used;
+  out->setup_ms = sv->setup_ms;
   return SIPG_OK;
 }
 

@@ -390,6 +390,7 @@ typedef struct {
   unsigned long long completed;
   unsigned long long rejected;
   size_t bytes_in_use;
+  double setup_ms;  /* host time spent at admission building operators and preconditioners (cumulative) */
 } sipg_server_stats_t;
 
 typedef struct sipg_server sipg_server;
