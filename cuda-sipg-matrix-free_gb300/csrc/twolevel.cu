@@ -133,17 +133,18 @@ __global__ void __launch_bounds__(kTlElemThreads)
 // parity is 1, else pb0), r.r and the stop test, and the corner sums cp of
 // the new r that the next z = M r starts from.
 template <int P>
-__global__ void __launch_bounds__(kTlElemThreads)
-    k_tl_update_restrict(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
-                         float* __restrict__ r, const float* __restrict__ Ap, float* __restrict__ cp, size_t noe,
-                         CgState<float>* st, ReduceScratch red, const __grid_constant__ TlHat<float, P> h) {
+__device__ __forceinline__ void tl_update_restrict_body(float* __restrict__ x, const float* __restrict__ pb0,
+                                                        const float* __restrict__ pb1, float* __restrict__ r,
+                                                        const float* __restrict__ Ap, float* __restrict__ cp, size_t noe,
+                                                        CgState<float>* st, const ReduceScratch& red,
+                                                        const TlHat<float, P>& h, int bid, int nb) {
   constexpr int N1 = P + 1;
   __shared__ float sh[32];
   if (*(volatile int*)&st->done) return;
   const float alpha = st->alpha;
   const float* __restrict__ p = st->parity ? pb1 : pb0;
   float acc = 0.f;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < noe; e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = (size_t)bid * blockDim.x + threadIdx.x; e < noe; e += (size_t)nb * blockDim.x) {
     float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
 #pragma unroll
     for (int i1 = 0; i1 < N1; ++i1) {
@@ -170,8 +171,16 @@ __global__ void __launch_bounds__(kTlElemThreads)
   }
   const float bt = block_sum<float, kTlElemThreads>(acc, sh);
   float total;
-  if (grid_sum_last<float, kTlElemThreads>(bt, red, blockIdx.x, gridDim.x, sh, &total) && threadIdx.x == 0)
+  if (grid_sum_last<float, kTlElemThreads>(bt, red, bid, nb, sh, &total) && threadIdx.x == 0)
     pcg_update_bookkeep<float>(st, total);
+}
+
+template <int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tl_update_restrict(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
+                         float* __restrict__ r, const float* __restrict__ Ap, float* __restrict__ cp, size_t noe,
+                         CgState<float>* st, ReduceScratch red, const __grid_constant__ TlHat<float, P> h) {
+  tl_update_restrict_body<P>(x, pb0, pb1, r, Ap, cp, noe, st, red, h, blockIdx.x, gridDim.x);
 }
 
 // b0 at vertex (vx, vy): the corner sums of the elements around it, in a fixed order
@@ -734,6 +743,14 @@ __global__ void __launch_bounds__(kTlTileThreads) k_tlb_up(const TlInst* __restr
   const int t = tl_tiles(v.lev[l].m + 1, kTlUp);
   if ((int)blockIdx.x >= t * t) return;
   tl_up_body<float>(v.lev[l], v.lev[l + 1], blockIdx.x % t, blockIdx.x / t);
+}
+template <int P>
+__global__ void __launch_bounds__(kTlElemThreads)
+    k_tlb_update_restrict(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
+  const TlInst& v = insts[first + blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  tl_update_restrict_body<P>(v.e, v.pdir, v.pdir, v.r, v.Ap, v.cp, (size_t)v.dim * v.dim, v.st,
+                             v.red, h, blockIdx.x, v.nblk);
 }
 template <int P>
 __global__ void __launch_bounds__(kTlElemThreads)
@@ -1440,12 +1457,15 @@ size_t twolevel_scratch_floats(const void* handle) {
   return n;
 }
 
-TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* z, CgState<float>* st,
-                     const ReduceScratch& red) {
+TlInst twolevel_inst(const void* handle, float* scratch, float* r, float* z, CgState<float>* st,
+                     const ReduceScratch& red, float* e, const float* pdir, const float* Ap) {
   const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
   TlInst v{};
   v.r = r;
   v.z = z;
+  v.e = e;
+  v.pdir = pdir;
+  v.Ap = Ap;
   v.fdm = tl.fdm;
   v.ainv = tl.ainv;
   v.st = st;
@@ -1491,26 +1511,48 @@ void tlb_elem_launch(int which, const TlInst* d, const TlPlan::Group& g, cudaStr
   const dim3 grid(g.nblk_max, g.count);
   if (which == 0)
     k_tlb_restrict_elem<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
-  else
+  else if (which == 1)
     k_tlb_finish<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
+  else
+    k_tlb_update_restrict<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
 }
 
-sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
-  if (plan.n == 0) return SIPG_OK;
-  const int n = plan.n;
+// One batched element kernel (0: restriction, 1: finish, 2: update with
+// restriction) for every degree group of the plan.
+void tlb_elem_all(int which, const TlInst* d, const TlPlan& plan, cudaStream_t s) {
   for (const TlPlan::Group& g : plan.groups) {
     switch (g.p) {
-      case 1: tlb_elem_launch<1>(0, d, g, s); break;
-      case 2: tlb_elem_launch<2>(0, d, g, s); break;
-      case 3: tlb_elem_launch<3>(0, d, g, s); break;
-      case 4: tlb_elem_launch<4>(0, d, g, s); break;
-      case 5: tlb_elem_launch<5>(0, d, g, s); break;
-      case 6: tlb_elem_launch<6>(0, d, g, s); break;
-      case 7: tlb_elem_launch<7>(0, d, g, s); break;
-      case 8: tlb_elem_launch<8>(0, d, g, s); break;
+      case 1: tlb_elem_launch<1>(which, d, g, s); break;
+      case 2: tlb_elem_launch<2>(which, d, g, s); break;
+      case 3: tlb_elem_launch<3>(which, d, g, s); break;
+      case 4: tlb_elem_launch<4>(which, d, g, s); break;
+      case 5: tlb_elem_launch<5>(which, d, g, s); break;
+      case 6: tlb_elem_launch<6>(which, d, g, s); break;
+      case 7: tlb_elem_launch<7>(which, d, g, s); break;
+      case 8: tlb_elem_launch<8>(which, d, g, s); break;
     }
   }
   count_launch(plan.groups.size());
+}
+
+sipg_status twolevel_enqueue_restrict_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
+  if (plan.n == 0) return SIPG_OK;
+  tlb_elem_all(0, d, plan, s);
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+sipg_status twolevel_enqueue_update_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
+  if (plan.n == 0) return SIPG_OK;
+  tlb_elem_all(2, d, plan, s);
+  SIPG_CUDA_TRY(cudaGetLastError());
+  return SIPG_OK;
+}
+
+sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s, bool cp_ready) {
+  if (plan.n == 0) return SIPG_OK;
+  const int n = plan.n;
+  if (!cp_ready) tlb_elem_all(0, d, plan, s);
   auto tiles = [&](int l, int tile) {
     const int t = tl_tiles(plan.side_max[l], tile);
     return dim3(t * t, n);
@@ -1525,19 +1567,7 @@ sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaSt
     k_tlb_up<<<tiles(l, kTlUp), kTlTileThreads, 0, s>>>(d, l);
     count_launch();
   }
-  for (const TlPlan::Group& g : plan.groups) {
-    switch (g.p) {
-      case 1: tlb_elem_launch<1>(1, d, g, s); break;
-      case 2: tlb_elem_launch<2>(1, d, g, s); break;
-      case 3: tlb_elem_launch<3>(1, d, g, s); break;
-      case 4: tlb_elem_launch<4>(1, d, g, s); break;
-      case 5: tlb_elem_launch<5>(1, d, g, s); break;
-      case 6: tlb_elem_launch<6>(1, d, g, s); break;
-      case 7: tlb_elem_launch<7>(1, d, g, s); break;
-      case 8: tlb_elem_launch<8>(1, d, g, s); break;
-    }
-  }
-  count_launch(plan.groups.size());
+  tlb_elem_all(1, d, plan, s);
   SIPG_CUDA_TRY(cudaGetLastError());
   return SIPG_OK;
 }
