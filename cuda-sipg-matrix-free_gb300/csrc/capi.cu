@@ -558,8 +558,8 @@ sipg_status sipg_op_destroy(sipg_op* op) {
   if (op->mixed_free) op->mixed_free(op->mixed);
   if (op->pcg_free) op->pcg_free(op->pcg);
   if (op->tl_free) op->tl_free(op->tl);
-  cudaFree(op->stage_in);
-  cudaFree(op->stage_out);
+  if (op->stage_in) cudaFree(op->stage_in);
+  if (op->stage_out) cudaFree(op->stage_out);
   for (cudaStream_t h : op->hs)
     if (h) cudaStreamDestroy(h);
   for (cudaEvent_t e : op->hev)

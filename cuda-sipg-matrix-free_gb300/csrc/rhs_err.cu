@@ -253,13 +253,33 @@ static void mesh_axes(int dim, std::vector<double>& xcol, std::vector<double>& y
   }
 }
 
+// The same axes on the device (one thread per axis, the same additions in
+// the same order: bit-identical to mesh_axes).
+__global__ void k_mesh_axes(double* __restrict__ xcol, double* __restrict__ yrow, int dim) {
+  const double delta = 1. / (double)dim;
+  if (threadIdx.x == 0) {
+    double xx = 0;
+    for (int j = 0; j < dim; ++j) {
+      xcol[j] = xx;
+      xx += delta;
+    }
+  } else if (threadIdx.x == 1) {
+    double yy = 1;
+    for (int i = 0; i < dim; ++i) {
+      yy -= delta;
+      yrow[i] = yy;
+    }
+  }
+}
+
+// Stream-ordered throughout (no host synchronisation): a right-hand side
+// queued behind other work on s, or beside other streams' work, waits for
+// nothing.
 sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, cudaStream_t s) {
-  std::vector<double> xc, yr;
-  mesh_axes(op->dim, xc, yr);
   double* d_axes = nullptr;
   SIPG_CUDA_TRY(cudaMallocAsync((void**)&d_axes, sizeof(double) * 2 * op->dim, s));
-  SIPG_CUDA_TRY(cudaMemcpyAsync(d_axes, xc.data(), sizeof(double) * op->dim, cudaMemcpyHostToDevice, s));
-  SIPG_CUDA_TRY(cudaMemcpyAsync(d_axes + op->dim, yr.data(), sizeof(double) * op->dim, cudaMemcpyHostToDevice, s));
+  k_mesh_axes<<<1, 2, 0, s>>>(d_axes, d_axes + op->dim, op->dim);
+  count_launch();
   ProblemArgs pa;
   pa.sol = sol;
   std::memset(&pa.modes, 0, sizeof(pa.modes));
@@ -269,8 +289,6 @@ sipg_status rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double*
   k_rhs<<<blocks, threads, 0, s>>>(d_b, op->p, op->dim, op->pen, pa, tb, d_axes, d_axes + op->dim);
   count_launch();
   SIPG_CUDA_TRY(cudaGetLastError());
-  // the host vectors xc/yr must outlive the async copies
-  SIPG_CUDA_TRY(cudaStreamSynchronize(s));
   SIPG_CUDA_TRY(cudaFreeAsync(d_axes, s));
   return SIPG_OK;
 }

@@ -1112,9 +1112,9 @@ sipg_status dalloc(TwoLevel& tl, T** out, size_t count) {
 std::mutex g_fdm_mutex;
 std::map<std::tuple<int, double, int>, std::vector<float>> g_fdm_cache;
 
-sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table);
+sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table, cudaStream_t ss);
 
-sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
+sipg_status build_blocks(sipg_op* op, std::vector<float>& table, cudaStream_t ss) {
   const auto key = std::make_tuple(op->p, op->pen, std::min(op->dim, 3));
   {
     std::lock_guard<std::mutex> lock(g_fdm_mutex);
@@ -1124,7 +1124,7 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
       return SIPG_OK;
     }
   }
-  const sipg_status st = build_blocks_probe(op, table);
+  const sipg_status st = build_blocks_probe(op, table, ss);
   if (st == SIPG_OK) {
     std::lock_guard<std::mutex> lock(g_fdm_mutex);
     g_fdm_cache[key] = table;
@@ -1132,7 +1132,7 @@ sipg_status build_blocks(sipg_op* op, std::vector<float>& table) {
   return st;
 }
 
-sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table) {
+sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table, cudaStream_t ss) {
   const int p = op->p, n1 = p + 1, nn = n1 * n1, dm = std::min(op->dim, 3), noe = dm * dm;
   sipg_op* small = nullptr;
   sipg_status st = sipg_op_create(dm, p, op->pen, &small);
@@ -1141,18 +1141,19 @@ sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table) {
   double *dx = nullptr, *dy = nullptr;
   std::vector<double> hx(n), hy(n);
   std::vector<std::vector<double>> blk(kTlTypes);
-  cudaError_t e = cudaMalloc(&dx, n * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&dy, n * sizeof(double));
+  cudaError_t e = cudaMallocAsync(&dx, n * sizeof(double), ss);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dy, n * sizeof(double), ss);
   for (int color = 0; color < 2 && e == cudaSuccess && st == SIPG_OK; ++color)
     for (int k = 0; k < nn && e == cudaSuccess && st == SIPG_OK; ++k) {
       std::fill(hx.begin(), hx.end(), 0.0);
       for (int el = 0; el < noe; ++el)
         if (((el / dm) + (el % dm)) % 2 == color) hx[(size_t)k * noe + el] = 1.0;
-      e = cudaMemcpy(dx, hx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(dx, hx.data(), n * sizeof(double), cudaMemcpyHostToDevice, ss);
       if (e != cudaSuccess) break;
-      st = sipg_apply_f64(small, dx, dy, nullptr);
+      st = sipg_apply_f64(small, dx, dy, ss);
       if (st != SIPG_OK) break;
-      e = cudaMemcpy(hy.data(), dy, n * sizeof(double), cudaMemcpyDeviceToHost);
+      e = cudaMemcpyAsync(hy.data(), dy, n * sizeof(double), cudaMemcpyDeviceToHost, ss);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ss);
       if (e != cudaSuccess) break;
       for (int el = 0; el < noe; ++el) {
         if (((el / dm) + (el % dm)) % 2 != color) continue;
@@ -1161,8 +1162,8 @@ sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table) {
         for (int j = 0; j < nn; ++j) B[(size_t)j * nn + k] = hy[(size_t)j * noe + el];
       }
     }
-  cudaFree(dx);
-  cudaFree(dy);
+  if (dx) cudaFreeAsync(dx, ss);
+  if (dy) cudaFreeAsync(dy, ss);
   sipg_op_destroy(small);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(e);
@@ -1180,34 +1181,35 @@ sipg_status build_blocks_probe(sipg_op* op, std::vector<float>& table) {
 
 // The level-0 vertex operator P^T A P, probed with the FP64 operator and nine
 // colours of vertices.
-sipg_status build_level0_probe(sipg_op* op, HostLevel& L0) {
+sipg_status build_level0_probe(sipg_op* op, HostLevel& L0, cudaStream_t ss) {
   const int dim = op->dim, p = op->p, n1 = dim + 1, nv = n1 * n1;
   const size_t noe = (size_t)dim * dim, n = (size_t)op->ndof;
   L0.m = dim;
   L0.S.assign((size_t)9 * nv, 0.0);
   double *xv = nullptr, *xd = nullptr, *yd = nullptr, *cp = nullptr, *yv = nullptr;
-  cudaError_t e = cudaMalloc(&xv, nv * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&yv, nv * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&xd, n * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&yd, n * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&cp, 4 * noe * sizeof(double));
+  cudaError_t e = cudaMallocAsync(&xv, nv * sizeof(double), ss);
+  if (e == cudaSuccess) e = cudaMallocAsync(&yv, nv * sizeof(double), ss);
+  if (e == cudaSuccess) e = cudaMallocAsync(&xd, n * sizeof(double), ss);
+  if (e == cudaSuccess) e = cudaMallocAsync(&yd, n * sizeof(double), ss);
+  if (e == cudaSuccess) e = cudaMallocAsync(&cp, 4 * noe * sizeof(double), ss);
   std::vector<double> hx(nv);
   std::vector<std::vector<double>> hys(9, std::vector<double>(nv));
   sipg_status st = SIPG_OK;
   for (int c = 0; c < 9 && e == cudaSuccess && st == SIPG_OK; ++c) {
     const int cx = c % 3, cy = c / 3;
     for (int v = 0; v < nv; ++v) hx[v] = ((v % n1) % 3 == cx && (v / n1) % 3 == cy) ? 1.0 : 0.0;
-    e = cudaMemcpy(xv, hx.data(), nv * sizeof(double), cudaMemcpyHostToDevice);
+    e = cudaMemcpyAsync(xv, hx.data(), nv * sizeof(double), cudaMemcpyHostToDevice, ss);
     if (e != cudaSuccess) break;
-    SIPG_TL_DISPATCH(tl_launch_prolong, double, p, op->tab, xv, xd, dim, (cudaStream_t)0)
+    SIPG_TL_DISPATCH(tl_launch_prolong, double, p, op->tab, xv, xd, dim, ss)
     count_launch();
-    st = sipg_apply_f64(op, xd, yd, nullptr);
+    st = sipg_apply_f64(op, xd, yd, ss);
     if (st != SIPG_OK) break;
-    SIPG_TL_DISPATCH(tl_launch_restrict_elem, double, p, op->tab, yd, cp, noe, (const int*)nullptr, (cudaStream_t)0)
-    k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads>>>(cp, yv, dim);
+    SIPG_TL_DISPATCH(tl_launch_restrict_elem, double, p, op->tab, yd, cp, noe, (const int*)nullptr, ss)
+    k_tl_restrict_vert<double><<<tl_grid(nv, kTlVecThreads, 1 << 30), kTlVecThreads, 0, ss>>>(cp, yv, dim);
     count_launch(2);
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(hys[c].data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hys[c].data(), yv, nv * sizeof(double), cudaMemcpyDeviceToHost, ss);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ss);
     if (e != cudaSuccess) break;
   }
   if (e == cudaSuccess && st == SIPG_OK)  // entry (v, u) is probe colour(u)'s result at v
@@ -1222,11 +1224,8 @@ sipg_status build_level0_probe(sipg_op* op, HostLevel& L0) {
                   hys[(uy % 3) * 3 + ux % 3][vy * n1 + vx];
             }
     });
-  cudaFree(xv);
-  cudaFree(yv);
-  cudaFree(xd);
-  cudaFree(yd);
-  cudaFree(cp);
+  for (double* q : {xv, yv, xd, yd, cp})
+    if (q) cudaFreeAsync(q, ss);
   if (st != SIPG_OK) return st;
   SIPG_CUDA_TRY(e);
   return SIPG_OK;
@@ -1253,14 +1252,14 @@ int tl_stamp_class(int v, int m) {
 // per side equals a row of the kTlStampMesh mesh (its two end vertices per
 // axis, or its middle one) and is copied from it: nine probes of a 6 x 6 mesh
 // instead of nine applies on the full mesh.
-sipg_status build_level0(sipg_op* op, HostLevel& L0) {
+sipg_status build_level0(sipg_op* op, HostLevel& L0, cudaStream_t ss) {
   const int dim = op->dim;
-  if (dim <= kTlStampMesh) return build_level0_probe(op, L0);
+  if (dim <= kTlStampMesh) return build_level0_probe(op, L0, ss);
   sipg_op* small = nullptr;
   sipg_status st = sipg_op_create(kTlStampMesh, op->p, op->pen, &small);
   if (st != SIPG_OK) return st;
   HostLevel Ls;
-  st = build_level0_probe(small, Ls);
+  st = build_level0_probe(small, Ls, ss);
   sipg_op_destroy(small);
   if (st != SIPG_OK) return st;
   const int n1 = dim + 1, nv = n1 * n1, ns = kTlStampMesh + 1, nvs = ns * ns;
@@ -1278,22 +1277,36 @@ sipg_status build_level0(sipg_op* op, HostLevel& L0) {
   return SIPG_OK;
 }
 
+// The set-up runs on a stream of its own with stream-ordered temporaries and
+// waits only for that stream: an operator built while other streams of the
+// process have work in flight (a serving lane's round) does not wait for it.
+sipg_status build_on(sipg_op* op, TwoLevel& tl, cudaStream_t ss);
+
 sipg_status build(sipg_op* op, TwoLevel& tl) {
+  cudaStream_t ss = nullptr;
+  SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking));
+  const sipg_status st = build_on(op, tl, ss);
+  const cudaError_t e = cudaStreamSynchronize(ss);  // host staging below outlives every copy
+  cudaStreamDestroy(ss);
+  if (st != SIPG_OK) return st;
+  SIPG_CUDA_TRY(e);
+  return SIPG_OK;
+}
+
+sipg_status build_on(sipg_op* op, TwoLevel& tl, cudaStream_t ss) {
   tl.dim = op->dim;
   tl.p = op->p;
-  const int nn = (op->p + 1) * (op->p + 1);
   std::vector<float> table;
-  sipg_status st = build_blocks(op, table);
+  sipg_status st = build_blocks(op, table, ss);
   if (st != SIPG_OK) return st;
   st = dalloc(tl, &tl.fdm, table.size());
   if (st != SIPG_OK) return st;
-  SIPG_CUDA_TRY(cudaMemcpy(tl.fdm, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
-  (void)nn;
+  SIPG_CUDA_TRY(cudaMemcpyAsync(tl.fdm, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
   st = dalloc(tl, &tl.cp, 4 * (size_t)op->noe);
   if (st != SIPG_OK) return st;
   // the vertex-grid hierarchy
   std::vector<HostLevel> H(1);
-  st = build_level0(op, H[0]);
+  st = build_level0(op, H[0], ss);
   if (st != SIPG_OK) return st;
   while (H.back().m > kTlCoarsestCells) {
     if ((int)H.size() >= kTlMaxLevels) {
@@ -1317,8 +1330,9 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
     std::vector<float> hs((size_t)9 * nv), hw(nv);
     for (size_t i = 0; i < hs.size(); ++i) hs[i] = (float)L.S[i];
     for (int v = 0; v < nv; ++v) hw[v] = (float)(L.omega / L.S[(size_t)4 * nv + v]);
-    SIPG_CUDA_TRY(cudaMemcpy(S, hs.data(), hs.size() * sizeof(float), cudaMemcpyHostToDevice));
-    SIPG_CUDA_TRY(cudaMemcpy(wd, hw.data(), hw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(S, hs.data(), hs.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(wd, hw.data(), hw.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
+    SIPG_CUDA_TRY(cudaStreamSynchronize(ss));  // hs, hw end with this iteration
     d.S = S;
     d.wd = wd;
     tl.lev.push_back(d);
@@ -1344,7 +1358,8 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
   std::vector<float> af(A.begin(), A.end());
   st = dalloc(tl, &tl.ainv, af.size());
   if (st != SIPG_OK) return st;
-  SIPG_CUDA_TRY(cudaMemcpy(tl.ainv, af.data(), af.size() * sizeof(float), cudaMemcpyHostToDevice));
+  SIPG_CUDA_TRY(cudaMemcpyAsync(tl.ainv, af.data(), af.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
+  SIPG_CUDA_TRY(cudaStreamSynchronize(ss));  // table and af end here
   return SIPG_OK;
 }
 

@@ -428,7 +428,9 @@ sipg_status sipg_selftest_barrier_timeout(int* gave_up);
 
 /* d_b = the right-hand side of test problem `sol` (f term + Nitsche terms of
  * the Dirichlet data u_exact).  Replaces sipg_sem_2d<T>::compute_rhs
- * (sipg_sem_2d.hpp:232-305), on the device.  `modes` is used by SIPG_SOL_MODES. */
+ * (sipg_sem_2d.hpp:232-305), on the device.  `modes` is used by SIPG_SOL_MODES.
+ * Stream-ordered: d_b is complete once the work queued on `stream` is; the
+ * call itself does not wait. */
 sipg_status sipg_rhs_f64(const sipg_op* op, int sol, const sipg_modes* modes, double* d_b, void* stream);
 /* err[0] = L2, err[1] = broken H1, err[2] = max nodal error of d_u against
  * test problem `sol`, at the LGL nodes as sipg_sem_2d<T>::err_norms
