@@ -481,6 +481,22 @@ sipg_status launch_groups(const std::vector<GroupLaunch>& gs, int mode, const Ap
 sipg_status server_alloc(sipg_server* sv) {
   const int cap = sv->opts.max_active;
   SIPG_CUDA_TRY(cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking));
+  {
+    // requests take their vectors from the device's default memory pool
+    // (stream-ordered); let it keep up to the budget mapped between
+    // synchronisations instead of returning it to the driver each time, so
+    // that an admission reuses memory rather than mapping it again
+    int dev = 0;
+    cudaMemPool_t pool = nullptr;
+    SIPG_CUDA_TRY(cudaGetDevice(&dev));
+    SIPG_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long keep = 0;  // the attribute is a 64-bit unsigned value
+    SIPG_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    if (keep < (unsigned long long)sv->opts.budget_bytes) {
+      keep = (unsigned long long)sv->opts.budget_bytes;
+      SIPG_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+  }
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d32, sizeof(CgState<float>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.d64, sizeof(CgState<double>) * cap));
   SIPG_CUDA_TRY(cudaMalloc(&sv->slots.fs, sizeof(FcgState) * cap));
