@@ -872,7 +872,7 @@ def _serve_stream(sipg, reqs, precision, max_active=256, budget=150 << 30):
                 srv.release(rid)
                 del inflight[rid]
     wall = time.perf_counter() - t0
-    setup_ms = srv.stats().setup_ms
+    setup_ms, prep_ms = srv.stats().setup_ms, srv.stats().prep_ms
     srv.close()
     lat.sort()
     q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
@@ -882,6 +882,7 @@ def _serve_stream(sipg, reqs, precision, max_active=256, budget=150 << 30):
             "peak_bytes_in_use": peak_bytes, "budget_bytes": budget,
             "arrival_span_s": reqs[-1][0] if reqs else 0.0,
             "admission_setup_s": setup_ms / 1e3,
+            "background_prep_s": prep_ms / 1e3,
             "dof_iterations": dof_its,
             "roofline": {"bound": "hbm", "achieved": algo_bytes / wall / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": algo_bytes / wall / 1e9 / peak, "algorithmic_bytes": algo_bytes,

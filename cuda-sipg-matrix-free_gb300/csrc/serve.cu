@@ -3,8 +3,9 @@
 //
 // Requests (mesh size, degree, penalty, right-hand side, relative tolerance,
 // precision) wait in a FIFO queue.  Each sipg_server_step():
-//   1. admits queued requests while their device footprint fits the budget and
-//      a state slot is free (a request larger than the whole budget is
+//   1. admits queued requests while their device footprint fits the budget,
+//      a state slot is free and (mixed requests) their preparation (below)
+//      has finished (a request larger than the whole budget is
 //      rejected); an admitted request gets its vectors from the stream-ordered
 //      pool allocator, its right-hand side built on the device, x = 0, and a
 //      slot in the device state arrays;
@@ -27,6 +28,12 @@
 // caller releases them), so memory and slots turn over while others run.
 // Meshes/operators are cached and shared; all solver state stays on the device.
 //
+// A mixed request's operator and two-level preconditioner (host probing and
+// Galerkin products, tens of milliseconds for the largest meshes) are built
+// by preparation threads from submission on, in submission order, on their
+// own streams; admission takes a request once its preparation is done, so
+// the stepping thread never waits for it while lanes have work.
+//
 // Requests run in three lanes by size (up to 2^18 DoF, up to 2^22, larger),
 // each with its own stream -- the smaller the solves, the higher the stream
 // priority -- its own descriptor staging and its own host mirror of the
@@ -37,11 +44,15 @@
 // solve's iteration.  The step blocks only when every lane with work is
 // mid-round.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <deque>
 #include <map>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 #include <vector>
@@ -163,6 +174,10 @@ struct Request {
   Clock::time_point t_submit, t_admit, t_done;
   sipg_request_result result{};
   int state = 0;  // 0 queued, 1 active, 2 done
+  // mixed requests: the operator and its preconditioner, built by a
+  // preparation thread while the request waits (0 pending, 1 done)
+  std::atomic<int> prepared{0};
+  sipg_status prep_status = SIPG_OK;
 };
 
 struct Slots {
@@ -226,7 +241,18 @@ struct sipg_server {
   size_t used = 0;
   Lane lanes[kLanes];
   unsigned long long completed = 0, rejected = 0;
-  double setup_ms = 0;  // admission: operator and preconditioner set-up
+  double setup_ms = 0;  // admission: operator and preconditioner set-up on the stepping thread
+  // preparation threads: build mixed requests' operators and preconditioners
+  // (host work and probes on their own streams) while the lanes run, in
+  // submission order
+  int device = 0;
+  std::mutex ops_mu;  // sv->ops is shared with the preparation threads
+  std::mutex prep_mu;
+  std::condition_variable prep_cv;
+  std::deque<Request*> prep_todo;
+  std::vector<std::thread> prep_workers;
+  bool prep_stop = false;
+  std::atomic<long long> prep_us{0};  // their busy time
 };
 
 namespace {
@@ -242,6 +268,7 @@ size_t footprint_of(int dim, int p, int precision) {
 }
 
 sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
+  std::lock_guard<std::mutex> lock(sv->ops_mu);
   const auto key = std::make_tuple(dim, p, pen);
   auto it = sv->ops.find(key);
   if (it != sv->ops.end()) {
@@ -255,6 +282,33 @@ sipg_status get_op(sipg_server* sv, int dim, int p, double pen, sipg_op** out) {
   *out = op;
   return SIPG_OK;
 }
+
+// A preparation thread: takes mixed requests in submission order and builds
+// each one's operator and two-level preconditioner (the first request of an
+// operator builds it; later ones find it).
+void prep_loop(sipg_server* sv) {
+  cudaSetDevice(sv->device);
+  for (;;) {
+    Request* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lock(sv->prep_mu);
+      sv->prep_cv.wait(lock, [&] { return sv->prep_stop || !sv->prep_todo.empty(); });
+      if (sv->prep_stop) return;
+      r = sv->prep_todo.front();
+      sv->prep_todo.pop_front();
+    }
+    const auto t0 = Clock::now();
+    sipg_op* op = nullptr;
+    sipg_status st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &op);
+    void* tl = nullptr;
+    if (st == SIPG_OK) st = twolevel_get(op, &tl);
+    sv->prep_us += std::chrono::duration_cast<std::chrono::microseconds>(Clock::now() - t0).count();
+    r->prep_status = st;
+    r->prepared.store(1, std::memory_order_release);
+  }
+}
+
+constexpr int kPrepThreads = 3;
 
 // Gives back what admit() took before one of its steps failed: the request
 // then holds no device memory and no slot.
@@ -489,6 +543,7 @@ sipg_status server_alloc(sipg_server* sv) {
     int dev = 0;
     cudaMemPool_t pool = nullptr;
     SIPG_CUDA_TRY(cudaGetDevice(&dev));
+    sv->device = dev;
     SIPG_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
     unsigned long long keep = 0;  // the attribute is a 64-bit unsigned value
     SIPG_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
@@ -543,6 +598,13 @@ sipg_status server_alloc(sipg_server* sv) {
 
 void server_free(sipg_server* sv) {
   if (!sv) return;
+  {
+    std::lock_guard<std::mutex> lock(sv->prep_mu);
+    sv->prep_stop = true;
+  }
+  sv->prep_cv.notify_all();
+  for (std::thread& t : sv->prep_workers) t.join();
+  sv->prep_workers.clear();
   for (Lane& L : sv->lanes)
     if (L.s) cudaStreamSynchronize(L.s);
   if (sv->s) cudaStreamSynchronize(sv->s);
@@ -909,6 +971,7 @@ sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** out) 
     server_free(sv);
     return st;
   }
+  for (int k = 0; k < kPrepThreads; ++k) sv->prep_workers.emplace_back(prep_loop, sv);
   *out = sv;
   return SIPG_OK;
 }
@@ -943,6 +1006,15 @@ sipg_status sipg_server_submit(sipg_server* sv, const sipg_request* req, unsigne
     return SIPG_ERR_REJECTED;
   }
   sv->queue.push_back(r);
+  if (r->req.precision != SIPG_F64) {
+    {
+      std::lock_guard<std::mutex> lock(sv->prep_mu);
+      sv->prep_todo.push_back(r);
+    }
+    sv->prep_cv.notify_one();
+  } else {
+    r->prepared.store(1, std::memory_order_release);
+  }
   return SIPG_OK;
 }
 
@@ -953,9 +1025,21 @@ sipg_status sipg_server_step(sipg_server* sv, int* n_active, int* n_completed) {
   while (!sv->queue.empty() && !sv->free_slots.empty()) {
     Request* r = sv->queue.front();
     if (sv->used + r->footprint > sv->opts.budget_bytes) break;  // FIFO: wait for memory
+    if (!r->prepared.load(std::memory_order_acquire)) break;     // FIFO: its preparation is still running
     const auto t_setup = Clock::now();
-    sipg_status st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &r->op);
-    if (st != SIPG_OK) return st;
+    sipg_status st = r->prep_status;
+    if (st == SIPG_OK) st = get_op(sv, r->req.dim, r->req.degree, r->req.pen, &r->op);
+    if (st != SIPG_OK) {
+      // the request retires with the error; the server goes on
+      sv->queue.pop_front();
+      r->t_admit = r->t_done = Clock::now();
+      r->result.status = st;
+      r->result.done = 1;
+      r->result.latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+      r->state = 2;
+      sv->rejected++;
+      continue;
+    }
     Lane& L = sv->lanes[lane_of(r->n)];
     st = admit(sv, r, L.s);
     sv->setup_ms += std::chrono::duration<double, std::milli>(Clock::now() - t_setup).count();
@@ -1062,6 +1146,7 @@ sipg_status sipg_server_stats(const sipg_server* sv, sipg_server_stats_t* out) {
   out->rejected = sv->rejected;
   out->bytes_in_use = sv->used;
   out->setup_ms = sv->setup_ms;
+  out->prep_ms = sv->prep_us.load() / 1e3;
   return SIPG_OK;
 }
 

@@ -68,7 +68,7 @@ class RequestResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("queued", C.c_int), ("active", C.c_int), ("completed", C.c_ulonglong), ("rejected", C.c_ulonglong),
-                ("bytes_in_use", C.c_size_t), ("setup_ms", C.c_double)]
+                ("bytes_in_use", C.c_size_t), ("setup_ms", C.c_double), ("prep_ms", C.c_double)]
 
 
 class Modes(C.Structure):

@@ -390,18 +390,23 @@ typedef struct {
   unsigned long long completed;
   unsigned long long rejected;
   size_t bytes_in_use;
-  double setup_ms;  /* host time spent at admission building operators and preconditioners (cumulative) */
+  double setup_ms;  /* admission time on the stepping thread (cumulative) */
+  double prep_ms;   /* busy time of the preparation threads that build mixed requests' operators and
+                       preconditioners while they wait (cumulative) */
 } sipg_server_stats_t;
 
 typedef struct sipg_server sipg_server;
 
-/* opts may be NULL (defaults in sipg_server_opts). */
+/* opts may be NULL (defaults in sipg_server_opts).  The server starts three
+ * preparation threads (joined by sipg_server_destroy). */
 sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** server);
 sipg_status sipg_server_destroy(sipg_server* server);
 /* Queues a request (FIFO); returns SIPG_ERR_REJECTED (and a retired result)
- * when its device footprint alone exceeds the budget. */
+ * when its device footprint alone exceeds the budget.  A mixed request's
+ * operator and two-level preconditioner are built by a preparation thread
+ * from here on, beside the lanes' work. */
 sipg_status sipg_server_submit(sipg_server* server, const sipg_request* req, unsigned long long* id);
-/* One scheduling step: admit what fits (FIFO), then for each of three
+/* One scheduling step: admit what fits and is prepared (FIFO), then for each of three
  * size-class lanes (up to 2^18 DoF, up to 2^22, larger; each on its own
  * stream, the smaller the higher its priority) whose previous round has
  * ended: correct / retire its requests and queue its next round of
