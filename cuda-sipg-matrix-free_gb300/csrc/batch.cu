@@ -268,7 +268,7 @@ static sipg_status batch_alloc(sipg_batch* b) {
   for (const BGroup& g : b->groups)
     for (int k : g.members) {
       BInst& i = b->inst[k];
-      htl.push_back(twolevel_inst(i.tl, i.tls, i.r32, i.z32, i.st32, i.red32, i.e32, i.p32, i.Ap32));
+      htl.push_back(twolevel_inst(i.tl, i.tls, i.r32, i.z32, i.st32, i.red32));
       tabs.push_back(&i.op->tab);
     }
   b->tlplan = twolevel_plan(htl.data(), tabs.data(), n);
@@ -306,12 +306,9 @@ static sipg_status batch_capture(sipg_batch* b) {
   const dim3 vg(b->bpi, b->n);
   // the launches counted while capturing are the graph's, not executed ones
   const unsigned long long c0 = g_launches.load();
-  // the corner sums of every instance's r (restarts happen between replays);
-  // each iteration's update forms them for the next
-  if (twolevel_enqueue_restrict_batched(b->d_tl, b->tlplan, b->cap) != SIPG_OK) err = cudaErrorUnknown;
   for (int k = 0; k < b->K && err == cudaSuccess; ++k) {
     // z = M r (two-level), p = z + beta p, Ap and alpha, then the update
-    if (twolevel_enqueue_batched(b->d_tl, b->tlplan, b->cap, true) != SIPG_OK) err = cudaErrorUnknown;
+    if (twolevel_enqueue_batched(b->d_tl, b->tlplan, b->cap) != SIPG_OK) err = cudaErrorUnknown;
     if (err != cudaSuccess) break;
     k_fcg_inner_pdirection_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
     count_launch();
@@ -322,7 +319,9 @@ static sipg_status batch_capture(sipg_batch* b) {
                                      b->inst[g.members[0]].op->tab, b->cap);
     }
     if (err != cudaSuccess) break;
-    if (twolevel_enqueue_update_batched(b->d_tl, b->tlplan, b->cap) != SIPG_OK) err = cudaErrorUnknown;
+    k_fcg_inner_pupdate_batched<<<vg, kVecThreads, 0, b->cap>>>(b->d_vec);
+    count_launch();
+    err = cudaGetLastError();
   }
   const unsigned long long c1 = g_launches.load();
   g_launches.fetch_sub(c1 - c0);

@@ -756,8 +756,7 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
     std::vector<const HostTables*> tabs;
     for (size_t j = 0; j < byp.size(); ++j) {
       Request* r = byp[j];
-      L.h_tl[j] = twolevel_inst(r->tl, r->tls, r->r32, r->z32, sv->slots.d32 + r->slot, r->red32, r->e32, r->p32,
-                                r->Ap32);
+      L.h_tl[j] = twolevel_inst(r->tl, r->tls, r->r32, r->z32, sv->slots.d32 + r->slot, r->red32);
       tabs.push_back(&r->op->tab);
     }
     tlplan = twolevel_plan(L.h_tl, tabs.data(), (int)byp.size());
@@ -774,24 +773,19 @@ sipg_status lane_launch(sipg_server* sv, Lane& L) {
     if (st == SIPG_OK) st = upload_groups<double>(g64, L.h_a64, L.d_a64, L.h_t64, L.d_t64, L.s);
     if (st != SIPG_OK) return st;
   }
-  if (!a32.empty()) {
-    // the corner sums of every mixed request's r (restarts happen between
-    // rounds); each iteration's update forms them for the next
-    sipg_status st = twolevel_enqueue_restrict_batched(L.d_tl, tlplan, L.s);
-    if (st != SIPG_OK) return st;
-  }
   for (int k = 0; k < sv->opts.iters_per_step; ++k) {
     if (!a32.empty()) {
       const dim3 vg(vec_bpi(nmax32, (int)a32.size()), (unsigned)a32.size());
-      sipg_status st = twolevel_enqueue_batched(L.d_tl, tlplan, L.s, true);
+      sipg_status st = twolevel_enqueue_batched(L.d_tl, tlplan, L.s);
       if (st != SIPG_OK) return st;
       k_fcg_inner_pdirection_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
       count_launch();
       SIPG_CUDA_TRY(cudaGetLastError());
       st = launch_groups<float>(g32, APPLY_DOT, L.d_a32, L.d_t32, L.s);
       if (st != SIPG_OK) return st;
-      st = twolevel_enqueue_update_batched(L.d_tl, tlplan, L.s);
-      if (st != SIPG_OK) return st;
+      k_fcg_inner_pupdate_batched<<<vg, kVecThreads, 0, L.s>>>(L.d_v32);
+      count_launch();
+      SIPG_CUDA_TRY(cudaGetLastError());
     }
     if (!a64.empty()) {
       sipg_status st = launch_groups<double>(g64, APPLY_CG, L.d_a64, L.d_t64, L.s);

@@ -267,9 +267,9 @@ static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_update_batched
   cg_update_body<float>(v.e32, v.p32, v.p32, v.r32, v.Ap32, v.n, v.st32, v.red32, blockIdx.x, v.nblk);
 }
 
-// The direction of the two-level-preconditioned inner CG: p = z + beta p
-// (first: p = z; z, r.z and beta come from the preconditioner; its update is
-// the preconditioner's fused update and restriction).
+// The same for the two-level-preconditioned inner CG: p = z + beta p (first:
+// p = z; z, r.z and beta come from the preconditioner), and the update with
+// the stop test on r.r (pcg_update_body).
 static __global__ void __launch_bounds__(kVecThreads)
     k_fcg_inner_pdirection_batched(const FcgInst* __restrict__ insts) {
   const FcgInst v = insts[blockIdx.y];
@@ -277,6 +277,12 @@ static __global__ void __launch_bounds__(kVecThreads)
   const CgState<float>* st = v.st32;
   if (*(volatile const int*)&st->done) return;
   cg_direction_body<float>(v.p32, v.z32, v.n, st->first != 0, st->beta, blockIdx.x, v.nblk);
+}
+
+static __global__ void __launch_bounds__(kVecThreads) k_fcg_inner_pupdate_batched(const FcgInst* __restrict__ insts) {
+  const FcgInst v = insts[blockIdx.y];
+  if ((int)blockIdx.x >= v.nblk) return;
+  pcg_update_body<float>(v.e32, v.p32, v.r32, v.Ap32, v.n, v.st32, v.red32, blockIdx.x, v.nblk);
 }
 
 }  // namespace sipg

@@ -26,11 +26,8 @@ struct TlLev {
 // One problem's preconditioner operands: z = M r with its own scratch (the
 // corner sums and every level's b, x, y), the op's shared tables.
 struct TlInst {
-  float* r;
+  const float* r;
   float* z;
-  float* e;            // the inner solution, direction and A p (the fused update)
-  const float* pdir;
-  const float* Ap;
   float* cp;           // [4][noe] corner sums
   const float* fdm;    // [16][3][nn] element block factors (fast diagonalisation)
   const float* ainv;   // the coarsest level's dense inverse
@@ -62,21 +59,13 @@ struct TlPlan {
 size_t twolevel_scratch_floats(const void* handle);
 size_t twolevel_scratch_floats_for(int dim);
 // An instance over `scratch` (twolevel_scratch_floats floats, 16-byte
-// aligned) for z = M r with the inner state st; e, pdir and Ap are the inner
-// solution, direction and A p that the fused update reads and writes.
-TlInst twolevel_inst(const void* handle, float* scratch, float* r, float* z, CgState<float>* st,
-                     const ReduceScratch& red, float* e, const float* pdir, const float* Ap);
+// aligned) for z = M r with the inner state st.
+TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* z, CgState<float>* st,
+                     const ReduceScratch& red);
 // The launch plan of h_insts[0..n) (degree-sorted; tabs[i]: instance i's op tables).
 TlPlan twolevel_plan(const TlInst* h_insts, const HostTables* const* tabs, int n);
 // Enqueues z = M r for every instance of d_insts (the device copy of the
-// planned array); each instance is skipped once its state says done.  With
-// cp_ready the corner sums of r are already in place and are not formed again.
-sipg_status twolevel_enqueue_batched(const TlInst* d_insts, const TlPlan& plan, cudaStream_t s, bool cp_ready);
-// The corner sums of every instance's r (before a round of iterations that
-// run with cp_ready).
-sipg_status twolevel_enqueue_restrict_batched(const TlInst* d_insts, const TlPlan& plan, cudaStream_t s);
-// The inner PCG update e += alpha p, r -= alpha Ap with r.r and the stop test,
-// fused with the restriction of the new r, for every instance.
-sipg_status twolevel_enqueue_update_batched(const TlInst* d_insts, const TlPlan& plan, cudaStream_t s);
+// planned array); each instance is skipped once its state says done.
+sipg_status twolevel_enqueue_batched(const TlInst* d_insts, const TlPlan& plan, cudaStream_t s);
 
 }  // namespace sipg

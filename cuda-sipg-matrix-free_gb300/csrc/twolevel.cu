@@ -746,14 +746,6 @@ __global__ void __launch_bounds__(kTlTileThreads) k_tlb_up(const TlInst* __restr
 }
 template <int P>
 __global__ void __launch_bounds__(kTlElemThreads)
-    k_tlb_update_restrict(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
-  const TlInst& v = insts[first + blockIdx.y];
-  if ((int)blockIdx.x >= v.nblk) return;
-  tl_update_restrict_body<P>(v.e, v.pdir, v.pdir, v.r, v.Ap, v.cp, (size_t)v.dim * v.dim, v.st,
-                             v.red, h, blockIdx.x, v.nblk);
-}
-template <int P>
-__global__ void __launch_bounds__(kTlElemThreads)
     k_tlb_finish(const TlInst* __restrict__ insts, int first, const __grid_constant__ TlHat<float, P> h) {
   const TlInst& v = insts[first + blockIdx.y];
   if ((int)blockIdx.x >= v.nblk || tlb_skip(v)) return;
@@ -1472,15 +1464,12 @@ size_t twolevel_scratch_floats(const void* handle) {
   return n;
 }
 
-TlInst twolevel_inst(const void* handle, float* scratch, float* r, float* z, CgState<float>* st,
-                     const ReduceScratch& red, float* e, const float* pdir, const float* Ap) {
+TlInst twolevel_inst(const void* handle, float* scratch, const float* r, float* z, CgState<float>* st,
+                     const ReduceScratch& red) {
   const TwoLevel& tl = *static_cast<const TwoLevel*>(handle);
   TlInst v{};
   v.r = r;
   v.z = z;
-  v.e = e;
-  v.pdir = pdir;
-  v.Ap = Ap;
   v.fdm = tl.fdm;
   v.ainv = tl.ainv;
   v.st = st;
@@ -1526,14 +1515,12 @@ void tlb_elem_launch(int which, const TlInst* d, const TlPlan::Group& g, cudaStr
   const dim3 grid(g.nblk_max, g.count);
   if (which == 0)
     k_tlb_restrict_elem<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
-  else if (which == 1)
-    k_tlb_finish<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
   else
-    k_tlb_update_restrict<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
+    k_tlb_finish<P><<<grid, kTlElemThreads, 0, s>>>(d, g.first, tl_hat<float, P>(*g.tab));
 }
 
-// One batched element kernel (0: restriction, 1: finish, 2: update with
-// restriction) for every degree group of the plan.
+// One batched element kernel (0: restriction, 1: finish) for every degree
+// group of the plan.
 void tlb_elem_all(int which, const TlInst* d, const TlPlan& plan, cudaStream_t s) {
   for (const TlPlan::Group& g : plan.groups) {
     switch (g.p) {
@@ -1550,24 +1537,10 @@ void tlb_elem_all(int which, const TlInst* d, const TlPlan& plan, cudaStream_t s
   count_launch(plan.groups.size());
 }
 
-sipg_status twolevel_enqueue_restrict_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
-  if (plan.n == 0) return SIPG_OK;
-  tlb_elem_all(0, d, plan, s);
-  SIPG_CUDA_TRY(cudaGetLastError());
-  return SIPG_OK;
-}
-
-sipg_status twolevel_enqueue_update_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
-  if (plan.n == 0) return SIPG_OK;
-  tlb_elem_all(2, d, plan, s);
-  SIPG_CUDA_TRY(cudaGetLastError());
-  return SIPG_OK;
-}
-
-sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s, bool cp_ready) {
+sipg_status twolevel_enqueue_batched(const TlInst* d, const TlPlan& plan, cudaStream_t s) {
   if (plan.n == 0) return SIPG_OK;
   const int n = plan.n;
-  if (!cp_ready) tlb_elem_all(0, d, plan, s);
+  tlb_elem_all(0, d, plan, s);
   auto tiles = [&](int l, int tile) {
     const int t = tl_tiles(plan.side_max[l], tile);
     return dim3(t * t, n);
