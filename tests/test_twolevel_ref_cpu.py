@@ -48,3 +48,37 @@ def test_twolevel_coarsening_of_odd_levels():
         xs_c = np.array([min(2 * J, m) for J in range(mc + 1)], dtype=float)
         assert np.allclose(P @ xs_c, xs_f)  # linear functions are reproduced
         assert np.allclose(P.sum(axis=1), 1.0)
+
+
+def _stamp_class(v, m, ms=6):
+    if v <= 2:
+        return v
+    if v >= m - 2:
+        return ms - (m - v)
+    return ms // 2
+
+
+def test_vertex_operator_rows_repeat_past_the_boundary(oracle):
+    """The set-up copies a large mesh's level-0 vertex operator P^T A P from a
+    6 x 6 mesh's (the two vertices at each end of an axis keep their rows,
+    every other vertex takes the middle one): the bilinear vertex functions
+    are continuous, so only boundary vertices see the Nitsche terms and the
+    element and face terms do not depend on the element size.  The probed
+    operators agree exactly."""
+    for p in (1, 2, 4, 6):
+        pen = float(p * p)
+        small = twolevel_ref.level0(oracle, p, 6, pen, twolevel_ref.prolongation(oracle, p, 6)).toarray()
+        for dim in (7, 11):
+            A = twolevel_ref.level0(oracle, p, dim, pen, twolevel_ref.prolongation(oracle, p, dim)).toarray()
+            n1 = dim + 1
+            for vy in range(n1):
+                for vx in range(n1):
+                    cy, cx = _stamp_class(vy, dim), _stamp_class(vx, dim)
+                    for dy in (-1, 0, 1):
+                        for dx in (-1, 0, 1):
+                            ux, uy = vx + dx, vy + dy
+                            if not (0 <= ux <= dim and 0 <= uy <= dim):
+                                continue
+                            got = A[vy * n1 + vx, uy * n1 + ux]
+                            want = small[cy * 7 + cx, (cy + dy) * 7 + cx + dx]
+                            assert got == want, (p, dim, vx, vy, dx, dy, got, want)
