@@ -1244,16 +1244,35 @@ int tl_stamp_class(int v, int m) {
 // per side equals a row of the kTlStampMesh mesh (its two end vertices per
 // axis, or its middle one) and is copied from it: nine probes of a 6 x 6 mesh
 // instead of nine applies on the full mesh.
+// The probed kTlStampMesh level per degree and penalty (the rows every larger
+// mesh copies), probed once per process.
+std::mutex g_stamp_mutex;
+std::map<std::pair<int, double>, HostLevel> g_stamp_cache;
+
 sipg_status build_level0(sipg_op* op, HostLevel& L0, cudaStream_t ss) {
   const int dim = op->dim;
   if (dim <= kTlStampMesh) return build_level0_probe(op, L0, ss);
-  sipg_op* small = nullptr;
-  sipg_status st = sipg_op_create(kTlStampMesh, op->p, op->pen, &small);
-  if (st != SIPG_OK) return st;
+  const auto key = std::make_pair(op->p, op->pen);
   HostLevel Ls;
-  st = build_level0_probe(small, Ls, ss);
-  sipg_op_destroy(small);
-  if (st != SIPG_OK) return st;
+  bool have = false;
+  {
+    std::lock_guard<std::mutex> lock(g_stamp_mutex);
+    auto it = g_stamp_cache.find(key);
+    if (it != g_stamp_cache.end()) {
+      Ls = it->second;
+      have = true;
+    }
+  }
+  if (!have) {
+    sipg_op* small = nullptr;
+    sipg_status st = sipg_op_create(kTlStampMesh, op->p, op->pen, &small);
+    if (st != SIPG_OK) return st;
+    st = build_level0_probe(small, Ls, ss);
+    sipg_op_destroy(small);
+    if (st != SIPG_OK) return st;
+    std::lock_guard<std::mutex> lock(g_stamp_mutex);
+    g_stamp_cache[key] = Ls;
+  }
   const int n1 = dim + 1, nv = n1 * n1, ns = kTlStampMesh + 1, nvs = ns * ns;
   L0.m = dim;
   L0.S.assign((size_t)9 * nv, 0.0);
@@ -1288,15 +1307,11 @@ sipg_status build(sipg_op* op, TwoLevel& tl) {
 sipg_status build_on(sipg_op* op, TwoLevel& tl, cudaStream_t ss) {
   tl.dim = op->dim;
   tl.p = op->p;
+  // everything on the host first: the element factors, the vertex levels,
+  // the coarsest level's inverse
   std::vector<float> table;
   sipg_status st = build_blocks(op, table, ss);
   if (st != SIPG_OK) return st;
-  st = dalloc(tl, &tl.fdm, table.size());
-  if (st != SIPG_OK) return st;
-  SIPG_CUDA_TRY(cudaMemcpyAsync(tl.fdm, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
-  st = dalloc(tl, &tl.cp, 4 * (size_t)op->noe);
-  if (st != SIPG_OK) return st;
-  // the vertex-grid hierarchy
   std::vector<HostLevel> H(1);
   st = build_level0(op, H[0], ss);
   if (st != SIPG_OK) return st;
@@ -1308,31 +1323,6 @@ sipg_status build_on(sipg_op* op, TwoLevel& tl, cudaStream_t ss) {
     H.back().omega = host_omega(H.back());
     H.push_back(host_galerkin(H.back()));
   }
-  for (const HostLevel& L : H) {
-    const int nv = (L.m + 1) * (L.m + 1);
-    TlLev<float> d{};
-    d.m = L.m;
-    float *S = nullptr, *wd = nullptr;
-    st = dalloc(tl, &S, (size_t)9 * nv);
-    if (st == SIPG_OK) st = dalloc(tl, &wd, nv);
-    if (st == SIPG_OK) st = dalloc(tl, &d.b, nv);
-    if (st == SIPG_OK) st = dalloc(tl, &d.x, nv);
-    if (st == SIPG_OK) st = dalloc(tl, &d.y, nv);
-    if (st != SIPG_OK) return st;
-    std::vector<float> hs((size_t)9 * nv), hw(nv);
-    for (size_t i = 0; i < hs.size(); ++i) hs[i] = (float)L.S[i];
-    for (int v = 0; v < nv; ++v) hw[v] = (float)(L.omega / L.S[(size_t)4 * nv + v]);
-    SIPG_CUDA_TRY(cudaMemcpyAsync(S, hs.data(), hs.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
-    SIPG_CUDA_TRY(cudaMemcpyAsync(wd, hw.data(), hw.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
-    SIPG_CUDA_TRY(cudaStreamSynchronize(ss));  // hs, hw end with this iteration
-    d.S = S;
-    d.wd = wd;
-    tl.lev.push_back(d);
-  }
-  std::vector<int> ms;
-  for (const TlLev<float>& L : tl.lev) ms.push_back(L.m);
-  tl.tail0 = tl_tail_level(ms.data(), (int)ms.size());
-  // the coarsest level's dense inverse
   const HostLevel& Lc = H.back();
   const int cn1 = Lc.m + 1, cnv = cn1 * cn1;
   std::vector<double> A((size_t)cnv * cnv, 0.0);
@@ -1348,10 +1338,61 @@ sipg_status build_on(sipg_op* op, TwoLevel& tl, cudaStream_t ss) {
     return SIPG_ERR_INVALID;
   }
   std::vector<float> af(A.begin(), A.end());
-  st = dalloc(tl, &tl.ainv, af.size());
+  std::vector<std::vector<float>> hs(H.size()), hw(H.size());
+  for (size_t l = 0; l < H.size(); ++l) {
+    const HostLevel& L = H[l];
+    const int nv = (L.m + 1) * (L.m + 1);
+    hs[l].resize((size_t)9 * nv);
+    hw[l].resize(nv);
+    for (size_t i = 0; i < hs[l].size(); ++i) hs[l][i] = (float)L.S[i];
+    for (int v = 0; v < nv; ++v) hw[l][v] = (float)(L.omega / L.S[(size_t)4 * nv + v]);
+  }
+  // one device allocation, carved in 256-byte aligned pieces
+  size_t total = 0;
+  auto piece = [&](size_t floats) {
+    const size_t at = total;
+    total += (floats * sizeof(float) + 255) & ~size_t(255);
+    return at;
+  };
+  const size_t o_fdm = piece(table.size()), o_cp = piece(4 * (size_t)op->noe), o_ainv = piece(af.size());
+  std::vector<size_t> o_lev(H.size());
+  for (size_t l = 0; l < H.size(); ++l) {
+    const size_t nv = (size_t)(H[l].m + 1) * (H[l].m + 1);
+    o_lev[l] = piece(9 * nv);
+    piece(nv);
+    piece(nv);
+    piece(nv);
+    piece(nv);
+  }
+  char* base = nullptr;
+  st = dalloc(tl, &base, total);
   if (st != SIPG_OK) return st;
+  auto at = [&](size_t off) { return reinterpret_cast<float*>(base + off); };
+  tl.fdm = at(o_fdm);
+  tl.cp = at(o_cp);
+  tl.ainv = at(o_ainv);
+  SIPG_CUDA_TRY(cudaMemcpyAsync(tl.fdm, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
   SIPG_CUDA_TRY(cudaMemcpyAsync(tl.ainv, af.data(), af.size() * sizeof(float), cudaMemcpyHostToDevice, ss));
-  SIPG_CUDA_TRY(cudaStreamSynchronize(ss));  // table and af end here
+  for (size_t l = 0; l < H.size(); ++l) {
+    const size_t nv = (size_t)(H[l].m + 1) * (H[l].m + 1);
+    const size_t step = (nv * sizeof(float) + 255) & ~size_t(255);
+    TlLev<float> d{};
+    d.m = H[l].m;
+    float* S = at(o_lev[l]);
+    float* wd = at(o_lev[l] + ((9 * nv * sizeof(float) + 255) & ~size_t(255)));
+    d.S = S;
+    d.wd = wd;
+    d.b = reinterpret_cast<float*>(reinterpret_cast<char*>(wd) + step);
+    d.x = reinterpret_cast<float*>(reinterpret_cast<char*>(wd) + 2 * step);
+    d.y = reinterpret_cast<float*>(reinterpret_cast<char*>(wd) + 3 * step);
+    SIPG_CUDA_TRY(cudaMemcpyAsync(S, hs[l].data(), hs[l].size() * sizeof(float), cudaMemcpyHostToDevice, ss));
+    SIPG_CUDA_TRY(cudaMemcpyAsync(wd, hw[l].data(), hw[l].size() * sizeof(float), cudaMemcpyHostToDevice, ss));
+    tl.lev.push_back(d);
+  }
+  std::vector<int> ms;
+  for (const TlLev<float>& L : tl.lev) ms.push_back(L.m);
+  tl.tail0 = tl_tail_level(ms.data(), (int)ms.size());
+  SIPG_CUDA_TRY(cudaStreamSynchronize(ss));  // the host staging above ends here
   return SIPG_OK;
 }
 
