@@ -308,7 +308,12 @@ void prep_loop(sipg_server* sv) {
   }
 }
 
-constexpr int kPrepThreads = 3;
+// preparation threads: up to six (a request's set-up is mostly host work,
+// tens of milliseconds at the largest meshes), fewer on a small host
+int prep_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(6u, hw / 2));
+}
 
 // Gives back what admit() took before one of its steps failed: the request
 // then holds no device memory and no slot.
@@ -965,7 +970,7 @@ sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** out) 
     server_free(sv);
     return st;
   }
-  for (int k = 0; k < kPrepThreads; ++k) sv->prep_workers.emplace_back(prep_loop, sv);
+  for (int k = 0, n = prep_threads(); k < n; ++k) sv->prep_workers.emplace_back(prep_loop, sv);
   *out = sv;
   return SIPG_OK;
 }

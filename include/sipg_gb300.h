@@ -397,8 +397,9 @@ typedef struct {
 
 typedef struct sipg_server sipg_server;
 
-/* opts may be NULL (defaults in sipg_server_opts).  The server starts three
- * preparation threads (joined by sipg_server_destroy). */
+/* opts may be NULL (defaults in sipg_server_opts).  The server starts up to
+ * six preparation threads (half the host's hardware threads; joined by
+ * sipg_server_destroy). */
 sipg_status sipg_server_create(const sipg_server_opts* opts, sipg_server** server);
 sipg_status sipg_server_destroy(sipg_server* server);
 /* Queues a request (FIFO); returns SIPG_ERR_REJECTED (and a retired result)
