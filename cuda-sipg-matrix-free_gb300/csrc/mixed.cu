@@ -275,8 +275,7 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
     // costs it more than the separate pass over p and z.)
     sipg_status pst = twolevel_enqueue(op, m.tl, m.r, m.z, m.st32, m.red32, s, true);
     if (pst != SIPG_OK) return pst;
-    SIPG_CUDA_TRY(launch_pdl(k_cg_direction<float>, dim3(vec_grid(m.n)), dim3(kVecThreads), 0, s, m.p[0],
-                             (const float*)m.z, m.n, (const CgState<float>*)m.st32));
+    k_cg_direction<float><<<vec_grid(m.n), kVecThreads, 0, s>>>(m.p[0], m.z, m.n, m.st32);
     count_launch();
     a.in = m.p[0];
     SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_DOT, a, op->tab, s));

@@ -132,7 +132,6 @@ __device__ __forceinline__ void cg_direction_body(T* __restrict__ p, const T* __
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) k_cg_direction(T* __restrict__ p, const T* __restrict__ r, size_t n,
                                                               const CgState<T>* st) {
-  pdl_begin();
   if (*(volatile const int*)&st->done) return;
   cg_direction_body<T>(p, r, n, st->first != 0, st->beta, blockIdx.x, gridDim.x);
 }

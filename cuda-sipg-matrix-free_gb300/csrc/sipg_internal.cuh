@@ -10,7 +10,6 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
-#include <utility>
 
 #include "sipg_gb300.h"
 
@@ -247,34 +246,6 @@ inline int reduce_capacity(int dim) {
 void set_error(const std::string& msg);
 extern std::atomic<unsigned long long> g_launches;
 inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
-
-// Programmatic dependent launch, for chains of short kernels in one stream:
-// launch_pdl lets the next kernel be launched while this one finishes
-// (cudaLaunchAttributeProgrammaticStreamSerialization); every kernel so
-// launched starts with pdl_begin(), which lets its own successor launch and
-// then waits until its predecessor has completed and its writes are visible
-// (griddepcontrol.wait), before it reads anything the predecessor wrote.  In
-// a kernel launched the ordinary way both instructions do nothing.
-__device__ __forceinline__ void pdl_begin() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
-template <typename... KArgs, typename... Args>
-cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                       Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
 
 #define SIPG_CUDA_TRY(call)                                                                      \
   do {                                                                                           \

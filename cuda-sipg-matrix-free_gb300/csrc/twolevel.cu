@@ -180,7 +180,6 @@ __global__ void __launch_bounds__(kTlElemThreads)
     k_tl_update_restrict(float* __restrict__ x, const float* __restrict__ pb0, const float* __restrict__ pb1,
                          float* __restrict__ r, const float* __restrict__ Ap, float* __restrict__ cp, size_t noe,
                          CgState<float>* st, ReduceScratch red, const __grid_constant__ TlHat<float, P> h) {
-  pdl_begin();
   tl_update_restrict_body<P>(x, pb0, pb1, r, Ap, cp, noe, st, red, h, blockIdx.x, gridDim.x);
 }
 
@@ -556,14 +555,12 @@ __host__ __device__ inline int tl_tiles(int verts, int tile) { return (verts + t
 template <typename T>
 __global__ void __launch_bounds__(kTlTileThreads)
     k_tl_down(TlLev<T> F, TlLev<T> C, const T* __restrict__ cp, int dim, const int* done) {
-  pdl_begin();
   if (tl_done(done)) return;
   const int t = tl_tiles(C.m + 1, kTlDown);
   tl_down_body<T>(F, C, cp, dim, blockIdx.x % t, blockIdx.x / t);
 }
 template <typename T>
 __global__ void __launch_bounds__(kTlTileThreads) k_tl_up(TlLev<T> F, TlLev<T> C, const int* done) {
-  pdl_begin();
   if (tl_done(done)) return;
   const int t = tl_tiles(F.m + 1, kTlUp);
   tl_up_body<T>(F, C, blockIdx.x % t, blockIdx.x / t);
@@ -578,7 +575,6 @@ template <typename T>
 __global__ void __launch_bounds__(kTlTailThreads)
     k_tl_tail(const __grid_constant__ TlLevels<T> L, int l0, int nl, const T* __restrict__ ainv,
               const T* __restrict__ cp, int dim, const int* done) {
-  pdl_begin();
   if (tl_done(done)) return;
   tl_tail_body<T>([&](int l) { return L.lev[l]; }, l0, nl, ainv, cp, dim);
 }
@@ -713,7 +709,6 @@ template <typename T, int P, int MODE>
 __global__ void __launch_bounds__(kTlElemThreads)
     k_tl_finish(const T* __restrict__ r, T* __restrict__ z, const T* __restrict__ x0, const T* __restrict__ fdm,
                 int dim, const __grid_constant__ TlHat<T, P> h, CgState<T>* st, ReduceScratch red) {
-  pdl_begin();
   if (MODE == 1 && *(volatile int*)&st->done) return;
   tl_finish_body<T, P, MODE>(r, z, x0, fdm, dim, h, st, red, blockIdx.x, gridDim.x);
 }
@@ -794,8 +789,8 @@ template <typename T, int P>
 void tl_launch_update_restrict(const HostTables& h, float* x, const float* pb0, const float* pb1, float* r,
                                const float* Ap, float* cp, size_t noe, CgState<float>* st, ReduceScratch red,
                                cudaStream_t s) {
-  launch_pdl(k_tl_update_restrict<P>, dim3(tl_grid(noe, kTlElemThreads, red.capacity)), dim3(kTlElemThreads), 0, s,
-             x, pb0, pb1, r, Ap, cp, noe, st, red, tl_hat<float, P>(h));
+  k_tl_update_restrict<P><<<tl_grid(noe, kTlElemThreads, red.capacity), kTlElemThreads, 0, s>>>(
+      x, pb0, pb1, r, Ap, cp, noe, st, red, tl_hat<float, P>(h));
 }
 template <typename T, int P>
 void tl_launch_prolong(const HostTables& h, const T* xv, T* out, int dim, cudaStream_t s) {
@@ -807,8 +802,8 @@ void tl_launch_finish(const HostTables& h, int mode, const T* r, T* z, const T* 
                       CgState<T>* st, ReduceScratch red, cudaStream_t s) {
   const size_t noe = (size_t)dim * dim;
   if (mode == 1)
-    launch_pdl(k_tl_finish<T, P, 1>, dim3(tl_grid(noe, kTlElemThreads, red.capacity)), dim3(kTlElemThreads), 0, s,
-               r, z, x0, fdm, dim, tl_hat<T, P>(h), st, red);
+    k_tl_finish<T, P, 1><<<tl_grid(noe, kTlElemThreads, red.capacity), kTlElemThreads, 0, s>>>(
+        r, z, x0, fdm, dim, tl_hat<T, P>(h), st, red);
   else
     k_tl_finish<T, P, 0><<<tl_grid(noe, kTlElemThreads, 152 * 32), kTlElemThreads, 0, s>>>(r, z, x0, fdm, dim,
                                                                                            tl_hat<T, P>(h), st, red);
@@ -1440,18 +1435,16 @@ sipg_status twolevel_enqueue(const sipg_op* op, const void* handle, const float*
   const int l0 = tl.tail0;
   for (int l = 0; l < l0; ++l) {
     const int t = tl_tiles(tl.lev[l + 1].m + 1, kTlDown);
-    launch_pdl(k_tl_down<float>, dim3(t * t), dim3(kTlTileThreads), 0, s, tl.lev[l], tl.lev[l + 1],
-               l == 0 ? (const float*)tl.cp : nullptr, dim, done);
+    k_tl_down<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], l == 0 ? tl.cp : nullptr, dim, done);
     count_launch();
   }
   TlLevels<float> levels{};
   for (int l = 0; l < nl; ++l) levels.lev[l] = tl.lev[l];
-  launch_pdl(k_tl_tail<float>, dim3(1), dim3(kTlTailThreads), 0, s, levels, l0, nl, (const float*)tl.ainv,
-             (const float*)tl.cp, dim, done);
+  k_tl_tail<float><<<1, kTlTailThreads, 0, s>>>(levels, l0, nl, tl.ainv, tl.cp, dim, done);
   count_launch();
   for (int l = l0 - 1; l >= 0; --l) {
     const int t = tl_tiles(tl.lev[l].m + 1, kTlUp);
-    launch_pdl(k_tl_up<float>, dim3(t * t), dim3(kTlTileThreads), 0, s, tl.lev[l], tl.lev[l + 1], done);
+    k_tl_up<float><<<t * t, kTlTileThreads, 0, s>>>(tl.lev[l], tl.lev[l + 1], done);
     count_launch();
   }
   SIPG_TL_DISPATCH(tl_launch_finish, float, tl.p, op->tab, st ? 1 : 0, r, z, tl.lev[0].y, tl.fdm, dim, st, red, s)
