@@ -33,6 +33,9 @@
 // float ones; the set-up probes with the double ones.
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <new>
@@ -952,24 +955,88 @@ bool tl_fdm(const std::vector<double>& B, const double* w, int n1, float* out) {
   return dmax > 0.0;
 }
 
-// Runs f(lo, hi) over [0, n) split across host threads when n is large (the
+// A fixed pool of host worker threads for the set-up's row loops (created on
+// first use, kept for the process): a loop is cut into one chunk per worker
+// and the caller waits for its own chunks.  Several callers (the solve
+// server's preparation threads) may share the pool; chunks never wait on
+// other chunks.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  int size() const { return (int)workers_.size(); }
+  // runs every task and returns when all have run
+  void run(std::vector<std::function<void()>>& tasks) {
+    std::mutex done_mu;
+    std::condition_variable done_cv;
+    size_t left = tasks.size();
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      for (std::function<void()>& t : tasks)
+        queue_.push_back([&t, &done_mu, &done_cv, &left] {
+          t();
+          std::lock_guard<std::mutex> l(done_mu);
+          if (--left == 0) done_cv.notify_all();
+        });
+    }
+    cv_.notify_all();
+    std::unique_lock<std::mutex> lock(done_mu);
+    done_cv.wait(lock, [&] { return left == 0; });
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (unsigned k = 0; k < hw; ++k)
+      workers_.emplace_back([this] {
+        for (;;) {
+          std::function<void()> task;
+          {
+            std::unique_lock<std::mutex> lock(mu_);
+            cv_.wait(lock, [&] { return stop_ || !queue_.empty(); });
+            if (stop_ && queue_.empty()) return;
+            task = std::move(queue_.front());
+            queue_.pop_front();
+          }
+          task();
+        }
+      });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread& t : workers_) t.join();
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> queue_;
+  std::vector<std::thread> workers_;
+  bool stop_ = false;
+};
+
+// Runs f(lo, hi) over [0, n) split across the host pool when n is large (the
 // set-up of a large mesh's hierarchy is host work proportional to its
-// vertices); each row range is written by one thread, so results do not
+// vertices); each row range is written by one chunk, so results do not
 // depend on the split.
 template <typename F>
 void host_rows(int n, F f) {
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int nt = (n >= 256 && hw > 1) ? (int)std::min<unsigned>(hw, (unsigned)(n / 64)) : 1;
+  HostPool& pool = HostPool::get();
+  const int nt = (n >= 128 && pool.size() > 1) ? std::min(pool.size(), n / 32) : 1;
   if (nt <= 1) {
     f(0, n);
     return;
   }
-  std::vector<std::thread> th;
+  std::vector<std::function<void()>> tasks;
   for (int t = 0; t < nt; ++t) {
     const int lo = (int)((long long)n * t / nt), hi = (int)((long long)n * (t + 1) / nt);
-    th.emplace_back([=] { f(lo, hi); });
+    tasks.emplace_back([=, &f] { f(lo, hi); });
   }
-  for (std::thread& t : th) t.join();
+  pool.run(tasks);
 }
 
 // Host 9-point stencil of one level: S[k * nv + v].
