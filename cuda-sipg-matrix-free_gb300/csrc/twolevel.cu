@@ -151,12 +151,22 @@ __device__ __forceinline__ void tl_update_restrict_body(float* __restrict__ x, c
     float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
 #pragma unroll
     for (int i1 = 0; i1 < N1; ++i1) {
+      // a row of nodes: every load first, so that they are in flight together
+      float xv[N1], pv[N1], rv[N1], av[N1];
+#pragma unroll
+      for (int i2 = 0; i2 < N1; ++i2) {
+        const size_t g = (size_t)(i1 * N1 + i2) * noe + e;
+        xv[i2] = x[g];
+        pv[i2] = p[g];
+        rv[i2] = r[g];
+        av[i2] = Ap[g];
+      }
       float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int i2 = 0; i2 < N1; ++i2) {
         const size_t g = (size_t)(i1 * N1 + i2) * noe + e;
-        x[g] = fmaf(alpha, p[g], x[g]);
-        const float ri = fmaf(-alpha, Ap[g], r[g]);
+        x[g] = fmaf(alpha, pv[i2], xv[i2]);
+        const float ri = fmaf(-alpha, av[i2], rv[i2]);
         r[g] = ri;
         acc = fmaf(ri, ri, acc);
         s0 = fmaf(h.l[0][i2], ri, s0);
