@@ -330,8 +330,7 @@ def run_ours(args):
         "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single GPU"),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": NDOF * 8, "d2h_bytes_per_step": NDOF * 8,
-                "steps": e2e_steps, "api": "sipg_apply_host_f64 (pinned host buffers, one apply per step: the apply reads the input from and "
-                       "writes the output to host memory across the host link)",
+                "steps": e2e_steps, "api": "sipg_apply_host_f64 (pinned host buffers, one apply per step)",
                 "matches_device_result": ok,
                 "copy_bound": {"ms_per_step": copy_ms, "gdofs": NDOF / (copy_ms * 1e-3) / 1e9,
                                "what": "the step's H2D and D2H run at once on two streams (torch copies), no apply"}},

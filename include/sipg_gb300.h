@@ -182,10 +182,8 @@ sipg_status sipg_apply_f32(const sipg_op* op, const float* d_in, float* d_out, v
  * apply loses log10(condition number) of them.  The apply of the
  * SIPG_INNER_PAIRS mixed solvers.  No reference counterpart. */
 sipg_status sipg_apply_pairs(const sipg_op* op, const float* d_in, float* d_out, void* stream);
-/* The same with host buffers, synchronously.  Page-locked, mapped buffers
- * (cudaHostAlloc, cudaHostRegister) are read and written by the apply itself
- * across the host link; other host memory is copied in and out in bands that
- * overlap the applies of earlier bands (device staging buffers kept in the op). */
+/* The same with host buffers: copies h_in to the device, applies, copies the
+ * result back, synchronously.  Device staging buffers are kept in the op. */
 sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, void* stream);
 
 /* ---- tile shapes and the autotuner (no reference counterpart: the

@@ -138,11 +138,10 @@ def test_apply_host_buffers(sipg, oracle):
 @pytest.mark.parametrize("p,d,tile", [(4, 300, None), (1, 1030, None), (6, 389, 2), (3, 260, "pernode"),
                                       (2, 515, 8), (8, 129, None)])
 def test_apply_host_buffers_banded_equals_device_apply(sipg, torch, p, d, tile):
-    """The host-buffer apply on page-locked buffers reads and writes them from
-    the kernel; on pageable ones it runs in bands of element rows (copy-in,
-    apply and copy-out overlapped), every band reading its halo rows from the
-    next band's copy.  Both results equal the device apply's bit for bit, with
-    the element tiles and the per-node tile, including ragged last bands."""
+    """The host-buffer apply runs in bands of element rows (copy-in, apply and
+    copy-out overlapped); every band reads its halo rows from the next band's
+    copy.  Its result equals the device apply's bit for bit, with the element
+    tiles and the per-node tile, including ragged last bands."""
     op = sipg.Operator(d, p, float(p * p) + 0.5)
     if tile == "pernode":
         op.set_pernode(1)
