@@ -651,30 +651,6 @@ sipg_status sipg_apply_host_f64(sipg_op* op, const double* h_in, double* h_out, 
   SIPG_CUDA_TRY(cudaSetDevice(op->device));
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = (size_t)op->ndof * sizeof(double);
-  {
-    // Host buffers the device can address (page-locked, mapped: what
-    // cudaHostAlloc / cudaHostRegister give under unified addressing): the
-    // apply reads u from and writes y to host memory itself, over the
-    // NVLink-C2C link of a Grace host, with no staging copies -- every step
-    // still moves the input and the output across the link once.
-    cudaPointerAttributes ai{}, ao{};
-    const bool mapped = cudaPointerGetAttributes(&ai, h_in) == cudaSuccess &&
-                        cudaPointerGetAttributes(&ao, h_out) == cudaSuccess && ai.type == cudaMemoryTypeHost &&
-                        ao.type == cudaMemoryTypeHost && ai.devicePointer && ao.devicePointer;
-    cudaGetLastError();  // a plain host pointer is not an error
-    int direct_ok = 0;
-    if (mapped) SIPG_CUDA_TRY(cudaDeviceGetAttribute(&direct_ok, cudaDevAttrCanUseHostPointerForRegisteredMem, op->device));
-    if (mapped && direct_ok) {
-      ApplyArgs<double> a{};
-      a.in = static_cast<const double*>(ai.devicePointer);
-      a.out = static_cast<double*>(ao.devicePointer);
-      a.dim = op->dim;
-      a.nu = op->pen;
-      SIPG_CUDA_TRY(launch_apply_f64(op->p, op->cfg64, APPLY_PLAIN, a, op->tab, s));
-      SIPG_CUDA_TRY(cudaStreamSynchronize(s));
-      return SIPG_OK;
-    }
-  }
   constexpr int kMaxBands = 16;
   // equal bands of a multiple of 8 rows (every tile's rows divide 8), ~64
   // rows each.  Measured at 1024^2, p = 4, end to end: 8 bands 15.3 GDoF/s,
