@@ -505,7 +505,6 @@ def mixed_metrics(torch, sipg, reps=3, cpu=True, fp64_peak=None, dim=512, p=6, i
     1e-10).  Every arm states its true residual and its L2 / H1 errors."""
     pen = float(p * p)
     op = sipg.Operator(dim, p, pen)
-    tiles = op.autotune()  # set-up, untimed: the tile shapes every arm's applies then use
     b = op.rhs("sinsin")
     n = op.ndof
     x = torch.zeros_like(b)
@@ -559,8 +558,6 @@ def mixed_metrics(torch, sipg, reps=3, cpu=True, fp64_peak=None, dim=512, p=6, i
     m = arms["mixed"]
     out = {"workload": "%dx%d quads, p=%d (%d DoF), pen %g, f = 8 pi^2 sin(2 pi x) sin(2 pi y), x0 = 0, "
                        "true relative residual 1e-10" % (dim, dim, p, n, pen),
-           "tiles": {k: {"elements_per_row": v[0], "rows": v[1], "threads_per_element": v[2], "ms_per_apply": v[3]}
-                     for k, v in tiles.items()},
            "solves_per_s": m["solves_per_s"], "ms": m["ms"], "true_rel_residual": m["true_rel_residual"],
            "L2_over_fp64_L2": m["L2"] / arms["fp64_reliable"]["L2"],
            "speedup_vs_fp64_reliable": arms["fp64_reliable"]["ms"] / m["ms"],
@@ -730,16 +727,6 @@ def _batch_case(torch, sipg, workloads, probs, cpu=True):
     FP64 around an FP32 inner CG, every problem to a true relative residual of
     1e-10) vs the same solves one at a time with the plain FP64 CG (relative
     1e-10 on its recursive residual; its true residuals are reported)."""
-    # the autotuner's tile shapes for a shape many problems share (set-up,
-    # untimed; a new operator of that (degree, mesh) starts from them)
-    shapes = {}
-    for d, p, pen, _ in probs:
-        shapes[(d, p, pen)] = shapes.get((d, p, pen), 0) + 1
-    for (d, p, pen), count in shapes.items():
-        if count >= 8:
-            tmp = sipg.Operator(d, p, pen)
-            tmp.autotune()
-            tmp.close()
     batch = sipg.Batch([(d, p, pen) for d, p, pen, _ in probs])
     bs = [batch.op(k).rhs("modes", sipg.Modes.make(*m)) for k, (_, _, _, m) in enumerate(probs)]
     xs = [torch.zeros_like(b) for b in bs]
