@@ -307,5 +307,4 @@ sipg_status twolevel_enqueue_restrict(const sipg_op* op, const void* handle, con
 sipg_status twolevel_enqueue_update(const sipg_op* op, const void* handle, float* x, const float* pb0,
                                     const float* pb1, float* r, const float* Ap, CgState<float>* st,
                                     const ReduceScratch& red, cudaStream_t s);
-int twolevel_levels(const void* handle);
 }  // namespace sipg

@@ -1555,10 +1555,6 @@ sipg_status twolevel_enqueue_update(const sipg_op* op, const void* handle, float
   return SIPG_OK;
 }
 
-// Levels of the vertex hierarchy (for reports), 0 if not built.
-int twolevel_levels(const void* handle) {
-  return handle ? (int)static_cast<const TwoLevel*>(handle)->lev.size() : 0;
-}
 
 // ---- many instances ----
 
