@@ -498,13 +498,6 @@ constexpr int kFlexibleInnerCap = 4000;
 
 // Flexible CG in FP64 with the FP32 inner CG as its preconditioner (see the
 // top of this file).
-// The recursively updated residual drifts from b - A x by the rounding of
-// each x += alpha d (of the order of eps |A| |x|, a few 1e-11 of |b| at 512^2,
-// p = 6): the true residual is checked once the recursion is below half the
-// target, which its last step usually brings it, so that the check passes
-// instead of costing an FP64 apply and a restart.
-constexpr double kFcgCheckFrac = 0.5;
-
 sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long long max_inner) {
   MixedCache& m = *v.m;
   const size_t n = v.n;
@@ -517,13 +510,12 @@ sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long lo
   if (st != SIPG_OK) return st;
   v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
   int first = 1;
-  bool checked = true;  // v.rel is a true residual b - A x (not the recursion's)
   for (;;) {
     if (!std::isfinite(v.rel)) {
       set_error("sipg_solve_mixed: non-finite residual");
       return SIPG_ERR_BREAKDOWN;
     }
-    if (checked && (v.rel <= o.outer_tol || rr == 0.0)) return SIPG_OK;
+    if (v.rel <= o.outer_tol || rr == 0.0) return SIPG_OK;
     if (v.outer >= o.max_outer || v.inner_total >= max_inner) return SIPG_ERR_NOT_CONVERGED;
     // z ~ A^-1 r: the FP32 inner CG from zero on r / ||r||
     k_fcg_restart<<<vb, kVecThreads, 0, s>>>(m.r64, m.r, m.e, n, m.st64, m.fs, m.st32, m.red32, (float)o.inner_tol,
@@ -574,14 +566,12 @@ sipg_status solve_flexible(Solve& v, int kind, const sipg_mixed_opts& o, long lo
     rr = m.st64_host->rr;
     v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
     first = 0;
-    checked = false;
-    if (v.rel <= kFcgCheckFrac * o.outer_tol || rr == 0.0) {
+    if (v.rel <= o.outer_tol) {
       // the recursion says done: recompute b - A x in FP64; continue (a
       // fresh direction history) if the drift left it above the target
       st = true_residual(v, &rr);
       if (st != SIPG_OK) return st;
       v.rel = (v.bnorm > 0) ? std::sqrt(rr) / v.bnorm : std::sqrt(rr);
-      checked = true;
       first = 1;
     }
   }
