@@ -311,10 +311,9 @@ sipg_status sipg_xpby_f32(size_t n, const float* d_x, float beta, float* d_y, vo
  * out-of-memory failure mid-sequence.  Its scratch is a fixed 64 KB device
  * array in the library (held by every GPU that loads it until exit), so
  * n <= 16,777,216; larger n returns SIPG_ERR_INVALID.  The first call on each
- * device looks up the array's device address: make that first call before any
- * stream capture.  The address is kept for the life of the process, so after
- * a cudaDeviceReset of a device this entry point must not be called on that
- * device again.  All calls share the array: calls that overlap on the GPU
+ * device looks up the array's device address and keeps it for the life of the
+ * process, so after a cudaDeviceReset of a device this entry point must not
+ * be called on that device again.  All calls share the array: calls that overlap on the GPU
  * (concurrent streams or threads) race and must be serialised by the caller.
  * Each call returns only once the result is in *result (it waits for the
  * stream); deterministic. */
