@@ -39,10 +39,8 @@
 // energy norm, in which rounding a smooth correction to FP32 is an error of
 // relative size ~sqrt(kappa) eps_32 (3e-4 at kappa = 2e7), while the residual
 // norm sees ~kappa eps_32 (~1).
-#include <algorithm>
 #include <cmath>
 #include <new>
-#include <type_traits>
 
 #include "sipg_apply_df.cuh"
 #include "sipg_cg_df.cuh"
@@ -141,12 +139,6 @@ struct MixedCache {
   float* z = nullptr;  // two-level inner kind: z = M r
   int* nz = nullptr;       // set-up: 1 if the start vector has a non-zero entry
   int* nz_host = nullptr;
-  // two-level inner kind: the whole inner solve as one graph launch, a
-  // conditional while node over one iteration (loop: its body-run counter)
-  cudaGraphExec_t exec_while = nullptr;
-  int while_gen = -1;
-  unsigned long long while_launches = 0;  // kernel launches of one body run
-  int* loop = nullptr;
   CgState<double>* st64 = nullptr;
   CgState<float>* st32 = nullptr;   // inner state, FP32 kind
   CgState<double>* stp = nullptr;   // inner state, pairs kind
@@ -179,8 +171,6 @@ struct MixedCache {
     cudaFree(p[0]);
     cudaFree(p[1]);
     cudaFree(Ap);
-    if (exec_while) cudaGraphExecDestroy(exec_while);
-    cudaFree(loop);
     cudaFree(z);
     cudaFree(nz);
     cudaFreeHost(nz_host);
@@ -328,71 +318,6 @@ sipg_status enqueue_iteration(sipg_op* op, MixedCache& m, int kind, cudaStream_t
   return SIPG_OK;
 }
 
-// The condition of the inner solve's while loop: go on while the inner state
-// is not done, and in any case for at most `cap` runs of the body, so that the
-// loop ends whatever the state holds.
-__global__ void k_inner_continue(cudaGraphConditionalHandle h, const CgState<float>* st, int* count, int cap) {
-  const int c = ++*count;
-  cudaGraphSetConditional(h, (!*(volatile const int*)&st->done && c < cap) ? 1u : 0u);
-}
-
-constexpr int kWhileCap = 8192;  // body runs per launch of the inner solve's graph
-
-// The two-level inner kind's solve as one graph: a conditional while node
-// whose body is one inner iteration and k_inner_continue.  One launch runs the
-// inner CG to its stop test with no host round trip and no iteration past it.
-sipg_status capture_while(sipg_op* op, MixedCache& m) {
-  if (m.exec_while && m.while_gen == op->tile_gen) return SIPG_OK;
-  if (m.exec_while) {
-    cudaGraphExecDestroy(m.exec_while);
-    m.exec_while = nullptr;
-  }
-  if (!m.loop) SIPG_CUDA_TRY(cudaMalloc(&m.loop, sizeof(int)));
-  ApplyArgs<float> none{};
-  none.dim = op->dim;
-  SIPG_CUDA_TRY(launch_apply_f32(op->p, op->cfg32, APPLY_PREPARE, none, op->tab, m.cap));
-  cudaGraph_t g = nullptr;
-  SIPG_CUDA_TRY(cudaGraphCreate(&g, 0));
-  cudaGraphConditionalHandle h{};
-  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
-  cudaGraphNodeParams cp{};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
-  sipg_status st = SIPG_OK;
-  if (e == cudaSuccess) {
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(m.cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      const unsigned long long c0 = g_launches.load();
-      st = enqueue_iteration(op, m, SIPG_INNER_F32_TWOLEVEL, m.cap);
-      if (st == SIPG_OK) {
-        k_inner_continue<<<1, 1, 0, m.cap>>>(h, m.st32, m.loop, kWhileCap);
-        count_launch();
-      }
-      const unsigned long long c1 = g_launches.load();
-      g_launches.fetch_sub(c1 - c0);
-      m.while_launches = c1 - c0;
-      cudaGraph_t captured = nullptr;
-      const cudaError_t end = cudaStreamEndCapture(m.cap, &captured);
-      if (e == cudaSuccess) e = end;
-    }
-  }
-  if (e == cudaSuccess && st == SIPG_OK) e = cudaGraphInstantiate(&m.exec_while, g, 0);
-  cudaGraphDestroy(g);
-  if (st != SIPG_OK) return st;
-  if (e != cudaSuccess) {
-    m.exec_while = nullptr;
-    set_error(std::string("inner solve graph: ") + cudaGetErrorString(e));
-    return SIPG_ERR_CUDA;
-  }
-  m.while_gen = op->tile_gen;
-  return SIPG_OK;
-}
-
 sipg_status capture(sipg_op* op, MixedCache& m, int kind, int K) {
   if (m.exec[kind] && m.exec_k[kind] == K && m.exec_gen[kind] == op->tile_gen) return SIPG_OK;
   if (m.exec[kind]) {
@@ -502,22 +427,6 @@ sipg_status true_residual(Solve& v, double* rr_out, bool plain = false) {
 // Replays the inner K-iteration graph until the inner state says done.
 template <typename StT>
 sipg_status run_inner(Solve& v, int kind, StT* st_dev, StT* st_host) {
-  if constexpr (std::is_same<StT, CgState<float>>::value) {
-    if (kind == SIPG_INNER_F32_TWOLEVEL && v.m->exec_while) {
-      // one launch runs the inner solve (restarted at iteration 0) to its
-      // stop test; again only if the cap on body runs ended it first
-      int it_prev = 0;
-      for (;;) {
-        SIPG_CUDA_TRY(cudaMemsetAsync(v.m->loop, 0, sizeof(int), v.s));
-        SIPG_CUDA_TRY(cudaGraphLaunch(v.m->exec_while, v.s));
-        SIPG_CUDA_TRY(cudaMemcpyAsync(st_host, st_dev, sizeof(StT), cudaMemcpyDeviceToHost, v.s));
-        SIPG_CUDA_TRY(cudaStreamSynchronize(v.s));
-        count_launch((unsigned long long)std::max(1, st_host->it - it_prev) * v.m->while_launches);
-        it_prev = st_host->it;
-        if (st_host->done) return SIPG_OK;
-      }
-    }
-  }
   for (;;) {
     SIPG_CUDA_TRY(cudaGraphLaunch(v.m->exec[kind], v.s));
     count_launch(v.m->exec_launches[kind]);
@@ -710,12 +619,7 @@ extern "C" sipg_status sipg_solve_mixed(sipg_op* op, double* d_x, const double* 
   }
   if (kind == SIPG_INNER_F32_TWOLEVEL && !m.z) SIPG_CUDA_TRY(cudaMalloc(&m.z, n * sizeof(float)));
   const int K = n <= (1u << 20) ? 32 : 8;  // inner iterations per graph launch
-  st = SIPG_ERR_UNSUPPORTED;
-  if (kind == SIPG_INNER_F32_TWOLEVEL) {
-    st = capture_while(op, m);
-    if (st != SIPG_OK) cudaGetLastError();  // no conditional graph here: K iterations per launch instead
-  }
-  if (st != SIPG_OK) st = capture(op, m, kind, K);
+  st = capture(op, m, kind, K);
   if (st != SIPG_OK) return st;
   const long long max_inner = o.max_inner > 0 ? o.max_inner : op->ndof;
   Solve v{op, &m, d_x, d_b, s, n, vec_grid(n), K, 0.0};
