@@ -170,3 +170,36 @@ def test_server_interleaved_precisions_against_the_oracle(sipg, oracle, torch):
         op.close()
         sv.release(rid)
     sv.close()
+
+
+def test_server_closes_with_preparations_pending(sipg, torch):
+    """Mixed requests start their preparation (operator and two-level
+    preconditioner, on the server's preparation threads) at submission; a
+    server closed before any step joins those threads and frees everything,
+    and a fresh server then serves the same requests."""
+    reqs = [(d, p, float(p * p)) for d, p in ((64, 4), (40, 6), (96, 3), (33, 8), (71, 2), (128, 5))]
+    srv = sipg.Server(budget_bytes=8 << 30, max_active=16, iters_per_step=8)
+    for d, p, pen in reqs:
+        _, st = srv.submit(d, p, pen, 1e-8, "sinsin", None, precision=sipg.F32)
+        assert st == 0
+    srv.close()
+    srv = sipg.Server(budget_bytes=8 << 30, max_active=16, iters_per_step=8)
+    ids = [srv.submit(d, p, pen, 1e-8, "sinsin", None, precision=sipg.F32)[0] for d, p, pen in reqs]
+    done = {}
+    import time
+
+    t_end = time.time() + 120
+    while time.time() < t_end:
+        srv.step()
+        for rid in ids:
+            if rid not in done:
+                r = srv.poll(rid)
+                if r.done:
+                    done[rid] = (r.status, r.rel_residual)
+        if len(done) == len(ids):
+            break
+    assert len(done) == len(ids)
+    for status, rel in done.values():
+        assert status == 0 and rel <= 1e-8
+    assert srv.stats().prep_ms > 0
+    srv.close()
