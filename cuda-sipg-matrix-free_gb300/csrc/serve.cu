@@ -613,13 +613,15 @@ void server_free(sipg_server* sv) {
   for (Lane& L : sv->lanes)
     if (L.s) cudaStreamSynchronize(L.s);
   if (sv->s) cudaStreamSynchronize(sv->s);
+  // every request, queued or not, is in sv->all (submit enters it there first)
   for (auto& kv : sv->all) {
     if (kv.second->mem) cudaFreeAsync(kv.second->mem, sv->s);
     if (kv.second->x64) cudaFreeAsync(kv.second->x64, sv->s);
     delete kv.second;
   }
-  for (Request* r : sv->queue)
-    if (!sv->all.count(r->id)) delete r;
+  sv->all.clear();
+  sv->queue.clear();
+  sv->prep_todo.clear();
   if (sv->s) cudaStreamSynchronize(sv->s);
   cudaFree(sv->slots.d32);
   cudaFree(sv->slots.d64);
