@@ -1125,20 +1125,34 @@ HostLevel host_galerkin(const HostLevel& F) {
 // omega = 1.52 / lambda_max(D^-1 A) (power iteration from a fixed vector)
 double host_omega(const HostLevel& L) {
   const int n1 = L.m + 1, nv = n1 * n1;
-  std::vector<double> x(nv), y;
+  std::vector<double> x(nv), y, nrm_row(n1), nx_row(n1);
   for (int v = 0; v < nv; ++v) x[v] = std::sin(0.7 * v + 0.3) + 0.5;
   double lam = 1.0;
   for (int it = 0; it < 40; ++it) {
     host_stencil_apply(L, x, y);
+    // per-row partial sums, then the rows in order: the same result for any split
+    host_rows(n1, [&](int lo, int hi) {
+      for (int vy = lo; vy < hi; ++vy) {
+        double a = 0.0, b = 0.0;
+        for (int v = vy * n1; v < (vy + 1) * n1; ++v) {
+          y[v] /= L.S[(size_t)4 * nv + v];
+          a += y[v] * y[v];
+          b += x[v] * x[v];
+        }
+        nrm_row[vy] = a;
+        nx_row[vy] = b;
+      }
+    });
     double nrm = 0.0, nx = 0.0;
-    for (int v = 0; v < nv; ++v) {
-      y[v] /= L.S[(size_t)4 * nv + v];
-      nrm += y[v] * y[v];
-      nx += x[v] * x[v];
+    for (int vy = 0; vy < n1; ++vy) {
+      nrm += nrm_row[vy];
+      nx += nx_row[vy];
     }
     lam = std::sqrt(nrm / nx);
     const double s = 1.0 / std::sqrt(nrm);
-    for (int v = 0; v < nv; ++v) x[v] = y[v] * s;
+    host_rows(n1, [&](int lo, int hi) {
+      for (int v = lo * n1; v < hi * n1; ++v) x[v] = y[v] * s;
+    });
   }
   return 1.6 / (1.05 * lam);
 }
