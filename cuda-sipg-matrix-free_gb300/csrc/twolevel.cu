@@ -1075,49 +1075,56 @@ void host_stencil_apply(const HostLevel& L, const std::vector<double>& x, std::v
   });
 }
 
-// the next level's stencil: P^T A P by probing with nine colours
+// The coarse vertices whose interpolation weight at fine vertex g is not
+// zero (one or two): the coarse vertices sit at the even fine vertices and
+// at m, an odd fine vertex other than m lies between two.
+inline int tl_parents(int g, int m, int* out) {
+  if (g % 2 == 0 || g == m) {
+    out[0] = (g + 1) / 2;
+    return 1;
+  }
+  out[0] = (g - 1) / 2;
+  out[1] = (g + 1) / 2;
+  return 2;
+}
+
+// the next level's stencil, C = P^T A P, entry by entry: for coarse vertex
+// v, every fine vertex f under it (weight P(f, v)), every neighbour g of f
+// (A(f, g)) and every coarse vertex u over g (P(g, u)) -- at most nine
+// neighbours u, all within one coarse cell of v
 HostLevel host_galerkin(const HostLevel& F) {
   HostLevel C;
   C.m = (F.m + 1) / 2;
-  const int cn1 = C.m + 1, cnv = cn1 * cn1, fn1 = F.m + 1, fnv = fn1 * fn1;
+  const int cn1 = C.m + 1, cnv = cn1 * cn1, fn1 = F.m + 1, fnv = fn1 * fn1, m = F.m;
   C.S.assign((size_t)9 * cnv, 0.0);
-  std::vector<double> xc(cnv), xf(fnv), yf;
-  std::vector<std::vector<double>> ycs(9, std::vector<double>(cnv));
-  for (int cy = 0; cy < 3; ++cy)
-    for (int cx = 0; cx < 3; ++cx) {
-      std::vector<double>& yc = ycs[cy * 3 + cx];
-      for (int v = 0; v < cnv; ++v) xc[v] = ((v % cn1) % 3 == cx && (v / cn1) % 3 == cy) ? 1.0 : 0.0;
-      host_rows(fn1, [&](int lo, int hi) {  // P
-        for (int iy = lo; iy < hi; ++iy)
-          for (int ix = 0; ix <= F.m; ++ix) {
-            double s = 0.0;
-            for (int I = std::max(0, (iy - 1) / 2); I <= std::min(C.m, (iy + 1) / 2 + 1); ++I)
-              for (int J = std::max(0, (ix - 1) / 2); J <= std::min(C.m, (ix + 1) / 2 + 1); ++J)
-                s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * xc[I * cn1 + J];
-            xf[iy * fn1 + ix] = s;
-          }
-      });
-      host_stencil_apply(F, xf, yf);
-      host_rows(cn1, [&](int lo, int hi) {  // P^T
-        for (int I = lo; I < hi; ++I)
-          for (int J = 0; J <= C.m; ++J) {
-            double s = 0.0;
-            for (int iy = std::max(0, 2 * I - 1); iy <= std::min(F.m, 2 * I + 1); ++iy)
-              for (int ix = std::max(0, 2 * J - 1); ix <= std::min(F.m, 2 * J + 1); ++ix)
-                s += tl_w<double>(ix, J, F.m) * tl_w<double>(iy, I, F.m) * yf[iy * fn1 + ix];
-            yc[I * cn1 + J] = s;
-          }
-      });
-    }
-  host_rows(cn1, [&](int lo, int hi) {  // entry (v, u) is probe colour(u)'s result at v
+  host_rows(cn1, [&](int lo, int hi) {
     for (int I = lo; I < hi; ++I)
-      for (int J = 0; J <= C.m; ++J)
-        for (int dy = -1; dy <= 1; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int ux = J + dx, uy = I + dy;
-            if (ux < 0 || uy < 0 || ux > C.m || uy > C.m) continue;
-            C.S[(size_t)((dy + 1) * 3 + (dx + 1)) * cnv + I * cn1 + J] = ycs[(uy % 3) * 3 + ux % 3][I * cn1 + J];
+      for (int J = 0; J <= C.m; ++J) {
+        double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int fy = std::max(0, 2 * I - 1); fy <= std::min(m, 2 * I + 1); ++fy) {
+          const double wy = tl_w<double>(fy, I, m);
+          if (wy == 0.0) continue;
+          for (int fx = std::max(0, 2 * J - 1); fx <= std::min(m, 2 * J + 1); ++fx) {
+            const double wx = tl_w<double>(fx, J, m);
+            if (wx == 0.0) continue;
+            const int f = fy * fn1 + fx;
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dx = -1; dx <= 1; ++dx) {
+                const int gx = fx + dx, gy = fy + dy;
+                if (gx < 0 || gy < 0 || gx > m || gy > m) continue;
+                const double a = F.S[(size_t)((dy + 1) * 3 + (dx + 1)) * fnv + f];
+                if (a == 0.0) continue;
+                int py[2], px[2];
+                const int ny = tl_parents(gy, m, py), nx = tl_parents(gx, m, px);
+                for (int iy = 0; iy < ny; ++iy)
+                  for (int ix = 0; ix < nx; ++ix)
+                    acc[(py[iy] - I + 1) * 3 + (px[ix] - J + 1)] +=
+                        wx * wy * a * tl_w<double>(gy, py[iy], m) * tl_w<double>(gx, px[ix], m);
+              }
           }
+        }
+        for (int k = 0; k < 9; ++k) C.S[(size_t)k * cnv + I * cn1 + J] = acc[k];
+      }
   });
   return C;
 }
